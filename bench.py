@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""Benchmark of the LINGO Tanimoto engine on one node.
+
+Default workload (rows_1m): 10,240 query molecules against a 1,000,000-molecule
+database from the same seeded generator (SMILES-like strings, lognormal length
+median 45 chars, clipped to 10-200); getMultipleRows in blocks of 1,024 rows,
+each a 1024 x 1,000,000 fp32 block kept in device memory.  One step = one
+block.  The value is logical pairs / device time in Gpairs/s, bit-exact to the
+CPU oracle (a spot check runs after timing).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun (N > 1) every rank runs independent replicas on its own GPU
+(the path has no exchange step); rank 0 prints one JSON line.
+``--impl reference`` times the reference's CPU implementation instead (its
+own compiled C code where it was built here, otherwise the oracle's C
+restatement) on the host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+DB_N = 1_000_000
+QUERY_N = 10_240
+BLOCK = 1024
+METRIC = "LINGO Tanimoto Gpairs/s bit-exact"
+WORKLOAD = ("rows_1m: getMultipleRows, 1,024-row blocks x 1,000,000-molecule database "
+            "(10,240 query rows, lognormal median 45 chars), fp32 block kept on device")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def make_sets():
+    from siml_gb300 import synthetic as S
+    t = time.time()
+    db = S.smiles_set(S.SEED_DB_1M, S.LOGNORMAL_45, DB_N)
+    q = S.smiles_set(S.SEED_DB_1M, S.LOGNORMAL_45, QUERY_N, first=DB_N)
+    log("generated + compiled %d + %d molecules in %.1f s" % (DB_N, QUERY_N, time.time() - t))
+    return db, q
+
+
+# ---------------------------------------------------------------- clocks ----
+class ClockSampler:
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+        self.th = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.th:
+            self.th.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[3:]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU arm ----
+def cpu_reference_rate(db, q, target_s=12.0, max_rows=1024):
+    """Times the reference's CPU path (its compiled C code when built here,
+    else the oracle's restatement) with all host threads on R rows x full DB."""
+    from oracle import cpulingo as O
+    ref_mod = O.reference_module("_CPULingo")
+    nthreads = os.cpu_count() or 1
+    L, C, ln, mg = db
+    QL, QC, Qln, Qmg = q
+
+    def run(r0, r1):
+        if ref_mod is not None:
+            return ref_mod.getTanimotoBlockParallel(
+                QL[r0:r1], QC[r0:r1], Qmg[r0:r1].reshape(-1, 1), Qln[r0:r1].reshape(-1, 1),
+                L, C, mg.reshape(-1, 1), ln.reshape(-1, 1), nthreads)
+        return O.tanimoto_block(q, db, r0, r1, nthreads=nthreads)
+
+    t = time.time()
+    run(0, 4)
+    dt = max(time.time() - t, 1e-3)
+    rows = int(max(4, min(max_rows, 4 * target_s / dt)))
+    t = time.time()
+    run(4, 4 + rows)
+    dt = time.time() - t
+    pairs = rows * L.shape[0]
+    return {"value": pairs / dt / 1e9, "unit": "Gpairs/s", "cores": nthreads,
+            "kind": "reference" if ref_mod is not None else "port",
+            "sample": "%d query rows x %d database molecules (%.2e pairs) in %.2f s" % (rows, L.shape[0], pairs, dt)}
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "port"], check=True)
+    db, q = make_sets()
+    from oracle import cpulingo as O
+    ref_mod = O.reference_module("_CPULingo")
+    nthreads = os.cpu_count() or 1
+    # each step: a bounded sample of the workload (rows x full database)
+    probe = cpu_reference_rate(db, q, target_s=2.0, max_rows=64)
+    rows = int(max(2, min(BLOCK, probe["value"] * 1e9 * 6.0 / DB_N)))
+    L, C, ln, mg = db
+
+    def step(r0):
+        r1 = r0 + rows
+        if ref_mod is not None:
+            ref_mod.getTanimotoBlockParallel(q[0][r0:r1], q[1][r0:r1], q[3][r0:r1].reshape(-1, 1),
+                                             q[2][r0:r1].reshape(-1, 1), L, C, mg.reshape(-1, 1),
+                                             ln.reshape(-1, 1), nthreads)
+        else:
+            O.tanimoto_block(q, db, r0, r1, nthreads=nthreads)
+
+    for w in range(args.warmup):
+        step((w * rows) % (QUERY_N - rows))
+    t = time.time()
+    for k in range(args.steps):
+        step(((args.warmup + k) * rows) % (QUERY_N - rows))
+    dt = time.time() - t
+    value = args.steps * rows * DB_N / dt / 1e9
+    kind = "reference" if ref_mod is not None else "port"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "rows_per_step": rows, "db_molecules": DB_N},
+        "cpu_baseline": {"value": value, "unit": "Gpairs/s", "cores": nthreads, "kind": kind,
+                         "sample": "%d query rows x %d molecules per step" % (rows, DB_N)},
+        "e2e": {"value": value, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------- GPU arm ----
+def gpu_arm(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from siml_gb300 import GPULingo
+    db, q = make_sets()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    gl = GPULingo(local, stream=stream)
+    t = time.time()
+    gl.set_qsmiles(*db)
+    gl.set_refsmiles(*q)
+    stats = gl.dbStats()
+    torch.cuda.synchronize()
+    log("database layout ready in %.2f s: %s" % (time.time() - t, stats))
+    nblocks = QUERY_N // BLOCK
+    out = torch.empty((BLOCK, DB_N), dtype=torch.float32, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+
+    def block_of(k):
+        b = (k * world + rank) % nblocks
+        return b * BLOCK, (b + 1) * BLOCK
+
+    for w in range(args.warmup):
+        r0, r1 = block_of(w)
+        gl.getMultipleRowsDevice(r0, r1, out=out)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    launches0 = gl.launchCount()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    kernel_ms = []
+    torch.cuda.synchronize()
+    wall0 = time.time()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+            ev[k][0].record(stream)
+        r0, r1 = block_of(args.warmup + k)
+        gl.getMultipleRowsDevice(r0, r1, out=out)
+        ev[k][1].record(stream)
+        kernel_ms.append(gl.lastKernelMs())
+    torch.cuda.synchronize()
+    wall = time.time() - wall0
+    launches = gl.launchCount() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    if world > 1:
+        tt = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(tt.item())
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    pairs_per_step = BLOCK * DB_N
+    value = world * args.steps * pairs_per_step / (total_ms / 1e3) / 1e9
+    ms_per_step = total_ms / args.steps
+
+    # spot parity check against the oracle (two rows of the last block)
+    from oracle import cpulingo as O
+    r0, r1 = block_of(args.warmup + args.steps - 1)
+    got = out[:2].cpu().numpy()
+    want = O.tanimoto_block(q, db, r0, r0 + 2, nthreads=os.cpu_count() or 1)
+    parity = bool(np.array_equal(got, want))
+
+    # roofline of the dominant kernel (k_rows): algorithmic bytes per launch
+    kms = statistics.mean(kernel_ms)
+    out_bytes = pairs_per_step * 4
+    db_bytes = stats["ngroups_total"] * 16 + stats["nchunks"] * 32 * 8 + stats["nchunks"] * 12
+    alg_bytes = out_bytes + db_bytes
+    achieved = alg_bytes / (kms / 1e3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = read_profile_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": "k_rows", "kernel_ms": kms,
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback"}
+
+    e2e = None
+    cpu = None
+    if rank == 0:
+        e2e = measure_e2e(gl, q, stream, dev, steps=min(3, args.steps))
+        if world == 1:
+            cpu = cpu_reference_rate(db, q)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded SMILES-like strings)",
+            "config": {"workload": WORKLOAD, "rows_per_step": BLOCK, "db_molecules": DB_N,
+                       "query_rows": QUERY_N, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "flushed between steps by a 256 MB write; each step also writes a 4 GB block",
+                       "db_layout": stats},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk, "parity_spot_check": parity, "wall_s_timed": wall,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def read_profile_traffic():
+    """DRAM bytes per k_rows launch from the committed ncu summary, if any."""
+    path = os.path.join(REPO, "profiles", "k_rows_rows1m.md")
+    try:
+        for ln in open(path):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":", 1)[1].strip().split()[0])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def measure_e2e(gl, q, stream, dev, steps=3):
+    """Same metric through the public API with host buffers: per step the
+    block's compiled query rows go host->device from pinned memory
+    (set_refsmiles) and the fp32 block comes back device->host into pinned
+    memory."""
+    import torch
+    QL, QC, Qln, Qmg = q
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    host_out = torch.empty((BLOCK, DB_N), dtype=torch.float32).pin_memory()
+    dev_out = torch.empty((BLOCK, DB_N), dtype=torch.float32, device=dev)
+    blocks = [(pin(QL[i * BLOCK:(i + 1) * BLOCK]), pin(QC[i * BLOCK:(i + 1) * BLOCK]),
+               pin(Qln[i * BLOCK:(i + 1) * BLOCK]), pin(Qmg[i * BLOCK:(i + 1) * BLOCK])) for i in range(steps + 1)]
+    h2d = sum(int(a.numel() * a.element_size()) for a in blocks[0])
+    d2h = BLOCK * DB_N * 4
+
+    def one(i):
+        b = blocks[i]
+        gl.set_refsmiles(b[0], b[1], b[2], b[3])
+        gl.getMultipleRowsDevice(0, BLOCK, out=dev_out)
+        host_out.copy_(dev_out, non_blocking=True)
+        torch.cuda.synchronize()
+
+    one(steps)  # warm
+    t = time.time()
+    for i in range(steps):
+        one(i)
+    dt = time.time() - t
+    gl.set_refsmiles(*q)  # restore the full query set
+    return {"value": steps * BLOCK * DB_N / dt / 1e9, "unit": "Gpairs/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "steps": steps}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,180 @@
+/*
+ * siml_gb300 — C ABI of a GB300-native (sm_103a) LINGO multiset-Tanimoto
+ * engine that drops in for pySIML's GPU path (pysiml.GPULingo, pysiml.compiler,
+ * pysiml.utilities).
+ *
+ * Conventions
+ *   - Every function returns an int status (SIML_OK == 0) unless noted;
+ *     siml_last_error() gives the message of the calling thread's last failure.
+ *   - Arrays are plain pointers with explicit sizes and row strides (in
+ *     elements).  `where` says whether array arguments are host (SIML_HOST)
+ *     or device (SIML_DEVICE) pointers.  Host-pointer calls return when the
+ *     result is in host memory; device-pointer calls are queued on the
+ *     engine's stream and return at once (siml_sync / siml_query_done).
+ *   - A handle is used by one host thread at a time; one handle per GPU
+ *     (the reference's "one GPULingo object per device", similarity.txt:121-145).
+ *   - "ref set" = the rows of a Tanimoto matrix (pySIML's set_refsmiles),
+ *     "query set" = its columns (set_qsmiles), as in
+ *     doc/html/_sources/concepts.txt:52-57.
+ *
+ * Every entry point cites the reference interface it replaces
+ * (file:line inside the reference project).
+ */
+#ifndef SIML_GB300_H
+#define SIML_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SIML_OK 0
+#define SIML_ERR_INVALID 1     /* bad argument (reference: ValueError / TypeError)      */
+#define SIML_ERR_STATE 2       /* set not initialised, no pending result                */
+#define SIML_ERR_CUDA 3        /* CUDA runtime failure                                  */
+#define SIML_ERR_NOMEM 4       /* device or host allocation failed                      */
+#define SIML_ERR_TIMEOUT 5     /* a bounded device wait gave up                         */
+#define SIML_ERR_UNSUPPORTED 6 /* input outside what the kernels accept (see message)   */
+#define SIML_ERR_RANGE 7       /* row range outside the ref set (reference: bare raise) */
+
+/* pointer location */
+#define SIML_HOST 0
+#define SIML_DEVICE 1
+
+/* synthetic length models (siml_synth_*) */
+#define SIML_SYNTH_UNIFORM_20_90 0
+#define SIML_SYNTH_LOGNORMAL_45 1
+#define SIML_SYNTH_BIMODAL_35_110 2
+
+typedef struct siml_engine siml_engine;
+
+/* ---- library ------------------------------------------------------------ */
+const char* siml_version(void);
+/* Message of the calling thread's last failing call ("" if none). */
+const char* siml_last_error(void);
+
+/* ---- engine lifetime ---------------------------------------------------- */
+/* GPULingo(deviceID) — pysiml/GPULingo.py:162-173 (context + stream per object). */
+int siml_create(int device, siml_engine** out);
+int siml_destroy(siml_engine* h);
+/* Run subsequent work on a caller-owned cudaStream_t (NULL: the engine's own). */
+int siml_set_stream(siml_engine* h, void* cuda_stream);
+/* stream.synchronize() inside retrieveAsyncResult — pysiml/GPULingo.py:546. */
+int siml_sync(siml_engine* h);
+/* asyncOperationsDone — pysiml/GPULingo.py:642-647; *done = 1 when idle. */
+int siml_query_done(siml_engine* h, int* done);
+
+/* ---- SMILES sets -------------------------------------------------------- */
+/* set_refsmiles(L, C, lengths, mags=None) — pysiml/GPULingo.py:187-242.
+ * lingos/counts: [n, width] with row stride ld; lengths/mags: [n].  mags may
+ * be NULL: magnitudes are then the sum of each row's first `length` counts
+ * (accumulateRefMagnitudes, pysiml/kernels.py:45-61).  Codes of a row must be
+ * strictly increasing (signed) and counts non-negative, as the compiler
+ * produces them; other input is rejected with SIML_ERR_UNSUPPORTED. */
+int siml_set_ref(siml_engine* h, const int32_t* lingos, const int32_t* counts,
+                 const int32_t* lengths, const int32_t* mags,
+                 int64_t n, int64_t width, int64_t ld, int where);
+/* set_qsmiles(L, C, lengths, mags=None) — pysiml/GPULingo.py:246-313.  The query
+ * set is the resident database; the engine builds its device layout here. */
+int siml_set_query(siml_engine* h, const int32_t* lingos, const int32_t* counts,
+                   const int32_t* lengths, const int32_t* mags,
+                   int64_t n, int64_t width, int64_t ld, int where);
+/* Sizes of the current sets (-1 when unset). */
+int siml_set_sizes(siml_engine* h, int64_t* nref, int64_t* nquery);
+
+/* ---- similarity calls --------------------------------------------------- */
+/* getMultipleRows[_async](rowbase, rowlimit) — pysiml/GPULingo.py:354-404,
+ * kernel gpuLingoSim3_multirow pysiml/kernels.py:315-352.  out: fp32
+ * [rowlimit-rowbase, nquery] with row stride ldo (>= nquery). */
+int siml_rows(siml_engine* h, int64_t rowbase, int64_t rowlimit,
+              float* out, int64_t ldo, int where);
+/* getTanimotoRow[_async](row) — pysiml/GPULingo.py:316-351, kernel
+ * gpuLingoSim3_srgf_T_tex2ns pysiml/kernels.py:234-270: both magnitudes are
+ * recomputed from the counts and a molecule with no LINGOs scores 0. */
+int siml_row_single(siml_engine* h, int64_t row, float* out, int where);
+/* getNeighbors[_async](rowbase, rowlimit, lo, hi, maxneighbors) —
+ * pysiml/GPULingo.py:467-534, kernel gpuGetNeighbors_multirow
+ * pysiml/kernels.py:393-475.  pitch = 16*ceil(maxneighbors/16) as the
+ * reference computes it (GPULingo.py:491).  idx: int32 [rows, pitch] query
+ * indices in ascending order; sims (may be NULL): fp32 [rows, pitch] beside
+ * them; counts: int32 [rows], larger than pitch when a row overflowed
+ * (counted in whole waves of 128 columns, as the reference does). */
+int siml_neighbors(siml_engine* h, int64_t rowbase, int64_t rowlimit,
+                   float lo, float hi, int64_t pitch,
+                   int32_t* idx, float* sims, int32_t* counts, int where);
+/* getMultipleHistogrammedRows[_async](rowbase, rowlimit) —
+ * pysiml/GPULingo.py:407-463, kernel gpuHistogrammedLingo_multirow
+ * pysiml/kernels.py:606-666.  out: int32 [rows, 101], row stride ldo >= 101. */
+int siml_hist101(siml_engine* h, int64_t rowbase, int64_t rowlimit,
+                 int32_t* out, int64_t ldo, int where);
+/* Per-row top-k (no reference counterpart; extends getNeighbors): the k
+ * largest similarities of each row, descending, ties to the lower query
+ * index; rows with fewer than k columns are padded with -1 / -1.0f.
+ * idx: int32 [rows, k], sims: fp32 [rows, k]. */
+int siml_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int64_t k,
+              int32_t* idx, float* sims, int where);
+/* Global similarity histogram over all pairs of a row block (no reference
+ * counterpart; a whole-block form of getMultipleHistogrammedRows):
+ * nbins = 1000, bin = min((unsigned)(t*1000.0f), 999).  out: uint64 [1000],
+ * accumulated into (not cleared), so successive blocks sum. */
+int siml_hist_global(siml_engine* h, int64_t rowbase, int64_t rowlimit,
+                     uint64_t* out, int where);
+
+/* ---- batched ragged neighbor jobs --------------------------------------- */
+/* Many independent (ref rows, query-set index range) threshold searches in
+ * one launch (no reference counterpart: the reference issues one
+ * getNeighbors call per job, GPULingo.py:467-513).  Job j covers ref rows
+ * [row_begin[j], row_end[j]) against query columns [col_begin[j], col_end[j])
+ * with the getNeighbors rule and pitch; its rows' results go to
+ * idx/sims/counts at row offset out_row[j] (idx, sims: [*, pitch];
+ * counts: [*]).  Indices are absolute query indices. */
+int siml_batch_neighbors(siml_engine* h, int64_t njobs,
+                         const int64_t* row_begin, const int64_t* row_end,
+                         const int64_t* col_begin, const int64_t* col_end,
+                         const int64_t* out_row, float lo, float hi, int64_t pitch,
+                         int32_t* idx, float* sims, int32_t* counts, int where);
+
+/* ---- SMILES compiler ---------------------------------------------------- */
+/* cSMILEStoMatrices / _ccompiler.SMILEStoMatrices — pysiml/compiler.py:53-82,
+ * pysiml/_ccompiler.cpp:276-381.  Strings are concatenated in buf, string s
+ * at [offsets[s], offsets[s+1]); a NUL, space, '\n' or '\r' ends a string.
+ * siml_compile_width returns the number of columns needed (max unique
+ * LINGOs over the batch) or a negative status. */
+int64_t siml_compile_width(const char* buf, const int64_t* offsets, int64_t n);
+/* Writes zero-padded int32 lingos/counts [n, width] and lengths/mags [n]. */
+int siml_compile_smiles(const char* buf, const int64_t* offsets, int64_t n,
+                        int32_t* lingos, int32_t* counts, int32_t* lengths,
+                        int32_t* mags, int64_t width);
+
+/* ---- utilities ---------------------------------------------------------- */
+/* rowHistogram101 — pysiml/utilities.py:44-55, pysiml/_cpuutil.cpp:52-126:
+ * per-row 101-bin uint32 histogram of an fp32 matrix [rows, cols] (row
+ * stride ld); bin = min((unsigned)(x*100), 100), negatives to bin 0. */
+int siml_row_histogram101(siml_engine* h, const float* data, int64_t rows, int64_t cols,
+                          int64_t ld, uint32_t* hist, int where);
+
+/* ---- synthetic workload sets (benchmarks and tests) --------------------- */
+int siml_synth_lengths(uint64_t seed, int dist, int64_t first, int64_t n, int32_t* lens);
+int siml_synth_smiles(uint64_t seed, int dist, int64_t first, int64_t n,
+                      char* buf, int64_t bufcap, int64_t* offsets);
+
+/* ---- introspection ------------------------------------------------------ */
+/* Device-layout statistics (no reference counterpart), prepared on demand:
+ * out[0] = (code, level) pairs in the database vocabulary, out[1] = bytes per
+ * stored entry, out[2] = 16-byte entry groups stored, out[3] = chunks of 32
+ * molecules, out[4] = largest chunk in groups per lane, out[5] = database
+ * molecules, out[6] / out[7] = largest count sum in the ref / query set. */
+int siml_db_stats(siml_engine* h, int64_t out[8]);
+/* Number of kernel launches this engine has issued since creation. */
+int64_t siml_launch_count(siml_engine* h);
+/* Average device time (ms) of the dominant kernel of the last call on this
+ * engine, measured with CUDA events on the engine's stream (0 if none). */
+double siml_last_kernel_ms(siml_engine* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIML_GB300_H */

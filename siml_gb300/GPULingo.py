@@ -1,0 +1,261 @@
+"""Drop-in for pySIML's ``pysiml.GPULingo.GPULingo`` (pysiml/GPULingo.py:158-648).
+
+Same constructor, method names, positional signatures, return shapes and
+async protocol as the reference; the work runs in the sm_103a kernels of
+``libsiml_gb300.so`` through its C ABI (include/siml_gb300.h).
+
+Differences a caller may notice (all listed in the repository's design notes):
+
+* The reference's texture-size limits (ref set <= 32768 rows, query set <=
+  65536 molecules, <= 32768 padded LINGO columns, GPULingo.py:206-207,
+  269-270) do not apply.
+* Input codes of each molecule must be strictly increasing and counts
+  non-negative (what the SMILES compiler produces); the reference's merge
+  silently computes something else for unsorted input, this raises
+  ``ValueError``.
+* ``getNeighbors`` returns at most ``pitch`` columns even when a row
+  overflowed (the reference copies ``max(count)`` columns and reads past its
+  buffer in that case, GPULingo.py:597-613).
+* ``retrieveAsyncResult`` without a pending call raises ``RuntimeError``
+  (the reference raises an undefined name, GPULingo.py:623-640).
+
+Inputs may be numpy arrays or torch tensors (CPU or CUDA).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+try:  # torch provides device buffers and stream interop; it is optional
+    import torch
+except Exception:  # pragma: no cover - torch is present wherever tests run
+    torch = None
+
+
+def _prep_matrix(a, what):
+    if torch is not None and isinstance(a, torch.Tensor):
+        if a.dim() != 2:
+            raise ValueError("%s did not have dimension 2" % what)
+        return a.to(torch.int32).contiguous()
+    a = np.ascontiguousarray(np.asarray(a), dtype=np.int32)
+    if a.ndim != 2:
+        raise ValueError("%s did not have dimension 2" % what)
+    return a
+
+
+def _prep_vector(a, n, what):
+    if a is None:
+        return None
+    if torch is not None and isinstance(a, torch.Tensor):
+        if not (a.dim() == 1 or (a.dim() == 2 and a.shape[1] == 1)):
+            raise ValueError("%s was not 1-D" % what)
+        a = a.reshape(-1).to(torch.int32).contiguous()
+    else:
+        a = np.asarray(a)
+        if not (a.ndim == 1 or (a.ndim == 2 and a.shape[1] == 1)):
+            raise ValueError("%s was not 1-D" % what)
+        a = np.ascontiguousarray(a.reshape(-1), dtype=np.int32)
+    if a.shape[0] != n:
+        raise ValueError("%s length did not equal number of rows of its Lingo matrix" % what)
+    return a
+
+
+def _where(*arrays):
+    for a in arrays:
+        if a is not None and torch is not None and isinstance(a, torch.Tensor) and a.is_cuda:
+            return N.SIML_DEVICE
+    return N.SIML_HOST
+
+
+class GPULingo:
+    """LINGO similarities on CUDA device *deviceID* (pysiml/GPULingo.py:158-173)."""
+
+    def __init__(self, deviceID=0, stream=None):
+        self.deviceID = deviceID
+        self.nref = 0
+        self.nquery = 0
+        self.rlengths = None
+        self.rshape = None
+        self.qshape = None
+        self.last_async_width = None
+        self._pending = None
+        self._h = ctypes.c_void_p()
+        L = N.lib()
+        N.check(L.siml_create(int(deviceID), ctypes.byref(self._h)), "siml_create")
+        # With torch present the engine runs on a torch stream so that device
+        # buffers from torch's caching allocator are ordered correctly.
+        if stream is None and torch is not None:
+            stream = torch.cuda.Stream(device=torch.device("cuda", deviceID))
+        self._stream = stream
+        if stream is not None:
+            N.check(L.siml_set_stream(self._h, ctypes.c_void_p(stream.cuda_stream)), "siml_set_stream")
+
+    @property
+    def stream(self):
+        """The torch stream the engine's kernels run on (None without torch)."""
+        return self._stream
+
+    def _enter(self):
+        """Orders the engine's stream after work queued on torch's current stream."""
+        if self._stream is not None:
+            self._stream.wait_stream(torch.cuda.current_stream(self._device()))
+
+    def _leave(self, *tensors):
+        """Keeps tensors written by the engine alive for its stream and orders
+        torch's current stream after the engine's work."""
+        if self._stream is not None:
+            for t in tensors:
+                if t is not None and isinstance(t, torch.Tensor) and t.is_cuda:
+                    t.record_stream(self._stream)
+            torch.cuda.current_stream(self._device()).wait_stream(self._stream)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                N.lib().siml_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # ------------------------------------------------------------------ sets
+    def _set(self, fn, mat, cnt, lengths, mags, tag):
+        L = N.lib()
+        mat = _prep_matrix(mat, "%s Lingo matrix" % tag)
+        cnt = _prep_matrix(cnt, "%s Lingo count matrix" % tag)
+        if tuple(mat.shape) != tuple(cnt.shape):
+            raise ValueError("%s Lingo and Lingo count matrix did not have identical shapes" % tag)
+        n, w = int(mat.shape[0]), int(mat.shape[1])
+        lengths = _prep_vector(lengths, n, "%s length vector" % tag)
+        mags = _prep_vector(mags, n, "%s magnitude vector" % tag)
+        where = _where(mat, cnt, lengths, mags)
+        self._enter()
+        N.check(fn(self._h, N.ptr(mat), N.ptr(cnt), N.ptr(lengths), N.ptr(mags), n, w, w, where), tag)
+        return n, w, lengths
+
+    def set_refsmiles(self, refsmilesmat, refcountsmat, reflengths, refmags=None):
+        """Sets the reference SMILES set (pysiml/GPULingo.py:187-242).  Magnitudes
+        default to the per-row count sums when *refmags* is None."""
+        n, w, lengths = self._set(N.lib().siml_set_ref, refsmilesmat, refcountsmat, reflengths, refmags,
+                                  "Reference")
+        self.nref = n
+        self.rshape = (n, w)
+        self.rlengths = lengths
+
+    def set_qsmiles(self, qsmilesmat, qcountsmat, querylengths, querymags=None):
+        """Sets the query SMILES set — the resident database (pysiml/GPULingo.py:246-313)."""
+        n, w, _ = self._set(N.lib().siml_set_query, qsmilesmat, qcountsmat, querylengths, querymags, "Query")
+        self.nquery = n
+        self.qshape = (n, w)
+
+    # --------------------------------------------------------------- helpers
+    def _device(self):
+        return torch.device("cuda", self.deviceID)
+
+    def _check_rows(self, rowbase, rowlimit):
+        if self.qshape is None or self.rshape is None:
+            raise RuntimeError("GPULingo object not fully initialized (call set_refsmiles and set_qsmiles)")
+        if rowbase < 0 or rowlimit > self.nref:
+            raise RuntimeError("row range [%d, %d) outside the reference set of %d rows" % (rowbase, rowlimit, self.nref))
+        if rowlimit < rowbase:
+            raise ValueError("negative dimensions are not allowed")
+
+    # ------------------------------------------------------------ row blocks
+    def getTanimotoRow(self, rowidx):
+        """Single Tanimoto row (pysiml/GPULingo.py:316-326)."""
+        self.getTanimotoRow_async(rowidx)
+        return self.retrieveAsyncResult()
+
+    def getTanimotoRow_async(self, rowidx):
+        """Queues one row; magnitudes are recomputed from the counts as the
+        reference's single-row kernel does (pysiml/kernels.py:234-270)."""
+        self._check_rows(rowidx, rowidx + 1)
+        nq = self.nquery
+        if torch is not None:
+            out = torch.empty((1, max(nq, 1)), dtype=torch.float32, device=self._device())
+            self._enter()
+            N.check(N.lib().siml_row_single(self._h, int(rowidx), out.data_ptr(), N.SIML_DEVICE), "getTanimotoRow")
+        else:
+            out = np.empty((1, max(nq, 1)), dtype=np.float32)
+            N.check(N.lib().siml_row_single(self._h, int(rowidx), out.ctypes.data, N.SIML_HOST), "getTanimotoRow")
+        self.last_async_width = nq
+        self._pending = ("matrix", out, nq)
+
+    def getMultipleRows(self, rowbase, rowlimit):
+        """Tanimoto rows [rowbase, rowlimit) x all queries (pysiml/GPULingo.py:354-363)."""
+        self.getMultipleRows_async(rowbase, rowlimit)
+        return self.retrieveAsyncResult()
+
+    def getMultipleRows_async(self, rowbase, rowlimit):
+        """Queues the row block (pysiml/GPULingo.py:366-404)."""
+        self._check_rows(rowbase, rowlimit)
+        rows, nq = rowlimit - rowbase, self.nquery
+        if torch is not None:
+            out = torch.empty((rows, max(nq, 1)), dtype=torch.float32, device=self._device())
+            self._enter()
+            N.check(N.lib().siml_rows(self._h, int(rowbase), int(rowlimit), out.data_ptr(), max(nq, 1),
+                                      N.SIML_DEVICE), "getMultipleRows")
+        else:
+            out = np.empty((rows, max(nq, 1)), dtype=np.float32)
+            N.check(N.lib().siml_rows(self._h, int(rowbase), int(rowlimit), out.ctypes.data, max(nq, 1),
+                                      N.SIML_HOST), "getMultipleRows")
+        self.last_async_width = nq
+        self._pending = ("matrix", out, nq)
+
+    def getMultipleRowsDevice(self, rowbase, rowlimit, out=None):
+        """Row block left in device memory as a CUDA float32 tensor [rows, nquery]
+        (or written into *out*, any row stride).  Ordered after the engine's
+        stream on torch's current stream."""
+        self._check_rows(rowbase, rowlimit)
+        rows, nq = rowlimit - rowbase, self.nquery
+        if out is None:
+            out = torch.empty((rows, max(nq, 1)), dtype=torch.float32, device=self._device())
+        if out.dtype != torch.float32 or not out.is_cuda or out.stride(1) != 1:
+            raise ValueError("out must be a CUDA float32 tensor with unit column stride")
+        self._enter()
+        N.check(N.lib().siml_rows(self._h, int(rowbase), int(rowlimit), out.data_ptr(), out.stride(0),
+                                  N.SIML_DEVICE), "getMultipleRowsDevice")
+        self._leave(out)
+        return out
+
+    # ----------------------------------------------------------- async glue
+    def retrieveAsyncResult(self):
+        """Result of the last async call (pysiml/GPULingo.py:538-640)."""
+        if self._pending is None:
+            raise RuntimeError("Error: tried to call retrieveAsyncResult without a pending asynchronous result")
+        kind, *payload = self._pending
+        self._pending = None
+        N.check(N.lib().siml_sync(self._h), "siml_sync")
+        if kind == "matrix":
+            out, width = payload
+            host = out.cpu().numpy() if torch is not None and isinstance(out, torch.Tensor) else out
+            return host[:, :width]
+        if kind == "ready":
+            return payload[0]
+        raise RuntimeError("unknown pending result")
+
+    def asyncOperationsDone(self):
+        """True once all queued work of this object has finished (pysiml/GPULingo.py:642-647)."""
+        done = ctypes.c_int(0)
+        N.check(N.lib().siml_query_done(self._h, ctypes.byref(done)), "asyncOperationsDone")
+        return bool(done.value)
+
+    # -------------------------------------------------------------- extras
+    def dbStats(self):
+        """Layout statistics of the resident database (dict)."""
+        a = (ctypes.c_int64 * 8)()
+        N.check(N.lib().siml_db_stats(self._h, a), "siml_db_stats")
+        keys = ["nvid", "entry_bytes", "ngroups_total", "nchunks", "max_ng", "n", "ref_max_entries", "qry_max_entries"]
+        return dict(zip(keys, [int(x) for x in a]))
+
+    def launchCount(self):
+        """Kernel launches issued by this object so far."""
+        return int(N.lib().siml_launch_count(self._h))
+
+    def lastKernelMs(self):
+        """Device time of the dominant kernel of the last call (CUDA events)."""
+        return float(N.lib().siml_last_kernel_ms(self._h))
+

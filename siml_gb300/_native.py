@@ -1,0 +1,117 @@
+"""ctypes binding of the native library (include/siml_gb300.h).
+
+The library is built in-tree by ``siml_gb300.build``; if it is missing this
+module raises instead of falling back to any other implementation.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libsiml_gb300.so")
+
+SIML_OK = 0
+SIML_ERR_INVALID = 1
+SIML_ERR_STATE = 2
+SIML_ERR_CUDA = 3
+SIML_ERR_NOMEM = 4
+SIML_ERR_TIMEOUT = 5
+SIML_ERR_UNSUPPORTED = 6
+SIML_ERR_RANGE = 7
+
+SIML_HOST = 0
+SIML_DEVICE = 1
+
+SYNTH_UNIFORM_20_90 = 0
+SYNTH_LOGNORMAL_45 = 1
+SYNTH_BIMODAL_35_110 = 2
+
+
+class SimlError(RuntimeError):
+    """A native call failed (CUDA error, allocation failure, timeout)."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int
+_F32 = ctypes.c_float
+_U64 = ctypes.c_uint64
+
+_SIGNATURES = {
+    "siml_version": (ctypes.c_char_p, []),
+    "siml_last_error": (ctypes.c_char_p, []),
+    "siml_create": (_I32, [_I32, ctypes.POINTER(_P)]),
+    "siml_destroy": (_I32, [_P]),
+    "siml_set_stream": (_I32, [_P, _P]),
+    "siml_sync": (_I32, [_P]),
+    "siml_query_done": (_I32, [_P, ctypes.POINTER(_I32)]),
+    "siml_set_ref": (_I32, [_P, _P, _P, _P, _P, _I64, _I64, _I64, _I32]),
+    "siml_set_query": (_I32, [_P, _P, _P, _P, _P, _I64, _I64, _I64, _I32]),
+    "siml_set_sizes": (_I32, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    "siml_rows": (_I32, [_P, _I64, _I64, _P, _I64, _I32]),
+    "siml_row_single": (_I32, [_P, _I64, _P, _I32]),
+    "siml_neighbors": (_I32, [_P, _I64, _I64, _F32, _F32, _I64, _P, _P, _P, _I32]),
+    "siml_hist101": (_I32, [_P, _I64, _I64, _P, _I64, _I32]),
+    "siml_topk": (_I32, [_P, _I64, _I64, _I64, _P, _P, _I32]),
+    "siml_hist_global": (_I32, [_P, _I64, _I64, _P, _I32]),
+    "siml_batch_neighbors": (_I32, [_P, _I64, _P, _P, _P, _P, _P, _F32, _F32, _I64, _P, _P, _P, _I32]),
+    "siml_compile_width": (_I64, [_P, _P, _I64]),
+    "siml_compile_smiles": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _I64]),
+    "siml_row_histogram101": (_I32, [_P, _P, _I64, _I64, _I64, _P, _I32]),
+    "siml_synth_lengths": (_I32, [_U64, _I32, _I64, _I64, _P]),
+    "siml_synth_smiles": (_I32, [_U64, _I32, _I64, _I64, _P, _I64, _P]),
+    "siml_db_stats": (_I32, [_P, _P]),
+    "siml_launch_count": (_I64, [_P]),
+    "siml_last_kernel_ms": (ctypes.c_double, [_P]),
+}
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Loads the native library (once) and declares every entry point."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                "siml_gb300 native library not found at %s; build it with "
+                "`python -m siml_gb300.build`" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    msg = lib().siml_last_error()
+    return msg.decode("utf-8", "replace") if msg else ""
+
+
+def check(rc: int, what: str = "") -> None:
+    """Maps a native status to the exception the reference raises for it."""
+    if rc == SIML_OK:
+        return
+    msg = last_error() or ("%s failed with status %d" % (what, rc))
+    if rc in (SIML_ERR_INVALID, SIML_ERR_UNSUPPORTED):
+        raise ValueError(msg)
+    if rc in (SIML_ERR_RANGE, SIML_ERR_STATE):
+        raise RuntimeError(msg)
+    raise SimlError(rc, msg)
+
+
+def ptr(a) -> int | None:
+    """Address of a numpy array or torch tensor (None for None)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()

@@ -1,0 +1,679 @@
+// Engine lifetime, SMILES-set upload and the device layout the similarity
+// kernels read.  The public C ABI is declared in include/siml_gb300.h.
+//
+// Set-up pipeline (all on the GPU except tiny scans):
+//   set_ref / set_query   upload [n, width] codes and counts, lengths, mags;
+//                         validate (codes strictly increasing, counts >= 0,
+//                         0 <= length <= width) and form count sums.
+//   vocabulary            hash every database (code, level) pair, level =
+//                         1..count, and number the pairs 1..nvid.
+//   database layout       windows of 256 molecules sorted by entry count,
+//                         chunks of 32, vids interleaved per lane.
+//   ref-row entries       each ref row as its list of vids (pairs absent from
+//                         the database are dropped; they cannot match).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "engine.h"
+#include "lingo_core.cuh"
+
+namespace siml {
+
+int cuda_fail(cudaError_t e, const char* what) {
+    int code = (e == cudaErrorMemoryAllocation) ? SIML_ERR_NOMEM : SIML_ERR_CUDA;
+    return fail(code, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+}
+
+int scratch_reserve(siml_engine* h, size_t bytes, void** out) {
+    if (bytes > h->scratch_bytes) {
+        if (h->scratch) {
+            SIML_CUDA(cudaStreamSynchronize(h->stream));
+            SIML_CUDA(cudaFree(h->scratch));
+            h->scratch = nullptr;
+            h->scratch_bytes = 0;
+        }
+        size_t want = std::max(bytes, (size_t)1 << 20);
+        SIML_CUDA(cudaMalloc(&h->scratch, want));
+        h->scratch_bytes = want;
+    }
+    *out = h->scratch;
+    return SIML_OK;
+}
+
+namespace {
+
+template <class T>
+int dev_alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    SIML_CUDA(cudaMalloc((void**)p, count * sizeof(T)));
+    return SIML_OK;
+}
+template <class T>
+void dev_free(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+void free_set(RawSet& s) {
+    dev_free(s.lingos); dev_free(s.counts); dev_free(s.len); dev_free(s.mag); dev_free(s.cmag);
+    s = RawSet();
+}
+void free_vocab(Vocab& v) { dev_free(v.keys); dev_free(v.vid); v = Vocab(); }
+void free_layout(DbLayout& d) {
+    dev_free(d.perm); dev_free(d.mag); dev_free(d.cmag); dev_free(d.len);
+    dev_free(d.ng); dev_free(d.off);
+    if (d.entries) cudaFree(d.entries);
+    d = DbLayout();
+}
+void free_rows(RowEntries& r) { dev_free(r.vid); r = RowEntries(); }
+
+constexpr int kErrUnsorted = 1;
+constexpr int kErrNegCount = 2;
+constexpr int kErrLength = 4;
+constexpr int kErrHashFull = 8;
+
+// ---------------------------------------------------------------- kernels --
+
+// Per molecule: validate, count sum (the magnitude accumulateRefMagnitudes /
+// accumulateQueryMagnitudes form, pysiml/kernels.py:45-79), statistics.
+__global__ void k_set_stats(const int32_t* __restrict__ lingos, const int32_t* __restrict__ counts,
+                            const int32_t* __restrict__ len, int64_t n, int64_t width,
+                            int32_t* __restrict__ cmag, int* err,
+                            unsigned long long* total, unsigned long long* maxe) {
+    int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long mine = 0;
+    if (m < n) {
+        int32_t L = len[m];
+        int e = 0;
+        if (L < 0 || L > width) {
+            e |= kErrLength;
+            L = 0;
+        }
+        const int32_t* lr = lingos + m * width;
+        const int32_t* cr = counts + m * width;
+        long long s = 0;
+        for (int32_t j = 0; j < L; j++) {
+            const int32_t c = cr[j];
+            if (c < 0) e |= kErrNegCount;
+            else s += c;
+            if (j > 0 && !(lr[j - 1] < lr[j])) e |= kErrUnsorted;
+        }
+        if (s > 0x7FFFFFFFll) { e |= kErrNegCount; s = 0x7FFFFFFF; }
+        cmag[m] = (int32_t)s;
+        if (e) atomicOr(err, e);
+        mine = (unsigned long long)s;
+    }
+    // warp-level reduce then one atomic per warp
+    unsigned long long sum = mine, mx = mine;
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_down_sync(0xFFFFFFFFu, sum, o);
+        unsigned long long t = __shfl_down_sync(0xFFFFFFFFu, mx, o);
+        mx = t > mx ? t : mx;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(total, sum);
+        atomicMax(maxe, mx);
+    }
+}
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return x;
+}
+__device__ __forceinline__ unsigned long long vkey(int32_t code, int32_t level) {
+    return ((unsigned long long)(uint32_t)level << 32) | (unsigned long long)(uint32_t)code;
+}
+
+// Inserts every (code, level) pair of the database into the hash.
+__global__ void k_vocab_insert(const int32_t* __restrict__ lingos, const int32_t* __restrict__ counts,
+                               const int32_t* __restrict__ len, int64_t n, int64_t width,
+                               unsigned long long* keys, int64_t cap,
+                               unsigned long long* inserted, int* err) {
+    const int64_t total = n * width;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t m = i / width;
+        const int32_t j = (int32_t)(i - m * width);
+        if (j >= len[m]) continue;
+        const int32_t code = lingos[i];
+        const int32_t c = counts[i];
+        for (int32_t lvl = 1; lvl <= c; lvl++) {
+            const unsigned long long k = vkey(code, lvl);
+            unsigned long long slot = mix64(k) & (unsigned long long)(cap - 1);
+            int64_t probes = 0;
+            for (;;) {
+                unsigned long long cur = keys[slot];
+                if (cur == k) break;
+                if (cur == kEmptyKey) {
+                    unsigned long long prev = atomicCAS(&keys[slot], kEmptyKey, k);
+                    if (prev == kEmptyKey) { atomicAdd(inserted, 1ull); break; }
+                    if (prev == k) break;
+                }
+                slot = (slot + 1) & (unsigned long long)(cap - 1);
+                if (++probes >= cap) { atomicOr(err, kErrHashFull); return; }
+            }
+        }
+    }
+}
+
+// Occupied slots per 1024-slot block.
+__global__ void k_vocab_count(const unsigned long long* __restrict__ keys, int64_t cap, int32_t* blockcount) {
+    __shared__ int warp_n[32];
+    const int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+    const bool occ = i < cap && keys[i] != kEmptyKey;
+    const unsigned b = __ballot_sync(0xFFFFFFFFu, occ);
+    if ((threadIdx.x & 31) == 0) warp_n[threadIdx.x >> 5] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int v = warp_n[threadIdx.x];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+        if (threadIdx.x == 0) blockcount[blockIdx.x] = v;
+    }
+}
+
+// vid = 1 + (occupied slots before this one), slot order.
+__global__ void k_vocab_assign(const unsigned long long* __restrict__ keys, int64_t cap,
+                               const int32_t* __restrict__ blockbase, uint32_t* vid) {
+    __shared__ int warp_n[32];
+    const int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+    const bool occ = i < cap && keys[i] != kEmptyKey;
+    const unsigned b = __ballot_sync(0xFFFFFFFFu, occ);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) warp_n[w] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int v = warp_n[threadIdx.x];
+        int incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        warp_n[threadIdx.x] = incl - v;
+    }
+    __syncthreads();
+    if (i < cap) {
+        const int rank = warp_n[w] + __popc(b & ((1u << lane) - 1u));
+        vid[i] = occ ? (uint32_t)(1 + blockbase[blockIdx.x] + rank) : 0u;
+    }
+}
+
+__device__ __forceinline__ uint32_t vocab_lookup(const unsigned long long* __restrict__ keys,
+                                                 const uint32_t* __restrict__ vid, int64_t cap,
+                                                 int32_t code, int32_t lvl) {
+    const unsigned long long k = vkey(code, lvl);
+    unsigned long long slot = mix64(k) & (unsigned long long)(cap - 1);
+    for (int64_t probes = 0; probes < cap; probes++) {
+        const unsigned long long cur = keys[slot];
+        if (cur == k) return vid[slot];
+        if (cur == kEmptyKey) return 0u;
+        slot = (slot + 1) & (unsigned long long)(cap - 1);
+    }
+    return 0u;
+}
+
+// One CTA of 256 threads per window: rank molecules by (entries, index).
+__global__ void k_window_sort(const int32_t* __restrict__ cmag, int64_t n, int32_t* perm) {
+    __shared__ long long key[kWindow];
+    const int64_t base = (int64_t)blockIdx.x * kWindow;
+    const int t = threadIdx.x;
+    const int64_t m = base + t;
+    // molecules past the end sort last
+    key[t] = m < n ? ((long long)cmag[m] << 20) | t : (0x7FFFFFFFll << 20) | t;
+    __syncthreads();
+    const long long mine = key[t];
+    int rank = 0;
+    for (int k = 0; k < kWindow; k++) rank += key[k] < mine;
+    perm[base + rank] = m < n ? (int32_t)m : -1;
+}
+
+// Per chunk: 16-byte groups per lane = ceil(max entries / entries-per-group),
+// rounded up to an even number of 8-entry steps; plus per-lane metadata.
+__global__ void k_chunk_meta(const int32_t* __restrict__ perm, const int32_t* __restrict__ cmag,
+                             const int32_t* __restrict__ mag, const int32_t* __restrict__ len,
+                             int64_t nchunks, int entries_per_group,
+                             int32_t* __restrict__ ng, int32_t* __restrict__ cmag_out,
+                             int32_t* __restrict__ mag_out, int32_t* __restrict__ len_out) {
+    const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= nchunks) return;
+    const int32_t m = perm[c * 32 + lane];
+    const int32_t e = m >= 0 ? cmag[m] : 0;
+    cmag_out[c * 32 + lane] = e;
+    mag_out[c * 32 + lane] = m >= 0 ? mag[m] : 0;
+    len_out[c * 32 + lane] = m >= 0 ? len[m] : 0;
+    int32_t mx = e;
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+    if (lane == 0) {
+        const int32_t steps = (mx + 7) / 8;                 // 8 entries per step
+        ng[c] = steps * (8 / entries_per_group);
+    }
+}
+
+// Writes each molecule's vid list into its chunk lane.
+template <typename ET>
+__global__ void k_fill_entries(const int32_t* __restrict__ lingos, const int32_t* __restrict__ counts,
+                               const int32_t* __restrict__ len, int64_t width,
+                               const int32_t* __restrict__ perm, const int64_t* __restrict__ off,
+                               int64_t nchunks,
+                               const unsigned long long* __restrict__ keys,
+                               const uint32_t* __restrict__ vid, int64_t cap,
+                               ET* __restrict__ entries) {
+    constexpr int EPG = 16 / sizeof(ET);
+    const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= nchunks * 32) return;
+    const int32_t m = perm[slot];
+    if (m < 0) return;
+    const int64_t c = slot >> 5;
+    const int lane = (int)(slot & 31);
+    const int32_t L = len[m];
+    const int32_t* lr = lingos + (int64_t)m * width;
+    const int32_t* cr = counts + (int64_t)m * width;
+    int64_t e = 0;
+    for (int32_t j = 0; j < L; j++) {
+        const int32_t code = lr[j], cnt = cr[j];
+        for (int32_t lvl = 1; lvl <= cnt; lvl++, e++) {
+            const uint32_t v = vocab_lookup(keys, vid, cap, code, lvl);
+            const int64_t g = off[c] + (e / EPG) * 32 + lane;
+            entries[g * EPG + (e % EPG)] = (ET)v;
+        }
+    }
+}
+
+// Each ref row as its vid list (stride entries, zero padded).
+__global__ void k_row_entries(const int32_t* __restrict__ lingos, const int32_t* __restrict__ counts,
+                              const int32_t* __restrict__ len, int64_t n, int64_t width,
+                              const unsigned long long* __restrict__ keys,
+                              const uint32_t* __restrict__ vid, int64_t cap,
+                              uint32_t* __restrict__ out, int64_t stride) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int32_t L = len[r];
+    const int32_t* lr = lingos + r * width;
+    const int32_t* cr = counts + r * width;
+    uint32_t* o = out + r * stride;
+    int64_t e = 0;
+    for (int32_t j = 0; j < L; j++) {
+        const int32_t code = lr[j], cnt = cr[j];
+        for (int32_t lvl = 1; lvl <= cnt; lvl++) {
+            const uint32_t v = vocab_lookup(keys, vid, cap, code, lvl);
+            if (v == 0u) break;   // higher levels of an absent pair are absent too
+            o[e++] = v;
+        }
+    }
+    for (; e < stride; e++) o[e] = 0u;
+}
+
+// ------------------------------------------------------------ host helpers --
+
+int upload_set(siml_engine* h, RawSet& s, const int32_t* lingos, const int32_t* counts,
+               const int32_t* lengths, const int32_t* mags, int64_t n, int64_t width,
+               int64_t ld, const char* what) {
+    if (n < 0 || width < 0 || ld < width)
+        return fail(SIML_ERR_INVALID, "%s: bad shape (n=%lld, width=%lld, ld=%lld)", what,
+                    (long long)n, (long long)width, (long long)ld);
+    if (n > 0 && (!lengths || (width > 0 && (!lingos || !counts))))
+        return fail(SIML_ERR_INVALID, "%s: NULL array", what);
+    if (n > 0x7FFFFFFFll) return fail(SIML_ERR_UNSUPPORTED, "%s: more than 2^31-1 molecules", what);
+    free_set(s);
+    const int64_t w = std::max<int64_t>(width, 1);
+    int rc;
+    if ((rc = dev_alloc(&s.lingos, (size_t)(n * w)))) return rc;
+    if ((rc = dev_alloc(&s.counts, (size_t)(n * w)))) return rc;
+    if ((rc = dev_alloc(&s.len, (size_t)n))) return rc;
+    if ((rc = dev_alloc(&s.mag, (size_t)n))) return rc;
+    if ((rc = dev_alloc(&s.cmag, (size_t)n))) return rc;
+    cudaStream_t st = h->stream;
+    if (n > 0) {
+        if (width > 0) {
+            SIML_CUDA(cudaMemcpy2DAsync(s.lingos, w * 4, lingos, ld * 4, width * 4, n, cudaMemcpyDefault, st));
+            SIML_CUDA(cudaMemcpy2DAsync(s.counts, w * 4, counts, ld * 4, width * 4, n, cudaMemcpyDefault, st));
+        } else {
+            SIML_CUDA(cudaMemsetAsync(s.lingos, 0, n * 4, st));
+            SIML_CUDA(cudaMemsetAsync(s.counts, 0, n * 4, st));
+        }
+        SIML_CUDA(cudaMemcpyAsync(s.len, lengths, n * 4, cudaMemcpyDefault, st));
+    }
+    SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), st));
+    SIML_CUDA(cudaMemsetAsync(h->d_counter, 0, 2 * sizeof(unsigned long long), st));
+    if (n > 0) {
+        k_set_stats<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s.lingos, s.counts, s.len, n, w, s.cmag,
+                                                                h->d_err, h->d_counter, h->d_counter + 1);
+        h->launches++;
+        SIML_CUDA(cudaGetLastError());
+        if (mags) SIML_CUDA(cudaMemcpyAsync(s.mag, mags, n * 4, cudaMemcpyDefault, st));
+        else SIML_CUDA(cudaMemcpyAsync(s.mag, s.cmag, n * 4, cudaMemcpyDeviceToDevice, st));
+    }
+    int err = 0;
+    unsigned long long stats[2] = {0, 0};
+    SIML_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SIML_CUDA(cudaMemcpyAsync(stats, h->d_counter, sizeof(stats), cudaMemcpyDeviceToHost, st));
+    SIML_CUDA(cudaStreamSynchronize(st));
+    s.n = n;
+    s.width = w;
+    s.total_entries = (int64_t)stats[0];
+    s.max_entries = (int64_t)stats[1];
+    if (err & kErrLength) { free_set(s); return fail(SIML_ERR_INVALID, "%s: a length is negative or exceeds the matrix width", what); }
+    if (err & kErrUnsorted) { free_set(s); return fail(SIML_ERR_UNSUPPORTED, "%s: LINGO codes of a molecule are not strictly increasing (sorted unique codes are required, as the SMILES compiler produces)", what); }
+    if (err & kErrNegCount) { free_set(s); return fail(SIML_ERR_UNSUPPORTED, "%s: negative or overflowing LINGO counts", what); }
+    return SIML_OK;
+}
+
+int build_vocab(siml_engine* h) {
+    free_vocab(h->vocab);
+    const RawSet& q = h->qry;
+    cudaStream_t st = h->stream;
+    int64_t cap = 1 << 16;
+    while (cap < 4 * std::min<int64_t>(q.total_entries, 1 << 22)) cap <<= 1;
+    for (int attempt = 0; attempt < 8; attempt++) {
+        Vocab& v = h->vocab;
+        int rc;
+        if ((rc = dev_alloc(&v.keys, (size_t)cap))) return rc;
+        v.cap = cap;
+        SIML_CUDA(cudaMemsetAsync(v.keys, 0xFF, cap * sizeof(unsigned long long), st));
+        SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), st));
+        SIML_CUDA(cudaMemsetAsync(h->d_counter, 0, sizeof(unsigned long long), st));
+        if (q.n > 0) {
+            const int64_t total = q.n * q.width;
+            const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, 65535LL * 8);
+            k_vocab_insert<<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.n, q.width, v.keys, cap,
+                                                 h->d_counter, h->d_err);
+            h->launches++;
+            SIML_CUDA(cudaGetLastError());
+        }
+        int err = 0;
+        unsigned long long ins = 0;
+        SIML_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        SIML_CUDA(cudaMemcpyAsync(&ins, h->d_counter, sizeof(ins), cudaMemcpyDeviceToHost, st));
+        SIML_CUDA(cudaStreamSynchronize(st));
+        if ((err & kErrHashFull) || (int64_t)ins * 2 > cap) {
+            free_vocab(v);
+            cap <<= 2;
+            continue;
+        }
+        // number the occupied slots
+        const int64_t nblk = (cap + 1023) / 1024;
+        int32_t* bcount = nullptr;
+        if ((rc = dev_alloc(&bcount, (size_t)nblk))) return rc;
+        if ((rc = dev_alloc(&v.vid, (size_t)cap))) { dev_free(bcount); return rc; }
+        k_vocab_count<<<(unsigned)nblk, 1024, 0, st>>>(v.keys, cap, bcount);
+        h->launches++;
+        std::vector<int32_t> hb((size_t)nblk);
+        SIML_CUDA(cudaMemcpyAsync(hb.data(), bcount, nblk * 4, cudaMemcpyDeviceToHost, st));
+        SIML_CUDA(cudaStreamSynchronize(st));
+        int64_t acc = 0;
+        for (auto& x : hb) { int32_t t = x; x = (int32_t)acc; acc += t; }
+        SIML_CUDA(cudaMemcpyAsync(bcount, hb.data(), nblk * 4, cudaMemcpyHostToDevice, st));
+        k_vocab_assign<<<(unsigned)nblk, 1024, 0, st>>>(v.keys, cap, bcount, v.vid);
+        h->launches++;
+        SIML_CUDA(cudaGetLastError());
+        SIML_CUDA(cudaStreamSynchronize(st));
+        dev_free(bcount);
+        v.nvid = acc;
+        return SIML_OK;
+    }
+    return fail(SIML_ERR_NOMEM, "vocabulary hash could not be sized");
+}
+
+int build_layout(siml_engine* h) {
+    free_layout(h->db);
+    const RawSet& q = h->qry;
+    DbLayout& d = h->db;
+    cudaStream_t st = h->stream;
+    d.n = q.n;
+    d.entry_bytes = h->vocab.nvid < 65535 ? 2 : 4;
+    const int64_t nwin = (q.n + kWindow - 1) / kWindow;
+    d.nchunks = (q.n + kChunk - 1) / kChunk;
+    const int64_t slots = nwin * kWindow;
+    int rc;
+    if ((rc = dev_alloc(&d.perm, (size_t)slots))) return rc;
+    if ((rc = dev_alloc(&d.mag, (size_t)slots))) return rc;
+    if ((rc = dev_alloc(&d.cmag, (size_t)slots))) return rc;
+    if ((rc = dev_alloc(&d.len, (size_t)slots))) return rc;
+    if ((rc = dev_alloc(&d.ng, (size_t)d.nchunks))) return rc;
+    if ((rc = dev_alloc(&d.off, (size_t)d.nchunks))) return rc;
+    if (q.n == 0) return SIML_OK;
+    k_window_sort<<<(unsigned)nwin, kWindow, 0, st>>>(q.cmag, q.n, d.perm);
+    h->launches++;
+    const int epg = 16 / d.entry_bytes;
+    k_chunk_meta<<<(unsigned)((d.nchunks + 7) / 8), 256, 0, st>>>(d.perm, q.cmag, q.mag, q.len, d.nchunks, epg,
+                                                                  d.ng, d.cmag, d.mag, d.len);
+    h->launches++;
+    SIML_CUDA(cudaGetLastError());
+    std::vector<int32_t> hng((size_t)d.nchunks);
+    std::vector<int64_t> hoff((size_t)d.nchunks);
+    SIML_CUDA(cudaMemcpyAsync(hng.data(), d.ng, d.nchunks * 4, cudaMemcpyDeviceToHost, st));
+    SIML_CUDA(cudaStreamSynchronize(st));
+    int64_t acc = 0, mx = 0;
+    for (int64_t c = 0; c < d.nchunks; c++) {
+        hoff[(size_t)c] = acc;
+        acc += (int64_t)hng[(size_t)c] * 32;
+        mx = std::max<int64_t>(mx, hng[(size_t)c]);
+    }
+    d.ngroups_total = acc;
+    d.max_ng = mx;
+    SIML_CUDA(cudaMemcpyAsync(d.off, hoff.data(), d.nchunks * 8, cudaMemcpyHostToDevice, st));
+    SIML_CUDA(cudaMalloc(&d.entries, (size_t)std::max<int64_t>(acc, 1) * 16));
+    SIML_CUDA(cudaMemsetAsync(d.entries, 0, (size_t)std::max<int64_t>(acc, 1) * 16, st));
+    const unsigned grid = (unsigned)((d.nchunks * 32 + 255) / 256);
+    if (d.entry_bytes == 2)
+        k_fill_entries<uint16_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.width, d.perm, d.off, d.nchunks,
+                                                       h->vocab.keys, h->vocab.vid, h->vocab.cap,
+                                                       (uint16_t*)d.entries);
+    else
+        k_fill_entries<uint32_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.width, d.perm, d.off, d.nchunks,
+                                                       h->vocab.keys, h->vocab.vid, h->vocab.cap,
+                                                       (uint32_t*)d.entries);
+    h->launches++;
+    SIML_CUDA(cudaGetLastError());
+    SIML_CUDA(cudaStreamSynchronize(st));
+    return SIML_OK;
+}
+
+int build_rows(siml_engine* h) {
+    free_rows(h->rows);
+    const RawSet& r = h->ref;
+    RowEntries& re = h->rows;
+    re.n = r.n;
+    re.stride = std::max<int64_t>(1, r.max_entries);
+    int rc;
+    if ((rc = dev_alloc(&re.vid, (size_t)(std::max<int64_t>(r.n, 1) * re.stride)))) return rc;
+    if (r.n > 0) {
+        k_row_entries<<<(unsigned)((r.n + 127) / 128), 128, 0, h->stream>>>(
+            r.lingos, r.counts, r.len, r.n, r.width, h->vocab.keys, h->vocab.vid, h->vocab.cap, re.vid, re.stride);
+        h->launches++;
+        SIML_CUDA(cudaGetLastError());
+    }
+    SIML_CUDA(cudaStreamSynchronize(h->stream));
+    return SIML_OK;
+}
+
+}  // namespace
+
+int ensure_prepared(siml_engine* h) {
+    if (h->ref.n < 0 || h->qry.n < 0) return fail(SIML_ERR_STATE, "both the ref set (set_refsmiles) and the query set (set_qsmiles) must be set");
+    int rc;
+    if (!h->layout_valid) {
+        h->rows_valid = false;
+        if ((rc = build_vocab(h))) return rc;
+        if ((rc = build_layout(h))) return rc;
+        h->layout_valid = true;
+    }
+    if (!h->rows_valid) {
+        if ((rc = build_rows(h))) return rc;
+        h->rows_valid = true;
+    }
+    return SIML_OK;
+}
+
+}  // namespace siml
+
+using namespace siml;
+
+#define SIML_GUARD(h)                                                   \
+    do {                                                                \
+        clear_error();                                                  \
+        if (!(h)) return fail(SIML_ERR_INVALID, "NULL engine handle");  \
+        cudaError_t _se = cudaSetDevice((h)->device);                   \
+        if (_se != cudaSuccess) return cuda_fail(_se, "cudaSetDevice"); \
+    } while (0)
+
+extern "C" {
+
+const char* siml_version(void) { return "siml_gb300 0.1 (sm_103a)"; }
+
+int siml_create(int device, siml_engine** out) {
+    clear_error();
+    if (!out) return fail(SIML_ERR_INVALID, "siml_create: NULL output");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+    if (device < 0 || device >= ndev) return fail(SIML_ERR_INVALID, "siml_create: no CUDA device %d (%d present)", device, ndev);
+    SIML_CUDA(cudaSetDevice(device));
+    siml_engine* h = new siml_engine();
+    h->device = device;
+    cudaDeviceProp prop;
+    SIML_CUDA(cudaGetDeviceProperties(&prop, device));
+    h->num_sms = prop.multiProcessorCount;
+    h->smem_optin = prop.sharedMemPerBlockOptin;
+    SIML_CUDA(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
+    h->stream = h->own_stream;
+    SIML_CUDA(cudaMalloc(&h->d_err, sizeof(int)));
+    SIML_CUDA(cudaMalloc(&h->d_counter, 4 * sizeof(unsigned long long)));
+    SIML_CUDA(cudaEventCreate(&h->ev0));
+    SIML_CUDA(cudaEventCreate(&h->ev1));
+    *out = h;
+    return SIML_OK;
+}
+
+int siml_destroy(siml_engine* h) {
+    clear_error();
+    if (!h) return SIML_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_set(h->ref);
+    free_set(h->qry);
+    free_vocab(h->vocab);
+    free_layout(h->db);
+    free_rows(h->rows);
+    if (h->scratch) cudaFree(h->scratch);
+    if (h->d_err) cudaFree(h->d_err);
+    if (h->d_counter) cudaFree(h->d_counter);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    delete h;
+    return SIML_OK;
+}
+
+int siml_set_stream(siml_engine* h, void* stream) {
+    SIML_GUARD(h);
+    h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+    return SIML_OK;
+}
+
+int siml_sync(siml_engine* h) {
+    SIML_GUARD(h);
+    SIML_CUDA(cudaStreamSynchronize(h->stream));
+    return SIML_OK;
+}
+
+int siml_query_done(siml_engine* h, int* done) {
+    SIML_GUARD(h);
+    if (!done) return fail(SIML_ERR_INVALID, "siml_query_done: NULL output");
+    cudaError_t e = cudaStreamQuery(h->stream);
+    if (e == cudaSuccess) { *done = 1; return SIML_OK; }
+    if (e == cudaErrorNotReady) { *done = 0; return SIML_OK; }
+    return cuda_fail(e, "cudaStreamQuery");
+}
+
+int siml_set_ref(siml_engine* h, const int32_t* lingos, const int32_t* counts, const int32_t* lengths,
+                 const int32_t* mags, int64_t n, int64_t width, int64_t ld, int where) {
+    SIML_GUARD(h);
+    (void)where;
+    h->rows_valid = false;
+    return upload_set(h, h->ref, lingos, counts, lengths, mags, n, width, ld, "set_refsmiles");
+}
+
+int siml_set_query(siml_engine* h, const int32_t* lingos, const int32_t* counts, const int32_t* lengths,
+                   const int32_t* mags, int64_t n, int64_t width, int64_t ld, int where) {
+    SIML_GUARD(h);
+    (void)where;
+    h->layout_valid = false;
+    h->rows_valid = false;
+    return upload_set(h, h->qry, lingos, counts, lengths, mags, n, width, ld, "set_qsmiles");
+}
+
+int siml_set_sizes(siml_engine* h, int64_t* nref, int64_t* nquery) {
+    SIML_GUARD(h);
+    if (nref) *nref = h->ref.n;
+    if (nquery) *nquery = h->qry.n;
+    return SIML_OK;
+}
+
+int siml_db_stats(siml_engine* h, int64_t out[8]) {
+    SIML_GUARD(h);
+    if (!out) return fail(SIML_ERR_INVALID, "siml_db_stats: NULL output");
+    int rc = ensure_prepared(h);
+    if (rc) return rc;
+    out[0] = h->vocab.nvid;
+    out[1] = h->db.entry_bytes;
+    out[2] = h->db.ngroups_total;
+    out[3] = h->db.nchunks;
+    out[4] = h->db.max_ng;
+    out[5] = h->db.n;
+    out[6] = h->ref.max_entries;
+    out[7] = h->qry.max_entries;
+    return SIML_OK;
+}
+
+int64_t siml_launch_count(siml_engine* h) { return h ? h->launches : -1; }
+
+double siml_last_kernel_ms(siml_engine* h) {
+    if (!h || !h->timed) return 0.0;
+    float ms = 0.f;
+    if (cudaEventSynchronize(h->ev1) != cudaSuccess) return 0.0;
+    if (cudaEventElapsedTime(&ms, h->ev0, h->ev1) != cudaSuccess) return 0.0;
+    return (double)ms;
+}
+
+static int rows_common(siml_engine* h, int64_t rowbase, int64_t rowlimit, float* out, int64_t ldo,
+                       int where, int mode) {
+    int rc;
+    if ((rc = ensure_prepared(h))) return rc;
+    if (rowbase < 0 || rowlimit > h->ref.n || rowlimit < rowbase)
+        return fail(SIML_ERR_RANGE, "row range [%lld, %lld) outside the ref set of %lld rows",
+                    (long long)rowbase, (long long)rowlimit, (long long)h->ref.n);
+    const int64_t rows = rowlimit - rowbase, nq = h->qry.n;
+    if (ldo < nq) return fail(SIML_ERR_INVALID, "output row stride %lld < query set size %lld", (long long)ldo, (long long)nq);
+    if (rows == 0 || nq == 0) return SIML_OK;
+    if (!out) return fail(SIML_ERR_INVALID, "NULL output");
+    RowsArgs a{rowbase, rowlimit, out, ldo, mode};
+    if (where == SIML_DEVICE) return launch_rows(h, a);
+    void* dbuf = nullptr;
+    if ((rc = scratch_reserve(h, (size_t)(rows * nq) * sizeof(float), &dbuf))) return rc;
+    a.out = (float*)dbuf;
+    a.ldo = nq;
+    if ((rc = launch_rows(h, a))) return rc;
+    SIML_CUDA(cudaMemcpy2DAsync(out, ldo * 4, dbuf, nq * 4, nq * 4, rows, cudaMemcpyDefault, h->stream));
+    SIML_CUDA(cudaStreamSynchronize(h->stream));
+    return SIML_OK;
+}
+
+int siml_rows(siml_engine* h, int64_t rowbase, int64_t rowlimit, float* out, int64_t ldo, int where) {
+    SIML_GUARD(h);
+    return rows_common(h, rowbase, rowlimit, out, ldo, where, kModeRows);
+}
+
+int siml_row_single(siml_engine* h, int64_t row, float* out, int where) {
+    SIML_GUARD(h);
+    return rows_common(h, row, row + 1, out, h->qry.n, where, kModeSingle);
+}
+
+}  // extern "C"

@@ -1,0 +1,118 @@
+// Engine state shared by the host orchestration (engine.cu) and the kernels
+// (kernels.cu).  Everything here is internal; the public surface is
+// include/siml_gb300.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+
+#include "siml_internal.h"
+
+namespace siml {
+
+// A SMILES set as uploaded: row-major [n, width] codes and counts, lengths,
+// effective magnitudes (user-given or the count sums) and count sums.
+struct RawSet {
+    int64_t n = -1;
+    int64_t width = 0;
+    int32_t* lingos = nullptr;
+    int32_t* counts = nullptr;
+    int32_t* len = nullptr;
+    int32_t* mag = nullptr;
+    int32_t* cmag = nullptr;
+    int64_t max_entries = 0;   // max over molecules of the count sum
+    int64_t total_entries = 0; // sum of count sums
+};
+
+// Open-addressing hash of the database's (code, level) pairs.  key =
+// (level << 32) | (uint32)code, empty slots hold kEmptyKey; vid[slot] is the
+// dense virtual id (1..nvid) of an occupied slot.
+constexpr unsigned long long kEmptyKey = 0xFFFFFFFFFFFFFFFFull;
+struct Vocab {
+    unsigned long long* keys = nullptr;
+    uint32_t* vid = nullptr;
+    int64_t cap = 0;      // power of two
+    int64_t nvid = 0;     // number of (code, level) pairs; vids are 1..nvid
+};
+
+// Database (query set) layout.  Molecules are grouped in windows of 256
+// sorted by entry count (ties by index) and cut into chunks of 32 (one warp,
+// one molecule per lane).  A chunk's entries are stored as ng groups of 16
+// bytes per lane, interleaved [group][lane] so a warp's load of one group is
+// 512 contiguous bytes; an entry is a vid (uint16 when nvid < 65536, else
+// uint32), 0 padding a molecule's list to the chunk's length.
+constexpr int kWindow = 256;
+constexpr int kChunk = 32;
+struct DbLayout {
+    int64_t n = 0;
+    int64_t nchunks = 0;
+    int entry_bytes = 2;          // 2 or 4
+    int32_t* perm = nullptr;      // [nchunks*32] original index or -1
+    int32_t* mag = nullptr;       // [nchunks*32] effective magnitude
+    int32_t* cmag = nullptr;      // [nchunks*32] count sums
+    int32_t* len = nullptr;       // [nchunks*32] unique-code counts
+    int32_t* ng = nullptr;        // [nchunks] 16-byte groups per lane
+    int64_t* off = nullptr;       // [nchunks] first group (16-byte units)
+    void* entries = nullptr;      // 16-byte groups
+    int64_t ngroups_total = 0;
+    int64_t max_ng = 0;
+};
+
+// Ref-set rows as vid lists (levels expanded, codes absent from the database
+// dropped), stride `stride` entries, zero padded.
+struct RowEntries {
+    int64_t n = 0;
+    int64_t stride = 0;
+    uint32_t* vid = nullptr;
+};
+
+}  // namespace siml
+
+struct siml_engine {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+    size_t smem_optin = 0;
+    siml::RawSet ref, qry;
+    bool layout_valid = false;
+    bool rows_valid = false;
+    siml::Vocab vocab;
+    siml::DbLayout db;
+    siml::RowEntries rows;
+    // device scratch reused across calls
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    int* d_err = nullptr;                 // device error word
+    unsigned long long* d_counter = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timed = false;
+    int64_t launches = 0;
+};
+
+namespace siml {
+
+// engine.cu
+int ensure_prepared(siml_engine* h);
+int scratch_reserve(siml_engine* h, size_t bytes, void** out);
+int cuda_fail(cudaError_t e, const char* what);
+
+// kernels.cu — launchers; all queue work on h->stream and return a status.
+struct RowsArgs {
+    int64_t rowbase, rowlimit;
+    float* out;          // device, [rows, ldo]
+    int64_t ldo;
+    int mode;            // kModeRows or kModeSingle
+};
+constexpr int kModeRows = 0;    // getMultipleRows: CPU-order fp32 union, zero test on magnitudes
+constexpr int kModeSingle = 1;  // getTanimotoRow: count-sum magnitudes, zero test on lengths
+int launch_rows(siml_engine* h, const RowsArgs& a);
+
+}  // namespace siml
+
+#define SIML_CUDA(call)                                              \
+    do {                                                             \
+        cudaError_t _e = (call);                                     \
+        if (_e != cudaSuccess) return siml::cuda_fail(_e, #call);    \
+    } while (0)

@@ -1,0 +1,194 @@
+"""GPU parity of getMultipleRows / getTanimotoRow against the oracle and the
+golden fixtures: bit-exact fp32 (the reference's own bar, GPU == CPU exactly,
+examples/benchmark.py:192)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine():
+    from siml_gb300 import GPULingo
+    return GPULingo(0)
+
+
+def _load(gl, ref, qry):
+    gl.set_refsmiles(ref[0], ref[1], ref[2], ref[3])
+    gl.set_qsmiles(qry[0], qry[1], qry[2], qry[3])
+
+
+def test_rows_match_golden(native, golden):
+    q = (golden["lingos"], golden["counts"], golden["lengths"], golden["mags"])
+    rows = golden["rows"]
+    gl = _engine()
+    _load(gl, tuple(a[rows] for a in q), q)
+    T = gl.getMultipleRows(0, len(rows))
+    assert T.dtype == np.float32 and T.shape == golden["tanimoto"].shape
+    assert np.array_equal(T, golden["tanimoto"])
+
+
+def test_allpairs_4096_bit_exact(native, oracle, set4096):
+    """The full 4096 x 4096 matrix, fetched in 256-row blocks as the
+    reference's benchmark does (examples/benchmark.py:127-135)."""
+    gl = _engine()
+    _load(gl, set4096, set4096)
+    n = set4096[0].shape[0]
+    G = np.empty((n, n), np.float32)
+    for base in range(0, n, 256):
+        G[base:base + 256] = gl.getMultipleRows(base, min(base + 256, n))
+    C = oracle.tanimoto_block(set4096, set4096, 0, n)
+    assert np.array_equal(G, C)
+    assert np.all(np.diag(G) == 1.0)
+    # one call for everything agrees too
+    assert np.array_equal(gl.getMultipleRows(0, n), C)
+
+
+def test_async_protocol(native, oracle, set4096):
+    gl = _engine()
+    _load(gl, set4096, set4096)
+    with pytest.raises(RuntimeError):
+        gl.retrieveAsyncResult()
+    gl.getMultipleRows_async(100, 164)
+    while not gl.asyncOperationsDone():
+        pass
+    got = gl.retrieveAsyncResult()
+    assert np.array_equal(got, oracle.tanimoto_block(set4096, set4096, 100, 164))
+    with pytest.raises(RuntimeError):
+        gl.retrieveAsyncResult()
+
+
+def test_row_ranges(native, set4096):
+    gl = _engine()
+    _load(gl, set4096, set4096)
+    with pytest.raises(RuntimeError):
+        gl.getMultipleRows(-1, 10)
+    with pytest.raises(RuntimeError):
+        gl.getMultipleRows(0, 4097)
+    assert gl.getMultipleRows(7, 7).shape == (0, 4096)
+    for a, b in [(0, 1), (31, 33), (4090, 4096), (1, 100)]:
+        assert gl.getMultipleRows(a, b).shape == (b - a, 4096)
+
+
+def test_tanimoto_row_uses_count_magnitudes(native, oracle, golden):
+    """getTanimotoRow recomputes magnitudes from counts and scores a
+    molecule without LINGOs as 0 (pysiml/kernels.py:122-159, 234-270)."""
+    q = (golden["lingos"], golden["counts"], golden["lengths"], golden["mags"])
+    gl = _engine()
+    wrong = q[3] + 7  # magnitudes that getMultipleRows uses but getTanimotoRow ignores
+    gl.set_refsmiles(q[0], q[1], q[2], wrong)
+    gl.set_qsmiles(q[0], q[1], q[2], wrong)
+    cm = q[1].sum(1).astype(np.int32)
+    n = len(golden["strings"])
+    isct = oracle.isct_block(q, q, 0, n)
+    for row in [0, 3, 4, 7, 30, 40, 60, 200]:
+        got = gl.getTanimotoRow(row)
+        assert got.shape == (1, n)
+        ln = q[2]
+        u = (cm[row] + cm - isct[row]).astype(np.float32)
+        want = np.where((ln[row] == 0) | (ln == 0), np.float32(0), isct[row].astype(np.float32) / u)
+        assert np.array_equal(got[0], want.astype(np.float32)), row
+    # and getMultipleRows does use the given magnitudes
+    assert np.array_equal(gl.getMultipleRows(0, 8), oracle.tanimoto_block((q[0], q[1], q[2], wrong),
+                                                                           (q[0], q[1], q[2], wrong), 0, 8))
+
+
+def test_default_magnitudes_are_count_sums(native, oracle, set4096):
+    gl = _engine()
+    L, C, ln, mg = set4096
+    gl.set_refsmiles(L[:300], C[:300], ln[:300])
+    gl.set_qsmiles(L, C, ln)
+    cm = C.sum(1).astype(np.int32)
+    assert np.array_equal(gl.getMultipleRows(0, 300),
+                          oracle.tanimoto_block((L[:300], C[:300], ln[:300], cm[:300]), (L, C, ln, cm), 0, 300))
+
+
+def _random_sets(rng, n, width, code_range, max_count, p_empty=0.05):
+    L = np.zeros((n, width), np.int32)
+    C = np.zeros((n, width), np.int32)
+    ln = np.zeros(n, np.int32)
+    for i in range(n):
+        k = 0 if rng.random() < p_empty else int(rng.integers(1, width + 1))
+        codes = np.unique(rng.integers(code_range[0], code_range[1], size=k).astype(np.int32))
+        L[i, :len(codes)] = codes
+        C[i, :len(codes)] = rng.integers(1, max_count + 1, size=len(codes))
+        ln[i] = len(codes)
+    mg = C.sum(1).astype(np.int32)
+    return L, C, ln, mg
+
+
+@pytest.mark.parametrize("case", ["small_vocab", "negative_codes", "high_counts", "zero_mags"])
+def test_rows_random_sets(native, oracle, case):
+    rng = np.random.default_rng({"small_vocab": 1, "negative_codes": 2, "high_counts": 3, "zero_mags": 4}[case])
+    if case == "small_vocab":
+        ref = _random_sets(rng, 77, 30, (0, 200), 3)
+        qry = _random_sets(rng, 1500, 30, (0, 200), 3)
+    elif case == "negative_codes":
+        ref = _random_sets(rng, 65, 40, (-(2 ** 31), 2 ** 31 - 1), 2)
+        qry = _random_sets(rng, 900, 40, (-(2 ** 31), 2 ** 31 - 1), 2)
+        qry[0][5, :ref[2][3]] = ref[0][3, :ref[2][3]]  # guarantee overlaps
+        qry[1][5, :ref[2][3]] = ref[1][3, :ref[2][3]]
+        qry[2][5] = ref[2][3]
+        qry = (qry[0], qry[1], qry[2], qry[1].sum(1).astype(np.int32))
+    elif case == "high_counts":  # counts past 255: 16-plane counters
+        ref = _random_sets(rng, 40, 12, (0, 30), 400)
+        qry = _random_sets(rng, 700, 12, (0, 30), 400)
+    else:
+        ref = _random_sets(rng, 50, 20, (0, 100), 2, p_empty=0.3)
+        qry = _random_sets(rng, 600, 20, (0, 100), 2, p_empty=0.3)
+        ref = (ref[0], ref[1], ref[2], np.where(np.arange(50) % 5 == 0, 0, ref[3]).astype(np.int32))
+    gl = _engine()
+    _load(gl, ref, qry)
+    got = gl.getMultipleRows(0, ref[0].shape[0])
+    assert np.array_equal(got, oracle.tanimoto_block(ref, qry, 0, ref[0].shape[0]))
+
+
+def test_large_vocabulary_uses_merge_path(native, oracle):
+    """A vocabulary too large for the shared-memory table takes the per-pair
+    merge kernel; results are the same."""
+    rng = np.random.default_rng(9)
+    ref = _random_sets(rng, 40, 64, (0, 10 ** 9), 2)
+    qry = _random_sets(rng, 2000, 64, (0, 10 ** 9), 2)
+    qry[0][:40] = ref[0]
+    qry[1][:40] = ref[1]
+    qry[2][:40] = ref[2]
+    qry = (qry[0], qry[1], qry[2], qry[1].sum(1).astype(np.int32))
+    gl = _engine()
+    _load(gl, ref, qry)
+    got = gl.getMultipleRows(0, 40)
+    assert np.array_equal(got, oracle.tanimoto_block(ref, qry, 0, 40))
+
+
+def test_invalid_sets_are_rejected(native):
+    gl = _engine()
+    L = np.array([[5, 3, 0]], np.int32)
+    C = np.array([[1, 1, 0]], np.int32)
+    with pytest.raises(ValueError):
+        gl.set_qsmiles(L, C, np.array([2], np.int32))
+    with pytest.raises(ValueError):
+        gl.set_qsmiles(np.array([[1, 2]], np.int32), np.array([[1, -1]], np.int32), np.array([2], np.int32))
+    with pytest.raises(ValueError):
+        gl.set_qsmiles(np.array([[1, 2]], np.int32), np.array([[1, 1]], np.int32), np.array([3], np.int32))
+    with pytest.raises(ValueError):
+        gl.set_qsmiles(np.zeros((2, 2), np.int32), np.zeros((2, 3), np.int32), np.zeros(2, np.int32))
+    with pytest.raises(RuntimeError):
+        gl.getMultipleRows(0, 1)
+
+
+def test_torch_device_inputs_and_outputs(native, oracle, set4096):
+    torch = pytest.importorskip("torch")
+    from siml_gb300 import GPULingo
+    s = torch.cuda.Stream()
+    gl = GPULingo(0, stream=s)
+    L, C, ln, mg = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in set4096)
+    gl.set_refsmiles(L[:512], C[:512], ln[:512], mg[:512])
+    gl.set_qsmiles(L, C, ln, mg)
+    out = gl.getMultipleRowsDevice(0, 512)
+    assert out.is_cuda and out.shape == (512, 4096)
+    want = oracle.tanimoto_block(set4096, set4096, 0, 512)
+    assert np.array_equal(out.cpu().numpy(), want)
+    # into a caller buffer with a padded row stride
+    buf = torch.full((64, 4100), -5.0, device="cuda")
+    gl.getMultipleRowsDevice(0, 64, out=buf[:, :4096])
+    got = buf.cpu().numpy()
+    assert np.array_equal(got[:, :4096], want[:64]) and np.all(got[:, 4096:] == -5.0)
+    assert gl.launchCount() > 0

@@ -1,0 +1,62 @@
+"""The C-ABI library: loads, exports every entry point include/siml_gb300.h
+declares, and reports errors through status codes (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests.conftest import REPO
+
+
+def header_symbols():
+    text = open(os.path.join(REPO, "include", "siml_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(siml_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(native):
+    syms = header_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(native, s), s
+
+
+def test_version_and_error_reporting(native):
+    from siml_gb300 import _native as N
+    assert b"sm_103a" in native.siml_version()
+    # bad arguments: status + message, no crash
+    rc = native.siml_compile_smiles(b"abc", None, 1, None, None, None, None, 4)
+    assert rc == N.SIML_ERR_INVALID
+    assert "bad arguments" in N.last_error()
+    with pytest.raises(ValueError):
+        N.check(rc)
+
+
+def test_null_handle_is_rejected(native):
+    from siml_gb300 import _native as N
+    assert native.siml_sync(None) == N.SIML_ERR_INVALID
+    assert native.siml_rows(None, 0, 1, None, 1, 0) == N.SIML_ERR_INVALID
+    assert native.siml_launch_count(None) == -1
+
+
+def test_gpulingo_fails_loudly_without_gpu(native):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from siml_gb300 import GPULingo, _native as N
+    with pytest.raises((N.SimlError, ValueError)):
+        GPULingo(0)
+
+
+def test_sliced_counter_host_unit(tmp_path):
+    """The bit-sliced counter and plane transpose of the kernels
+    (siml_gb300/csrc/lingo_core.cuh) checked against scalar sums on the host."""
+    import subprocess
+    exe = str(tmp_path / "sct")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(REPO, "siml_gb300", "csrc"),
+                    "-I", os.path.join(REPO, "include"),
+                    os.path.join(REPO, "tests", "native", "sliced_counter_test.cpp"), "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
