@@ -207,13 +207,14 @@ def gpu_arm(args):
     stats = gl.dbStats()
     torch.cuda.synchronize()
     log("database layout ready in %.2f s: %s" % (time.time() - t, stats))
-    nblocks = QUERY_N // BLOCK
-    out = torch.empty((BLOCK, DB_N), dtype=torch.float32, device=dev)
+    rows_step = args.rows_per_step
+    nblocks = QUERY_N // rows_step
+    out = torch.empty((rows_step, DB_N), dtype=torch.float32, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
 
     def block_of(k):
         b = (k * world + rank) % nblocks
-        return b * BLOCK, (b + 1) * BLOCK
+        return b * rows_step, (b + 1) * rows_step
 
     for w in range(args.warmup):
         r0, r1 = block_of(w)
@@ -248,7 +249,7 @@ def gpu_arm(args):
         total_ms = float(tt.item())
         torch.distributed.barrier()
     clk = clocks.stop()
-    pairs_per_step = BLOCK * DB_N
+    pairs_per_step = rows_step * DB_N
     value = world * args.steps * pairs_per_step / (total_ms / 1e3) / 1e9
     ms_per_step = total_ms / args.steps
 
@@ -279,7 +280,7 @@ def gpu_arm(args):
 
     e2e = None
     cpu = None
-    if rank == 0:
+    if rank == 0 and not args.no_extras:
         e2e = measure_e2e(gl, q, stream, dev, steps=min(3, args.steps))
         if world == 1:
             cpu = cpu_reference_rate(db, q)
@@ -288,7 +289,7 @@ def gpu_arm(args):
             "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded SMILES-like strings)",
-            "config": {"workload": WORKLOAD, "rows_per_step": BLOCK, "db_molecules": DB_N,
+            "config": {"workload": WORKLOAD, "rows_per_step": rows_step, "db_molecules": DB_N,
                        "query_rows": QUERY_N, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "flushed between steps by a 256 MB write; each step also writes a 4 GB block",
                        "db_layout": stats},
@@ -351,6 +352,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--rows-per-step", type=int, default=BLOCK,
+                    help="rows per block (smaller blocks for profiler captures)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the end-to-end and CPU-baseline legs (profiler runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)

@@ -221,6 +221,50 @@ class GPULingo:
         self._leave(out)
         return out
 
+    # ------------------------------------------------------------- neighbors
+    def getNeighbors(self, rowbase, rowlimit, lowerbound, upperbound=1.1, maxneighbors=None):
+        """Query indices with lowerbound <= T < upperbound per ref row
+        (pysiml/GPULingo.py:516-534).  Returns (matrix [rows, max count], counts
+        [rows]); entries of row i beyond counts[i] are undefined, and a count
+        above the pitch 16*ceil(maxneighbors/16) marks an overflowed row."""
+        self.getNeighbors_async(rowbase, rowlimit, lowerbound, upperbound, maxneighbors)
+        return self.retrieveAsyncResult()
+
+    def getNeighbors_async(self, rowbase, rowlimit, lowerbound, upperbound=1.1, maxneighbors=None):
+        """Queues a neighbour search (pysiml/GPULingo.py:467-513)."""
+        self._queue_neighbors(rowbase, rowlimit, lowerbound, upperbound, maxneighbors, False)
+
+    def getNeighborsWithSimilarities(self, rowbase, rowlimit, lowerbound, upperbound=1.1, maxneighbors=None):
+        """As getNeighbors, plus the fp32 similarity of each listed neighbour:
+        returns (indices, similarities, counts)."""
+        self._queue_neighbors(rowbase, rowlimit, lowerbound, upperbound, maxneighbors, True)
+        return self.retrieveAsyncResult()
+
+    def _queue_neighbors(self, rowbase, rowlimit, lowerbound, upperbound, maxneighbors, with_sims):
+        self._check_rows(rowbase, rowlimit)
+        if maxneighbors is None:
+            maxneighbors = self.nquery
+        pitch = 16 * ((int(maxneighbors) + 15) // 16)
+        rows = rowlimit - rowbase
+        L = N.lib()
+        args = (self._h, int(rowbase), int(rowlimit), ctypes.c_float(lowerbound), ctypes.c_float(upperbound), pitch)
+        if torch is not None:
+            dev = self._device()
+            idx = torch.empty((rows, max(pitch, 1)), dtype=torch.int32, device=dev)
+            sims = torch.empty((rows, max(pitch, 1)), dtype=torch.float32, device=dev) if with_sims else None
+            cnt = torch.empty(max(rows, 1), dtype=torch.int32, device=dev)
+            self._enter()
+            N.check(L.siml_neighbors(*args, idx.data_ptr(), N.ptr(sims), cnt.data_ptr(), N.SIML_DEVICE),
+                    "getNeighbors")
+        else:
+            idx = np.empty((rows, max(pitch, 1)), dtype=np.int32)
+            sims = np.empty((rows, max(pitch, 1)), dtype=np.float32) if with_sims else None
+            cnt = np.empty(max(rows, 1), dtype=np.int32)
+            N.check(L.siml_neighbors(*args, idx.ctypes.data, N.ptr(sims), cnt.ctypes.data, N.SIML_HOST),
+                    "getNeighbors")
+        self.last_async_width = maxneighbors
+        self._pending = ("neighbors", idx, sims, cnt, pitch, rows)
+
     # ----------------------------------------------------------- async glue
     def retrieveAsyncResult(self):
         """Result of the last async call (pysiml/GPULingo.py:538-640)."""
@@ -233,6 +277,16 @@ class GPULingo:
             out, width = payload
             host = out.cpu().numpy() if torch is not None and isinstance(out, torch.Tensor) else out
             return host[:, :width]
+        if kind == "neighbors":
+            idx, sims, cnt, pitch, rows = payload
+            host = lambda a: a.cpu().numpy() if torch is not None and isinstance(a, torch.Tensor) else a
+            counts = host(cnt)[:rows].copy()
+            ncols = int(min(counts.max(), pitch)) if rows else 0
+            mat = host(idx[:, :ncols]) if rows else np.empty((0, 0), np.int32)
+            if sims is None:
+                return np.ascontiguousarray(mat), counts
+            return np.ascontiguousarray(mat), np.ascontiguousarray(host(sims[:, :ncols]) if rows else
+                                                                   np.empty((0, 0), np.float32)), counts
         if kind == "ready":
             return payload[0]
         raise RuntimeError("unknown pending result")

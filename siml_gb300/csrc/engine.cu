@@ -62,7 +62,7 @@ void free_set(RawSet& s) {
 }
 void free_vocab(Vocab& v) { dev_free(v.keys); dev_free(v.vid); v = Vocab(); }
 void free_layout(DbLayout& d) {
-    dev_free(d.perm); dev_free(d.mag); dev_free(d.cmag); dev_free(d.len);
+    dev_free(d.perm); dev_free(d.meta);
     dev_free(d.ng); dev_free(d.off);
     if (d.entries) cudaFree(d.entries);
     d = DbLayout();
@@ -232,21 +232,24 @@ __global__ void k_window_sort(const int32_t* __restrict__ cmag, int64_t n, int32
     perm[base + rank] = m < n ? (int32_t)m : -1;
 }
 
+// Natural order: slot i holds molecule i.
+__global__ void k_identity_perm(int64_t n, int64_t slots, int32_t* perm) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < slots) perm[i] = i < n ? (int32_t)i : -1;
+}
+
 // Per chunk: 16-byte groups per lane = ceil(max entries / entries-per-group),
 // rounded up to an even number of 8-entry steps; plus per-lane metadata.
 __global__ void k_chunk_meta(const int32_t* __restrict__ perm, const int32_t* __restrict__ cmag,
                              const int32_t* __restrict__ mag, const int32_t* __restrict__ len,
                              int64_t nchunks, int entries_per_group,
-                             int32_t* __restrict__ ng, int32_t* __restrict__ cmag_out,
-                             int32_t* __restrict__ mag_out, int32_t* __restrict__ len_out) {
+                             int32_t* __restrict__ ng, int4* __restrict__ meta) {
     const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (c >= nchunks) return;
     const int32_t m = perm[c * 32 + lane];
     const int32_t e = m >= 0 ? cmag[m] : 0;
-    cmag_out[c * 32 + lane] = e;
-    mag_out[c * 32 + lane] = m >= 0 ? mag[m] : 0;
-    len_out[c * 32 + lane] = m >= 0 ? len[m] : 0;
+    meta[c * 32 + lane] = make_int4(m, m >= 0 ? mag[m] : 0, e, m >= 0 ? len[m] : 0);
     int32_t mx = e;
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
     if (lane == 0) {
@@ -420,33 +423,32 @@ int build_vocab(siml_engine* h) {
     return fail(SIML_ERR_NOMEM, "vocabulary hash could not be sized");
 }
 
-int build_layout(siml_engine* h) {
-    free_layout(h->db);
+int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
+    free_layout(d);
     const RawSet& q = h->qry;
-    DbLayout& d = h->db;
     cudaStream_t st = h->stream;
     d.n = q.n;
+    d.sorted = sorted;
     d.entry_bytes = h->vocab.nvid < 65535 ? 2 : 4;
     const int64_t nwin = (q.n + kWindow - 1) / kWindow;
     d.nchunks = (q.n + kChunk - 1) / kChunk;
     const int64_t slots = nwin * kWindow;
     int rc;
     if ((rc = dev_alloc(&d.perm, (size_t)slots))) return rc;
-    if ((rc = dev_alloc(&d.mag, (size_t)slots))) return rc;
-    if ((rc = dev_alloc(&d.cmag, (size_t)slots))) return rc;
-    if ((rc = dev_alloc(&d.len, (size_t)slots))) return rc;
+    if ((rc = dev_alloc(&d.meta, (size_t)slots))) return rc;
     if ((rc = dev_alloc(&d.ng, (size_t)d.nchunks))) return rc;
-    if ((rc = dev_alloc(&d.off, (size_t)d.nchunks))) return rc;
+    if ((rc = dev_alloc(&d.off, (size_t)d.nchunks + 1))) return rc;
     if (q.n == 0) return SIML_OK;
-    k_window_sort<<<(unsigned)nwin, kWindow, 0, st>>>(q.cmag, q.n, d.perm);
+    if (sorted) k_window_sort<<<(unsigned)nwin, kWindow, 0, st>>>(q.cmag, q.n, d.perm);
+    else k_identity_perm<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(q.n, slots, d.perm);
     h->launches++;
     const int epg = 16 / d.entry_bytes;
     k_chunk_meta<<<(unsigned)((d.nchunks + 7) / 8), 256, 0, st>>>(d.perm, q.cmag, q.mag, q.len, d.nchunks, epg,
-                                                                  d.ng, d.cmag, d.mag, d.len);
+                                                                  d.ng, d.meta);
     h->launches++;
     SIML_CUDA(cudaGetLastError());
     std::vector<int32_t> hng((size_t)d.nchunks);
-    std::vector<int64_t> hoff((size_t)d.nchunks);
+    std::vector<int64_t> hoff((size_t)d.nchunks + 1);
     SIML_CUDA(cudaMemcpyAsync(hng.data(), d.ng, d.nchunks * 4, cudaMemcpyDeviceToHost, st));
     SIML_CUDA(cudaStreamSynchronize(st));
     int64_t acc = 0, mx = 0;
@@ -455,9 +457,10 @@ int build_layout(siml_engine* h) {
         acc += (int64_t)hng[(size_t)c] * 32;
         mx = std::max<int64_t>(mx, hng[(size_t)c]);
     }
+    hoff[(size_t)d.nchunks] = acc;
     d.ngroups_total = acc;
     d.max_ng = mx;
-    SIML_CUDA(cudaMemcpyAsync(d.off, hoff.data(), d.nchunks * 8, cudaMemcpyHostToDevice, st));
+    SIML_CUDA(cudaMemcpyAsync(d.off, hoff.data(), (d.nchunks + 1) * 8, cudaMemcpyHostToDevice, st));
     SIML_CUDA(cudaMalloc(&d.entries, (size_t)std::max<int64_t>(acc, 1) * 16));
     SIML_CUDA(cudaMemsetAsync(d.entries, 0, (size_t)std::max<int64_t>(acc, 1) * 16, st));
     const unsigned grid = (unsigned)((d.nchunks * 32 + 255) / 256);
@@ -500,14 +503,29 @@ int ensure_prepared(siml_engine* h) {
     int rc;
     if (!h->layout_valid) {
         h->rows_valid = false;
+        h->nat_valid = h->sorted_valid = false;
+        free_layout(h->db_nat);
+        free_layout(h->db_sorted);
         if ((rc = build_vocab(h))) return rc;
-        if ((rc = build_layout(h))) return rc;
         h->layout_valid = true;
     }
     if (!h->rows_valid) {
         if ((rc = build_rows(h))) return rc;
         h->rows_valid = true;
     }
+    return SIML_OK;
+}
+
+int ensure_layout(siml_engine* h, bool sorted, const DbLayout** out) {
+    int rc = ensure_prepared(h);
+    if (rc) return rc;
+    bool& valid = sorted ? h->sorted_valid : h->nat_valid;
+    DbLayout& d = sorted ? h->db_sorted : h->db_nat;
+    if (!valid) {
+        if ((rc = build_layout(h, d, sorted))) return rc;
+        valid = true;
+    }
+    *out = &d;
     return SIML_OK;
 }
 
@@ -560,7 +578,8 @@ int siml_destroy(siml_engine* h) {
     free_set(h->ref);
     free_set(h->qry);
     free_vocab(h->vocab);
-    free_layout(h->db);
+    free_layout(h->db_nat);
+    free_layout(h->db_sorted);
     free_rows(h->rows);
     if (h->scratch) cudaFree(h->scratch);
     if (h->d_err) cudaFree(h->d_err);
@@ -620,14 +639,15 @@ int siml_set_sizes(siml_engine* h, int64_t* nref, int64_t* nquery) {
 int siml_db_stats(siml_engine* h, int64_t out[8]) {
     SIML_GUARD(h);
     if (!out) return fail(SIML_ERR_INVALID, "siml_db_stats: NULL output");
-    int rc = ensure_prepared(h);
+    const DbLayout* d = nullptr;
+    int rc = ensure_layout(h, false, &d);
     if (rc) return rc;
     out[0] = h->vocab.nvid;
-    out[1] = h->db.entry_bytes;
-    out[2] = h->db.ngroups_total;
-    out[3] = h->db.nchunks;
-    out[4] = h->db.max_ng;
-    out[5] = h->db.n;
+    out[1] = d->entry_bytes;
+    out[2] = d->ngroups_total;
+    out[3] = d->nchunks;
+    out[4] = d->max_ng;
+    out[5] = d->n;
     out[6] = h->ref.max_entries;
     out[7] = h->qry.max_entries;
     return SIML_OK;
@@ -669,6 +689,36 @@ static int rows_common(siml_engine* h, int64_t rowbase, int64_t rowlimit, float*
 int siml_rows(siml_engine* h, int64_t rowbase, int64_t rowlimit, float* out, int64_t ldo, int where) {
     SIML_GUARD(h);
     return rows_common(h, rowbase, rowlimit, out, ldo, where, kModeRows);
+}
+
+int siml_neighbors(siml_engine* h, int64_t rowbase, int64_t rowlimit, float lo, float hi, int64_t pitch,
+                   int32_t* idx, float* sims, int32_t* counts, int where) {
+    SIML_GUARD(h);
+    int rc;
+    if ((rc = ensure_prepared(h))) return rc;
+    if (rowbase < 0 || rowlimit > h->ref.n || rowlimit < rowbase)
+        return fail(SIML_ERR_RANGE, "row range [%lld, %lld) outside the ref set of %lld rows",
+                    (long long)rowbase, (long long)rowlimit, (long long)h->ref.n);
+    if (pitch < 0 || pitch > 0x7FFFFFFFll) return fail(SIML_ERR_INVALID, "siml_neighbors: bad pitch %lld", (long long)pitch);
+    const int64_t rows = rowlimit - rowbase;
+    if (rows == 0) return SIML_OK;
+    if (!counts || (pitch > 0 && !idx)) return fail(SIML_ERR_INVALID, "siml_neighbors: NULL output");
+    NbrCall c{rowbase, rowlimit, lo, hi, pitch, idx, sims, counts};
+    if (where == SIML_DEVICE) return launch_neighbors(h, c);
+    const size_t ib = (size_t)(rows * pitch) * 4, cb = (size_t)rows * 4;
+    const size_t need = ((ib + 255) / 256 * 256) * (sims ? 2 : 1) + cb;
+    void* buf = nullptr;
+    if ((rc = scratch_reserve(h, need, &buf))) return rc;
+    char* b = (char*)buf;
+    c.idx = (int32_t*)b;
+    c.sims = sims ? (float*)(b + (ib + 255) / 256 * 256) : nullptr;
+    c.counts = (int32_t*)(b + ((ib + 255) / 256 * 256) * (sims ? 2 : 1));
+    if ((rc = launch_neighbors(h, c))) return rc;
+    if (ib) SIML_CUDA(cudaMemcpyAsync(idx, c.idx, ib, cudaMemcpyDefault, h->stream));
+    if (ib && sims) SIML_CUDA(cudaMemcpyAsync(sims, c.sims, ib, cudaMemcpyDefault, h->stream));
+    SIML_CUDA(cudaMemcpyAsync(counts, c.counts, cb, cudaMemcpyDefault, h->stream));
+    SIML_CUDA(cudaStreamSynchronize(h->stream));
+    return SIML_OK;
 }
 
 int siml_row_single(siml_engine* h, int64_t row, float* out, int where) {

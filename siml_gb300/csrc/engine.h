@@ -36,9 +36,11 @@ struct Vocab {
     int64_t nvid = 0;     // number of (code, level) pairs; vids are 1..nvid
 };
 
-// Database (query set) layout.  Molecules are grouped in windows of 256
-// sorted by entry count (ties by index) and cut into chunks of 32 (one warp,
-// one molecule per lane).  A chunk's entries are stored as ng groups of 16
+// Database (query set) layout.  Molecules are cut into chunks of 32 (one
+// warp, one molecule per lane), either in their natural order (full-matrix
+// output: a warp's 32 stores per row are one contiguous 128-byte line) or
+// sorted by entry count inside windows of 256 (fused kernels, where lanes of
+// a warp then have nearly equal amounts of work).  A chunk's entries are stored as ng groups of 16
 // bytes per lane, interleaved [group][lane] so a warp's load of one group is
 // 512 contiguous bytes; an entry is a vid (uint16 when nvid < 65536, else
 // uint32), 0 padding a molecule's list to the chunk's length.
@@ -49,14 +51,13 @@ struct DbLayout {
     int64_t nchunks = 0;
     int entry_bytes = 2;          // 2 or 4
     int32_t* perm = nullptr;      // [nchunks*32] original index or -1
-    int32_t* mag = nullptr;       // [nchunks*32] effective magnitude
-    int32_t* cmag = nullptr;      // [nchunks*32] count sums
-    int32_t* len = nullptr;       // [nchunks*32] unique-code counts
+    int4* meta = nullptr;         // [nchunks*32] {original index or -1, magnitude, count sum, length}
     int32_t* ng = nullptr;        // [nchunks] 16-byte groups per lane
-    int64_t* off = nullptr;       // [nchunks] first group (16-byte units)
+    int64_t* off = nullptr;       // [nchunks + 1] first group (16-byte units); chunks are contiguous
     void* entries = nullptr;      // 16-byte groups
     int64_t ngroups_total = 0;
     int64_t max_ng = 0;
+    bool sorted = false;
 };
 
 // Ref-set rows as vid lists (levels expanded, codes absent from the database
@@ -76,10 +77,11 @@ struct siml_engine {
     int num_sms = 0;
     size_t smem_optin = 0;
     siml::RawSet ref, qry;
-    bool layout_valid = false;
+    bool layout_valid = false;   // vocabulary of the current query set
     bool rows_valid = false;
     siml::Vocab vocab;
-    siml::DbLayout db;
+    siml::DbLayout db_nat, db_sorted;
+    bool nat_valid = false, sorted_valid = false;
     siml::RowEntries rows;
     // device scratch reused across calls
     void* scratch = nullptr;
@@ -95,6 +97,8 @@ namespace siml {
 
 // engine.cu
 int ensure_prepared(siml_engine* h);
+// Natural-order (sorted == false) or window-sorted database layout.
+int ensure_layout(siml_engine* h, bool sorted, const DbLayout** out);
 int scratch_reserve(siml_engine* h, size_t bytes, void** out);
 int cuda_fail(cudaError_t e, const char* what);
 
@@ -108,6 +112,15 @@ struct RowsArgs {
 constexpr int kModeRows = 0;    // getMultipleRows: CPU-order fp32 union, zero test on magnitudes
 constexpr int kModeSingle = 1;  // getTanimotoRow: count-sum magnitudes, zero test on lengths
 int launch_rows(siml_engine* h, const RowsArgs& a);
+struct NbrCall {
+    int64_t rowbase, rowlimit;
+    float lo, hi;
+    int64_t pitch;
+    int32_t* idx;        // device [rows, pitch]
+    float* sims;         // device [rows, pitch] or null
+    int32_t* counts;     // device [rows]
+};
+int launch_neighbors(siml_engine* h, const NbrCall& c);
 
 }  // namespace siml
 

@@ -1,19 +1,26 @@
 // Similarity kernels (sm_103a).
 //
-// k_rows — block of Tanimoto rows (getMultipleRows, pysiml/kernels.py:315-352;
-// getTanimotoRow, :234-270).  One CTA per (32-row group, database slice):
-//   1. the CTA clears a shared-memory table T[vid] (one 32-bit word per
+// Table kernels (k_rows, k_nbr): one CTA per (32-row group, database slice).
+//   1. The CTA clears a shared-memory table T[vid] (one 32-bit word per
 //      database (code, level) pair) and sets bit r of T[vid] for every entry
-//      of its row r — rows are the reference's SIML-ref rows;
-//   2. each warp walks database chunks of 32 molecules (one per lane); a lane
-//      loads its molecule's entries 8 at a time (one 16-byte coalesced load,
-//      512 bytes per warp) and adds the eight T words into a bit-sliced
-//      counter, so 32 row intersections advance per table read;
-//   3. the counter is transposed into 32 row counts and each pair's Tanimoto
-//      is formed in the reference's fp32 operation order and stored.
-// k_rows_merge — the reference's per-pair sorted merge, used only when the
+//      of its row r.  Rows are the reference's SIML-ref rows.
+//   2. Each warp streams a contiguous range of database chunks (32 molecules,
+//      one per lane).  Consecutive chunks are contiguous in memory, so the
+//      entry loads (16 bytes per lane, 512 contiguous bytes per warp) are
+//      prefetched two steps ahead straight across chunk boundaries, and the
+//      per-lane metadata one chunk ahead.  Eight T words per step go into a
+//      bit-sliced counter: 32 row intersections advance per table read.
+//   3. At the end of a chunk an epilogue consumes the counter:
+//      k_rows transposes it into 32 row counts and stores 32 Tanimotos;
+//      k_nbr compares all 32 counts against a conservative per-lane integer
+//      threshold in bit-sliced form (~40 instructions for 32 pairs) and runs
+//      the reference's exact neighbour test only for the rows that pass.
+// k_nbr_finish puts each row's neighbours in ascending order, or recomputes
+// a row with the reference's ordered wave scan when it overflowed.
+// k_rows_merge is the reference's per-pair sorted merge, used only when the
 // table would not fit in shared memory or counts exceed 16 bits.
 #include <algorithm>
+#include <cmath>
 
 #include "engine.h"
 #include "lingo_core.cuh"
@@ -22,7 +29,8 @@ namespace siml {
 
 namespace {
 
-constexpr int kRowsThreads = 512;
+constexpr int kThreads = 1024;
+constexpr int kNbrSortMax = 2048;   // rows with more hits are recomputed in order
 
 // getMultipleRows: _CPULingo.c:53-71 order — ((float)amag + bmag) - isct in
 // fp32, then isct / union with IEEE round-to-nearest; 0 when a magnitude is 0.
@@ -40,7 +48,13 @@ __device__ __forceinline__ float tanimoto_single(int isct, int amag, int bmag, i
     return __fdiv_rn(__int2float_rn(isct), __int2float_rn(u));
 }
 
-struct RowsParams {
+// A molecule's magnitude admits the fast epilogue when 1 <= mag <= 32768 and
+// mag >= its count sum: then for any pair isct <= min(magA, magB), the union
+// magA + magB - isct lies in [1, 65536] and the fp32 sum order of the
+// reference is exact, so isct / union can use div_small.
+__device__ __forceinline__ bool fast_mag(int mag, int cmag) { return mag >= 1 && mag <= 32768 && mag >= cmag; }
+
+struct GroupParams {
     // ref rows
     const uint32_t* row_vid;
     int64_t row_stride;
@@ -53,37 +67,44 @@ struct RowsParams {
     const void* entries;
     const int64_t* off;
     const int32_t* ng;
-    const int32_t* perm;
-    const int32_t* dmag;
-    const int32_t* dcmag;
-    const int32_t* dlen;
+    const int4* meta;
     int64_t nchunks;
     int vt_words;
-    // output
-    float* out;
-    int64_t ldo;
     int mode;
 };
 
-template <int NP, typename ET>
-__global__ void __launch_bounds__(kRowsThreads, 1) k_rows(const RowsParams p) {
-    extern __shared__ __align__(16) uint32_t smem[];
-    uint32_t* T = smem;
-    int32_t* s_amag = (int32_t*)(smem + p.vt_words);
-    int32_t* s_alen = s_amag + 32;
+struct RowSmem {
+    int amag[32];
+    int alen[32];
+    __align__(16) float amagf[32];
+    int allfast;
+    int min_amag;
+};
 
+// Clears T, sets bit r of T[vid] for the entries of row r, fills RowSmem.
+// Returns the number of rows of the group.
+__device__ __forceinline__ int build_table(uint32_t* T, RowSmem& rs, const GroupParams& p) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
-    const int64_t row0 = (int64_t)blockIdx.x * 32;  // relative to rowbase
+    const int64_t row0 = (int64_t)blockIdx.x * 32;
     const int nr = min(32, p.rows - (int)row0);
-
     for (int i = threadIdx.x * 4; i < p.vt_words; i += blockDim.x * 4)
         *reinterpret_cast<uint4*>(T + i) = make_uint4(0u, 0u, 0u, 0u);
-    if (threadIdx.x < 32) {
-        const int r = threadIdx.x;
+    if (warp == 0) {
+        const int r = lane;
         const int64_t gr = p.rowbase + row0 + r;
-        s_amag[r] = r < nr ? (p.mode == kModeSingle ? p.row_cmag[gr] : p.row_mag[gr]) : 0;
-        s_alen[r] = r < nr ? p.row_len[gr] : 0;
+        const int am = r < nr ? (p.mode == kModeSingle ? p.row_cmag[gr] : p.row_mag[gr]) : 0;
+        rs.amag[r] = am;
+        rs.amagf[r] = (float)am;
+        rs.alen[r] = r < nr ? p.row_len[gr] : 0;
+        const bool f = r >= nr || (p.mode == kModeRows && fast_mag(am, p.row_cmag[gr]));
+        const unsigned all = __ballot_sync(0xFFFFFFFFu, f);
+        int mn = r < nr ? am : 0x7FFFFFFF;
+        for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
+        if (r == 0) {
+            rs.allfast = all == 0xFFFFFFFFu;
+            rs.min_amag = mn;
+        }
     }
     __syncthreads();
     for (int r = warp; r < nr; r += nwarps) {
@@ -94,68 +115,229 @@ __global__ void __launch_bounds__(kRowsThreads, 1) k_rows(const RowsParams p) {
         }
     }
     __syncthreads();
+    return nr;
+}
 
+// Chunks [wb, we) of this warp: the CTA's slice split contiguously.
+__device__ __forceinline__ void warp_range(const GroupParams& p, int64_t& wb, int64_t& we) {
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int64_t cb = p.nchunks * blockIdx.y / gridDim.y;
     const int64_t ce = p.nchunks * (blockIdx.y + 1) / gridDim.y;
-    for (int64_t c = cb + warp; c < ce; c += nwarps) {
-        const int ng = p.ng[c];
-        const uint4* ep = reinterpret_cast<const uint4*>(p.entries) + p.off[c] + lane;
-        SlicedCounter<NP> acc;
-        acc.clear();
-        if (sizeof(ET) == 2) {
-            for (int s = 0; s < ng; s++) {
-                const uint4 q = __ldg(ep + (int64_t)s * 32);
-                acc.add8(T[q.x & 0xFFFFu], T[q.x >> 16], T[q.y & 0xFFFFu], T[q.y >> 16],
-                         T[q.z & 0xFFFFu], T[q.z >> 16], T[q.w & 0xFFFFu], T[q.w >> 16]);
-            }
-        } else {
-            for (int s = 0; s < ng; s += 2) {
-                const uint4 q0 = __ldg(ep + (int64_t)s * 32);
-                const uint4 q1 = __ldg(ep + (int64_t)(s + 1) * 32);
-                acc.add8(T[q0.x], T[q0.y], T[q0.z], T[q0.w], T[q1.x], T[q1.y], T[q1.z], T[q1.w]);
-            }
+    wb = cb + (ce - cb) * warp / nwarps;
+    we = cb + (ce - cb) * (warp + 1) / nwarps;
+}
+
+// Streams the entries of chunks [wb, we) through the bit-sliced counter and
+// calls epi(chunk, meta, counter) at the end of each chunk.  All lanes of the
+// warp are in the same chunk at the same time.
+template <int NP, typename ET, class Epi>
+__device__ __forceinline__ void stream_chunks(const uint32_t* __restrict__ T, const GroupParams& p,
+                                              int64_t wb, int64_t we, Epi& epi) {
+    if (wb >= we) return;
+    constexpr int SPG = sizeof(ET) == 2 ? 1 : 2;  // 16-byte groups per 8-entry step
+    const int lane = threadIdx.x & 31;
+    const uint4* E = reinterpret_cast<const uint4*>(p.entries) + lane;
+    const int64_t gend = p.off[we];
+    int64_t g = p.off[wb];
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    uint4 n0 = zero, n1 = zero, m0 = zero, m1 = zero;
+    if (g < gend) { n0 = __ldg(E + g); if (SPG == 2) n1 = __ldg(E + g + 32); }
+    if (g + 32 * SPG < gend) { m0 = __ldg(E + g + 32 * SPG); if (SPG == 2) m1 = __ldg(E + g + 32 * SPG + 32); }
+    int64_t c = wb;
+    int4 meta = __ldg(p.meta + c * 32 + lane);
+    int steps = p.ng[c] / SPG;
+    int4 meta_next = make_int4(-1, 0, 0, 0);
+    int ng_next = 0;
+    if (c + 1 < we) { meta_next = __ldg(p.meta + (c + 1) * 32 + lane); ng_next = p.ng[c + 1]; }
+    SlicedCounter<NP> acc;
+    acc.clear();
+    for (;;) {
+        while (steps == 0) {
+            epi(c, meta, acc);
+            acc.clear();
+            if (++c >= we) return;
+            meta = meta_next;
+            steps = ng_next / SPG;
+            if (c + 1 < we) { meta_next = __ldg(p.meta + (c + 1) * 32 + lane); ng_next = p.ng[c + 1]; }
         }
-        RowCounts<NP> rc;
-        counts_from_planes<NP>(acc, rc);
-        const int64_t slot = c * 32 + lane;
-        const int32_t m = p.perm[slot];
-        if (m < 0) continue;
-        const int32_t bmag = p.mode == kModeSingle ? p.dcmag[slot] : p.dmag[slot];
-        const int32_t blen = p.dlen[slot];
-        float* o = p.out + row0 * p.ldo + m;
-#pragma unroll
-        for (int r = 0; r < 32; r++) {
-            if (r < nr) {
-                const int is = (int)row_count<NP>(rc, r);
-                const float t = p.mode == kModeSingle ? tanimoto_single(is, s_amag[r], bmag, s_alen[r], blen)
-                                                      : tanimoto_rows(is, s_amag[r], bmag);
-                o[(int64_t)r * p.ldo] = t;
-            }
-        }
+        const uint4 c0 = n0, c1 = n1;
+        n0 = m0;
+        n1 = m1;
+        g += 32 * SPG;
+        const int64_t gn = g + 32 * SPG;
+        if (gn < gend) { m0 = __ldg(E + gn); if (SPG == 2) m1 = __ldg(E + gn + 32); }
+        else { m0 = zero; m1 = zero; }
+        if (SPG == 1)
+            acc.add8(T[c0.x & 0xFFFFu], T[c0.x >> 16], T[c0.y & 0xFFFFu], T[c0.y >> 16],
+                     T[c0.z & 0xFFFFu], T[c0.z >> 16], T[c0.w & 0xFFFFu], T[c0.w >> 16]);
+        else
+            acc.add8(T[c0.x], T[c0.y], T[c0.z], T[c0.w], T[c1.x], T[c1.y], T[c1.z], T[c1.w]);
+        steps--;
     }
 }
 
-struct MergeParams {
+// ------------------------------------------------------------- k_rows ----
+template <int NP>
+struct RowsEpi {
+    const RowSmem& rs;
+    int nr;
+    int mode;
+    float* out;     // first row of this group
+    int64_t ldo;
+
+    __device__ __forceinline__ void operator()(int64_t, const int4& meta, const SlicedCounter<NP>& acc) {
+        const int32_t m = meta.x;
+        if (m < 0) return;
+        RowCounts<NP> rc;
+        counts_from_planes<NP>(acc, rc);
+        const int32_t bmag = mode == kModeSingle ? meta.z : meta.y;
+        float* o = out + m;
+        if (rs.allfast && fast_mag(bmag, meta.z)) {
+            // union = ((float)amag + bmag) - isct, all exact: the reference's order
+            const float bf = small_int_to_float((uint32_t)bmag);
+            const float4* am4 = reinterpret_cast<const float4*>(rs.amagf);
+#pragma unroll
+            for (int r4 = 0; r4 < 8; r4++) {
+                const float4 a4 = am4[r4];
+                const float av[4] = {a4.x, a4.y, a4.z, a4.w};
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int r = 4 * r4 + k;
+                    if (r < nr) {
+                        const float isf = small_int_to_float(row_count<NP>(rc, r));
+                        const float u = __fsub_rn(__fadd_rn(av[k], bf), isf);
+                        o[(int64_t)r * ldo] = div_small(isf, u);
+                    }
+                }
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < 32; r++) {
+                if (r < nr) {
+                    const int is = (int)row_count<NP>(rc, r);
+                    const float t = mode == kModeSingle ? tanimoto_single(is, rs.amag[r], bmag, rs.alen[r], meta.w)
+                                                        : tanimoto_rows(is, rs.amag[r], bmag);
+                    o[(int64_t)r * ldo] = t;
+                }
+            }
+        }
+    }
+};
+
+template <int NP, typename ET>
+__global__ void __launch_bounds__(kThreads, 1) k_rows(const GroupParams p, float* out, int64_t ldo) {
+    extern __shared__ __align__(16) uint32_t T[];
+    __shared__ RowSmem rs;
+    const int nr = build_table(T, rs, p);
+    int64_t wb, we;
+    warp_range(p, wb, we);
+    RowsEpi<NP> epi{rs, nr, p.mode, out + (int64_t)blockIdx.x * 32 * ldo, ldo};
+    stream_chunks<NP, ET>(T, p, wb, we, epi);
+}
+
+// -------------------------------------------------------------- k_nbr ----
+struct NbrArgs {
+    float lo, hi;
+    float thr_scale;   // conservative lo / (1 + lo)
+    int thr_mode;      // 0: threshold test, 1: every row is a candidate, 2: nothing can match
+    int64_t pitch;
+    int32_t* idx;      // [rows, pitch]
+    float* sims;       // [rows, pitch] or null
+    int32_t* counts;   // [rows], zeroed before the launch
+};
+
+// Bit r of the result is set when the count of row r (bit-sliced in planes)
+// is >= th.  MSB-first compare: eq tracks rows equal so far, gt rows greater.
+template <int NP>
+__device__ __forceinline__ uint32_t sliced_ge(const SlicedCounter<NP>& acc, uint32_t th) {
+    if (th >= (1u << NP)) return 0u;
+    uint32_t gt = 0u, eq = 0xFFFFFFFFu;
+#pragma unroll
+    for (int p = NP - 1; p >= 0; p--) {
+        const uint32_t tb = 0u - ((th >> p) & 1u);   // all ones where the threshold bit is 1
+        gt |= eq & acc.plane[p] & ~tb;
+        eq &= ~(acc.plane[p] ^ tb);
+    }
+    return gt | eq;
+}
+
+template <int NP>
+__device__ __forceinline__ int sliced_row(const SlicedCounter<NP>& acc, int r) {
+    int v = 0;
+#pragma unroll
+    for (int p = 0; p < NP; p++) v |= (int)((acc.plane[p] >> r) & 1u) << p;
+    return v;
+}
+
+// getNeighbors' per-pair test (pysiml/kernels.py:437-448): fp32 magnitude
+// bound min/max >= lo, then lo <= t < hi.
+__device__ __forceinline__ bool neighbor_test(int isct, int ma, int mb, float lo, float hi, float& t) {
+    const float bound = __fdiv_rn(__int2float_rn(min(ma, mb)), __int2float_rn(max(ma, mb)));
+    if (!(bound >= lo)) return false;
+    t = tanimoto_rows(isct, ma, mb);
+    return t >= lo && t < hi;
+}
+
+template <int NP>
+struct NbrEpi {
+    const RowSmem& rs;
+    int nr;
+    int64_t row0;      // first output row of this group
+    NbrArgs a;
+
+    __device__ __forceinline__ void operator()(int64_t, const int4& meta, const SlicedCounter<NP>& acc) {
+        const int32_t m = meta.x;
+        if (m < 0 || a.thr_mode == 2) return;
+        const int32_t mb = meta.y;
+        uint32_t cand;
+        if (a.thr_mode == 1) {
+            cand = 0xFFFFFFFFu;
+        } else {
+            // exact t >= lo > 0 implies isct >= lo/(1+lo) * (ma + mb) >= th
+            const float s = (float)rs.min_amag + (float)mb;
+            const float thf = floorf(a.thr_scale * s);
+            const uint32_t th = thf <= 0.0f ? 0u : (thf >= 4.0e9f ? 0xFFFFFFFFu : (uint32_t)thf);
+            cand = sliced_ge<NP>(acc, th);
+        }
+        if (nr < 32) cand &= (1u << nr) - 1u;
+        while (cand) {
+            const int r = __ffs(cand) - 1;
+            cand &= cand - 1u;
+            const int is = sliced_row<NP>(acc, r);
+            float t;
+            if (!neighbor_test(is, rs.amag[r], mb, a.lo, a.hi, t)) continue;
+            const int64_t row = row0 + r;
+            const int pos = atomicAdd(a.counts + row, 1);
+            if (pos < a.pitch) {
+                a.idx[row * a.pitch + pos] = m;
+                if (a.sims) a.sims[row * a.pitch + pos] = t;
+            }
+        }
+    }
+};
+
+template <int NP, typename ET>
+__global__ void __launch_bounds__(kThreads, 1) k_nbr(const GroupParams p, const NbrArgs a) {
+    extern __shared__ __align__(16) uint32_t T[];
+    __shared__ RowSmem rs;
+    const int nr = build_table(T, rs, p);
+    int64_t wb, we;
+    warp_range(p, wb, we);
+    NbrEpi<NP> epi{rs, nr, (int64_t)blockIdx.x * 32, a};
+    stream_chunks<NP, ET>(T, p, wb, we, epi);
+}
+
+// ------------------------------------------------------- k_nbr_finish ----
+struct RawArgs {
     const int32_t *rl, *rc, *rlen, *rmag, *rcmag;
     int64_t rw;
     const int32_t *ql, *qc, *qlen, *qmag, *qcmag;
     int64_t qw, nq;
     int64_t rowbase;
-    float* out;
-    int64_t ldo;
-    int mode;
 };
 
-// Sorted merge per pair (pysiml/_CPULingo.c:53-71, pysiml/kernels.py:162-199).
-__global__ void k_rows_merge(const MergeParams p) {
-    const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t r = p.rowbase + blockIdx.y;
-    if (col >= p.nq) return;
-    const int32_t* a = p.rl + r * p.rw;
-    const int32_t* as = p.rc + r * p.rw;
-    const int32_t* b = p.ql + col * p.qw;
-    const int32_t* bs = p.qc + col * p.qw;
-    const int32_t alen = p.rlen[r], blen = p.qlen[col];
+__device__ __forceinline__ int merge_isct(const int32_t* a, const int32_t* as, int32_t alen,
+                                          const int32_t* b, const int32_t* bs, int32_t blen) {
     int32_t i = 0, j = 0, isct = 0;
     while (i < alen && j < blen) {
         const int32_t x = a[i], y = b[j];
@@ -163,11 +345,109 @@ __global__ void k_rows_merge(const MergeParams p) {
         else if (x < y) i++;
         else j++;
     }
-    const float t = p.mode == kModeSingle ? tanimoto_single(isct, p.rcmag[r], p.qcmag[col], alen, blen)
-                                          : tanimoto_rows(isct, p.rmag[r], p.qmag[col]);
-    p.out[(int64_t)blockIdx.y * p.ldo + col] = t;
+    return isct;
 }
 
+// One CTA (128 threads) per output row.  Rows whose hits fit and number at
+// most kNbrSortMax are sorted by column; the others (or all rows when
+// force_ordered) are recomputed with the reference's ordered scan: waves of
+// 128 columns, hits written in column order while they fit in pitch, the
+// count growing by whole waves, stopping after the first wave that takes it
+// above pitch (pysiml/kernels.py:433-474).
+__global__ void __launch_bounds__(128) k_nbr_finish(const RawArgs ra, const NbrArgs a, int force_ordered) {
+    __shared__ int skey[kNbrSortMax];
+    __shared__ float sval[kNbrSortMax];
+    __shared__ int wcount[4];
+    const int64_t row = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int32_t* idx = a.idx + row * a.pitch;
+    float* sims = a.sims ? a.sims + row * a.pitch : nullptr;
+    const int n = force_ordered ? 0x7FFFFFFF : a.counts[row];
+    if (!force_ordered && n <= a.pitch && n <= kNbrSortMax) {
+        if (n <= 1) return;
+        int N = 1;
+        while (N < n) N <<= 1;
+        for (int i = tid; i < N; i += blockDim.x) {
+            skey[i] = i < n ? idx[i] : 0x7FFFFFFF;
+            sval[i] = (i < n && sims) ? sims[i] : 0.0f;
+        }
+        __syncthreads();
+        for (int k = 2; k <= N; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = tid; i < N; i += blockDim.x) {
+                    const int ixj = i ^ j;
+                    if (ixj > i) {
+                        const bool asc = (i & k) == 0;
+                        if ((skey[i] > skey[ixj]) == asc) {
+                            const int tk = skey[i]; skey[i] = skey[ixj]; skey[ixj] = tk;
+                            const float tv = sval[i]; sval[i] = sval[ixj]; sval[ixj] = tv;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int i = tid; i < n; i += blockDim.x) {
+            idx[i] = skey[i];
+            if (sims) sims[i] = sval[i];
+        }
+        return;
+    }
+    // ordered recompute
+    const int64_t r = ra.rowbase + row;
+    const int32_t* ar = ra.rl + r * ra.rw;
+    const int32_t* acnt = ra.rc + r * ra.rw;
+    const int32_t alen = ra.rlen[r], ma = ra.rmag[r];
+    int64_t count = 0;
+    for (int64_t base = 0; base < ra.nq; base += 128) {
+        const int64_t col = base + tid;
+        bool flag = false;
+        float t = 0.0f;
+        if (col < ra.nq) {
+            const int32_t mb = ra.qmag[col];
+            const float bound = __fdiv_rn(__int2float_rn(min(ma, mb)), __int2float_rn(max(ma, mb)));
+            if (bound >= a.lo) {
+                const int is = merge_isct(ar, acnt, alen, ra.ql + col * ra.qw, ra.qc + col * ra.qw, ra.qlen[col]);
+                t = tanimoto_rows(is, ma, mb);
+                flag = t >= a.lo && t < a.hi;
+            }
+        }
+        const unsigned b = __ballot_sync(0xFFFFFFFFu, flag);
+        if (lane == 0) wcount[warp] = __popc(b);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int w = 0; w < 4; w++) {
+            const int cw = wcount[w];
+            if (w < warp) before += cw;
+            total += cw;
+        }
+        const int64_t pos = count + before + __popc(b & ((1u << lane) - 1u));
+        if (flag && pos < a.pitch) {
+            idx[pos] = (int32_t)col;
+            if (sims) sims[pos] = t;
+        }
+        count += total;
+        __syncthreads();
+        if (count > a.pitch) break;
+    }
+    if (tid == 0) a.counts[row] = (int32_t)(count < 0x7FFFFFFF ? count : 0x7FFFFFFF);
+}
+
+// ------------------------------------------------------ k_rows_merge ----
+// Sorted merge per pair (pysiml/_CPULingo.c:53-71, pysiml/kernels.py:162-199).
+__global__ void k_rows_merge(const RawArgs ra, float* out, int64_t ldo, int mode) {
+    const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t r = ra.rowbase + blockIdx.y;
+    if (col >= ra.nq) return;
+    const int32_t alen = ra.rlen[r], blen = ra.qlen[col];
+    const int isct = merge_isct(ra.rl + r * ra.rw, ra.rc + r * ra.rw, alen,
+                                ra.ql + col * ra.qw, ra.qc + col * ra.qw, blen);
+    const float t = mode == kModeSingle ? tanimoto_single(isct, ra.rcmag[r], ra.qcmag[col], alen, blen)
+                                        : tanimoto_rows(isct, ra.rmag[r], ra.qmag[col]);
+    out[(int64_t)blockIdx.y * ldo + col] = t;
+}
+
+// ---------------------------------------------------------- launchers ----
 int planes_needed(int64_t max_count) {
     int b = 0;
     while (b < 62 && (1ll << b) <= max_count) b++;
@@ -175,7 +455,7 @@ int planes_needed(int64_t max_count) {
 }
 
 // Splits of the database per row group so that groups x splits fills whole
-// waves of one CTA per SM and every CTA still has plenty of chunks.
+// waves of one CTA per SM and every warp still has several chunks.
 int choose_splits(int64_t groups, int64_t nchunks, int num_sms, int nwarps) {
     int best = 1;
     double best_cost = 1e300;
@@ -183,27 +463,79 @@ int choose_splits(int64_t groups, int64_t nchunks, int num_sms, int nwarps) {
     for (int64_t s = 1; s <= max_s; s++) {
         const int64_t ctas = groups * s;
         const int64_t waves = (ctas + num_sms - 1) / num_sms;
-        // time ~ waves * (work per CTA + fixed set-up), work per CTA ~ 1/s
         const double cost = (double)waves * (1.0 / (double)s + 0.004);
         if (cost < best_cost * 0.999) { best_cost = cost; best = (int)s; }
     }
     return best;
 }
 
+RawArgs raw_args(siml_engine* h, int64_t rowbase) {
+    RawArgs m;
+    m.rl = h->ref.lingos; m.rc = h->ref.counts; m.rlen = h->ref.len; m.rmag = h->ref.mag; m.rcmag = h->ref.cmag;
+    m.rw = h->ref.width;
+    m.ql = h->qry.lingos; m.qc = h->qry.counts; m.qlen = h->qry.len; m.qmag = h->qry.mag; m.qcmag = h->qry.cmag;
+    m.qw = h->qry.width; m.nq = h->qry.n;
+    m.rowbase = rowbase;
+    return m;
+}
+
+// Table kernels are usable when T fits in shared memory and 16-bit counters
+// suffice; fills p and the dynamic shared-memory size.
+bool table_params(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t rows, int mode,
+                  GroupParams& p, size_t& smem, int& np) {
+    const int vt_words = (int)((h->vocab.nvid + 1 + 3) / 4 * 4);
+    smem = (size_t)vt_words * 4;
+    np = planes_needed(std::min(h->ref.max_entries, h->qry.max_entries));
+    if (smem + sizeof(RowSmem) + 64 > h->smem_optin || np > 16) return false;
+    np = np <= 8 ? 8 : 16;
+    p.row_vid = h->rows.vid;
+    p.row_stride = h->rows.stride;
+    p.row_mag = h->ref.mag;
+    p.row_cmag = h->ref.cmag;
+    p.row_len = h->ref.len;
+    p.rowbase = rowbase;
+    p.rows = (int)rows;
+    p.entries = d->entries;
+    p.off = d->off;
+    p.ng = d->ng;
+    p.meta = d->meta;
+    p.nchunks = d->nchunks;
+    p.vt_words = vt_words;
+    p.mode = mode;
+    return true;
+}
+
+template <class K>
+int set_smem(K kernel, size_t smem) {
+    SIML_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return SIML_OK;
+}
+
 template <int NP, typename ET>
-int launch_rows_t(siml_engine* h, const RowsParams& p, int64_t groups, size_t smem) {
-    static bool attr_set = false;
-    static size_t attr_bytes = 0;
-    if (!attr_set || attr_bytes < smem) {
-        SIML_CUDA(cudaFuncSetAttribute(k_rows<NP, ET>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_set = true;
-        attr_bytes = smem;
-    }
-    const int nwarps = kRowsThreads / 32;
-    const int s = choose_splits(groups, p.nchunks, h->num_sms, nwarps);
+int launch_rows_t(siml_engine* h, const GroupParams& p, size_t smem, float* out, int64_t ldo) {
+    const int64_t groups = (p.rows + 31) / 32;
+    int rc = set_smem(k_rows<NP, ET>, smem);
+    if (rc) return rc;
+    const int s = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
     dim3 grid((unsigned)groups, (unsigned)s);
     SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
-    k_rows<NP, ET><<<grid, kRowsThreads, smem, h->stream>>>(p);
+    k_rows<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, out, ldo);
+    SIML_CUDA(cudaGetLastError());
+    SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+    h->timed = true;
+    h->launches++;
+    return SIML_OK;
+}
+
+template <int NP, typename ET>
+int launch_nbr_t(siml_engine* h, const GroupParams& p, size_t smem, const NbrArgs& a) {
+    const int64_t groups = (p.rows + 31) / 32;
+    int rc = set_smem(k_nbr<NP, ET>, smem);
+    if (rc) return rc;
+    const int s = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
+    dim3 grid((unsigned)groups, (unsigned)s);
+    SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+    k_nbr<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, a);
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
     h->timed = true;
@@ -214,55 +546,67 @@ int launch_rows_t(siml_engine* h, const RowsParams& p, int64_t groups, size_t sm
 }  // namespace
 
 int launch_rows(siml_engine* h, const RowsArgs& a) {
+    const DbLayout* d = nullptr;
+    int rc = ensure_layout(h, false, &d);
+    if (rc) return rc;
     const int64_t rows = a.rowlimit - a.rowbase;
-    const int64_t groups = (rows + 31) / 32;
-    const int vt_words = (int)((h->vocab.nvid + 1 + 3) / 4 * 4);
-    const size_t smem = (size_t)vt_words * 4 + 64 * 4;
-    const int np = planes_needed(std::min(h->ref.max_entries, h->qry.max_entries));
-    const bool table_ok = smem <= h->smem_optin && np <= 16 && groups <= 0x7FFFFFFF;
-    if (table_ok) {
-        RowsParams p;
-        p.row_vid = h->rows.vid;
-        p.row_stride = h->rows.stride;
-        p.row_mag = h->ref.mag;
-        p.row_cmag = h->ref.cmag;
-        p.row_len = h->ref.len;
-        p.rowbase = a.rowbase;
-        p.rows = (int)rows;
-        p.entries = h->db.entries;
-        p.off = h->db.off;
-        p.ng = h->db.ng;
-        p.perm = h->db.perm;
-        p.dmag = h->db.mag;
-        p.dcmag = h->db.cmag;
-        p.dlen = h->db.len;
-        p.nchunks = h->db.nchunks;
-        p.vt_words = vt_words;
-        p.out = a.out;
-        p.ldo = a.ldo;
-        p.mode = a.mode;
-        if (np <= 8)
-            return h->db.entry_bytes == 2 ? launch_rows_t<8, uint16_t>(h, p, groups, smem)
-                                          : launch_rows_t<8, uint32_t>(h, p, groups, smem);
-        return h->db.entry_bytes == 2 ? launch_rows_t<16, uint16_t>(h, p, groups, smem)
-                                      : launch_rows_t<16, uint32_t>(h, p, groups, smem);
+    GroupParams p;
+    size_t smem = 0;
+    int np = 0;
+    if (table_params(h, d, a.rowbase, rows, a.mode, p, smem, np)) {
+        if (np == 8)
+            return d->entry_bytes == 2 ? launch_rows_t<8, uint16_t>(h, p, smem, a.out, a.ldo)
+                                       : launch_rows_t<8, uint32_t>(h, p, smem, a.out, a.ldo);
+        return d->entry_bytes == 2 ? launch_rows_t<16, uint16_t>(h, p, smem, a.out, a.ldo)
+                                   : launch_rows_t<16, uint32_t>(h, p, smem, a.out, a.ldo);
     }
-    MergeParams m;
-    m.rl = h->ref.lingos; m.rc = h->ref.counts; m.rlen = h->ref.len; m.rmag = h->ref.mag; m.rcmag = h->ref.cmag;
-    m.rw = h->ref.width;
-    m.ql = h->qry.lingos; m.qc = h->qry.counts; m.qlen = h->qry.len; m.qmag = h->qry.mag; m.qcmag = h->qry.cmag;
-    m.qw = h->qry.width; m.nq = h->qry.n;
-    m.rowbase = a.rowbase;
-    m.out = a.out;
-    m.ldo = a.ldo;
-    m.mode = a.mode;
     if (rows > 65535) return fail(SIML_ERR_UNSUPPORTED, "merge path: more than 65535 rows per call");
     dim3 grid((unsigned)((h->qry.n + 255) / 256), (unsigned)rows);
     SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
-    k_rows_merge<<<grid, 256, 0, h->stream>>>(m);
+    k_rows_merge<<<grid, 256, 0, h->stream>>>(raw_args(h, a.rowbase), a.out, a.ldo, a.mode);
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
     h->timed = true;
+    h->launches++;
+    return SIML_OK;
+}
+
+int launch_neighbors(siml_engine* h, const NbrCall& c) {
+    const DbLayout* d = nullptr;
+    int rc = ensure_layout(h, true, &d);
+    if (rc) return rc;
+    const int64_t rows = c.rowlimit - c.rowbase;
+    NbrArgs a;
+    a.lo = c.lo;
+    a.hi = c.hi;
+    a.pitch = c.pitch;
+    a.idx = c.idx;
+    a.sims = c.sims;
+    a.counts = c.counts;
+    if (std::isnan(c.lo)) {
+        a.thr_mode = 2;
+    } else if (c.lo <= 0.0f) {
+        a.thr_mode = 1;
+    } else {
+        a.thr_mode = 0;
+    }
+    a.thr_scale = a.thr_mode == 0 ? (float)((double)c.lo / (1.0 + (double)c.lo) * (1.0 - 1.0 / 4096.0)) : 0.0f;
+    SIML_CUDA(cudaMemsetAsync(c.counts, 0, rows * sizeof(int32_t), h->stream));
+    GroupParams p;
+    size_t smem = 0;
+    int np = 0;
+    int force_ordered = 1;
+    if (table_params(h, d, c.rowbase, rows, kModeRows, p, smem, np)) {
+        force_ordered = 0;
+        if (np == 8)
+            rc = d->entry_bytes == 2 ? launch_nbr_t<8, uint16_t>(h, p, smem, a) : launch_nbr_t<8, uint32_t>(h, p, smem, a);
+        else
+            rc = d->entry_bytes == 2 ? launch_nbr_t<16, uint16_t>(h, p, smem, a) : launch_nbr_t<16, uint32_t>(h, p, smem, a);
+        if (rc) return rc;
+    }
+    if (rows > 0x7FFFFFFF) return fail(SIML_ERR_UNSUPPORTED, "too many rows");
+    k_nbr_finish<<<(unsigned)rows, 128, 0, h->stream>>>(raw_args(h, c.rowbase), a, force_ordered);
+    SIML_CUDA(cudaGetLastError());
     h->launches++;
     return SIML_OK;
 }

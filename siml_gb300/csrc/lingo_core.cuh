@@ -136,4 +136,32 @@ SIML_HD uint32_t bin_of(float s, uint32_t top) {
     return b < top ? b : top;
 }
 
+#if defined(__CUDACC__)
+// Correctly rounded quotient a / b of two integers for 0 <= a <= 2^24 and
+// 1 <= b <= 2^16, by Markstein's correction of a reciprocal estimate
+// (P. Markstein, IBM J. Res. Dev. 34(1), 1990): q0 = a*y, r = a - q0*b
+// (exact with one fused multiply-add), q = q0 + r*y rounded once.  With y the
+// hardware reciprocal estimate (relative error < 2^-22) the unrounded q is
+// within about 2^-21 ulp of a/b, while a/b (b not a power of two) lies at
+// least 1/(b * 2^25) relative, i.e. > 2^-18 ulp, from any rounding midpoint,
+// so the single rounding lands on RN(a/b); for b a power of two every step is
+// exact.  tests/native/division_test.cu checks all a <= b <= 2^14 against
+// __fdiv_rn on the GPU.
+__device__ __forceinline__ float div_small(float af, float bf) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(bf));
+    const float q0 = __fmul_rn(af, y);
+    const float r = __fmaf_rn(-q0, bf, af);
+    return __fmaf_rn(r, y, q0);
+}
+__device__ __forceinline__ float div_small_int(int a, int b) {
+    return div_small(__int2float_rn(a), __int2float_rn(b));
+}
+// Exact fp32 value of an integer 0 <= i < 2^23 with full-rate integer and
+// fp32 adds: the bit pattern 0x4B000000 | i is the float 2^23 + i.
+__device__ __forceinline__ float small_int_to_float(uint32_t i) {
+    return __fsub_rn(__uint_as_float(0x4B000000u | i), 8388608.0f);
+}
+#endif
+
 }  // namespace siml

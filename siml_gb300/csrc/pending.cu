@@ -6,11 +6,6 @@ using namespace siml;
 
 extern "C" {
 
-int siml_neighbors(siml_engine* h, int64_t, int64_t, float, float, int64_t, int32_t*, float*, int32_t*, int) {
-    clear_error();
-    (void)h;
-    return fail(SIML_ERR_UNSUPPORTED, "siml_neighbors: not available in this build");
-}
 int siml_hist101(siml_engine* h, int64_t, int64_t, int32_t*, int64_t, int) {
     clear_error();
     (void)h;
