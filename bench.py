@@ -37,6 +37,8 @@ DB_N = 1_000_000
 QUERY_N = 10_240
 BLOCK = 1024
 METRIC = "LINGO Tanimoto Gpairs/s bit-exact"
+NBR_WORKLOAD = ("nbr_1m: getNeighbors T >= 0.7 (indices + fp32 similarities, pitch 1,024), 1,024-row blocks x "
+                "1,000,000-molecule database (lognormal median 45 chars)")
 WORKLOAD = ("rows_1m: getMultipleRows, 1,024-row blocks x 1,000,000-molecule database "
             "(10,240 query rows, lognormal median 45 chars), fp32 block kept on device")
 
@@ -216,9 +218,24 @@ def gpu_arm(args):
         b = (k * world + rank) % nblocks
         return b * rows_step, (b + 1) * rows_step
 
+    nbr = args.workload == "nbr_1m"
+    if nbr:
+        del out
+        pitch = 1024
+        nb_idx = torch.empty((rows_step, pitch), dtype=torch.int32, device=dev)
+        nb_sims = torch.empty((rows_step, pitch), dtype=torch.float32, device=dev)
+        nb_cnt = torch.empty(rows_step, dtype=torch.int32, device=dev)
+        out = None
+
+    def run_step(r0, r1):
+        if nbr:
+            gl.neighborsDevice(r0, r1, 0.7, 1.1, pitch, nb_idx, nb_sims, nb_cnt)
+        else:
+            gl.getMultipleRowsDevice(r0, r1, out=out)
+
     for w in range(args.warmup):
         r0, r1 = block_of(w)
-        gl.getMultipleRowsDevice(r0, r1, out=out)
+        run_step(r0, r1)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -235,7 +252,7 @@ def gpu_arm(args):
             flush.fill_(float(k))
             ev[k][0].record(stream)
         r0, r1 = block_of(args.warmup + k)
-        gl.getMultipleRowsDevice(r0, r1, out=out)
+        run_step(r0, r1)
         ev[k][1].record(stream)
         kernel_ms.append(gl.lastKernelMs())
     torch.cuda.synchronize()
@@ -256,13 +273,20 @@ def gpu_arm(args):
     # spot parity check against the oracle (two rows of the last block)
     from oracle import cpulingo as O
     r0, r1 = block_of(args.warmup + args.steps - 1)
-    got = out[:2].cpu().numpy()
-    want = O.tanimoto_block(q, db, r0, r0 + 2, nthreads=os.cpu_count() or 1)
-    parity = bool(np.array_equal(got, want))
+    if nbr:
+        oi, os_, oc = O.neighbors_block(q, db, r0, r0 + 4, 0.7, 1.1, pitch, nthreads=os.cpu_count() or 1)
+        gc = nb_cnt[:4].cpu().numpy()
+        gi = nb_idx[:4].cpu().numpy()
+        parity = bool(np.array_equal(gc, oc) and all(
+            np.array_equal(gi[i, :min(gc[i], pitch)], oi[i, :min(oc[i], pitch)]) for i in range(4)))
+    else:
+        got = out[:2].cpu().numpy()
+        want = O.tanimoto_block(q, db, r0, r0 + 2, nthreads=os.cpu_count() or 1)
+        parity = bool(np.array_equal(got, want))
 
     # roofline of the dominant kernel (k_rows): algorithmic bytes per launch
     kms = statistics.mean(kernel_ms)
-    out_bytes = pairs_per_step * 4
+    out_bytes = 0 if nbr else pairs_per_step * 4
     db_bytes = stats["ngroups_total"] * 16 + stats["nchunks"] * 32 * 8 + stats["nchunks"] * 12
     alg_bytes = out_bytes + db_bytes
     achieved = alg_bytes / (kms / 1e3) / 1e9
@@ -274,13 +298,13 @@ def gpu_arm(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     traffic = read_profile_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": "k_rows", "kernel_ms": kms,
+                "traffic": traffic, "kernel": "k_nbr" if nbr else "k_rows", "kernel_ms": kms,
                 "algorithmic_bytes_per_launch": alg_bytes,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback"}
 
     e2e = None
     cpu = None
-    if rank == 0 and not args.no_extras:
+    if rank == 0 and not args.no_extras and not nbr:
         e2e = measure_e2e(gl, q, stream, dev, steps=min(3, args.steps))
         if world == 1:
             cpu = cpu_reference_rate(db, q)
@@ -289,7 +313,7 @@ def gpu_arm(args):
             "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded SMILES-like strings)",
-            "config": {"workload": WORKLOAD, "rows_per_step": rows_step, "db_molecules": DB_N,
+            "config": {"workload": WORKLOAD if not nbr else NBR_WORKLOAD, "rows_per_step": rows_step, "db_molecules": DB_N,
                        "query_rows": QUERY_N, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "flushed between steps by a 256 MB write; each step also writes a 4 GB block",
                        "db_layout": stats},
@@ -354,6 +378,8 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--rows-per-step", type=int, default=BLOCK,
                     help="rows per block (smaller blocks for profiler captures)")
+    ap.add_argument("--workload", choices=["rows_1m", "nbr_1m"], default="rows_1m",
+                    help="rows_1m: getMultipleRows blocks (default); nbr_1m: getNeighbors blocks at T >= 0.7")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the end-to-end and CPU-baseline legs (profiler runs)")
     args = ap.parse_args()

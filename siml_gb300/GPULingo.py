@@ -240,6 +240,16 @@ class GPULingo:
         self._queue_neighbors(rowbase, rowlimit, lowerbound, upperbound, maxneighbors, True)
         return self.retrieveAsyncResult()
 
+    def neighborsDevice(self, rowbase, rowlimit, lowerbound, upperbound, pitch, idx, sims, counts):
+        """Neighbour search into caller-provided CUDA tensors: idx int32
+        [rows, pitch], sims float32 [rows, pitch] or None, counts int32 [rows]."""
+        self._check_rows(rowbase, rowlimit)
+        self._enter()
+        N.check(N.lib().siml_neighbors(self._h, int(rowbase), int(rowlimit), ctypes.c_float(lowerbound),
+                                       ctypes.c_float(upperbound), int(pitch), idx.data_ptr(), N.ptr(sims),
+                                       counts.data_ptr(), N.SIML_DEVICE), "neighborsDevice")
+        self._leave(idx, sims, counts)
+
     def _queue_neighbors(self, rowbase, rowlimit, lowerbound, upperbound, maxneighbors, with_sims):
         self._check_rows(rowbase, rowlimit)
         if maxneighbors is None:

@@ -118,6 +118,12 @@ __device__ __forceinline__ int build_table(uint32_t* T, RowSmem& rs, const Group
     return nr;
 }
 
+// Hint: bring [p, p + bytes) into L2 with one bulk prefetch (no completion
+// to wait for).  p and bytes are multiples of 16.
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+    if (bytes) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // Chunks [wb, we) of this warp: the CTA's slice split contiguously.
 __device__ __forceinline__ void warp_range(const GroupParams& p, int64_t& wb, int64_t& we) {
     const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -145,10 +151,19 @@ __device__ __forceinline__ void stream_chunks(const uint32_t* __restrict__ T, co
     if (g + 32 * SPG < gend) { m0 = __ldg(E + g + 32 * SPG); if (SPG == 2) m1 = __ldg(E + g + 32 * SPG + 32); }
     int64_t c = wb;
     int4 meta = __ldg(p.meta + c * 32 + lane);
-    int steps = p.ng[c] / SPG;
+    int ng_cur = p.ng[c];
+    int steps = ng_cur / SPG;
     int4 meta_next = make_int4(-1, 0, 0, 0);
     int ng_next = 0;
     if (c + 1 < we) { meta_next = __ldg(p.meta + (c + 1) * 32 + lane); ng_next = p.ng[c + 1]; }
+    // the entry block of the next chunk is pulled into L2 one chunk ahead, so
+    // the two-step register prefetch only has to cover L2 latency
+    const char* Eb = reinterpret_cast<const char*>(p.entries);
+    int64_t next_off = g + (int64_t)ng_cur * 32;   // first group of chunk c + 1
+    if (lane == 0) {
+        prefetch_l2(Eb + g * 16, (uint32_t)ng_cur * 512u);
+        if (c + 1 < we) prefetch_l2(Eb + next_off * 16, (uint32_t)ng_next * 512u);
+    }
     SlicedCounter<NP> acc;
     acc.clear();
     for (;;) {
@@ -158,7 +173,12 @@ __device__ __forceinline__ void stream_chunks(const uint32_t* __restrict__ T, co
             if (++c >= we) return;
             meta = meta_next;
             steps = ng_next / SPG;
-            if (c + 1 < we) { meta_next = __ldg(p.meta + (c + 1) * 32 + lane); ng_next = p.ng[c + 1]; }
+            next_off += (int64_t)ng_next * 32;            // first group of chunk c + 1
+            if (c + 1 < we) {
+                meta_next = __ldg(p.meta + (c + 1) * 32 + lane);
+                ng_next = p.ng[c + 1];
+                if (lane == 0) prefetch_l2(Eb + next_off * 16, (uint32_t)ng_next * 512u);
+            }
         }
         const uint4 c0 = n0, c1 = n1;
         n0 = m0;
