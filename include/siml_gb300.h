@@ -154,6 +154,10 @@ int siml_compile_smiles(const char* buf, const int64_t* offsets, int64_t n,
  * stride ld); bin = min((unsigned)(x*100), 100), negatives to bin 0. */
 int siml_row_histogram101(siml_engine* h, const float* data, int64_t rows, int64_t cols,
                           int64_t ld, uint32_t* hist, int where);
+/* The same for an fp64 matrix (the reference accepts float64 too,
+ * pysiml/_cpuutil.cpp:89-101); the product x*100 is formed in fp64. */
+int siml_row_histogram101_f64(siml_engine* h, const double* data, int64_t rows, int64_t cols,
+                              int64_t ld, uint32_t* hist, int where);
 
 /* ---- synthetic workload sets (benchmarks and tests) --------------------- */
 int siml_synth_lengths(uint64_t seed, int dist, int64_t first, int64_t n, int32_t* lens);

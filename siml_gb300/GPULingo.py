@@ -221,6 +221,90 @@ class GPULingo:
         self._leave(out)
         return out
 
+    # ------------------------------------------------------------ histograms
+    def getMultipleHistogrammedRows(self, rowbase, rowlimit):
+        """Per-row 101-bin histograms of rows [rowbase, rowlimit), bins
+        (unsigned)(T*100) (pysiml/GPULingo.py:407-417); int32 [rows, 101]."""
+        self.getMultipleHistogrammedRows_async(rowbase, rowlimit)
+        return self.retrieveAsyncResult()
+
+    def getMultipleHistogrammedRows_async(self, rowbase, rowlimit):
+        """Queues the histograms (pysiml/GPULingo.py:420-463)."""
+        self._check_rows(rowbase, rowlimit)
+        rows = rowlimit - rowbase
+        L = N.lib()
+        if torch is not None:
+            out = torch.empty((rows, 112), dtype=torch.int32, device=self._device())
+            self._enter()
+            if rows:
+                N.check(L.siml_hist101(self._h, int(rowbase), int(rowlimit), out.data_ptr(), 112, N.SIML_DEVICE),
+                        "getMultipleHistogrammedRows")
+        else:
+            out = np.zeros((rows, 112), dtype=np.int32)
+            if rows:
+                N.check(L.siml_hist101(self._h, int(rowbase), int(rowlimit), out.ctypes.data, 112, N.SIML_HOST),
+                        "getMultipleHistogrammedRows")
+        self.last_async_width = 101
+        self._pending = ("matrix", out, 101)
+
+    def getSimilarityHistogram(self, rowbase, rowlimit, out=None):
+        """One 1000-bin histogram of every similarity of rows [rowbase,
+        rowlimit) x all queries, bin min((unsigned)(T*1000), 999); uint64
+        [1000].  Accumulates into *out* when given (numpy or CUDA tensor)."""
+        self._check_rows(rowbase, rowlimit)
+        L = N.lib()
+        if torch is not None and isinstance(out, torch.Tensor) and out.is_cuda:
+            if out.dtype != torch.int64 or out.numel() != 1000:
+                raise ValueError("out must be a CUDA int64 tensor of 1000 elements")
+            self._enter()
+            N.check(L.siml_hist_global(self._h, int(rowbase), int(rowlimit), out.data_ptr(), N.SIML_DEVICE),
+                    "getSimilarityHistogram")
+            self._leave(out)
+            return out
+        host = np.zeros(1000, dtype=np.uint64) if out is None else out
+        if host.dtype != np.uint64 or host.shape != (1000,) or not host.flags.c_contiguous:
+            raise ValueError("out must be a contiguous uint64 array of 1000 elements")
+        self._enter()
+        N.check(L.siml_hist_global(self._h, int(rowbase), int(rowlimit), host.ctypes.data, N.SIML_HOST),
+                "getSimilarityHistogram")
+        return host
+
+    # ----------------------------------------------------------------- top-k
+    def getTopK(self, rowbase, rowlimit, k):
+        """The k most similar queries of each ref row in [rowbase, rowlimit):
+        (indices int32 [rows, k], similarities float32 [rows, k]), best first,
+        ties to the lower query index; rows with fewer than k queries are
+        padded with -1 / -1.0."""
+        self._check_rows(rowbase, rowlimit)
+        rows = rowlimit - rowbase
+        k = int(k)
+        if k < 1:
+            raise ValueError("k must be >= 1")
+        L = N.lib()
+        if torch is not None:
+            idx = torch.empty((rows, k), dtype=torch.int32, device=self._device())
+            sims = torch.empty((rows, k), dtype=torch.float32, device=self._device())
+            self._enter()
+            if rows:
+                N.check(L.siml_topk(self._h, int(rowbase), int(rowlimit), k, idx.data_ptr(), sims.data_ptr(),
+                                    N.SIML_DEVICE), "getTopK")
+            N.check(L.siml_sync(self._h), "siml_sync")
+            return idx.cpu().numpy(), sims.cpu().numpy()
+        idx = np.empty((rows, k), dtype=np.int32)
+        sims = np.empty((rows, k), dtype=np.float32)
+        if rows:
+            N.check(L.siml_topk(self._h, int(rowbase), int(rowlimit), k, idx.ctypes.data, sims.ctypes.data,
+                                N.SIML_HOST), "getTopK")
+        return idx, sims
+
+    def topKDevice(self, rowbase, rowlimit, k, idx, sims):
+        """Top-k into caller CUDA tensors idx int32 [rows, k], sims float32 [rows, k]."""
+        self._check_rows(rowbase, rowlimit)
+        self._enter()
+        N.check(N.lib().siml_topk(self._h, int(rowbase), int(rowlimit), int(k), idx.data_ptr(), sims.data_ptr(),
+                                  N.SIML_DEVICE), "topKDevice")
+        self._leave(idx, sims)
+
     # ------------------------------------------------------------- neighbors
     def getNeighbors(self, rowbase, rowlimit, lowerbound, upperbound=1.1, maxneighbors=None):
         """Query indices with lowerbound <= T < upperbound per ref row

@@ -64,6 +64,7 @@ _SIGNATURES = {
     "siml_compile_width": (_I64, [_P, _P, _I64]),
     "siml_compile_smiles": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _I64]),
     "siml_row_histogram101": (_I32, [_P, _P, _I64, _I64, _I64, _P, _I32]),
+    "siml_row_histogram101_f64": (_I32, [_P, _P, _I64, _I64, _I64, _P, _I32]),
     "siml_synth_lengths": (_I32, [_U64, _I32, _I64, _I64, _P]),
     "siml_synth_smiles": (_I32, [_U64, _I32, _I64, _I64, _P, _I64, _P]),
     "siml_db_stats": (_I32, [_P, _P]),

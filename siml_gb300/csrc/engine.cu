@@ -721,6 +721,113 @@ int siml_neighbors(siml_engine* h, int64_t rowbase, int64_t rowlimit, float lo, 
     return SIML_OK;
 }
 
+static int check_range(siml_engine* h, int64_t rowbase, int64_t rowlimit) {
+    if (rowbase < 0 || rowlimit > h->ref.n || rowlimit < rowbase)
+        return fail(SIML_ERR_RANGE, "row range [%lld, %lld) outside the ref set of %lld rows",
+                    (long long)rowbase, (long long)rowlimit, (long long)h->ref.n);
+    return SIML_OK;
+}
+
+int siml_hist101(siml_engine* h, int64_t rowbase, int64_t rowlimit, int32_t* out, int64_t ldo, int where) {
+    SIML_GUARD(h);
+    int rc;
+    if ((rc = ensure_prepared(h))) return rc;
+    if ((rc = check_range(h, rowbase, rowlimit))) return rc;
+    if (ldo < 101) return fail(SIML_ERR_INVALID, "siml_hist101: row stride %lld < 101", (long long)ldo);
+    const int64_t rows = rowlimit - rowbase;
+    if (rows == 0) return SIML_OK;
+    if (!out) return fail(SIML_ERR_INVALID, "siml_hist101: NULL output");
+    if (where == SIML_DEVICE) return launch_hist(h, rowbase, rowlimit, false, out, ldo);
+    void* buf = nullptr;
+    if ((rc = scratch_reserve(h, (size_t)rows * 101 * 4, &buf))) return rc;
+    if ((rc = launch_hist(h, rowbase, rowlimit, false, buf, 101))) return rc;
+    SIML_CUDA(cudaMemcpy2DAsync(out, ldo * 4, buf, 101 * 4, 101 * 4, rows, cudaMemcpyDefault, h->stream));
+    SIML_CUDA(cudaStreamSynchronize(h->stream));
+    return SIML_OK;
+}
+
+int siml_hist_global(siml_engine* h, int64_t rowbase, int64_t rowlimit, uint64_t* out, int where) {
+    SIML_GUARD(h);
+    int rc;
+    if ((rc = ensure_prepared(h))) return rc;
+    if ((rc = check_range(h, rowbase, rowlimit))) return rc;
+    if (!out) return fail(SIML_ERR_INVALID, "siml_hist_global: NULL output");
+    if (rowlimit == rowbase) return SIML_OK;
+    if (where == SIML_DEVICE) return launch_hist(h, rowbase, rowlimit, true, out, 0);
+    void* buf = nullptr;
+    if ((rc = scratch_reserve(h, 1000 * 8, &buf))) return rc;
+    SIML_CUDA(cudaMemcpyAsync(buf, out, 1000 * 8, cudaMemcpyDefault, h->stream));
+    if ((rc = launch_hist(h, rowbase, rowlimit, true, buf, 0))) return rc;
+    SIML_CUDA(cudaMemcpyAsync(out, buf, 1000 * 8, cudaMemcpyDefault, h->stream));
+    SIML_CUDA(cudaStreamSynchronize(h->stream));
+    return SIML_OK;
+}
+
+static int row_hist_common(siml_engine* h, const void* data, bool f64, int64_t rows, int64_t cols, int64_t ld,
+                           uint32_t* hist, int where) {
+    SIML_GUARD(h);
+    if (rows < 0 || cols < 0 || ld < cols) return fail(SIML_ERR_INVALID, "rowHistogram101: bad shape");
+    if (rows == 0) return SIML_OK;
+    if (!data || !hist) return fail(SIML_ERR_INVALID, "rowHistogram101: NULL array");
+    if (where == SIML_DEVICE) return launch_row_hist101(h, data, f64, rows, cols, ld, hist);
+    const size_t es = f64 ? 8 : 4;
+    const size_t in_bytes = (size_t)rows * cols * es, out_bytes = (size_t)rows * 101 * 4;
+    void* buf = nullptr;
+    int rc;
+    if ((rc = scratch_reserve(h, (in_bytes + 255) / 256 * 256 + out_bytes, &buf))) return rc;
+    char* b = (char*)buf;
+    uint32_t* dh = (uint32_t*)(b + (in_bytes + 255) / 256 * 256);
+    if (cols) SIML_CUDA(cudaMemcpy2DAsync(b, cols * es, data, ld * es, cols * es, rows, cudaMemcpyDefault, h->stream));
+    if ((rc = launch_row_hist101(h, b, f64, rows, cols, cols, dh))) return rc;
+    SIML_CUDA(cudaMemcpyAsync(hist, dh, out_bytes, cudaMemcpyDefault, h->stream));
+    SIML_CUDA(cudaStreamSynchronize(h->stream));
+    return SIML_OK;
+}
+
+int siml_row_histogram101(siml_engine* h, const float* data, int64_t rows, int64_t cols, int64_t ld,
+                          uint32_t* hist, int where) {
+    return row_hist_common(h, data, false, rows, cols, ld, hist, where);
+}
+
+int siml_row_histogram101_f64(siml_engine* h, const double* data, int64_t rows, int64_t cols, int64_t ld,
+                              uint32_t* hist, int where) {
+    return row_hist_common(h, data, true, rows, cols, ld, hist, where);
+}
+
+int siml_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int64_t k, int32_t* idx, float* sims, int where) {
+    SIML_GUARD(h);
+    int rc;
+    if ((rc = ensure_prepared(h))) return rc;
+    if ((rc = check_range(h, rowbase, rowlimit))) return rc;
+    if (k < 1 || k > (1 << 20)) return fail(SIML_ERR_INVALID, "siml_topk: k = %lld out of range", (long long)k);
+    const int64_t rows = rowlimit - rowbase;
+    if (rows == 0) return SIML_OK;
+    if (!idx || !sims) return fail(SIML_ERR_INVALID, "siml_topk: NULL output");
+    int32_t* di = idx;
+    float* ds = sims;
+    const size_t ob = (size_t)rows * k * 4;
+    void* own = nullptr;
+    if (where != SIML_DEVICE) {
+        SIML_CUDA(cudaMallocAsync(&own, 2 * ob, h->stream));
+        di = (int32_t*)own;
+        ds = (float*)((char*)own + ob);
+    }
+    rc = launch_topk(h, rowbase, rowlimit, (int)k, di, ds);
+    int err = 0;
+    if (!rc) {
+        SIML_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        if (where != SIML_DEVICE) {
+            SIML_CUDA(cudaMemcpyAsync(idx, di, ob, cudaMemcpyDefault, h->stream));
+            SIML_CUDA(cudaMemcpyAsync(sims, ds, ob, cudaMemcpyDefault, h->stream));
+        }
+        SIML_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    if (own) cudaFreeAsync(own, h->stream);
+    if (rc) return rc;
+    if (err) return fail(SIML_ERR_TIMEOUT, "siml_topk: a heap lock wait exceeded its bound; result discarded");
+    return SIML_OK;
+}
+
 int siml_row_single(siml_engine* h, int64_t row, float* out, int where) {
     SIML_GUARD(h);
     return rows_common(h, row, row + 1, out, h->qry.n, where, kModeSingle);

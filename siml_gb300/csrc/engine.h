@@ -121,6 +121,15 @@ struct NbrCall {
     int32_t* counts;     // device [rows]
 };
 int launch_neighbors(siml_engine* h, const NbrCall& c);
+// Per-row 101-bin int32 histograms (out [rows, ldo], zeroed here) or one
+// 1000-bin uint64 histogram accumulated into out.
+int launch_hist(siml_engine* h, int64_t rowbase, int64_t rowlimit, bool global, void* out, int64_t ldo);
+// Per-row top-k into idx / sims [rows, k]; a bounded lock wait that expires
+// sets *h->d_err (read back by the caller).
+int launch_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int k, int32_t* idx, float* sims);
+// rowHistogram101 of a dense fp32 / fp64 device matrix into uint32 [rows, 101].
+int launch_row_hist101(siml_engine* h, const void* data, bool f64, int64_t rows, int64_t cols, int64_t ld,
+                       uint32_t* hist);
 
 }  // namespace siml
 

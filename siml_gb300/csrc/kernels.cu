@@ -347,6 +347,295 @@ __global__ void __launch_bounds__(kThreads, 1) k_nbr(const GroupParams p, const 
     stream_chunks<NP, ET>(T, p, wb, we, epi);
 }
 
+// ------------------------------------------------------------- k_hist ----
+// Histograms of all pairs of a row block: per row, 101 bins of
+// (unsigned)(t*100) (getMultipleHistogrammedRows, pysiml/kernels.py:606-666),
+// or one 1000-bin histogram of min((unsigned)(t*1000), 999) for the block.
+// Counts go to shared memory and are flushed with one atomic per bin per CTA.
+constexpr int kBins101 = 101;
+constexpr int kBins1000 = 1000;
+
+// bin of a similarity: (unsigned)(t * scale) clamped to top; the product is
+// one fp32 multiply as in the reference, truncated by a round-toward-zero add
+// of 2^23 (exact floor for 0 <= s < 2^23).
+__device__ __forceinline__ uint32_t bin_fast(float t, float scale, uint32_t top) {
+    const float s = __fmul_rn(t, scale);
+    const uint32_t b = __float_as_uint(__fadd_rz(s, 8388608.0f)) - 0x4B000000u;
+    return b < top ? b : top;
+}
+
+template <int NP, bool GLOBAL>
+struct HistEpi {
+    const RowSmem& rs;
+    int nr;
+    uint32_t* H;   // shared: [32][101] or [1000]
+
+    __device__ __forceinline__ void operator()(int64_t, const int4& meta, const SlicedCounter<NP>& acc) {
+        if (meta.x < 0) return;
+        const int32_t bmag = meta.y;
+        RowCounts<NP> rc;
+        counts_from_planes<NP>(acc, rc);
+        const float scale = GLOBAL ? 1000.0f : 100.0f;
+        const uint32_t top = GLOBAL ? 999u : 100u;
+        if (rs.allfast && fast_mag(bmag, meta.z)) {
+            const float bf = small_int_to_float((uint32_t)bmag);
+#pragma unroll
+            for (int r = 0; r < 32; r++) {
+                if (r < nr) {
+                    const float isf = small_int_to_float(row_count<NP>(rc, r));
+                    const float t = div_small(isf, __fsub_rn(__fadd_rn(rs.amagf[r], bf), isf));
+                    const uint32_t b = bin_fast(t, scale, top);
+                    atomicAdd(H + (GLOBAL ? b : r * kBins101 + b), 1u);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < 32; r++) {
+                if (r < nr) {
+                    const float t = tanimoto_rows((int)row_count<NP>(rc, r), rs.amag[r], bmag);
+                    const uint32_t b = bin_of(__fmul_rn(t, scale), top);
+                    atomicAdd(H + (GLOBAL ? b : r * kBins101 + b), 1u);
+                }
+            }
+        }
+    }
+};
+
+// out: GLOBAL ? uint64 [1000] (accumulated) : int32 [rows, ldo] (zeroed first)
+template <int NP, typename ET, bool GLOBAL>
+__global__ void __launch_bounds__(kThreads, 1) k_hist(const GroupParams p, void* out, int64_t ldo) {
+    extern __shared__ __align__(16) uint32_t T[];
+    __shared__ RowSmem rs;
+    __shared__ uint32_t H[GLOBAL ? kBins1000 : 32 * kBins101];
+    for (int i = threadIdx.x; i < (GLOBAL ? kBins1000 : 32 * kBins101); i += blockDim.x) H[i] = 0u;
+    const int nr = build_table(T, rs, p);   // synchronizes the block
+    int64_t wb, we;
+    warp_range(p, wb, we);
+    HistEpi<NP, GLOBAL> epi{rs, nr, H};
+    stream_chunks<NP, ET>(T, p, wb, we, epi);
+    __syncthreads();
+    if (GLOBAL) {
+        unsigned long long* o = reinterpret_cast<unsigned long long*>(out);
+        for (int i = threadIdx.x; i < kBins1000; i += blockDim.x)
+            if (H[i]) atomicAdd(o + i, (unsigned long long)H[i]);
+    } else {
+        int32_t* o = reinterpret_cast<int32_t*>(out) + (int64_t)blockIdx.x * 32 * ldo;
+        for (int i = threadIdx.x; i < nr * kBins101; i += blockDim.x) {
+            const int r = i / kBins101, b = i - r * kBins101;
+            if (H[i]) atomicAdd(o + (int64_t)r * ldo + b, (int)H[i]);
+        }
+    }
+}
+
+// Merge-path fallback: one thread per pair, global atomics.
+template <bool GLOBAL>
+__global__ void k_hist_merge(const struct RawArgs ra, void* out, int64_t ldo);
+
+// ------------------------------------------------------------- k_topk ----
+// Per-row top-k (k <= kTopkMax): the k largest similarities of each row,
+// ties to the lower query index.  Each CTA keeps, per row, a heap of the k
+// best (t, index) pairs seen in its database slice, ordered worst-first so the
+// root is the row's current k-th best.  The bit-sliced filter uses the lowest
+// root among the 32 rows (it only ever rises, so stale reads are
+// conservative); pairs that pass are checked exactly and inserted under a
+// per-row shared-memory lock whose spin is bounded (on expiry the CTA sets an
+// error word instead of waiting).  Heaps go to a scratch buffer
+// [rows][splits][k] that k_topk_merge reduces per row.
+constexpr int kTopkMax = 256;
+constexpr int kTopkSpinLimit = 1 << 22;
+
+struct TopkSmem {
+    int lock[32];
+    int size[32];
+    float theta[32];
+    int theta_idx[32];
+    int theta_min_bits;   // float bits of the lowest full-heap root, -1.0f until all rows are full
+    int err;
+};
+
+// a is worse than b: lower similarity, or equal similarity and higher index
+__device__ __forceinline__ bool worse(float ta, int ia, float tb, int ib) {
+    return ta < tb || (ta == tb && ia > ib);
+}
+
+__device__ void heap_sift_up(float* ht, int* hi, int i) {
+    while (i > 0) {
+        const int par = (i - 1) >> 1;
+        if (!worse(ht[i], hi[i], ht[par], hi[par])) return;
+        const float tt = ht[i]; ht[i] = ht[par]; ht[par] = tt;
+        const int ti = hi[i]; hi[i] = hi[par]; hi[par] = ti;
+        i = par;
+    }
+}
+
+__device__ void heap_sift_down(float* ht, int* hi, int n) {
+    int i = 0;
+    for (;;) {
+        const int l = 2 * i + 1, r = l + 1;
+        int w = i;
+        if (l < n && worse(ht[l], hi[l], ht[w], hi[w])) w = l;
+        if (r < n && worse(ht[r], hi[r], ht[w], hi[w])) w = r;
+        if (w == i) return;
+        const float tt = ht[i]; ht[i] = ht[w]; ht[w] = tt;
+        const int ti = hi[i]; hi[i] = hi[w]; hi[w] = ti;
+        i = w;
+    }
+}
+
+template <int NP>
+struct TopkEpi {
+    const RowSmem& rs;
+    TopkSmem& ts;
+    float* ht;   // [32][k]
+    int* hi;     // [32][k]
+    int nr;
+    int k;
+
+    __device__ __forceinline__ void operator()(int64_t, const int4& meta, const SlicedCounter<NP>& acc) {
+        const int32_t m = meta.x;
+        if (m < 0) return;
+        const int32_t mb = meta.y;
+        const float tmin = __int_as_float(*(volatile int*)&ts.theta_min_bits);
+        uint32_t th = 0u;
+        if (tmin > 0.0f) {
+            const float sc = tmin / (1.0f + tmin) * (1.0f - 1.0f / 4096.0f);
+            const float thf = floorf(sc * ((float)rs.min_amag + (float)mb));
+            th = thf <= 0.0f ? 0u : (thf >= 4.0e9f ? 0xFFFFFFFFu : (uint32_t)thf);
+        }
+        uint32_t cand = sliced_ge<NP>(acc, th);
+        if (nr < 32) cand &= (1u << nr) - 1u;
+        while (cand) {
+            const int r = __ffs(cand) - 1;
+            cand &= cand - 1u;
+            const float t = tanimoto_rows(sliced_row<NP>(acc, r), rs.amag[r], mb);
+            if (*(volatile int*)&ts.size[r] == k &&
+                !worse(*(volatile float*)&ts.theta[r], *(volatile int*)&ts.theta_idx[r], t, m))
+                continue;
+            int spins = 0;
+            bool got = true;
+            while (atomicCAS(&ts.lock[r], 0, 1) != 0) {
+                if (++spins > kTopkSpinLimit) { got = false; break; }
+                __nanosleep(32);
+            }
+            if (!got) { atomicOr(&ts.err, 1); continue; }
+            __threadfence_block();
+            float* rt = ht + r * k;
+            int* ri = hi + r * k;
+            int n = ts.size[r];
+            if (n < k) {
+                rt[n] = t; ri[n] = m;
+                heap_sift_up(rt, ri, n);
+                ts.size[r] = ++n;
+            } else if (worse(rt[0], ri[0], t, m)) {
+                rt[0] = t; ri[0] = m;
+                heap_sift_down(rt, ri, k);
+            }
+            if (n == k) {
+                ts.theta[r] = rt[0];
+                ts.theta_idx[r] = ri[0];
+                __threadfence_block();
+                float mn = 3.0e38f;
+                for (int q = 0; q < nr; q++) {
+                    const float v = *(volatile int*)&ts.size[q] == k ? *(volatile float*)&ts.theta[q] : -1.0f;
+                    mn = fminf(mn, v);
+                }
+                if (mn >= 0.0f) atomicMax(&ts.theta_min_bits, __float_as_int(mn));
+            }
+            __threadfence_block();
+            atomicExch(&ts.lock[r], 0);
+        }
+    }
+};
+
+// scratch: float t[rows][splits][k] followed by int idx[rows][splits][k]
+template <int NP, typename ET>
+__global__ void __launch_bounds__(kThreads, 1) k_topk(const GroupParams p, int k, float* part_t, int* part_i,
+                                                      int* err) {
+    extern __shared__ __align__(16) uint32_t T[];
+    __shared__ RowSmem rs;
+    __shared__ TopkSmem ts;
+    float* ht = reinterpret_cast<float*>(T + p.vt_words);
+    int* hi = reinterpret_cast<int*>(ht + 32 * k);
+    if (threadIdx.x < 32) {
+        ts.lock[threadIdx.x] = 0;
+        ts.size[threadIdx.x] = 0;
+        ts.theta[threadIdx.x] = -1.0f;
+        ts.theta_idx[threadIdx.x] = 0x7FFFFFFF;
+    }
+    if (threadIdx.x == 0) {
+        ts.theta_min_bits = __float_as_int(-1.0f);
+        ts.err = 0;
+    }
+    const int nr = build_table(T, rs, p);   // synchronizes the block
+    int64_t wb, we;
+    warp_range(p, wb, we);
+    TopkEpi<NP> epi{rs, ts, ht, hi, nr, k};
+    stream_chunks<NP, ET>(T, p, wb, we, epi);
+    __syncthreads();
+    const int splits = gridDim.y;
+    for (int i = threadIdx.x; i < nr * k; i += blockDim.x) {
+        const int r = i / k, j = i - r * k;
+        const int64_t row = (int64_t)blockIdx.x * 32 + r;
+        const int64_t o = (row * splits + blockIdx.y) * k + j;
+        const bool ok = j < ts.size[r];
+        part_t[o] = ok ? ht[r * k + j] : -3.0e38f;
+        part_i[o] = ok ? hi[r * k + j] : -1;
+    }
+    if (threadIdx.x == 0 && ts.err) atomicOr(err, 1);
+}
+
+// One CTA per row: bitonic sort of the row's splits x k partial entries by
+// (similarity descending, index ascending) and the first k written out.
+constexpr int kTopkMergeMax = 8192;
+__global__ void __launch_bounds__(512) k_topk_merge(const float* part_t, const int* part_i, int splits, int k,
+                                                    int32_t* idx, float* sims) {
+    extern __shared__ __align__(16) uint32_t sm[];
+    const int n = splits * k;
+    int N = 1;
+    while (N < n) N <<= 1;
+    float* st = reinterpret_cast<float*>(sm);
+    int* si = reinterpret_cast<int*>(st + N);
+    const int64_t row = blockIdx.x;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        st[i] = i < n ? part_t[row * n + i] : -3.0e38f;
+        si[i] = i < n ? part_i[row * n + i] : -1;
+    }
+    __syncthreads();
+    // "before(a, b)": a ranks before b (invalid entries, index -1, rank last)
+    for (int kk = 2; kk <= N; kk <<= 1) {
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < N; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const bool asc = (i & kk) == 0;
+                    const bool vi = si[i] >= 0, vj = si[ixj] >= 0;
+                    // b_before_a: element ixj ranks before element i
+                    bool ji;
+                    if (vi != vj) ji = vj;
+                    else if (!vi) ji = false;
+                    else ji = worse(st[i], si[i], st[ixj], si[ixj]);
+                    if (ji == asc) {
+                        const float tt = st[i]; st[i] = st[ixj]; st[ixj] = tt;
+                        const int ti = si[i]; si[i] = si[ixj]; si[ixj] = ti;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int j = threadIdx.x; j < k; j += blockDim.x) {
+        const bool ok = j < n && si[j] >= 0;
+        idx[row * k + j] = ok ? si[j] : -1;
+        sims[row * k + j] = ok ? st[j] : -1.0f;
+    }
+}
+
+// Fallback (no table or k > kTopkMax): one CTA per row scans every column
+// with the sorted merge and keeps a k-heap in shared memory under the same
+// bounded lock, then sorts it.
+__global__ void __launch_bounds__(256) k_topk_rowscan(const struct RawArgs ra, int k, int32_t* idx, float* sims,
+                                                      int* err);
+
 // ------------------------------------------------------- k_nbr_finish ----
 struct RawArgs {
     const int32_t *rl, *rc, *rlen, *rmag, *rcmag;
@@ -467,6 +756,98 @@ __global__ void k_rows_merge(const RawArgs ra, float* out, int64_t ldo, int mode
     out[(int64_t)blockIdx.y * ldo + col] = t;
 }
 
+__global__ void __launch_bounds__(256) k_topk_rowscan(const RawArgs ra, int k, int32_t* idx, float* sims,
+                                                      int* err) {
+    extern __shared__ __align__(16) uint32_t sm[];
+    float* ht = reinterpret_cast<float*>(sm);
+    int* hi = reinterpret_cast<int*>(ht + k);
+    __shared__ int lock, size, err_s;
+    if (threadIdx.x == 0) { lock = 0; size = 0; err_s = 0; }
+    __syncthreads();
+    const int64_t r = ra.rowbase + blockIdx.x;
+    const int32_t* a = ra.rl + r * ra.rw;
+    const int32_t* as = ra.rc + r * ra.rw;
+    const int32_t alen = ra.rlen[r], ma = ra.rmag[r];
+    for (int64_t col = threadIdx.x; col < ra.nq; col += blockDim.x) {
+        const int is = merge_isct(a, as, alen, ra.ql + col * ra.qw, ra.qc + col * ra.qw, ra.qlen[col]);
+        const float t = tanimoto_rows(is, ma, ra.qmag[col]);
+        const int m = (int)col;
+        if (*(volatile int*)&size == k && !worse(*(volatile float*)&ht[0], *(volatile int*)&hi[0], t, m)) continue;
+        int spins = 0;
+        bool got = true;
+        while (atomicCAS(&lock, 0, 1) != 0) {
+            if (++spins > kTopkSpinLimit) { got = false; break; }
+            __nanosleep(32);
+        }
+        if (!got) { atomicOr(&err_s, 1); continue; }
+        __threadfence_block();
+        int n = size;
+        if (n < k) {
+            ht[n] = t; hi[n] = m;
+            heap_sift_up(ht, hi, n);
+            size = n + 1;
+        } else if (worse(ht[0], hi[0], t, m)) {
+            ht[0] = t; hi[0] = m;
+            heap_sift_down(ht, hi, k);
+        }
+        __threadfence_block();
+        atomicExch(&lock, 0);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // heap sort into best-first order
+        int n = size;
+        for (int end = n - 1; end > 0; end--) {
+            const float tt = ht[0]; ht[0] = ht[end]; ht[end] = tt;
+            const int ti = hi[0]; hi[0] = hi[end]; hi[end] = ti;
+            heap_sift_down(ht, hi, end);
+        }
+        if (err_s) atomicOr(err, 1);
+    }
+    __syncthreads();
+    // after the sort position 0 holds the best entry
+    for (int j = threadIdx.x; j < k; j += blockDim.x) {
+        const bool ok = j < size;
+        idx[(int64_t)blockIdx.x * k + j] = ok ? hi[j] : -1;
+        sims[(int64_t)blockIdx.x * k + j] = ok ? ht[j] : -1.0f;
+    }
+}
+
+template <bool GLOBAL>
+__global__ void k_hist_merge(const RawArgs ra, void* out, int64_t ldo) {
+    const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t r = ra.rowbase + blockIdx.y;
+    if (col >= ra.nq) return;
+    const int isct = merge_isct(ra.rl + r * ra.rw, ra.rc + r * ra.rw, ra.rlen[r],
+                                ra.ql + col * ra.qw, ra.qc + col * ra.qw, ra.qlen[col]);
+    const float t = tanimoto_rows(isct, ra.rmag[r], ra.qmag[col]);
+    if (GLOBAL) atomicAdd(reinterpret_cast<unsigned long long*>(out) + bin_of(__fmul_rn(t, 1000.0f), 999u), 1ull);
+    else atomicAdd(reinterpret_cast<int32_t*>(out) + (int64_t)blockIdx.y * ldo + bin_of(__fmul_rn(t, 100.0f), 100u), 1);
+}
+
+// rowHistogram101 (pysiml/_cpuutil.cpp:52-72): one CTA per row of a dense
+// matrix, 101 shared bins, bin = (unsigned)(x*100) clamped to 100 (the
+// product in the input's precision), values below zero and NaN to bin 0.
+template <typename F>
+__global__ void k_row_hist101(const F* __restrict__ data, int64_t cols, int64_t ld, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t H[kBins101];
+    for (int i = threadIdx.x; i < kBins101; i += blockDim.x) H[i] = 0u;
+    __syncthreads();
+    const F* row = data + (int64_t)blockIdx.x * ld;
+    for (int64_t c = threadIdx.x; c < cols; c += blockDim.x) {
+        uint32_t b;
+        if (sizeof(F) == 4) {
+            b = bin_of(__fmul_rn((float)row[c], 100.0f), 100u);
+        } else {
+            const double s = __dmul_rn((double)row[c], 100.0);
+            b = !(s >= 0.0) ? 0u : (s >= 100.0 ? 100u : (uint32_t)s);
+        }
+        atomicAdd(H + b, 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kBins101; i += blockDim.x) hist[(int64_t)blockIdx.x * kBins101 + i] = H[i];
+}
+
 // ---------------------------------------------------------- launchers ----
 int planes_needed(int64_t max_count) {
     int b = 0;
@@ -563,7 +944,126 @@ int launch_nbr_t(siml_engine* h, const GroupParams& p, size_t smem, const NbrArg
     return SIML_OK;
 }
 
+template <int NP, typename ET, bool GLOBAL>
+int launch_hist_t(siml_engine* h, const GroupParams& p, size_t smem, void* out, int64_t ldo) {
+    const int64_t groups = (p.rows + 31) / 32;
+    int rc = set_smem(k_hist<NP, ET, GLOBAL>, smem);
+    if (rc) return rc;
+    const int s = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
+    dim3 grid((unsigned)groups, (unsigned)s);
+    SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+    k_hist<NP, ET, GLOBAL><<<grid, kThreads, smem, h->stream>>>(p, out, ldo);
+    SIML_CUDA(cudaGetLastError());
+    SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+    h->timed = true;
+    h->launches++;
+    return SIML_OK;
+}
+
+template <int NP, typename ET>
+int launch_topk_t(siml_engine* h, const GroupParams& p, size_t smem, int k, int splits, float* pt, int* pi) {
+    const int64_t groups = (p.rows + 31) / 32;
+    int rc = set_smem(k_topk<NP, ET>, smem);
+    if (rc) return rc;
+    dim3 grid((unsigned)groups, (unsigned)splits);
+    SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+    k_topk<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, k, pt, pi, h->d_err);
+    SIML_CUDA(cudaGetLastError());
+    SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+    h->timed = true;
+    h->launches++;
+    return SIML_OK;
+}
+
 }  // namespace
+
+int launch_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int k, int32_t* idx, float* sims) {
+    const DbLayout* d = nullptr;
+    int rc = ensure_layout(h, true, &d);
+    if (rc) return rc;
+    const int64_t rows = rowlimit - rowbase;
+    SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+    GroupParams p;
+    size_t smem = 0;
+    int np = 0;
+    const size_t heap_bytes = (size_t)32 * k * 8;
+    if (k <= kTopkMax && table_params(h, d, rowbase, rows, kModeRows, p, smem, np) &&
+        smem + heap_bytes + sizeof(RowSmem) + sizeof(TopkSmem) + 64 <= h->smem_optin) {
+        const int64_t groups = (rows + 31) / 32;
+        int splits = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
+        while (splits > 1 && (int64_t)splits * k > kTopkMergeMax) splits--;
+        const size_t part = (size_t)rows * splits * k;
+        void* buf = nullptr;
+        if ((rc = scratch_reserve(h, part * 8, &buf))) return rc;
+        float* pt = reinterpret_cast<float*>(buf);
+        int* pi = reinterpret_cast<int*>(pt + part);
+        const size_t sm = smem + heap_bytes;
+        const bool u16 = d->entry_bytes == 2;
+        if (np == 8) rc = u16 ? launch_topk_t<8, uint16_t>(h, p, sm, k, splits, pt, pi) : launch_topk_t<8, uint32_t>(h, p, sm, k, splits, pt, pi);
+        else rc = u16 ? launch_topk_t<16, uint16_t>(h, p, sm, k, splits, pt, pi) : launch_topk_t<16, uint32_t>(h, p, sm, k, splits, pt, pi);
+        if (rc) return rc;
+        int N = 1;
+        while (N < splits * k) N <<= 1;
+        const size_t msm = (size_t)N * 8;
+        if ((rc = set_smem(k_topk_merge, msm))) return rc;
+        k_topk_merge<<<(unsigned)rows, 512, msm, h->stream>>>(pt, pi, splits, k, idx, sims);
+        SIML_CUDA(cudaGetLastError());
+        h->launches++;
+    } else {
+        if ((size_t)k * 8 + 64 > h->smem_optin) return fail(SIML_ERR_UNSUPPORTED, "top-k: k = %d too large", k);
+        const size_t sm = (size_t)k * 8;
+        if ((rc = set_smem(k_topk_rowscan, sm))) return rc;
+        SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+        k_topk_rowscan<<<(unsigned)rows, 256, sm, h->stream>>>(raw_args(h, rowbase), k, idx, sims, h->d_err);
+        SIML_CUDA(cudaGetLastError());
+        SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+        h->timed = true;
+        h->launches++;
+    }
+    return SIML_OK;
+}
+
+int launch_hist(siml_engine* h, int64_t rowbase, int64_t rowlimit, bool global, void* out, int64_t ldo) {
+    const DbLayout* d = nullptr;
+    int rc = ensure_layout(h, true, &d);
+    if (rc) return rc;
+    const int64_t rows = rowlimit - rowbase;
+    if (!global) SIML_CUDA(cudaMemset2DAsync(out, ldo * 4, 0, kBins101 * 4, rows, h->stream));
+    GroupParams p;
+    size_t smem = 0;
+    int np = 0;
+    if (table_params(h, d, rowbase, rows, kModeRows, p, smem, np) &&
+        smem + (global ? kBins1000 : 32 * kBins101) * 4 + sizeof(RowSmem) + 64 <= h->smem_optin) {
+        const bool u16 = d->entry_bytes == 2;
+        if (global) {
+            if (np == 8) return u16 ? launch_hist_t<8, uint16_t, true>(h, p, smem, out, ldo) : launch_hist_t<8, uint32_t, true>(h, p, smem, out, ldo);
+            return u16 ? launch_hist_t<16, uint16_t, true>(h, p, smem, out, ldo) : launch_hist_t<16, uint32_t, true>(h, p, smem, out, ldo);
+        }
+        if (np == 8) return u16 ? launch_hist_t<8, uint16_t, false>(h, p, smem, out, ldo) : launch_hist_t<8, uint32_t, false>(h, p, smem, out, ldo);
+        return u16 ? launch_hist_t<16, uint16_t, false>(h, p, smem, out, ldo) : launch_hist_t<16, uint32_t, false>(h, p, smem, out, ldo);
+    }
+    if (rows > 65535) return fail(SIML_ERR_UNSUPPORTED, "merge path: more than 65535 rows per call");
+    dim3 grid((unsigned)((h->qry.n + 255) / 256), (unsigned)rows);
+    SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+    if (global) k_hist_merge<true><<<grid, 256, 0, h->stream>>>(raw_args(h, rowbase), out, ldo);
+    else k_hist_merge<false><<<grid, 256, 0, h->stream>>>(raw_args(h, rowbase), out, ldo);
+    SIML_CUDA(cudaGetLastError());
+    SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+    h->timed = true;
+    h->launches++;
+    return SIML_OK;
+}
+
+int launch_row_hist101(siml_engine* h, const void* data, bool f64, int64_t rows, int64_t cols, int64_t ld,
+                       uint32_t* hist) {
+    if (rows == 0) return SIML_OK;
+    if (rows > 0x7FFFFFFF) return fail(SIML_ERR_UNSUPPORTED, "rowHistogram101: too many rows");
+    if (f64) k_row_hist101<double><<<(unsigned)rows, 256, 0, h->stream>>>((const double*)data, cols, ld, hist);
+    else k_row_hist101<float><<<(unsigned)rows, 256, 0, h->stream>>>((const float*)data, cols, ld, hist);
+    SIML_CUDA(cudaGetLastError());
+    h->launches++;
+    return SIML_OK;
+}
 
 int launch_rows(siml_engine* h, const RowsArgs& a) {
     const DbLayout* d = nullptr;
