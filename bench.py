@@ -37,6 +37,10 @@ DB_N = 1_000_000
 QUERY_N = 10_240
 BLOCK = 1024
 METRIC = "LINGO Tanimoto Gpairs/s bit-exact"
+TOPK_WORKLOAD = ("topk_1m: top-100 per row (ties to lower index), 1,024-row blocks x 1,000,000-molecule "
+                 "database")
+HIST_WORKLOAD = ("hist_1m: 1000-bin uint64 histogram of every similarity, 1,024-row blocks x 1,000,000-molecule "
+                 "database")
 NBR_WORKLOAD = ("nbr_1m: getNeighbors T >= 0.7 (indices + fp32 similarities, pitch 1,024), 1,024-row blocks x "
                 "1,000,000-molecule database (lognormal median 45 chars)")
 WORKLOAD = ("rows_1m: getMultipleRows, 1,024-row blocks x 1,000,000-molecule database "
@@ -218,18 +222,27 @@ def gpu_arm(args):
         b = (k * world + rank) % nblocks
         return b * rows_step, (b + 1) * rows_step
 
-    nbr = args.workload == "nbr_1m"
-    if nbr:
+    wl = args.workload
+    nbr = wl == "nbr_1m"
+    fused = wl != "rows_1m"
+    if fused:
         del out
-        pitch = 1024
+        out = None
+        pitch, topk_k = 1024, 100
         nb_idx = torch.empty((rows_step, pitch), dtype=torch.int32, device=dev)
         nb_sims = torch.empty((rows_step, pitch), dtype=torch.float32, device=dev)
         nb_cnt = torch.empty(rows_step, dtype=torch.int32, device=dev)
-        out = None
+        tk_idx = torch.empty((rows_step, topk_k), dtype=torch.int32, device=dev)
+        tk_sims = torch.empty((rows_step, topk_k), dtype=torch.float32, device=dev)
+        hist = torch.zeros(1000, dtype=torch.int64, device=dev)
 
     def run_step(r0, r1):
-        if nbr:
+        if wl == "nbr_1m":
             gl.neighborsDevice(r0, r1, 0.7, 1.1, pitch, nb_idx, nb_sims, nb_cnt)
+        elif wl == "topk_1m":
+            gl.topKDevice(r0, r1, topk_k, tk_idx, tk_sims)
+        elif wl == "hist_1m":
+            gl.getSimilarityHistogram(r0, r1, out=hist)
         else:
             gl.getMultipleRowsDevice(r0, r1, out=out)
 
@@ -279,6 +292,12 @@ def gpu_arm(args):
         gi = nb_idx[:4].cpu().numpy()
         parity = bool(np.array_equal(gc, oc) and all(
             np.array_equal(gi[i, :min(gc[i], pitch)], oi[i, :min(oc[i], pitch)]) for i in range(4)))
+    elif wl == "topk_1m":
+        oi, os_ = O.topk_block(q, db, r0, r0 + 2, topk_k, nthreads=os.cpu_count() or 1)
+        parity = bool(np.array_equal(tk_idx[:2].cpu().numpy(), oi) and np.array_equal(tk_sims[:2].cpu().numpy(), os_))
+    elif wl == "hist_1m":
+        # histogram total: every pair of every step (warm-up included) counted once
+        parity = int(hist.sum().item()) == (args.warmup + args.steps) * pairs_per_step
     else:
         got = out[:2].cpu().numpy()
         want = O.tanimoto_block(q, db, r0, r0 + 2, nthreads=os.cpu_count() or 1)
@@ -286,7 +305,7 @@ def gpu_arm(args):
 
     # roofline of the dominant kernel (k_rows): algorithmic bytes per launch
     kms = statistics.mean(kernel_ms)
-    out_bytes = 0 if nbr else pairs_per_step * 4
+    out_bytes = 0 if fused else pairs_per_step * 4
     db_bytes = stats["ngroups_total"] * 16 + stats["nchunks"] * 32 * 8 + stats["nchunks"] * 12
     alg_bytes = out_bytes + db_bytes
     achieved = alg_bytes / (kms / 1e3) / 1e9
@@ -298,13 +317,14 @@ def gpu_arm(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     traffic = read_profile_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": "k_nbr" if nbr else "k_rows", "kernel_ms": kms,
+                "traffic": traffic, "kernel": {"rows_1m": "k_rows", "nbr_1m": "k_nbr", "topk_1m": "k_topk",
+                                               "hist_1m": "k_hist"}[wl], "kernel_ms": kms,
                 "algorithmic_bytes_per_launch": alg_bytes,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback"}
 
     e2e = None
     cpu = None
-    if rank == 0 and not args.no_extras and not nbr:
+    if rank == 0 and not args.no_extras and not fused:
         e2e = measure_e2e(gl, q, stream, dev, steps=min(3, args.steps))
         if world == 1:
             cpu = cpu_reference_rate(db, q)
@@ -313,7 +333,8 @@ def gpu_arm(args):
             "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded SMILES-like strings)",
-            "config": {"workload": WORKLOAD if not nbr else NBR_WORKLOAD, "rows_per_step": rows_step, "db_molecules": DB_N,
+            "config": {"workload": {"rows_1m": WORKLOAD, "nbr_1m": NBR_WORKLOAD, "topk_1m": TOPK_WORKLOAD,
+                                    "hist_1m": HIST_WORKLOAD}[wl], "rows_per_step": rows_step, "db_molecules": DB_N,
                        "query_rows": QUERY_N, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "flushed between steps by a 256 MB write; each step also writes a 4 GB block",
                        "db_layout": stats},
@@ -378,8 +399,9 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--rows-per-step", type=int, default=BLOCK,
                     help="rows per block (smaller blocks for profiler captures)")
-    ap.add_argument("--workload", choices=["rows_1m", "nbr_1m"], default="rows_1m",
-                    help="rows_1m: getMultipleRows blocks (default); nbr_1m: getNeighbors blocks at T >= 0.7")
+    ap.add_argument("--workload", choices=["rows_1m", "nbr_1m", "topk_1m", "hist_1m"], default="rows_1m",
+                    help="rows_1m: getMultipleRows blocks (default); nbr_1m: getNeighbors at T >= 0.7; "
+                         "topk_1m: top-100 per row; hist_1m: 1000-bin histogram of every pair")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the end-to-end and CPU-baseline legs (profiler runs)")
     args = ap.parse_args()

@@ -25,19 +25,77 @@ int cuda_fail(cudaError_t e, const char* what) {
     return fail(code, "CUDA error in %s: %s", what, cudaGetErrorString(e));
 }
 
-int scratch_reserve(siml_engine* h, size_t bytes, void** out) {
-    if (bytes > h->scratch_bytes) {
-        if (h->scratch) {
+int scratch_reserve(siml_engine* h, size_t bytes, void** out, int slot) {
+    if (bytes > h->scratch_bytes[slot]) {
+        if (h->scratch[slot]) {
             SIML_CUDA(cudaStreamSynchronize(h->stream));
-            SIML_CUDA(cudaFree(h->scratch));
-            h->scratch = nullptr;
-            h->scratch_bytes = 0;
+            SIML_CUDA(cudaFree(h->scratch[slot]));
+            h->scratch[slot] = nullptr;
+            h->scratch_bytes[slot] = 0;
         }
-        size_t want = std::max(bytes, (size_t)1 << 20);
-        SIML_CUDA(cudaMalloc(&h->scratch, want));
-        h->scratch_bytes = want;
+        size_t want = std::max(bytes, (size_t)1 << 16);
+        SIML_CUDA(cudaMalloc(&h->scratch[slot], want));
+        h->scratch_bytes[slot] = want;
     }
-    *out = h->scratch;
+    *out = h->scratch[slot];
+    return SIML_OK;
+}
+
+namespace {
+constexpr int kOrderBuckets = 4096;
+
+// Counting sort of rows by min(magnitude, 4095): bucket sizes ...
+__global__ void k_order_count(const int32_t* __restrict__ mag, int64_t rowbase, int64_t rows, int32_t* bucket) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < rows) atomicAdd(bucket + min(max(mag[rowbase + i], 0), kOrderBuckets - 1), 1);
+}
+// ... exclusive prefix over the buckets (one block) ...
+__global__ void k_order_scan(int32_t* bucket) {
+    __shared__ int32_t part[1024];
+    const int t = threadIdx.x;
+    int32_t v[4], s = 0;
+    for (int j = 0; j < 4; j++) { v[j] = bucket[4 * t + j]; s += v[j]; }
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int32_t x = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += x;
+        __syncthreads();
+    }
+    int32_t run = part[t] - s;
+    for (int j = 0; j < 4; j++) { bucket[4 * t + j] = run; run += v[j]; }
+}
+// ... and placement (order inside a bucket is arbitrary; every row's result
+// is independent of the grouping).
+__global__ void k_order_scatter(const int32_t* __restrict__ mag, int64_t rowbase, int64_t rows, int32_t* bucket,
+                                int32_t* order) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < rows) {
+        const int pos = atomicAdd(bucket + min(max(mag[rowbase + i], 0), kOrderBuckets - 1), 1);
+        order[pos] = (int32_t)(rowbase + i);
+    }
+}
+}  // namespace
+
+int row_order_by_magnitude(siml_engine* h, int64_t rowbase, int64_t rowlimit, const int32_t** order) {
+    const int64_t rows = rowlimit - rowbase;
+    void* ob = nullptr;
+    void* bb = nullptr;
+    int rc;
+    if ((rc = scratch_reserve(h, (size_t)std::max<int64_t>(rows, 1) * 4, &ob, kSlotOrder))) return rc;
+    if ((rc = scratch_reserve(h, kOrderBuckets * 4, &bb, kSlotSmall))) return rc;
+    int32_t* bucket = (int32_t*)bb;
+    SIML_CUDA(cudaMemsetAsync(bucket, 0, kOrderBuckets * 4, h->stream));
+    if (rows > 0) {
+        const unsigned g = (unsigned)((rows + 255) / 256);
+        k_order_count<<<g, 256, 0, h->stream>>>(h->ref.mag, rowbase, rows, bucket);
+        k_order_scan<<<1, 1024, 0, h->stream>>>(bucket);
+        k_order_scatter<<<g, 256, 0, h->stream>>>(h->ref.mag, rowbase, rows, bucket, (int32_t*)ob);
+        h->launches += 3;
+        SIML_CUDA(cudaGetLastError());
+    }
+    *order = (const int32_t*)ob;
     return SIML_OK;
 }
 
@@ -581,7 +639,8 @@ int siml_destroy(siml_engine* h) {
     free_layout(h->db_nat);
     free_layout(h->db_sorted);
     free_rows(h->rows);
-    if (h->scratch) cudaFree(h->scratch);
+    for (int i = 0; i < 4; i++)
+        if (h->scratch[i]) cudaFree(h->scratch[i]);
     if (h->d_err) cudaFree(h->d_err);
     if (h->d_counter) cudaFree(h->d_counter);
     if (h->ev0) cudaEventDestroy(h->ev0);

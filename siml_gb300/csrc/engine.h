@@ -83,9 +83,9 @@ struct siml_engine {
     siml::DbLayout db_nat, db_sorted;
     bool nat_valid = false, sorted_valid = false;
     siml::RowEntries rows;
-    // device scratch reused across calls
-    void* scratch = nullptr;
-    size_t scratch_bytes = 0;
+    // device scratch reused across calls, one buffer per purpose (siml::kSlot*)
+    void* scratch[4] = {nullptr, nullptr, nullptr, nullptr};
+    size_t scratch_bytes[4] = {0, 0, 0, 0};
     int* d_err = nullptr;                 // device error word
     unsigned long long* d_counter = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -99,7 +99,16 @@ namespace siml {
 int ensure_prepared(siml_engine* h);
 // Natural-order (sorted == false) or window-sorted database layout.
 int ensure_layout(siml_engine* h, bool sorted, const DbLayout** out);
-int scratch_reserve(siml_engine* h, size_t bytes, void** out);
+// Scratch slots: host-call staging, per-call row order, top-k partial heaps,
+// small counters.
+constexpr int kSlotStage = 0;
+constexpr int kSlotOrder = 1;
+constexpr int kSlotPartial = 2;
+constexpr int kSlotSmall = 3;
+int scratch_reserve(siml_engine* h, size_t bytes, void** out, int slot = kSlotStage);
+// Rows [rowbase, rowlimit) of the ref set ordered by magnitude (absolute row
+// indices, device array of rowlimit - rowbase entries, in kSlotOrder).
+int row_order_by_magnitude(siml_engine* h, int64_t rowbase, int64_t rowlimit, const int32_t** order);
 int cuda_fail(cudaError_t e, const char* what);
 
 // kernels.cu — launchers; all queue work on h->stream and return a status.

@@ -63,6 +63,7 @@ struct GroupParams {
     const int32_t* row_len;
     int64_t rowbase;
     int rows;
+    const int32_t* row_order;   // absolute row of group position i, or null for rowbase + i
     // database layout
     const void* entries;
     const int64_t* off;
@@ -76,6 +77,7 @@ struct GroupParams {
 struct RowSmem {
     int amag[32];
     int alen[32];
+    int orow[32];            // output row (relative to rowbase) of group row r
     __align__(16) float amagf[32];
     int allfast;
     int min_amag;
@@ -92,7 +94,8 @@ __device__ __forceinline__ int build_table(uint32_t* T, RowSmem& rs, const Group
         *reinterpret_cast<uint4*>(T + i) = make_uint4(0u, 0u, 0u, 0u);
     if (warp == 0) {
         const int r = lane;
-        const int64_t gr = p.rowbase + row0 + r;
+        const int64_t gr = r < nr ? (p.row_order ? (int64_t)p.row_order[row0 + r] : p.rowbase + row0 + r) : p.rowbase;
+        rs.orow[r] = (int)(gr - p.rowbase);
         const int am = r < nr ? (p.mode == kModeSingle ? p.row_cmag[gr] : p.row_mag[gr]) : 0;
         rs.amag[r] = am;
         rs.amagf[r] = (float)am;
@@ -108,7 +111,7 @@ __device__ __forceinline__ int build_table(uint32_t* T, RowSmem& rs, const Group
     }
     __syncthreads();
     for (int r = warp; r < nr; r += nwarps) {
-        const uint32_t* rv = p.row_vid + (p.rowbase + row0 + r) * p.row_stride;
+        const uint32_t* rv = p.row_vid + (int64_t)(p.rowbase + rs.orow[r]) * p.row_stride;
         for (int64_t e = lane; e < p.row_stride; e += 32) {
             const uint32_t v = rv[e];
             if (v) atomicOr(&T[v], 1u << r);
@@ -326,7 +329,7 @@ struct NbrEpi {
             const int is = sliced_row<NP>(acc, r);
             float t;
             if (!neighbor_test(is, rs.amag[r], mb, a.lo, a.hi, t)) continue;
-            const int64_t row = row0 + r;
+            const int64_t row = rs.orow[r];
             const int pos = atomicAdd(a.counts + row, 1);
             if (pos < a.pitch) {
                 a.idx[row * a.pitch + pos] = m;
@@ -419,10 +422,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_hist(const GroupParams p, void*
         for (int i = threadIdx.x; i < kBins1000; i += blockDim.x)
             if (H[i]) atomicAdd(o + i, (unsigned long long)H[i]);
     } else {
-        int32_t* o = reinterpret_cast<int32_t*>(out) + (int64_t)blockIdx.x * 32 * ldo;
+        int32_t* o = reinterpret_cast<int32_t*>(out);
         for (int i = threadIdx.x; i < nr * kBins101; i += blockDim.x) {
             const int r = i / kBins101, b = i - r * kBins101;
-            if (H[i]) atomicAdd(o + (int64_t)r * ldo + b, (int)H[i]);
+            if (H[i]) atomicAdd(o + (int64_t)rs.orow[r] * ldo + b, (int)H[i]);
         }
     }
 }
@@ -434,22 +437,26 @@ __global__ void k_hist_merge(const struct RawArgs ra, void* out, int64_t ldo);
 // ------------------------------------------------------------- k_topk ----
 // Per-row top-k (k <= kTopkMax): the k largest similarities of each row,
 // ties to the lower query index.  Each CTA keeps, per row, a heap of the k
-// best (t, index) pairs seen in its database slice, ordered worst-first so the
-// root is the row's current k-th best.  The bit-sliced filter uses the lowest
-// root among the 32 rows (it only ever rises, so stale reads are
-// conservative); pairs that pass are checked exactly and inserted under a
-// per-row shared-memory lock whose spin is bounded (on expiry the CTA sets an
-// error word instead of waiting).  Heaps go to a scratch buffer
-// [rows][splits][k] that k_topk_merge reduces per row.
+// best (t, index) pairs of its database slice, worst first, so the root is
+// the row's current k-th best; the root's (t, index) is also published as one
+// 64-bit word (never torn, only rising) with the coefficient of a
+// conservative integer test.  Warp 0 first fills the heaps from the slice's
+// first chunks with no locks (lane r owns row r, values reach it through a
+// shared-memory transpose); then every warp streams the rest, tests each pair
+// against its own row's threshold, computes the exact similarity only for
+// pairs that pass, and inserts under a per-row lock whose spin is bounded (on
+// expiry the CTA sets an error word instead of waiting).  Heaps go to a
+// scratch buffer [rows][splits][k] that k_topk_merge reduces per row.
 constexpr int kTopkMax = 256;
 constexpr int kTopkSpinLimit = 1 << 22;
 
 struct TopkSmem {
     int lock[32];
     int size[32];
-    float theta[32];
-    int theta_idx[32];
-    int theta_min_bits;   // float bits of the lowest full-heap root, -1.0f until all rows are full
+    unsigned long long root[32];   // (float bits of t) << 32 | index of the k-th best, 0 until full
+    float coef[32];                 // t >= root.t implies isct >= coef * (magA + magB)
+    int coef_min_bits;              // float bits of the lowest coef once every heap is full
+    float stage_t[32][33];          // warm-up transpose: [lane][row]
     int err;
 };
 
@@ -482,68 +489,157 @@ __device__ void heap_sift_down(float* ht, int* hi, int n) {
     }
 }
 
+// Inserts (t, m) into row r's heap; caller holds row r (lock or ownership).
+// Publishes the new k-th best when the heap is full.
+__device__ __forceinline__ void heap_offer(TopkSmem& ts, float* ht, int* hi, int k, int r, float t, int m) {
+    float* rt = ht + r * k;
+    int* ri = hi + r * k;
+    int n = ts.size[r];
+    if (n < k) {
+        rt[n] = t; ri[n] = m;
+        heap_sift_up(rt, ri, n);
+        ts.size[r] = ++n;
+    } else if (worse(rt[0], ri[0], t, m)) {
+        rt[0] = t; ri[0] = m;
+        heap_sift_down(rt, ri, k);
+    } else {
+        return;
+    }
+    if (n == k) {
+        const float th = rt[0];
+        ts.coef[r] = th > 0.0f ? th / (1.0f + th) * (1.0f - 1.0f / 4096.0f) : 0.0f;
+        __threadfence_block();
+        *(volatile unsigned long long*)&ts.root[r] =
+            ((unsigned long long)__float_as_uint(th) << 32) | (unsigned long long)(uint32_t)ri[0];
+    }
+}
+
+// Raises the lowest-coefficient word from the rows' current coefficients
+// (0 while a heap is not full).  Coefficients only rise, so racing updates
+// leave a valid lower bound.
+__device__ __forceinline__ void update_coef_min(TopkSmem& ts, int nr) {
+    float mn = 3.0e38f;
+    for (int q = 0; q < nr; q++) {
+        const float cq = *(volatile unsigned long long*)&ts.root[q] == 0ull ? 0.0f : *(volatile float*)&ts.coef[q];
+        mn = fminf(mn, cq);
+    }
+    if (mn > 0.0f) atomicMax(&ts.coef_min_bits, __float_as_int(mn));
+}
+
+__device__ __forceinline__ bool beats_root(unsigned long long root, float t, int m) {
+    if (root == 0ull) return true;   // heap not full yet
+    return worse(__uint_as_float((uint32_t)(root >> 32)), (int)(uint32_t)root, t, m);
+}
+
+// Warm-up: every pair of a chunk, inserted by the lane that owns the row.
+template <int NP>
+struct TopkWarmEpi {
+    const RowSmem& rs;
+    TopkSmem& ts;
+    float* ht;
+    int* hi;
+    int nr, k;
+
+    __device__ __forceinline__ void operator()(int64_t, const int4& meta, const SlicedCounter<NP>& acc) {
+        const int lane = threadIdx.x & 31;
+        RowCounts<NP> rc;
+        counts_from_planes<NP>(acc, rc);
+#pragma unroll
+        for (int r = 0; r < 32; r++)
+            ts.stage_t[lane][r] = meta.x >= 0 && r < nr ? tanimoto_rows((int)row_count<NP>(rc, r), rs.amag[r], meta.y)
+                                                        : 0.0f;
+        __syncwarp();
+        for (int s = 0; s < 32; s++) {
+            const int m = __shfl_sync(0xFFFFFFFFu, meta.x, s);
+            if (m >= 0 && lane < nr) heap_offer(ts, ht, hi, k, lane, ts.stage_t[s][lane], m);
+        }
+        __syncwarp();
+    }
+};
+
+// Main phase.  A lane first compares all 32 counts, bit-sliced, against
+// the threshold implied by the lowest row coefficient, then each remaining
+// row against its own bound and k-th best, giving a per-lane row mask; the
+// warp skips the chunk when no lane has a candidate.  Rows with candidates
+// are visited in an order rotated by warp id (so warps do not queue on the
+// same lock); per row one lane takes the lock for the whole warp and the
+// passing lanes insert in turn.
 template <int NP>
 struct TopkEpi {
     const RowSmem& rs;
     TopkSmem& ts;
-    float* ht;   // [32][k]
-    int* hi;     // [32][k]
-    int nr;
-    int k;
+    float* ht;
+    int* hi;
+    int nr, k;
 
     __device__ __forceinline__ void operator()(int64_t, const int4& meta, const SlicedCounter<NP>& acc) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         const int32_t m = meta.x;
-        if (m < 0) return;
         const int32_t mb = meta.y;
-        const float tmin = __int_as_float(*(volatile int*)&ts.theta_min_bits);
+        const float mbf = (float)mb;
         uint32_t th = 0u;
-        if (tmin > 0.0f) {
-            const float sc = tmin / (1.0f + tmin) * (1.0f - 1.0f / 4096.0f);
-            const float thf = floorf(sc * ((float)rs.min_amag + (float)mb));
+        const float cmin = __int_as_float(*(volatile int*)&ts.coef_min_bits);
+        if (cmin > 0.0f) {
+            const float thf = floorf(cmin * ((float)rs.min_amag + mbf));
             th = thf <= 0.0f ? 0u : (thf >= 4.0e9f ? 0xFFFFFFFFu : (uint32_t)thf);
         }
-        uint32_t cand = sliced_ge<NP>(acc, th);
+        uint32_t cand = m >= 0 ? sliced_ge<NP>(acc, th) : 0u;
         if (nr < 32) cand &= (1u << nr) - 1u;
-        while (cand) {
-            const int r = __ffs(cand) - 1;
-            cand &= cand - 1u;
-            const float t = tanimoto_rows(sliced_row<NP>(acc, r), rs.amag[r], mb);
-            if (*(volatile int*)&ts.size[r] == k &&
-                !worse(*(volatile float*)&ts.theta[r], *(volatile int*)&ts.theta_idx[r], t, m))
-                continue;
-            int spins = 0;
-            bool got = true;
-            while (atomicCAS(&ts.lock[r], 0, 1) != 0) {
-                if (++spins > kTopkSpinLimit) { got = false; break; }
-                __nanosleep(32);
-            }
-            if (!got) { atomicOr(&ts.err, 1); continue; }
-            __threadfence_block();
-            float* rt = ht + r * k;
-            int* ri = hi + r * k;
-            int n = ts.size[r];
-            if (n < k) {
-                rt[n] = t; ri[n] = m;
-                heap_sift_up(rt, ri, n);
-                ts.size[r] = ++n;
-            } else if (worse(rt[0], ri[0], t, m)) {
-                rt[0] = t; ri[0] = m;
-                heap_sift_down(rt, ri, k);
-            }
-            if (n == k) {
-                ts.theta[r] = rt[0];
-                ts.theta_idx[r] = ri[0];
-                __threadfence_block();
-                float mn = 3.0e38f;
-                for (int q = 0; q < nr; q++) {
-                    const float v = *(volatile int*)&ts.size[q] == k ? *(volatile float*)&ts.theta[q] : -1.0f;
-                    mn = fminf(mn, v);
+        if (!__any_sync(0xFFFFFFFFu, cand != 0u)) return;
+        RowCounts<NP> rc;
+        counts_from_planes<NP>(acc, rc);
+        uint32_t pm = 0u;   // rows whose pair may enter the heap
+#pragma unroll
+        for (int r = 0; r < 32; r++) {
+            if ((cand >> r) & 1u) {
+                const uint32_t is = row_count<NP>(rc, r);
+                const float coef = *(volatile float*)&ts.coef[r];
+                if (!((float)is < coef * (rs.amagf[r] + mbf))) {
+                    const float t = tanimoto_rows((int)is, rs.amag[r], mb);
+                    if (beats_root(*(volatile unsigned long long*)&ts.root[r], t, m)) pm |= 1u << r;
                 }
-                if (mn >= 0.0f) atomicMax(&ts.theta_min_bits, __float_as_int(mn));
             }
-            __threadfence_block();
-            atomicExch(&ts.lock[r], 0);
         }
+        const uint32_t rows_any = __reduce_or_sync(0xFFFFFFFFu, pm);
+        if (rows_any == 0u) return;
+        const uint32_t rot = (rows_any >> (warp & 31)) | (warp & 31 ? rows_any << (32 - (warp & 31)) : 0u);
+        uint32_t left = rot;
+        bool changed = false;
+        while (left) {
+            const int j = __ffs(left) - 1;
+            left &= left - 1u;
+            const int r = (j + warp) & 31;
+            const bool pass = (pm >> r) & 1u;
+            float t = 0.0f;
+            if (pass) t = tanimoto_rows((int)row_count_dyn<NP>(rc, r), rs.amag[r], mb);
+            const unsigned b = __ballot_sync(0xFFFFFFFFu, pass);
+            const int leader = __ffs(b) - 1;
+            int got = 1;
+            if (lane == leader) {
+                int spins = 0;
+                while (atomicCAS(&ts.lock[r], 0, 1) != 0) {
+                    if (++spins > kTopkSpinLimit) { got = 0; break; }
+                }
+                if (!got) atomicOr(&ts.err, 1);
+                __threadfence_block();
+            }
+            got = __shfl_sync(0xFFFFFFFFu, got, leader);
+            if (got) {
+                unsigned rest = b;
+                while (rest) {
+                    const int L = __ffs(rest) - 1;
+                    rest &= rest - 1u;
+                    if (lane == L) heap_offer(ts, ht, hi, k, r, t, m);
+                    __syncwarp();
+                }
+                if (lane == leader) {
+                    __threadfence_block();
+                    atomicExch(&ts.lock[r], 0);
+                }
+                changed = true;
+            }
+        }
+        if (changed && lane == 0) update_coef_min(ts, nr);
     }
 };
 
@@ -559,23 +655,35 @@ __global__ void __launch_bounds__(kThreads, 1) k_topk(const GroupParams p, int k
     if (threadIdx.x < 32) {
         ts.lock[threadIdx.x] = 0;
         ts.size[threadIdx.x] = 0;
-        ts.theta[threadIdx.x] = -1.0f;
-        ts.theta_idx[threadIdx.x] = 0x7FFFFFFF;
+        ts.root[threadIdx.x] = 0ull;
+        ts.coef[threadIdx.x] = 0.0f;
     }
     if (threadIdx.x == 0) {
-        ts.theta_min_bits = __float_as_int(-1.0f);
         ts.err = 0;
+        ts.coef_min_bits = 0;
     }
     const int nr = build_table(T, rs, p);   // synchronizes the block
-    int64_t wb, we;
-    warp_range(p, wb, we);
+    const int64_t cb = p.nchunks * blockIdx.y / gridDim.y;
+    const int64_t ce = p.nchunks * (blockIdx.y + 1) / gridDim.y;
+    const int64_t want_warm = (k + 31) / 32 + 8;
+    const int64_t warm = (ce - cb) < want_warm ? (ce - cb) : want_warm;
+    if ((threadIdx.x >> 5) == 0) {
+        TopkWarmEpi<NP> we{rs, ts, ht, hi, nr, k};
+        stream_chunks<NP, ET>(T, p, cb, cb + warm, we);
+        __syncwarp();
+        if (threadIdx.x == 0) update_coef_min(ts, nr);
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int64_t rb = cb + warm;
+    const int64_t wb = rb + (ce - rb) * warp / nwarps, wend = rb + (ce - rb) * (warp + 1) / nwarps;
     TopkEpi<NP> epi{rs, ts, ht, hi, nr, k};
-    stream_chunks<NP, ET>(T, p, wb, we, epi);
+    stream_chunks<NP, ET>(T, p, wb, wend, epi);
     __syncthreads();
     const int splits = gridDim.y;
     for (int i = threadIdx.x; i < nr * k; i += blockDim.x) {
         const int r = i / k, j = i - r * k;
-        const int64_t row = (int64_t)blockIdx.x * 32 + r;
+        const int64_t row = rs.orow[r];
         const int64_t o = (row * splits + blockIdx.y) * k + j;
         const bool ok = j < ts.size[r];
         part_t[o] = ok ? ht[r * k + j] : -3.0e38f;
@@ -601,7 +709,6 @@ __global__ void __launch_bounds__(512) k_topk_merge(const float* part_t, const i
         si[i] = i < n ? part_i[row * n + i] : -1;
     }
     __syncthreads();
-    // "before(a, b)": a ranks before b (invalid entries, index -1, rank last)
     for (int kk = 2; kk <= N; kk <<= 1) {
         for (int j = kk >> 1; j > 0; j >>= 1) {
             for (int i = threadIdx.x; i < N; i += blockDim.x) {
@@ -609,7 +716,7 @@ __global__ void __launch_bounds__(512) k_topk_merge(const float* part_t, const i
                 if (ixj > i) {
                     const bool asc = (i & kk) == 0;
                     const bool vi = si[i] >= 0, vj = si[ixj] >= 0;
-                    // b_before_a: element ixj ranks before element i
+                    // ji: element ixj ranks before element i (invalid entries, index -1, last)
                     bool ji;
                     if (vi != vj) ji = vj;
                     else if (!vi) ji = false;
@@ -762,7 +869,8 @@ __global__ void __launch_bounds__(256) k_topk_rowscan(const RawArgs ra, int k, i
     float* ht = reinterpret_cast<float*>(sm);
     int* hi = reinterpret_cast<int*>(ht + k);
     __shared__ int lock, size, err_s;
-    if (threadIdx.x == 0) { lock = 0; size = 0; err_s = 0; }
+    __shared__ unsigned long long root;   // published k-th best, 0 until the heap is full
+    if (threadIdx.x == 0) { lock = 0; size = 0; err_s = 0; root = 0ull; }
     __syncthreads();
     const int64_t r = ra.rowbase + blockIdx.x;
     const int32_t* a = ra.rl + r * ra.rw;
@@ -772,7 +880,7 @@ __global__ void __launch_bounds__(256) k_topk_rowscan(const RawArgs ra, int k, i
         const int is = merge_isct(a, as, alen, ra.ql + col * ra.qw, ra.qc + col * ra.qw, ra.qlen[col]);
         const float t = tanimoto_rows(is, ma, ra.qmag[col]);
         const int m = (int)col;
-        if (*(volatile int*)&size == k && !worse(*(volatile float*)&ht[0], *(volatile int*)&hi[0], t, m)) continue;
+        if (!beats_root(*(volatile unsigned long long*)&root, t, m)) continue;
         int spins = 0;
         bool got = true;
         while (atomicCAS(&lock, 0, 1) != 0) {
@@ -782,21 +890,27 @@ __global__ void __launch_bounds__(256) k_topk_rowscan(const RawArgs ra, int k, i
         if (!got) { atomicOr(&err_s, 1); continue; }
         __threadfence_block();
         int n = size;
+        bool changed = true;
         if (n < k) {
             ht[n] = t; hi[n] = m;
             heap_sift_up(ht, hi, n);
-            size = n + 1;
+            size = ++n;
         } else if (worse(ht[0], hi[0], t, m)) {
             ht[0] = t; hi[0] = m;
             heap_sift_down(ht, hi, k);
+        } else {
+            changed = false;
         }
+        if (changed && n == k)
+            *(volatile unsigned long long*)&root =
+                ((unsigned long long)__float_as_uint(ht[0]) << 32) | (unsigned long long)(uint32_t)hi[0];
         __threadfence_block();
         atomicExch(&lock, 0);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         // heap sort into best-first order
-        int n = size;
+        const int n = size;
         for (int end = n - 1; end > 0; end--) {
             const float tt = ht[0]; ht[0] = ht[end]; ht[end] = tt;
             const int ti = hi[0]; hi[0] = hi[end]; hi[end] = ti;
@@ -805,7 +919,6 @@ __global__ void __launch_bounds__(256) k_topk_rowscan(const RawArgs ra, int k, i
         if (err_s) atomicOr(err, 1);
     }
     __syncthreads();
-    // after the sort position 0 holds the best entry
     for (int j = threadIdx.x; j < k; j += blockDim.x) {
         const bool ok = j < size;
         idx[(int64_t)blockIdx.x * k + j] = ok ? hi[j] : -1;
@@ -896,6 +1009,7 @@ bool table_params(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t ro
     p.row_len = h->ref.len;
     p.rowbase = rowbase;
     p.rows = (int)rows;
+    p.row_order = nullptr;
     p.entries = d->entries;
     p.off = d->off;
     p.ng = d->ng;
@@ -989,12 +1103,13 @@ int launch_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int k, int32_
     const size_t heap_bytes = (size_t)32 * k * 8;
     if (k <= kTopkMax && table_params(h, d, rowbase, rows, kModeRows, p, smem, np) &&
         smem + heap_bytes + sizeof(RowSmem) + sizeof(TopkSmem) + 64 <= h->smem_optin) {
+        if ((rc = row_order_by_magnitude(h, rowbase, rowlimit, &p.row_order))) return rc;
         const int64_t groups = (rows + 31) / 32;
         int splits = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
         while (splits > 1 && (int64_t)splits * k > kTopkMergeMax) splits--;
         const size_t part = (size_t)rows * splits * k;
         void* buf = nullptr;
-        if ((rc = scratch_reserve(h, part * 8, &buf))) return rc;
+        if ((rc = scratch_reserve(h, part * 8, &buf, kSlotPartial))) return rc;
         float* pt = reinterpret_cast<float*>(buf);
         int* pi = reinterpret_cast<int*>(pt + part);
         const size_t sm = smem + heap_bytes;
@@ -1034,6 +1149,7 @@ int launch_hist(siml_engine* h, int64_t rowbase, int64_t rowlimit, bool global, 
     int np = 0;
     if (table_params(h, d, rowbase, rows, kModeRows, p, smem, np) &&
         smem + (global ? kBins1000 : 32 * kBins101) * 4 + sizeof(RowSmem) + 64 <= h->smem_optin) {
+        if ((rc = row_order_by_magnitude(h, rowbase, rowlimit, &p.row_order))) return rc;
         const bool u16 = d->entry_bytes == 2;
         if (global) {
             if (np == 8) return u16 ? launch_hist_t<8, uint16_t, true>(h, p, smem, out, ldo) : launch_hist_t<8, uint32_t, true>(h, p, smem, out, ldo);
@@ -1118,6 +1234,7 @@ int launch_neighbors(siml_engine* h, const NbrCall& c) {
     int force_ordered = 1;
     if (table_params(h, d, c.rowbase, rows, kModeRows, p, smem, np)) {
         force_ordered = 0;
+        if ((rc = row_order_by_magnitude(h, c.rowbase, c.rowlimit, &p.row_order))) return rc;
         if (np == 8)
             rc = d->entry_bytes == 2 ? launch_nbr_t<8, uint16_t>(h, p, smem, a) : launch_nbr_t<8, uint32_t>(h, p, smem, a);
         else

@@ -125,6 +125,23 @@ SIML_HD uint32_t row_count(const RowCounts<NP>& rc, int r) {
     return v;
 }
 
+// Row count for a row index known only at run time (a byte extract per word).
+template <int NP>
+SIML_HD uint32_t row_count_dyn(const RowCounts<NP>& rc, int r) {
+    uint32_t lo = 0, hi = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        if ((r & 7) == k) {
+            lo = rc.lo[k];
+            if (NP == 16) hi = rc.hi[k];
+        }
+    }
+    const int sh = 8 * (r >> 3);
+    uint32_t v = (lo >> sh) & 0xFFu;
+    if (NP == 16) v |= ((hi >> sh) & 0xFFu) << 8;
+    return v;
+}
+
 // Histogram bins, identical to the oracle's rules:
 // 101 bins: (unsigned)(t*100) clamped to 100, below zero / NaN to 0
 // (pysiml/_cpuutil.cpp:64-66, pysiml/kernels.py:660-661);

@@ -36,6 +36,10 @@ static int run(int trials, int max_masks) {
         siml::counts_from_planes<NP>(c, rc);
         for (int r = 0; r < 32; r++) {
             uint32_t got = siml::row_count<NP>(rc, r);
+            if (siml::row_count_dyn<NP>(rc, r) != got) {
+                std::printf("NP=%d row_count_dyn differs at row %d\n", NP, r);
+                return 1;
+            }
             if (got != ref[r]) {
                 std::printf("NP=%d trial %d row %d: got %u want %u (nmask %d)\n", NP, t, r, got, ref[r], nmask);
                 return 1;
