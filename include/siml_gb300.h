@@ -115,6 +115,20 @@ int siml_hist101(siml_engine* h, int64_t rowbase, int64_t rowlimit,
  * idx: int32 [rows, k], sims: fp32 [rows, k]. */
 int siml_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int64_t k,
               int32_t* idx, float* sims, int where);
+/* siml_topk without any device allocation (no counterpart in the reference).
+ * For callers that cannot allocate device memory on the request path (a
+ * caller-owned memory pool, a strict memory budget, a service that must not
+ * let a request trigger cudaMalloc): all scratch comes from one 16 MiB static
+ * __device__ array of the library, held by every GPU that loads it until the
+ * process exits.  idx / sims are device pointers [rows, k].  The engine's
+ * device layout must already exist (any earlier similarity call builds it),
+ * else SIML_ERR_STATE; requests needing more than 16 MiB of scratch are
+ * refused with SIML_ERR_INVALID.  All calls share the array and it keeps the
+ * last call's contents: calls that overlap on the GPU race, so serialize
+ * them.  The first call on each device looks up the array's address; make it
+ * before any stream capture. */
+int siml_topk_noalloc(siml_engine* h, int64_t rowbase, int64_t rowlimit, int64_t k,
+                      int32_t* idx, float* sims);
 /* Global similarity histogram over all pairs of a row block (no reference
  * counterpart; a whole-block form of getMultipleHistogrammedRows):
  * nbins = 1000, bin = min((unsigned)(t*1000.0f), 999).  out: uint64 [1000],

@@ -42,7 +42,6 @@ int scratch_reserve(siml_engine* h, size_t bytes, void** out, int slot) {
 }
 
 namespace {
-constexpr int kOrderBuckets = 4096;
 
 // Counting sort of rows by min(magnitude, 4095): bucket sizes ...
 __global__ void k_order_count(const int32_t* __restrict__ mag, int64_t rowbase, int64_t rows, int32_t* bucket) {
@@ -78,6 +77,20 @@ __global__ void k_order_scatter(const int32_t* __restrict__ mag, int64_t rowbase
 }
 }  // namespace
 
+int row_order_into(siml_engine* h, int64_t rowbase, int64_t rowlimit, int32_t* order, int32_t* bucket) {
+    const int64_t rows = rowlimit - rowbase;
+    SIML_CUDA(cudaMemsetAsync(bucket, 0, kOrderBuckets * 4, h->stream));
+    if (rows > 0) {
+        const unsigned g = (unsigned)((rows + 255) / 256);
+        k_order_count<<<g, 256, 0, h->stream>>>(h->ref.mag, rowbase, rows, bucket);
+        k_order_scan<<<1, 1024, 0, h->stream>>>(bucket);
+        k_order_scatter<<<g, 256, 0, h->stream>>>(h->ref.mag, rowbase, rows, bucket, order);
+        h->launches += 3;
+        SIML_CUDA(cudaGetLastError());
+    }
+    return SIML_OK;
+}
+
 int row_order_by_magnitude(siml_engine* h, int64_t rowbase, int64_t rowlimit, const int32_t** order) {
     const int64_t rows = rowlimit - rowbase;
     void* ob = nullptr;
@@ -85,16 +98,7 @@ int row_order_by_magnitude(siml_engine* h, int64_t rowbase, int64_t rowlimit, co
     int rc;
     if ((rc = scratch_reserve(h, (size_t)std::max<int64_t>(rows, 1) * 4, &ob, kSlotOrder))) return rc;
     if ((rc = scratch_reserve(h, kOrderBuckets * 4, &bb, kSlotSmall))) return rc;
-    int32_t* bucket = (int32_t*)bb;
-    SIML_CUDA(cudaMemsetAsync(bucket, 0, kOrderBuckets * 4, h->stream));
-    if (rows > 0) {
-        const unsigned g = (unsigned)((rows + 255) / 256);
-        k_order_count<<<g, 256, 0, h->stream>>>(h->ref.mag, rowbase, rows, bucket);
-        k_order_scan<<<1, 1024, 0, h->stream>>>(bucket);
-        k_order_scatter<<<g, 256, 0, h->stream>>>(h->ref.mag, rowbase, rows, bucket, (int32_t*)ob);
-        h->launches += 3;
-        SIML_CUDA(cudaGetLastError());
-    }
+    if ((rc = row_order_into(h, rowbase, rowlimit, (int32_t*)ob, (int32_t*)bb))) return rc;
     *order = (const int32_t*)ob;
     return SIML_OK;
 }

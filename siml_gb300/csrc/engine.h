@@ -109,6 +109,9 @@ int scratch_reserve(siml_engine* h, size_t bytes, void** out, int slot = kSlotSt
 // Rows [rowbase, rowlimit) of the ref set ordered by magnitude (absolute row
 // indices, device array of rowlimit - rowbase entries, in kSlotOrder).
 int row_order_by_magnitude(siml_engine* h, int64_t rowbase, int64_t rowlimit, const int32_t** order);
+// The same into caller buffers: order[rowlimit - rowbase], bucket[4096].
+constexpr int kOrderBuckets = 4096;
+int row_order_into(siml_engine* h, int64_t rowbase, int64_t rowlimit, int32_t* order, int32_t* bucket);
 int cuda_fail(cudaError_t e, const char* what);
 
 // kernels.cu — launchers; all queue work on h->stream and return a status.
@@ -136,6 +139,19 @@ int launch_hist(siml_engine* h, int64_t rowbase, int64_t rowlimit, bool global, 
 // Per-row top-k into idx / sims [rows, k]; a bounded lock wait that expires
 // sets *h->d_err (read back by the caller).
 int launch_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int k, int32_t* idx, float* sims);
+// The same in pieces, for callers that bring their own buffers: the plan
+// gives the number of database splits of the table path (0: per-row scan
+// without scratch) and the partial-heap entries it needs; the core takes the
+// row order (rows ordered by magnitude, ignored by the scan) and partial
+// buffers float[partial_entries] / int[partial_entries].
+struct TopkPlan {
+    int splits = 0;
+    size_t partial_entries = 0;
+};
+int topk_plan(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t rowlimit, int k, TopkPlan& plan);
+int launch_topk_core(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t rowlimit, int k,
+                     const TopkPlan& plan, const int32_t* order, float* part_t, int* part_i, int32_t* idx,
+                     float* sims);
 // rowHistogram101 of a dense fp32 / fp64 device matrix into uint32 [rows, 101].
 int launch_row_hist101(siml_engine* h, const void* data, bool f64, int64_t rows, int64_t cols, int64_t ld,
                        uint32_t* hist);

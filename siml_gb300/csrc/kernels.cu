@@ -1091,51 +1091,81 @@ int launch_topk_t(siml_engine* h, const GroupParams& p, size_t smem, int k, int 
 
 }  // namespace
 
+int topk_plan(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t rowlimit, int k, TopkPlan& plan) {
+    const int64_t rows = rowlimit - rowbase;
+    GroupParams p;
+    size_t smem = 0;
+    int np = 0;
+    plan.splits = 0;
+    plan.partial_entries = 0;
+    const size_t heap_bytes = (size_t)32 * k * 8;
+    if (k <= kTopkMax && table_params(h, d, rowbase, rows, kModeRows, p, smem, np) &&
+        smem + heap_bytes + sizeof(RowSmem) + sizeof(TopkSmem) + 64 <= h->smem_optin) {
+        const int64_t groups = (rows + 31) / 32;
+        int splits = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
+        while (splits > 1 && (int64_t)splits * k > kTopkMergeMax) splits--;
+        plan.splits = splits;
+        plan.partial_entries = (size_t)rows * splits * k;
+    } else if ((size_t)k * 8 + 64 > h->smem_optin) {
+        return fail(SIML_ERR_UNSUPPORTED, "top-k: k = %d too large", k);
+    }
+    return SIML_OK;
+}
+
+int launch_topk_core(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t rowlimit, int k,
+                     const TopkPlan& plan, const int32_t* order, float* part_t, int* part_i, int32_t* idx,
+                     float* sims) {
+    const int64_t rows = rowlimit - rowbase;
+    int rc;
+    SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+    if (plan.splits > 0) {
+        GroupParams p;
+        size_t smem = 0;
+        int np = 0;
+        table_params(h, d, rowbase, rows, kModeRows, p, smem, np);
+        p.row_order = order;
+        const size_t sm = smem + (size_t)32 * k * 8;
+        const bool u16 = d->entry_bytes == 2;
+        if (np == 8) rc = u16 ? launch_topk_t<8, uint16_t>(h, p, sm, k, plan.splits, part_t, part_i) : launch_topk_t<8, uint32_t>(h, p, sm, k, plan.splits, part_t, part_i);
+        else rc = u16 ? launch_topk_t<16, uint16_t>(h, p, sm, k, plan.splits, part_t, part_i) : launch_topk_t<16, uint32_t>(h, p, sm, k, plan.splits, part_t, part_i);
+        if (rc) return rc;
+        int N = 1;
+        while (N < plan.splits * k) N <<= 1;
+        const size_t msm = (size_t)N * 8;
+        if ((rc = set_smem(k_topk_merge, msm))) return rc;
+        k_topk_merge<<<(unsigned)rows, 512, msm, h->stream>>>(part_t, part_i, plan.splits, k, idx, sims);
+        SIML_CUDA(cudaGetLastError());
+        h->launches++;
+        return SIML_OK;
+    }
+    const size_t sm = (size_t)k * 8;
+    if ((rc = set_smem(k_topk_rowscan, sm))) return rc;
+    SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+    k_topk_rowscan<<<(unsigned)rows, 256, sm, h->stream>>>(raw_args(h, rowbase), k, idx, sims, h->d_err);
+    SIML_CUDA(cudaGetLastError());
+    SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+    h->timed = true;
+    h->launches++;
+    return SIML_OK;
+}
+
 int launch_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int k, int32_t* idx, float* sims) {
     const DbLayout* d = nullptr;
     int rc = ensure_layout(h, true, &d);
     if (rc) return rc;
-    const int64_t rows = rowlimit - rowbase;
-    SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
-    GroupParams p;
-    size_t smem = 0;
-    int np = 0;
-    const size_t heap_bytes = (size_t)32 * k * 8;
-    if (k <= kTopkMax && table_params(h, d, rowbase, rows, kModeRows, p, smem, np) &&
-        smem + heap_bytes + sizeof(RowSmem) + sizeof(TopkSmem) + 64 <= h->smem_optin) {
-        if ((rc = row_order_by_magnitude(h, rowbase, rowlimit, &p.row_order))) return rc;
-        const int64_t groups = (rows + 31) / 32;
-        int splits = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
-        while (splits > 1 && (int64_t)splits * k > kTopkMergeMax) splits--;
-        const size_t part = (size_t)rows * splits * k;
+    TopkPlan plan;
+    if ((rc = topk_plan(h, d, rowbase, rowlimit, k, plan))) return rc;
+    const int32_t* order = nullptr;
+    float* pt = nullptr;
+    int* pi = nullptr;
+    if (plan.splits > 0) {
+        if ((rc = row_order_by_magnitude(h, rowbase, rowlimit, &order))) return rc;
         void* buf = nullptr;
-        if ((rc = scratch_reserve(h, part * 8, &buf, kSlotPartial))) return rc;
-        float* pt = reinterpret_cast<float*>(buf);
-        int* pi = reinterpret_cast<int*>(pt + part);
-        const size_t sm = smem + heap_bytes;
-        const bool u16 = d->entry_bytes == 2;
-        if (np == 8) rc = u16 ? launch_topk_t<8, uint16_t>(h, p, sm, k, splits, pt, pi) : launch_topk_t<8, uint32_t>(h, p, sm, k, splits, pt, pi);
-        else rc = u16 ? launch_topk_t<16, uint16_t>(h, p, sm, k, splits, pt, pi) : launch_topk_t<16, uint32_t>(h, p, sm, k, splits, pt, pi);
-        if (rc) return rc;
-        int N = 1;
-        while (N < splits * k) N <<= 1;
-        const size_t msm = (size_t)N * 8;
-        if ((rc = set_smem(k_topk_merge, msm))) return rc;
-        k_topk_merge<<<(unsigned)rows, 512, msm, h->stream>>>(pt, pi, splits, k, idx, sims);
-        SIML_CUDA(cudaGetLastError());
-        h->launches++;
-    } else {
-        if ((size_t)k * 8 + 64 > h->smem_optin) return fail(SIML_ERR_UNSUPPORTED, "top-k: k = %d too large", k);
-        const size_t sm = (size_t)k * 8;
-        if ((rc = set_smem(k_topk_rowscan, sm))) return rc;
-        SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
-        k_topk_rowscan<<<(unsigned)rows, 256, sm, h->stream>>>(raw_args(h, rowbase), k, idx, sims, h->d_err);
-        SIML_CUDA(cudaGetLastError());
-        SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
-        h->timed = true;
-        h->launches++;
+        if ((rc = scratch_reserve(h, plan.partial_entries * 8, &buf, kSlotPartial))) return rc;
+        pt = reinterpret_cast<float*>(buf);
+        pi = reinterpret_cast<int*>(pt + plan.partial_entries);
     }
-    return SIML_OK;
+    return launch_topk_core(h, d, rowbase, rowlimit, k, plan, order, pt, pi, idx, sims);
 }
 
 int launch_hist(siml_engine* h, int64_t rowbase, int64_t rowlimit, bool global, void* out, int64_t ldo) {
