@@ -347,6 +347,256 @@ def gpu_arm(args):
     return 0
 
 
+# ------------------------------------------------------ ragged jobs ----
+RAGGED_DB_N = 2_000_000
+RAGGED_JOBS = 4096
+RAGGED_LO = 0.6
+RAGGED_MAXN = 128
+RAGGED_WORKLOAD = ("ragged_2m: 4,096 getNeighbors jobs (T >= 0.6, pitch 128, indices + fp32 similarities) over a "
+                   "resident 2,000,000-molecule database (bimodal lengths: 70% median 35, 30% median 110 chars) "
+                   "used as both sides; per job a log-uniform 1-2,048-row range against a log-uniform "
+                   "1,000-200,000-molecule range")
+
+
+def ragged_sets_and_jobs(njobs):
+    from siml_gb300 import synthetic as S
+    t = time.time()
+    db = S.smiles_set(S.SEED_RAGGED, S.BIMODAL_35_110, RAGGED_DB_N)
+    jobs = S.ragged_jobs(S.SEED_RAGGED, RAGGED_DB_N, njobs)
+    log("generated + compiled %d molecules and %d jobs in %.1f s" % (RAGGED_DB_N, njobs, time.time() - t))
+    return db, jobs
+
+
+def ragged_cpu_rate(db, jobs, target_s=10.0):
+    """The oracle's neighbour search on the smallest jobs, all host threads."""
+    from oracle import cpulingo as O
+    nthreads = os.cpu_count() or 1
+    pairs = (jobs[:, 1] - jobs[:, 0]) * (jobs[:, 3] - jobs[:, 2])
+    order = np.argsort(pairs, kind="stable")
+    O.neighbors_range_block(db, db, *[int(x) for x in jobs[order[0]]], RAGGED_LO, 1.1, RAGGED_MAXN,
+                            nthreads=nthreads)
+    done, t, n = 0, time.time(), 0
+    for i in order:
+        O.neighbors_range_block(db, db, *[int(x) for x in jobs[i]], RAGGED_LO, 1.1, RAGGED_MAXN,
+                                nthreads=nthreads)
+        done += int(pairs[i])
+        n += 1
+        if time.time() - t > target_s:
+            break
+    dt = time.time() - t
+    return {"value": done / dt / 1e9, "unit": "Gpairs/s", "cores": nthreads, "kind": "port",
+            "sample": "the %d smallest of the %d jobs (%.2e pairs) in %.2f s" % (n, len(jobs), done, dt)}
+
+
+def ragged_reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "port"], check=True)
+    db, jobs = ragged_sets_and_jobs(args.ragged_jobs)
+    for _ in range(args.warmup):
+        ragged_cpu_rate(db, jobs, target_s=1.0)
+    rates = [ragged_cpu_rate(db, jobs, target_s=8.0) for _ in range(args.steps)]
+    value = statistics.mean(r["value"] for r in rates)
+    cpu = dict(rates[-1])
+    cpu["value"] = value
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": RAGGED_WORKLOAD, "jobs": args.ragged_jobs, "db_molecules": RAGGED_DB_N},
+        "cpu_baseline": cpu,
+        "e2e": {"value": value, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def ragged_arm(args):
+    """Batched ragged jobs: one persistent launch per step, replayed from a
+    CUDA graph, against the plain path (one getNeighbors-over-a-range call per
+    job) on the same GPU, outputs compared bit for bit."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from siml_gb300 import GPULingo
+    db, jobs = ragged_sets_and_jobs(args.ragged_jobs)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    gl = GPULingo(local, stream=stream)
+    t = time.time()
+    gl.set_qsmiles(*db)
+    gl.set_refsmiles(*db)
+    stats = gl.dbStats()
+    torch.cuda.synchronize()
+    log("database layout ready in %.2f s: %s" % (time.time() - t, stats))
+    t = time.time()
+    plan = gl.planNeighborBatch(jobs, RAGGED_LO, 1.1, RAGGED_MAXN, tile_chunks=args.tile_chunks)
+    plan_s = time.time() - t
+    log("plan: %d items, tile %d chunks, %.2e pairs, %.2f GB streamed per run, planned in %.2f s"
+        % (plan.nitems, plan.tile_chunks, plan.pairs, plan.stream_bytes / 1e9, plan_s))
+    idx, sims, cnt = plan.buffers(with_sims=True)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+
+    # capture one run in a CUDA graph (after a warm-up run on the capture stream)
+    cap = torch.cuda.Stream(device=dev)
+    cap.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(cap):
+        plan.run(idx, sims, cnt, stream=cap)
+    torch.cuda.current_stream().wait_stream(cap)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        plan.run(idx, sims, cnt, stream=torch.cuda.current_stream())
+    kernels_per_run = 2   # k_batch_nbr + k_nbr_finish
+
+    for _ in range(args.warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    cur = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    wall0 = time.time()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        ev[k][0].record(cur)
+        graph.replay()
+        ev[k][1].record(cur)
+    torch.cuda.synchronize()
+    wall = time.time() - wall0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    if world > 1:
+        tt = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(tt.item())
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    value = world * args.steps * plan.pairs / (total_ms / 1e3) / 1e9
+    ms_per_step = total_ms / args.steps
+
+    # plain path: one call per job on the same resident database
+    idx2 = torch.empty_like(idx)
+    sims2 = torch.empty_like(sims)
+    cnt2 = torch.empty_like(cnt)
+    J = plan.jobs.tolist()
+
+    def plain(sel):
+        for rb, re, cb, ce, o in sel:
+            if re > rb:
+                gl.neighborsRangeDevice(rb, re, cb, ce, RAGGED_LO, 1.1, plan.pitch, idx2[o:o + re - rb],
+                                        sims2[o:o + re - rb], cnt2[o:o + re - rb])
+
+    plain(J[:64])
+    torch.cuda.synchronize()
+    l0 = gl.launchCount()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(cur)
+    plain(J)
+    p1.record(cur)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1)
+    plain_launches = gl.launchCount() - l0
+    plain_value = plan.pairs / (plain_ms / 1e3) / 1e9
+
+    # bit-exact: batched == plain for every job, and spot jobs == oracle
+    c1 = cnt[:plan.rows_out]
+    same = bool(torch.equal(c1, cnt2[:plan.rows_out]))
+    if same:
+        k = torch.clamp(c1, max=plan.pitch)
+        mask = torch.arange(plan.pitch, device=dev)[None, :] < k[:, None]
+        a1, a2 = idx[:plan.rows_out], idx2[:plan.rows_out]
+        s1, s2 = sims[:plan.rows_out].view(torch.int32), sims2[:plan.rows_out].view(torch.int32)
+        same = bool(torch.equal(torch.where(mask, a1, 0), torch.where(mask, a2, 0)) and
+                    torch.equal(torch.where(mask, s1, 0), torch.where(mask, s2, 0)))
+    from oracle import cpulingo as O
+    pairs = (jobs[:, 1] - jobs[:, 0]) * (jobs[:, 3] - jobs[:, 2])
+    spot = [int(i) for i in np.argsort(pairs, kind="stable")[:6]]
+    hc, hi_, hs = cnt.cpu().numpy(), idx.cpu().numpy(), sims.cpu().numpy()
+    oracle_ok = True
+    for i in spot:
+        rb, re, cb, ce, o = J[i]
+        oi, os_, oc = O.neighbors_range_block(db, db, rb, re, cb, ce, RAGGED_LO, 1.1, RAGGED_MAXN,
+                                              nthreads=os.cpu_count() or 1)
+        gc = hc[o:o + re - rb]
+        oracle_ok &= bool(np.array_equal(gc, oc))
+        for r in range(re - rb):
+            kk = min(int(gc[r]), plan.pitch)
+            oracle_ok &= bool(np.array_equal(hi_[o + r, :kk], oi[r, :kk]) and
+                              np.array_equal(hs[o + r, :kk].view(np.uint32), os_[r, :kk].view(np.uint32)))
+
+    # roofline of k_batch_nbr: database bytes streamed per run / step time
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = plan.stream_bytes / (ms_per_step / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "k_batch_nbr (+ k_nbr_finish)", "kernel_ms": ms_per_step,
+                "algorithmic_bytes_per_launch": plan.stream_bytes,
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback"}
+
+    e2e = cpu = None
+    if rank == 0 and not args.no_extras:
+        # public API with host buffers: plan from the host job list, run,
+        # results back to pinned host memory
+        hidx = torch.empty(idx.shape, dtype=torch.int32).pin_memory()
+        hsims = torch.empty(sims.shape, dtype=torch.float32).pin_memory()
+        hcnt = torch.empty(cnt.shape, dtype=torch.int32).pin_memory()
+
+        def one():
+            p = gl.planNeighborBatch(jobs, RAGGED_LO, 1.1, RAGGED_MAXN, tile_chunks=plan.tile_chunks)
+            p.run(idx, sims, cnt)
+            hidx.copy_(idx, non_blocking=True)
+            hsims.copy_(sims, non_blocking=True)
+            hcnt.copy_(cnt, non_blocking=True)
+            torch.cuda.synchronize()
+
+        one()
+        t = time.time()
+        n_e2e = min(3, args.steps)
+        for _ in range(n_e2e):
+            one()
+        dt = time.time() - t
+        e2e = {"value": n_e2e * plan.pairs / dt / 1e9, "unit": "Gpairs/s",
+               "h2d_bytes_per_step": int(plan.jobs.nbytes),
+               "d2h_bytes_per_step": int(hidx.numel() * 4 + hsims.numel() * 4 + hcnt.numel() * 4),
+               "steps": n_e2e, "note": "includes planning (fixed tile) and the host job-list upload"}
+        if world == 1:
+            cpu = ragged_cpu_rate(db, jobs)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded SMILES-like strings)",
+            "config": {"workload": RAGGED_WORKLOAD, "jobs": args.ragged_jobs, "db_molecules": RAGGED_DB_N,
+                       "pairs_per_step": plan.pairs, "items": plan.nitems, "tile_chunks": plan.tile_chunks,
+                       "plan_s": plan_s, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "flushed between steps by a 256 MB write; the database layout (%.2f GB) exceeds L2"
+                             % (stats["ngroups_total"] * 16 / 1e9),
+                       "db_layout": stats},
+            "plain": {"value": plain_value, "unit": "Gpairs/s", "ms": plain_ms, "launches": plain_launches,
+                      "path": "one neighborsRangeDevice call per job (siml_neighbors_range)"},
+            "batched_over_plain": value / plain_value,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": args.steps * kernels_per_run, "clocks": clk,
+            "parity_batched_equals_plain": same, "parity_spot_check": oracle_ok, "wall_s_timed": wall,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def read_profile_traffic():
     """DRAM bytes per k_rows launch from the committed ncu summary, if any."""
     path = os.path.join(REPO, "profiles", "k_rows_rows1m.md")
@@ -399,12 +649,19 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--rows-per-step", type=int, default=BLOCK,
                     help="rows per block (smaller blocks for profiler captures)")
-    ap.add_argument("--workload", choices=["rows_1m", "nbr_1m", "topk_1m", "hist_1m"], default="rows_1m",
+    ap.add_argument("--workload", choices=["rows_1m", "nbr_1m", "topk_1m", "hist_1m", "ragged_2m"],
+                    default="rows_1m",
                     help="rows_1m: getMultipleRows blocks (default); nbr_1m: getNeighbors at T >= 0.7; "
-                         "topk_1m: top-100 per row; hist_1m: 1000-bin histogram of every pair")
+                         "topk_1m: top-100 per row; hist_1m: 1000-bin histogram of every pair; "
+                         "ragged_2m: 4,096 batched neighbour jobs vs the plain per-job path")
+    ap.add_argument("--ragged-jobs", type=int, default=RAGGED_JOBS, help="jobs of the ragged_2m workload")
+    ap.add_argument("--tile-chunks", type=int, default=0,
+                    help="ragged_2m: chunks per work item (0: autotuned when the plan is made)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the end-to-end and CPU-baseline legs (profiler runs)")
     args = ap.parse_args()
+    if args.workload == "ragged_2m":
+        return ragged_reference_arm(args) if args.impl == "reference" else ragged_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
     return gpu_arm(args)

@@ -136,19 +136,47 @@ int siml_topk_noalloc(siml_engine* h, int64_t rowbase, int64_t rowlimit, int64_t
 int siml_hist_global(siml_engine* h, int64_t rowbase, int64_t rowlimit,
                      uint64_t* out, int where);
 
-/* ---- batched ragged neighbor jobs --------------------------------------- */
-/* Many independent (ref rows, query-set index range) threshold searches in
- * one launch (no reference counterpart: the reference issues one
- * getNeighbors call per job, GPULingo.py:467-513).  Job j covers ref rows
- * [row_begin[j], row_end[j]) against query columns [col_begin[j], col_end[j])
- * with the getNeighbors rule and pitch; its rows' results go to
- * idx/sims/counts at row offset out_row[j] (idx, sims: [*, pitch];
- * counts: [*]).  Indices are absolute query indices. */
-int siml_batch_neighbors(siml_engine* h, int64_t njobs,
-                         const int64_t* row_begin, const int64_t* row_end,
-                         const int64_t* col_begin, const int64_t* col_end,
-                         const int64_t* out_row, float lo, float hi, int64_t pitch,
+/* getNeighbors restricted to query columns [col_begin, col_end) (no
+ * reference counterpart; the reference searches the whole query set,
+ * pysiml/kernels.py:420-470).  Same rule, pitch and output as
+ * siml_neighbors; indices are absolute query indices and an overflowing row
+ * is counted in waves of 128 columns starting at col_begin.  This is the
+ * plain one-call-per-job path that siml_batch_* replaces. */
+int siml_neighbors_range(siml_engine* h, int64_t rowbase, int64_t rowlimit,
+                         int64_t col_begin, int64_t col_end,
+                         float lo, float hi, int64_t pitch,
                          int32_t* idx, float* sims, int32_t* counts, int where);
+
+/* ---- batched ragged neighbor jobs --------------------------------------- */
+/* Many independent threshold searches of different shapes, planned once and
+ * run as one persistent launch (no reference counterpart: the reference
+ * issues one getNeighbors call per job, pysiml/GPULingo.py:467-513).
+ * jobs: int64 [njobs, 5] = {row_begin, row_end, col_begin, col_end, out_row}:
+ * ref rows [row_begin, row_end) against query columns [col_begin, col_end)
+ * with getNeighbors' rule, results of ref row r in output row
+ * out_row + (r - row_begin).  Output rows of different jobs must not
+ * overlap; an output row covered by no job gets count 0.  tile_chunks is
+ * the number of 32-molecule chunks per work item; <= 0 lets the plan time
+ * candidates on a sample of the jobs and keep the fastest.  A plan is tied
+ * to the engine's current sets: siml_batch_run refuses it (SIML_ERR_STATE)
+ * once set_ref / set_query replaced them.  Destroy plans before the engine. */
+typedef struct siml_batch siml_batch;
+int siml_batch_create(siml_engine* h, int64_t njobs, const int64_t* jobs,
+                      float lo, float hi, int64_t pitch, int64_t tile_chunks,
+                      siml_batch** out);
+/* rows_out: output rows the plan writes (max out_row + rows over jobs);
+ * nitems: work items; tile_chunks: the tile the plan uses; stream_bytes:
+ * database bytes (entries and per-molecule metadata) one run reads.  NULL
+ * skips an output. */
+int siml_batch_info(siml_batch* b, int64_t* rows_out, int64_t* nitems, int64_t* tile_chunks,
+                    int64_t* stream_bytes);
+/* Queues the plan on stream (a cudaStream_t; NULL: the engine's stream):
+ * device outputs idx, sims (may be NULL): [rows_out, pitch]; counts:
+ * [rows_out], with siml_neighbors' meaning.  No host synchronization and
+ * no allocation, so a run may be captured in a CUDA graph and replayed.
+ * Runs of one plan must not overlap on the GPU (they share a queue head). */
+int siml_batch_run(siml_batch* b, int32_t* idx, float* sims, int32_t* counts, void* stream);
+int siml_batch_destroy(siml_batch* b);
 
 /* ---- SMILES compiler ---------------------------------------------------- */
 /* cSMILEStoMatrices / _ccompiler.SMILEStoMatrices — pysiml/compiler.py:53-82,

@@ -274,6 +274,19 @@ def neighbors_block(ref, qry, rowbase, rowlimit, lo, hi=1.1, maxneighbors=None, 
     return idx, sims, counts
 
 
+def neighbors_range_block(ref, qry, rowbase, rowlimit, col_begin, col_end, lo, hi=1.1, maxneighbors=None,
+                          nthreads=0):
+    """getNeighbors against query columns [col_begin, col_end) only: the
+    reference's search run on that slice of the query set (so overflow waves
+    start at col_begin), indices shifted back to absolute query indices."""
+    sl = tuple(None if x is None else np.asarray(x)[col_begin:col_end] for x in qry)
+    if maxneighbors is None:
+        maxneighbors = np.asarray(qry[0]).shape[0]
+    idx, sims, counts = neighbors_block(ref, sl, rowbase, rowlimit, lo, hi, maxneighbors, nthreads)
+    idx = np.where(idx >= 0, idx + np.int32(col_begin), idx).astype(np.int32)
+    return idx, sims, counts
+
+
 def hist101_block(ref, qry, rowbase, rowlimit, nthreads=0):
     """int32 [rows, 101] — getMultipleHistogrammedRows (pysiml/kernels.py:606-666)."""
     a, keep = _args(ref, qry, rowbase, rowlimit)

@@ -334,28 +334,65 @@ class GPULingo:
                                        counts.data_ptr(), N.SIML_DEVICE), "neighborsDevice")
         self._leave(idx, sims, counts)
 
-    def _queue_neighbors(self, rowbase, rowlimit, lowerbound, upperbound, maxneighbors, with_sims):
+    def neighborsRangeDevice(self, rowbase, rowlimit, colbegin, colend, lowerbound, upperbound, pitch, idx, sims,
+                             counts):
+        """neighborsDevice restricted to query columns [colbegin, colend):
+        absolute indices, overflow counted in waves of 128 from colbegin."""
+        self._check_rows(rowbase, rowlimit)
+        self._enter()
+        N.check(N.lib().siml_neighbors_range(self._h, int(rowbase), int(rowlimit), int(colbegin), int(colend),
+                                             ctypes.c_float(lowerbound), ctypes.c_float(upperbound), int(pitch),
+                                             idx.data_ptr(), N.ptr(sims), counts.data_ptr(), N.SIML_DEVICE),
+                "neighborsRangeDevice")
+        self._leave(idx, sims, counts)
+
+    def getNeighborsRange(self, rowbase, rowlimit, colbegin, colend, lowerbound, upperbound=1.1,
+                          maxneighbors=None):
+        """getNeighbors over query columns [colbegin, colend) only."""
+        self._queue_neighbors(rowbase, rowlimit, lowerbound, upperbound, maxneighbors, False, (colbegin, colend))
+        return self.retrieveAsyncResult()
+
+    def planNeighborBatch(self, jobs, lowerbound, upperbound=1.1, maxneighbors=None, tile_chunks=0):
+        """A reusable plan (siml_gb300.batch.NeighborBatch) of ragged jobs
+        (row_begin, row_end, col_begin, col_end[, out_row])."""
+        from .batch import NeighborBatch
+        return NeighborBatch(self, jobs, lowerbound, upperbound, maxneighbors, tile_chunks)
+
+    def getNeighborsBatch(self, jobs, lowerbound, upperbound=1.1, maxneighbors=None, with_sims=False):
+        """Runs ragged jobs in one batch; returns one getNeighbors-style
+        result per job."""
+        plan = self.planNeighborBatch(jobs, lowerbound, upperbound, maxneighbors)
+        idx, sims, cnt = plan.buffers(with_sims)
+        plan.run(idx, sims, cnt)
+        return plan.split(idx, sims, cnt)
+
+    def _queue_neighbors(self, rowbase, rowlimit, lowerbound, upperbound, maxneighbors, with_sims, cols=None):
         self._check_rows(rowbase, rowlimit)
         if maxneighbors is None:
             maxneighbors = self.nquery
         pitch = 16 * ((int(maxneighbors) + 15) // 16)
         rows = rowlimit - rowbase
         L = N.lib()
-        args = (self._h, int(rowbase), int(rowlimit), ctypes.c_float(lowerbound), ctypes.c_float(upperbound), pitch)
+        if cols is None:
+            fn = L.siml_neighbors
+            args = (self._h, int(rowbase), int(rowlimit), ctypes.c_float(lowerbound), ctypes.c_float(upperbound),
+                    pitch)
+        else:
+            fn = L.siml_neighbors_range
+            args = (self._h, int(rowbase), int(rowlimit), int(cols[0]), int(cols[1]), ctypes.c_float(lowerbound),
+                    ctypes.c_float(upperbound), pitch)
         if torch is not None:
             dev = self._device()
             idx = torch.empty((rows, max(pitch, 1)), dtype=torch.int32, device=dev)
             sims = torch.empty((rows, max(pitch, 1)), dtype=torch.float32, device=dev) if with_sims else None
             cnt = torch.empty(max(rows, 1), dtype=torch.int32, device=dev)
             self._enter()
-            N.check(L.siml_neighbors(*args, idx.data_ptr(), N.ptr(sims), cnt.data_ptr(), N.SIML_DEVICE),
-                    "getNeighbors")
+            N.check(fn(*args, idx.data_ptr(), N.ptr(sims), cnt.data_ptr(), N.SIML_DEVICE), "getNeighbors")
         else:
             idx = np.empty((rows, max(pitch, 1)), dtype=np.int32)
             sims = np.empty((rows, max(pitch, 1)), dtype=np.float32) if with_sims else None
             cnt = np.empty(max(rows, 1), dtype=np.int32)
-            N.check(L.siml_neighbors(*args, idx.ctypes.data, N.ptr(sims), cnt.ctypes.data, N.SIML_HOST),
-                    "getNeighbors")
+            N.check(fn(*args, idx.ctypes.data, N.ptr(sims), cnt.ctypes.data, N.SIML_HOST), "getNeighbors")
         self.last_async_width = maxneighbors
         self._pending = ("neighbors", idx, sims, cnt, pitch, rows)
 

@@ -61,7 +61,11 @@ _SIGNATURES = {
     "siml_topk": (_I32, [_P, _I64, _I64, _I64, _P, _P, _I32]),
     "siml_hist_global": (_I32, [_P, _I64, _I64, _P, _I32]),
     "siml_topk_noalloc": (_I32, [_P, _I64, _I64, _I64, _P, _P]),
-    "siml_batch_neighbors": (_I32, [_P, _I64, _P, _P, _P, _P, _P, _F32, _F32, _I64, _P, _P, _P, _I32]),
+    "siml_neighbors_range": (_I32, [_P, _I64, _I64, _I64, _I64, _F32, _F32, _I64, _P, _P, _P, _I32]),
+    "siml_batch_create": (_I32, [_P, _I64, _P, _F32, _F32, _I64, _I64, _P]),
+    "siml_batch_info": (_I32, [_P, _P, _P, _P, _P]),
+    "siml_batch_run": (_I32, [_P, _P, _P, _P, _P]),
+    "siml_batch_destroy": (_I32, [_P]),
     "siml_compile_width": (_I64, [_P, _P, _I64]),
     "siml_compile_smiles": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _I64]),
     "siml_row_histogram101": (_I32, [_P, _P, _I64, _I64, _I64, _P, _I32]),

@@ -680,6 +680,7 @@ int siml_set_ref(siml_engine* h, const int32_t* lingos, const int32_t* counts, c
     SIML_GUARD(h);
     (void)where;
     h->rows_valid = false;
+    h->generation++;
     return upload_set(h, h->ref, lingos, counts, lengths, mags, n, width, ld, "set_refsmiles");
 }
 
@@ -689,6 +690,7 @@ int siml_set_query(siml_engine* h, const int32_t* lingos, const int32_t* counts,
     (void)where;
     h->layout_valid = false;
     h->rows_valid = false;
+    h->generation++;
     return upload_set(h, h->qry, lingos, counts, lengths, mags, n, width, ld, "set_qsmiles");
 }
 
@@ -754,19 +756,22 @@ int siml_rows(siml_engine* h, int64_t rowbase, int64_t rowlimit, float* out, int
     return rows_common(h, rowbase, rowlimit, out, ldo, where, kModeRows);
 }
 
-int siml_neighbors(siml_engine* h, int64_t rowbase, int64_t rowlimit, float lo, float hi, int64_t pitch,
-                   int32_t* idx, float* sims, int32_t* counts, int where) {
+int siml_neighbors_range(siml_engine* h, int64_t rowbase, int64_t rowlimit, int64_t col_begin, int64_t col_end,
+                         float lo, float hi, int64_t pitch, int32_t* idx, float* sims, int32_t* counts, int where) {
     SIML_GUARD(h);
     int rc;
     if ((rc = ensure_prepared(h))) return rc;
     if (rowbase < 0 || rowlimit > h->ref.n || rowlimit < rowbase)
         return fail(SIML_ERR_RANGE, "row range [%lld, %lld) outside the ref set of %lld rows",
                     (long long)rowbase, (long long)rowlimit, (long long)h->ref.n);
+    if (col_begin < 0 || col_end > h->qry.n || col_end < col_begin)
+        return fail(SIML_ERR_RANGE, "column range [%lld, %lld) outside the query set of %lld molecules",
+                    (long long)col_begin, (long long)col_end, (long long)h->qry.n);
     if (pitch < 0 || pitch > 0x7FFFFFFFll) return fail(SIML_ERR_INVALID, "siml_neighbors: bad pitch %lld", (long long)pitch);
     const int64_t rows = rowlimit - rowbase;
     if (rows == 0) return SIML_OK;
     if (!counts || (pitch > 0 && !idx)) return fail(SIML_ERR_INVALID, "siml_neighbors: NULL output");
-    NbrCall c{rowbase, rowlimit, lo, hi, pitch, idx, sims, counts};
+    NbrCall c{rowbase, rowlimit, col_begin, col_end, lo, hi, pitch, idx, sims, counts};
     if (where == SIML_DEVICE) return launch_neighbors(h, c);
     const size_t ib = (size_t)(rows * pitch) * 4, cb = (size_t)rows * 4;
     const size_t need = ((ib + 255) / 256 * 256) * (sims ? 2 : 1) + cb;
@@ -782,6 +787,13 @@ int siml_neighbors(siml_engine* h, int64_t rowbase, int64_t rowlimit, float lo, 
     SIML_CUDA(cudaMemcpyAsync(counts, c.counts, cb, cudaMemcpyDefault, h->stream));
     SIML_CUDA(cudaStreamSynchronize(h->stream));
     return SIML_OK;
+}
+
+int siml_neighbors(siml_engine* h, int64_t rowbase, int64_t rowlimit, float lo, float hi, int64_t pitch,
+                   int32_t* idx, float* sims, int32_t* counts, int where) {
+    SIML_GUARD(h);
+    return siml_neighbors_range(h, rowbase, rowlimit, 0, h->qry.n < 0 ? 0 : h->qry.n, lo, hi, pitch, idx, sims,
+                                counts, where);
 }
 
 static int check_range(siml_engine* h, int64_t rowbase, int64_t rowlimit) {

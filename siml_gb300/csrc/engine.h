@@ -91,6 +91,7 @@ struct siml_engine {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed = false;
     int64_t launches = 0;
+    uint64_t generation = 0;              // bumped whenever a set is replaced (plans made before are stale)
 };
 
 namespace siml {
@@ -126,6 +127,7 @@ constexpr int kModeSingle = 1;  // getTanimotoRow: count-sum magnitudes, zero te
 int launch_rows(siml_engine* h, const RowsArgs& a);
 struct NbrCall {
     int64_t rowbase, rowlimit;
+    int64_t col_begin, col_end;   // database columns searched
     float lo, hi;
     int64_t pitch;
     int32_t* idx;        // device [rows, pitch]
@@ -133,6 +135,15 @@ struct NbrCall {
     int32_t* counts;     // device [rows]
 };
 int launch_neighbors(siml_engine* h, const NbrCall& c);
+// Batched neighbour search: items (two int4 each) pulled by a persistent
+// kernel, then the per-output-row finish; rowinfo[rows_out] = {ref row,
+// col_begin, col_end, 0} (ref row -1: unused row).  Queued on st only.
+int batch_nbr_usable(siml_engine* h, const DbLayout* d);
+int launch_batch_neighbors(siml_engine* h, const DbLayout* d, const int4* items, int64_t nitems, unsigned int* head,
+                           const int4* rowinfo, int64_t rows_out, float lo, float hi, int64_t pitch,
+                           int32_t* idx, float* sims, int32_t* counts, cudaStream_t st);
+// Chunks of the window-sorted layout that hold database columns [c0, c1).
+void sorted_chunk_range(const DbLayout* d, int64_t c0, int64_t c1, int64_t& chunk_begin, int64_t& chunk_end);
 // Per-row 101-bin int32 histograms (out [rows, ldo], zeroed here) or one
 // 1000-bin uint64 histogram accumulated into out.
 int launch_hist(siml_engine* h, int64_t rowbase, int64_t rowlimit, bool global, void* out, int64_t ldo);

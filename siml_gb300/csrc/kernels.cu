@@ -70,6 +70,7 @@ struct GroupParams {
     const int32_t* ng;
     const int4* meta;
     int64_t nchunks;
+    int64_t chunk_begin, chunk_end;   // chunks this launch covers (a column range)
     int vt_words;
     int mode;
 };
@@ -130,8 +131,9 @@ __device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
 // Chunks [wb, we) of this warp: the CTA's slice split contiguously.
 __device__ __forceinline__ void warp_range(const GroupParams& p, int64_t& wb, int64_t& we) {
     const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int64_t cb = p.nchunks * blockIdx.y / gridDim.y;
-    const int64_t ce = p.nchunks * (blockIdx.y + 1) / gridDim.y;
+    const int64_t n = p.chunk_end - p.chunk_begin;
+    const int64_t cb = p.chunk_begin + n * blockIdx.y / gridDim.y;
+    const int64_t ce = p.chunk_begin + n * (blockIdx.y + 1) / gridDim.y;
     wb = cb + (ce - cb) * warp / nwarps;
     we = cb + (ce - cb) * (warp + 1) / nwarps;
 }
@@ -267,7 +269,28 @@ struct NbrArgs {
     int32_t* idx;      // [rows, pitch]
     float* sims;       // [rows, pitch] or null
     int32_t* counts;   // [rows], zeroed before the launch
+    int32_t col_begin, col_end;   // database columns searched
+    const int4* rowinfo;          // per output row {ref row, col_begin, col_end, 0}; null: rowbase + row, [col_begin, col_end)
 };
+
+NbrArgs nbr_args(float lo, float hi, int64_t pitch, int32_t* idx, float* sims, int32_t* counts,
+                 int64_t col_begin, int64_t col_end) {
+    NbrArgs a;
+    a.lo = lo;
+    a.hi = hi;
+    a.pitch = pitch;
+    a.idx = idx;
+    a.sims = sims;
+    a.counts = counts;
+    a.col_begin = (int32_t)col_begin;
+    a.col_end = (int32_t)col_end;
+    a.rowinfo = nullptr;
+    if (std::isnan(lo)) a.thr_mode = 2;
+    else if (lo <= 0.0f) a.thr_mode = 1;
+    else a.thr_mode = 0;
+    a.thr_scale = a.thr_mode == 0 ? (float)((double)lo / (1.0 + (double)lo) * (1.0 - 1.0 / 4096.0)) : 0.0f;
+    return a;
+}
 
 // Bit r of the result is set when the count of row r (bit-sliced in planes)
 // is >= th.  MSB-first compare: eq tracks rows equal so far, gt rows greater.
@@ -310,7 +333,7 @@ struct NbrEpi {
 
     __device__ __forceinline__ void operator()(int64_t, const int4& meta, const SlicedCounter<NP>& acc) {
         const int32_t m = meta.x;
-        if (m < 0 || a.thr_mode == 2) return;
+        if (m < a.col_begin || m >= a.col_end || a.thr_mode == 2) return;
         const int32_t mb = meta.y;
         uint32_t cand;
         if (a.thr_mode == 1) {
@@ -663,8 +686,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_topk(const GroupParams p, int k
         ts.coef_min_bits = 0;
     }
     const int nr = build_table(T, rs, p);   // synchronizes the block
-    const int64_t cb = p.nchunks * blockIdx.y / gridDim.y;
-    const int64_t ce = p.nchunks * (blockIdx.y + 1) / gridDim.y;
+    const int64_t cb = p.chunk_begin + (p.chunk_end - p.chunk_begin) * blockIdx.y / gridDim.y;
+    const int64_t ce = p.chunk_begin + (p.chunk_end - p.chunk_begin) * (blockIdx.y + 1) / gridDim.y;
     const int64_t want_warm = (k + 31) / 32 + 8;
     const int64_t warm = (ce - cb) < want_warm ? (ce - cb) : want_warm;
     if ((threadIdx.x >> 5) == 0) {
@@ -743,6 +766,93 @@ __global__ void __launch_bounds__(512) k_topk_merge(const float* part_t, const i
 __global__ void __launch_bounds__(256) k_topk_rowscan(const struct RawArgs ra, int k, int32_t* idx, float* sims,
                                                       int* err);
 
+// -------------------------------------------------------- k_batch_nbr ----
+// Persistent batched neighbour search over ragged jobs (a job = a range of
+// ref rows against a range of database columns).  The plan splits every job
+// into work items of at most 32 rows x a chunk range; one CTA per SM pulls
+// items from a device queue head.  The shared table is updated incrementally:
+// an item whose rows differ from the CTA's current rows first clears the
+// current rows' bits (their vid lists, not the whole table) and then sets its
+// own.  Lanes outside the job's columns are masked in the epilogue.
+// Item layout: two int4 {row0, nrows, out_row0, col_begin}, {col_end, c0, c1, 0}.
+__device__ __forceinline__ void set_rows(uint32_t* T, RowSmem& rs, const GroupParams& p, int64_t row0, int nr,
+                                         int64_t out0) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    if (warp == 0) {
+        const int r = lane;
+        const int64_t gr = r < nr ? row0 + r : row0;
+        const int am = r < nr ? p.row_mag[gr] : 0;
+        rs.orow[r] = (int)(out0 + r);
+        rs.amag[r] = am;
+        rs.amagf[r] = (float)am;
+        rs.alen[r] = r < nr ? p.row_len[gr] : 0;
+        const bool f = r >= nr || fast_mag(am, p.row_cmag[gr]);
+        const unsigned all = __ballot_sync(0xFFFFFFFFu, f);
+        int mn = r < nr ? am : 0x7FFFFFFF;
+        for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
+        if (r == 0) {
+            rs.allfast = all == 0xFFFFFFFFu;
+            rs.min_amag = mn;
+        }
+    }
+    for (int r = warp; r < nr; r += nwarps) {
+        const uint32_t* rv = p.row_vid + (row0 + r) * p.row_stride;
+        for (int64_t e = lane; e < p.row_stride; e += 32) {
+            const uint32_t v = rv[e];
+            if (v) atomicOr(&T[v], 1u << r);
+        }
+    }
+}
+
+__device__ __forceinline__ void clear_rows(uint32_t* T, const GroupParams& p, int64_t row0, int nr) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    for (int r = warp; r < nr; r += nwarps) {
+        const uint32_t* rv = p.row_vid + (row0 + r) * p.row_stride;
+        for (int64_t e = lane; e < p.row_stride; e += 32) {
+            const uint32_t v = rv[e];
+            if (v) T[v] = 0u;
+        }
+    }
+}
+
+template <int NP, typename ET>
+__global__ void __launch_bounds__(kThreads, 1) k_batch_nbr(const GroupParams p, const int4* __restrict__ items,
+                                                           int64_t nitems, unsigned int* head, NbrArgs a) {
+    extern __shared__ __align__(16) uint32_t T[];
+    __shared__ RowSmem rs;
+    __shared__ long long s_item;
+    __shared__ long long cur_row0, cur_out0;
+    __shared__ int cur_nr;
+    for (int i = threadIdx.x * 4; i < p.vt_words; i += blockDim.x * 4)
+        *reinterpret_cast<uint4*>(T + i) = make_uint4(0u, 0u, 0u, 0u);
+    if (threadIdx.x == 0) { cur_row0 = -1; cur_out0 = -1; cur_nr = 0; }
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (long long)atomicAdd(head, 1u);
+        __syncthreads();
+        const long long w = s_item;
+        if (w >= nitems) break;
+        const int4 ia = items[2 * w], ib = items[2 * w + 1];
+        const int64_t row0 = ia.x, out0 = ia.z;
+        const int nr = ia.y;
+        if (row0 != cur_row0 || nr != cur_nr || out0 != cur_out0) {
+            if (cur_nr > 0) clear_rows(T, p, cur_row0, cur_nr);
+            __syncthreads();
+            set_rows(T, rs, p, row0, nr, out0);
+            if (threadIdx.x == 0) { cur_row0 = row0; cur_nr = nr; cur_out0 = out0; }
+            __syncthreads();
+        }
+        NbrArgs ai = a;
+        ai.col_begin = ia.w;
+        ai.col_end = ib.x;
+        const int64_t c0 = ib.y, c1 = ib.z;
+        const int64_t wb = c0 + (c1 - c0) * warp / nwarps, we = c0 + (c1 - c0) * (warp + 1) / nwarps;
+        NbrEpi<NP> epi{rs, nr, out0, ai};
+        stream_chunks<NP, ET>(T, p, wb, we, epi);
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------- k_nbr_finish ----
 struct RawArgs {
     const int32_t *rl, *rc, *rlen, *rmag, *rcmag;
@@ -776,6 +886,15 @@ __global__ void __launch_bounds__(128) k_nbr_finish(const RawArgs ra, const NbrA
     __shared__ int wcount[4];
     const int64_t row = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int64_t ref_row = ra.rowbase + row;
+    int64_t col0 = a.col_begin, col1 = a.col_end;
+    if (a.rowinfo) {
+        const int4 ri = a.rowinfo[row];
+        if (ri.x < 0) return;   // output row not covered by any job
+        ref_row = ri.x;
+        col0 = ri.y;
+        col1 = ri.z;
+    }
     int32_t* idx = a.idx + row * a.pitch;
     float* sims = a.sims ? a.sims + row * a.pitch : nullptr;
     const int n = force_ordered ? 0x7FFFFFFF : a.counts[row];
@@ -809,17 +928,17 @@ __global__ void __launch_bounds__(128) k_nbr_finish(const RawArgs ra, const NbrA
         }
         return;
     }
-    // ordered recompute
-    const int64_t r = ra.rowbase + row;
+    // ordered recompute over [col0, col1), waves of 128 from col0
+    const int64_t r = ref_row;
     const int32_t* ar = ra.rl + r * ra.rw;
     const int32_t* acnt = ra.rc + r * ra.rw;
     const int32_t alen = ra.rlen[r], ma = ra.rmag[r];
     int64_t count = 0;
-    for (int64_t base = 0; base < ra.nq; base += 128) {
+    for (int64_t base = col0; base < col1; base += 128) {
         const int64_t col = base + tid;
         bool flag = false;
         float t = 0.0f;
-        if (col < ra.nq) {
+        if (col < col1) {
             const int32_t mb = ra.qmag[col];
             const float bound = __fdiv_rn(__int2float_rn(min(ma, mb)), __int2float_rn(max(ma, mb)));
             if (bound >= a.lo) {
@@ -1015,6 +1134,8 @@ bool table_params(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t ro
     p.ng = d->ng;
     p.meta = d->meta;
     p.nchunks = d->nchunks;
+    p.chunk_begin = 0;
+    p.chunk_end = d->nchunks;
     p.vt_words = vt_words;
     p.mode = mode;
     return true;
@@ -1047,7 +1168,7 @@ int launch_nbr_t(siml_engine* h, const GroupParams& p, size_t smem, const NbrArg
     const int64_t groups = (p.rows + 31) / 32;
     int rc = set_smem(k_nbr<NP, ET>, smem);
     if (rc) return rc;
-    const int s = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
+    const int s = choose_splits(groups, p.chunk_end - p.chunk_begin, h->num_sms, kThreads / 32);
     dim3 grid((unsigned)groups, (unsigned)s);
     SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
     k_nbr<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, a);
@@ -1089,7 +1210,56 @@ int launch_topk_t(siml_engine* h, const GroupParams& p, size_t smem, int k, int 
     return SIML_OK;
 }
 
+template <int NP, typename ET>
+int launch_batch_t(siml_engine* h, const GroupParams& p, size_t smem, const int4* items, int64_t nitems,
+                   unsigned int* head, const NbrArgs& a, cudaStream_t st) {
+    int rc = set_smem(k_batch_nbr<NP, ET>, smem);
+    if (rc) return rc;
+    k_batch_nbr<NP, ET><<<(unsigned)h->num_sms, kThreads, smem, st>>>(p, items, nitems, head, a);
+    SIML_CUDA(cudaGetLastError());
+    return SIML_OK;
+}
+
 }  // namespace
+
+int batch_nbr_usable(siml_engine* h, const DbLayout* d) {
+    GroupParams p;
+    size_t smem = 0;
+    int np = 0;
+    return table_params(h, d, 0, 1, kModeRows, p, smem, np) ? 1 : 0;
+}
+
+int launch_batch_neighbors(siml_engine* h, const DbLayout* d, const int4* items, int64_t nitems, unsigned int* head,
+                           const int4* rowinfo, int64_t rows_out, float lo, float hi, int64_t pitch,
+                           int32_t* idx, float* sims, int32_t* counts, cudaStream_t st) {
+    NbrArgs a = nbr_args(lo, hi, pitch, idx, sims, counts, 0, 0);
+    a.rowinfo = rowinfo;
+    SIML_CUDA(cudaMemsetAsync(counts, 0, rows_out * sizeof(int32_t), st));
+    SIML_CUDA(cudaMemsetAsync(head, 0, sizeof(unsigned int), st));
+    GroupParams p;
+    size_t smem = 0;
+    int np = 0;
+    int force_ordered = 1;
+    int rc;
+    if (nitems > 0 && table_params(h, d, 0, 1, kModeRows, p, smem, np)) {
+        force_ordered = 0;
+        if (np == 8)
+            rc = d->entry_bytes == 2 ? launch_batch_t<8, uint16_t>(h, p, smem, items, nitems, head, a, st)
+                                     : launch_batch_t<8, uint32_t>(h, p, smem, items, nitems, head, a, st);
+        else
+            rc = d->entry_bytes == 2 ? launch_batch_t<16, uint16_t>(h, p, smem, items, nitems, head, a, st)
+                                     : launch_batch_t<16, uint32_t>(h, p, smem, items, nitems, head, a, st);
+        if (rc) return rc;
+        h->launches++;
+    }
+    if (rows_out > 0) {
+        k_nbr_finish<<<(unsigned)rows_out, 128, 0, st>>>(raw_args(h, 0), a, force_ordered);
+        SIML_CUDA(cudaGetLastError());
+        h->launches++;
+    }
+    return SIML_OK;
+}
+
 
 int topk_plan(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t rowlimit, int k, TopkPlan& plan) {
     const int64_t rows = rowlimit - rowbase;
@@ -1237,33 +1407,28 @@ int launch_rows(siml_engine* h, const RowsArgs& a) {
     return SIML_OK;
 }
 
+void sorted_chunk_range(const DbLayout* d, int64_t c0, int64_t c1, int64_t& chunk_begin, int64_t& chunk_end) {
+    const int64_t per_window = kWindow / kChunk;
+    chunk_begin = (c0 / kWindow) * per_window;
+    chunk_end = std::min<int64_t>(d->nchunks, ((c1 + kWindow - 1) / kWindow) * per_window);
+    if (c1 <= c0) chunk_end = chunk_begin;
+}
+
+
 int launch_neighbors(siml_engine* h, const NbrCall& c) {
     const DbLayout* d = nullptr;
     int rc = ensure_layout(h, true, &d);
     if (rc) return rc;
     const int64_t rows = c.rowlimit - c.rowbase;
-    NbrArgs a;
-    a.lo = c.lo;
-    a.hi = c.hi;
-    a.pitch = c.pitch;
-    a.idx = c.idx;
-    a.sims = c.sims;
-    a.counts = c.counts;
-    if (std::isnan(c.lo)) {
-        a.thr_mode = 2;
-    } else if (c.lo <= 0.0f) {
-        a.thr_mode = 1;
-    } else {
-        a.thr_mode = 0;
-    }
-    a.thr_scale = a.thr_mode == 0 ? (float)((double)c.lo / (1.0 + (double)c.lo) * (1.0 - 1.0 / 4096.0)) : 0.0f;
+    NbrArgs a = nbr_args(c.lo, c.hi, c.pitch, c.idx, c.sims, c.counts, c.col_begin, c.col_end);
     SIML_CUDA(cudaMemsetAsync(c.counts, 0, rows * sizeof(int32_t), h->stream));
     GroupParams p;
     size_t smem = 0;
     int np = 0;
     int force_ordered = 1;
-    if (table_params(h, d, c.rowbase, rows, kModeRows, p, smem, np)) {
+    if (c.col_end > c.col_begin && table_params(h, d, c.rowbase, rows, kModeRows, p, smem, np)) {
         force_ordered = 0;
+        sorted_chunk_range(d, c.col_begin, c.col_end, p.chunk_begin, p.chunk_end);
         if ((rc = row_order_by_magnitude(h, c.rowbase, c.rowlimit, &p.row_order))) return rc;
         if (np == 8)
             rc = d->entry_bytes == 2 ? launch_nbr_t<8, uint16_t>(h, p, smem, a) : launch_nbr_t<8, uint32_t>(h, p, smem, a);

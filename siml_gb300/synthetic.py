@@ -44,3 +44,19 @@ def smiles_set(seed: int, dist: int, n: int, first: int = 0):
     """Compiled set: (lingos [n,w], counts [n,w], lengths [n], mags [n])."""
     buf, off = smiles_buffer(seed, dist, n, first)
     return compile_buffer(buf, off)
+
+
+def ragged_jobs(seed: int, n_db: int, njobs: int, rows_max: int = 2048, cols_min: int = 1000,
+                cols_max: int = 200_000):
+    """Neighbour jobs over one n_db-molecule set used as both sides: int64
+    [njobs, 4] {row_begin, row_end, col_begin, col_end}.  Row counts are
+    log-uniform in [1, rows_max], column counts log-uniform in [cols_min,
+    cols_max]; both ranges start uniformly at random."""
+    rng = np.random.default_rng(seed)
+    nr = np.floor(np.exp(rng.uniform(0.0, np.log(rows_max + 1), njobs))).astype(np.int64).clip(1, rows_max)
+    nc = np.floor(np.exp(rng.uniform(np.log(cols_min), np.log(cols_max + 1), njobs))).astype(np.int64)
+    nc = nc.clip(cols_min, min(cols_max, n_db))
+    nr = nr.clip(1, n_db)
+    rb = np.floor(rng.random(njobs) * (n_db - nr + 1)).astype(np.int64)
+    cb = np.floor(rng.random(njobs) * (n_db - nc + 1)).astype(np.int64)
+    return np.ascontiguousarray(np.stack([rb, rb + nr, cb, cb + nc], 1))

@@ -1,0 +1,158 @@
+"""Batched ragged neighbour jobs and the column-range search against the
+oracle: each job (ref rows, query columns) must give exactly what the
+reference's getNeighbors (pysiml/kernels.py:393-475) gives on that slice of
+the query set — counts (overflow waves starting at the slice's first column),
+ascending absolute indices and bit-identical similarities — whatever the tile
+shape, order of work items, or CUDA-graph replay."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine(ref, qry):
+    from siml_gb300 import GPULingo
+    gl = GPULingo(0)
+    gl.set_refsmiles(*ref)
+    gl.set_qsmiles(*qry)
+    return gl
+
+
+def _cmp(oracle, ref, qry, job, res, lo, hi, maxneighbors, with_sims=True):
+    rb, re, cb, ce = job[:4]
+    oidx, osims, ocnt = oracle.neighbors_range_block(ref, qry, rb, re, cb, ce, lo, hi, maxneighbors)
+    if with_sims:
+        idx, sims, cnt = res
+    else:
+        idx, cnt = res
+        sims = None
+    assert np.array_equal(cnt, ocnt), job
+    pitch = oidx.shape[1]
+    for r in range(re - rb):
+        k = min(int(cnt[r]), pitch)
+        assert np.array_equal(idx[r, :k], oidx[r, :k]), (job, r)
+        if sims is not None:
+            assert np.array_equal(sims[r, :k].view(np.uint32), osims[r, :k].view(np.uint32)), (job, r)
+
+
+def _golden_sets(golden):
+    q = (golden["lingos"], golden["counts"], golden["lengths"], golden["mags"])
+    return q, q
+
+
+@pytest.mark.parametrize("cols", [(0, 533), (7, 300), (128, 129), (256, 512), (500, 533), (40, 40)])
+@pytest.mark.parametrize("lo,hi,maxn", [(0.3, 1.1, None), (0.02, 1.1, 10), (0.0, 0.5, 40)])
+def test_neighbors_range_golden(native, oracle, golden, cols, lo, hi, maxn):
+    ref, qry = _golden_sets(golden)
+    gl = _engine(ref, qry)
+    n = ref[0].shape[0]
+    cb, ce = cols
+    m, c = gl.getNeighborsRange(0, n, cb, ce, lo, hi, maxn)
+    _cmp(oracle, ref, qry, (0, n, cb, ce), (m, c), lo, hi, maxn, with_sims=False)
+
+
+def _ragged_jobs(rng, nref, nq, njobs):
+    jobs = []
+    for _ in range(njobs):
+        nr = int(rng.integers(0, 70))
+        rb = int(rng.integers(0, nref - nr + 1))
+        w = int(rng.integers(0, nq + 1))
+        cb = int(rng.integers(0, nq - w + 1))
+        jobs.append((rb, rb + nr, cb, cb + w))
+    return jobs
+
+
+@pytest.mark.parametrize("tile", [1, 3, 64, 0])
+def test_batch_ragged_jobs(native, oracle, set4096, tile):
+    rng = np.random.default_rng(7 + tile)
+    gl = _engine(set4096, set4096)
+    jobs = _ragged_jobs(rng, 4096, 4096, 24)
+    jobs += [(0, 32, 0, 4096), (4090, 4096, 4000, 4096), (10, 10, 0, 100), (50, 60, 300, 300)]
+    lo, hi, maxn = 0.06, 1.1, 48
+    plan = gl.planNeighborBatch(jobs, lo, hi, maxn, tile_chunks=tile)
+    assert plan.tile_chunks >= 1
+    idx, sims, cnt = plan.buffers(with_sims=True)
+    plan.run(idx, sims, cnt)
+    for job, res in zip(jobs, plan.split(idx, sims, cnt)):
+        _cmp(oracle, set4096, set4096, job, res, lo, hi, maxn)
+
+
+def test_batch_matches_plain_path_and_overflow(native, oracle, set4096):
+    """Low threshold and a small pitch: many rows overflow; the batch gives
+    the plain per-job path's result and the oracle's."""
+    gl = _engine(set4096, set4096)
+    jobs = [(0, 40, 0, 4096), (40, 41, 1000, 3000), (100, 133, 129, 2177), (3000, 3100, 3500, 4096)]
+    lo, maxn = 0.05, 20
+    res = gl.getNeighborsBatch(jobs, lo, 1.1, maxn, with_sims=True)
+    for job, r in zip(jobs, res):
+        _cmp(oracle, set4096, set4096, job, r, lo, 1.1, maxn)
+        m, c = gl.getNeighborsRange(*job, lo, 1.1, maxn)
+        assert np.array_equal(c, r[2])
+        for i in range(len(c)):
+            k = min(int(c[i]), 32)
+            assert np.array_equal(m[i, :k], r[0][i, :k])
+    assert any(np.any(r[2] > 32) for r in res)
+
+
+def test_batch_output_rows_and_gaps(native, oracle, set4096):
+    """Explicit output rows with a gap: rows of no job get count 0."""
+    import torch
+    gl = _engine(set4096, set4096)
+    jobs = [(5, 9, 0, 2048, 10), (200, 202, 2048, 4096, 0)]
+    plan = gl.planNeighborBatch(jobs, 0.06, 1.1, 16)
+    assert plan.rows_out == 14
+    idx, sims, cnt = plan.buffers()
+    cnt.fill_(-7)   # every output row's count is written
+    plan.run(idx, sims, cnt)
+    c = cnt.cpu().numpy()
+    assert np.all(c[2:10] == 0)
+    for job, res in zip(jobs, plan.split(idx, sims, cnt)):
+        _cmp(oracle, set4096, set4096, job, res, 0.06, 1.1, 16, with_sims=False)
+    del torch
+
+
+def test_batch_graph_replay(native, oracle, set4096):
+    """A run captured in a CUDA graph replays to the same result."""
+    import torch
+    gl = _engine(set4096, set4096)
+    rng = np.random.default_rng(11)
+    jobs = _ragged_jobs(rng, 4096, 4096, 16)
+    plan = gl.planNeighborBatch(jobs, 0.06, 1.1, 32, tile_chunks=16)
+    idx, sims, cnt = plan.buffers(with_sims=True)
+    plan.run(idx, sims, cnt)
+    ref_res = plan.split(idx, sims, cnt)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):   # warm-up run on the capture stream
+        plan.run(idx, sims, cnt, stream=s)
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        plan.run(idx, sims, cnt, stream=torch.cuda.current_stream())
+    for _ in range(3):
+        idx.fill_(-1)
+        cnt.fill_(-1)
+        g.replay()
+        got = plan.split(idx, sims, cnt)
+        for a, b in zip(got, ref_res):
+            assert np.array_equal(a[2], b[2])
+            for i in range(len(a[2])):
+                k = min(int(a[2][i]), plan.pitch)
+                assert np.array_equal(a[0][i, :k], b[0][i, :k])
+                assert np.array_equal(a[1][i, :k].view(np.uint32), b[1][i, :k].view(np.uint32))
+
+
+def test_batch_plan_errors(native, set4096):
+    from siml_gb300 import synthetic as S
+    gl = _engine(set4096, set4096)
+    with pytest.raises(ValueError):   # two jobs write output row 3
+        gl.planNeighborBatch([(0, 4, 0, 10, 0), (10, 12, 0, 10, 3)], 0.5)
+    with pytest.raises(RuntimeError):
+        gl.planNeighborBatch([(0, 4, 0, 5000)], 0.5)
+    with pytest.raises(RuntimeError):
+        gl.getNeighborsRange(0, 4, 10, 5, 0.5)
+    plan = gl.planNeighborBatch([(0, 4, 0, 100)], 0.5, 1.1, 16)
+    idx, sims, cnt = plan.buffers()
+    gl.set_qsmiles(*S.smiles_set(S.SEED_ALLPAIRS, S.UNIFORM_20_90, 512))
+    with pytest.raises(RuntimeError):   # the plan belongs to the replaced set
+        plan.run(idx, sims, cnt)
