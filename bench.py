@@ -210,6 +210,10 @@ def gpu_arm(args):
     t = time.time()
     gl.set_qsmiles(*db)
     gl.set_refsmiles(*q)
+    if args.rows_window:
+        gl.setRowsWindow(args.rows_window)
+    if args.rows_entries >= 0:
+        gl.setRowsEntries(args.rows_entries)
     stats = gl.dbStats()
     torch.cuda.synchronize()
     log("database layout ready in %.2f s: %s" % (time.time() - t, stats))
@@ -336,6 +340,7 @@ def gpu_arm(args):
             "config": {"workload": {"rows_1m": WORKLOAD, "nbr_1m": NBR_WORKLOAD, "topk_1m": TOPK_WORKLOAD,
                                     "hist_1m": HIST_WORKLOAD}[wl], "rows_per_step": rows_step, "db_molecules": DB_N,
                        "query_rows": QUERY_N, "parallelism": "replicas" if world > 1 else "single",
+                       "rows_window": gl.rowsWindow(), "rows_entries": gl.rowsEntries(),
                        "l2": "flushed between steps by a 256 MB write; each step also writes a 4 GB block",
                        "db_layout": stats},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
@@ -539,10 +544,15 @@ def ragged_arm(args):
     except (OSError, ValueError):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = plan.stream_bytes / (ms_per_step / 1e3) / 1e9
+    out_bytes = plan.rows_out * (plan.pitch * 8 + 4)
+    alg_bytes = plan.unique_bytes + out_bytes
+    achieved = alg_bytes / (ms_per_step / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "k_batch_nbr (+ k_nbr_finish)", "kernel_ms": ms_per_step,
-                "algorithmic_bytes_per_launch": plan.stream_bytes,
+                "traffic": read_profile_traffic("k_batch_nbr_ragged2m.md"), "kernel": "k_batch_nbr (+ k_nbr_finish)",
+                "kernel_ms": ms_per_step, "algorithmic_bytes_per_launch": alg_bytes,
+                "streamed_bytes_per_launch": plan.stream_bytes,
+                "note": "algorithmic bytes = every job's database range once + the output lists; the kernel "
+                        "streams each range once per 32-row group (mostly L2 hits) and is bound by integer issue",
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback"}
 
     e2e = cpu = None
@@ -597,9 +607,10 @@ def ragged_arm(args):
     return 0
 
 
-def read_profile_traffic():
-    """DRAM bytes per k_rows launch from the committed ncu summary, if any."""
-    path = os.path.join(REPO, "profiles", "k_rows_rows1m.md")
+def read_profile_traffic(name="k_rows_rows1m.md"):
+    """DRAM bytes per launch of the dominant kernel from its committed ncu
+    summary (a "traffic_bytes_per_launch:" line), if any."""
+    path = os.path.join(REPO, "profiles", name)
     try:
         for ln in open(path):
             if ln.startswith("traffic_bytes_per_launch:"):
@@ -655,6 +666,11 @@ def main():
                          "topk_1m: top-100 per row; hist_1m: 1000-bin histogram of every pair; "
                          "ragged_2m: 4,096 batched neighbour jobs vs the plain per-job path")
     ap.add_argument("--ragged-jobs", type=int, default=RAGGED_JOBS, help="jobs of the ragged_2m workload")
+    ap.add_argument("--rows-window", type=int, default=0,
+                    help="sort window of the full-matrix layout (32, 64, 128, 256; 0: library default)")
+    ap.add_argument("--rows-entries", type=int, default=-1,
+                    help="entry format of the full-matrix layout (0 auto, 1 u16, 2 u32, 3 byte offsets; "
+                         "-1: library default)")
     ap.add_argument("--tile-chunks", type=int, default=0,
                     help="ragged_2m: chunks per work item (0: autotuned when the plan is made)")
     ap.add_argument("--no-extras", action="store_true",

@@ -166,10 +166,11 @@ int siml_batch_create(siml_engine* h, int64_t njobs, const int64_t* jobs,
                       siml_batch** out);
 /* rows_out: output rows the plan writes (max out_row + rows over jobs);
  * nitems: work items; tile_chunks: the tile the plan uses; stream_bytes:
- * database bytes (entries and per-molecule metadata) one run reads.  NULL
+ * database bytes (entries and per-molecule metadata) one run streams, every
+ * work item's chunks; unique_bytes: every job's database range once.  NULL
  * skips an output. */
 int siml_batch_info(siml_batch* b, int64_t* rows_out, int64_t* nitems, int64_t* tile_chunks,
-                    int64_t* stream_bytes);
+                    int64_t* stream_bytes, int64_t* unique_bytes);
 /* Queues the plan on stream (a cudaStream_t; NULL: the engine's stream):
  * device outputs idx, sims (may be NULL): [rows_out, pitch]; counts:
  * [rows_out], with siml_neighbors' meaning.  No host synchronization and
@@ -213,6 +214,24 @@ int siml_synth_smiles(uint64_t seed, int dist, int64_t first, int64_t n,
  * molecules, out[4] = largest chunk in groups per lane, out[5] = database
  * molecules, out[6] / out[7] = largest count sum in the ref / query set. */
 int siml_db_stats(siml_engine* h, int64_t out[8]);
+/* Layout tuning (no reference counterpart).  SIML_TUNE_ROWS_WINDOW: the
+ * full-matrix layout (siml_rows, siml_row_single) sorts database molecules by
+ * entry count inside windows of 32 (natural order), 64, 128 or 256 molecules;
+ * wider windows pad less but scatter each warp's stores over more of a row.
+ * Changing it drops the current full-matrix layout (rebuilt on next use). */
+#define SIML_TUNE_ROWS_WINDOW 1
+/* SIML_TUNE_ROWS_ENTRIES: how the full-matrix layout stores entries:
+ * SIML_ENTRIES_AUTO (2-byte vids when the vocabulary allows, else 4-byte),
+ * SIML_ENTRIES_U32 (4-byte vids), SIML_ENTRIES_OFFSETS (4-byte table byte
+ * offsets: no index arithmetic in the inner loop, twice the bytes of 2-byte
+ * vids).  Changing it drops the current full-matrix layout. */
+#define SIML_TUNE_ROWS_ENTRIES 2
+#define SIML_ENTRIES_AUTO 0
+#define SIML_ENTRIES_U16 1     /* as AUTO: 2-byte when the vocabulary allows */
+#define SIML_ENTRIES_U32 2
+#define SIML_ENTRIES_OFFSETS 3
+int siml_set_tuning(siml_engine* h, int key, int64_t value);
+int siml_get_tuning(siml_engine* h, int key, int64_t* value);
 /* Number of kernel launches this engine has issued since creation. */
 int64_t siml_launch_count(siml_engine* h);
 /* Average device time (ms) of the dominant kernel of the last call on this

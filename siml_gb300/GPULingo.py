@@ -436,6 +436,26 @@ class GPULingo:
         keys = ["nvid", "entry_bytes", "ngroups_total", "nchunks", "max_ng", "n", "ref_max_entries", "qry_max_entries"]
         return dict(zip(keys, [int(x) for x in a]))
 
+    def setRowsWindow(self, window):
+        """Sort window (32 = natural order, 64, 128 or 256) of the layout the
+        full-matrix calls stream; see SIML_TUNE_ROWS_WINDOW."""
+        N.check(N.lib().siml_set_tuning(self._h, N.SIML_TUNE_ROWS_WINDOW, int(window)), "setRowsWindow")
+
+    def setRowsEntries(self, fmt):
+        """Entry format of the full-matrix layout (SIML_ENTRIES_AUTO, _U16,
+        _U32 or _OFFSETS); see SIML_TUNE_ROWS_ENTRIES."""
+        N.check(N.lib().siml_set_tuning(self._h, N.SIML_TUNE_ROWS_ENTRIES, int(fmt)), "setRowsEntries")
+
+    def rowsEntries(self):
+        v = ctypes.c_int64()
+        N.check(N.lib().siml_get_tuning(self._h, N.SIML_TUNE_ROWS_ENTRIES, ctypes.byref(v)), "rowsEntries")
+        return int(v.value)
+
+    def rowsWindow(self):
+        v = ctypes.c_int64()
+        N.check(N.lib().siml_get_tuning(self._h, N.SIML_TUNE_ROWS_WINDOW, ctypes.byref(v)), "rowsWindow")
+        return int(v.value)
+
     def launchCount(self):
         """Kernel launches issued by this object so far."""
         return int(N.lib().siml_launch_count(self._h))

@@ -24,6 +24,13 @@ SIML_ERR_RANGE = 7
 SIML_HOST = 0
 SIML_DEVICE = 1
 
+SIML_TUNE_ROWS_WINDOW = 1
+SIML_TUNE_ROWS_ENTRIES = 2
+SIML_ENTRIES_AUTO = 0
+SIML_ENTRIES_U16 = 1
+SIML_ENTRIES_U32 = 2
+SIML_ENTRIES_OFFSETS = 3
+
 SYNTH_UNIFORM_20_90 = 0
 SYNTH_LOGNORMAL_45 = 1
 SYNTH_BIMODAL_35_110 = 2
@@ -63,7 +70,7 @@ _SIGNATURES = {
     "siml_topk_noalloc": (_I32, [_P, _I64, _I64, _I64, _P, _P]),
     "siml_neighbors_range": (_I32, [_P, _I64, _I64, _I64, _I64, _F32, _F32, _I64, _P, _P, _P, _I32]),
     "siml_batch_create": (_I32, [_P, _I64, _P, _F32, _F32, _I64, _I64, _P]),
-    "siml_batch_info": (_I32, [_P, _P, _P, _P, _P]),
+    "siml_batch_info": (_I32, [_P, _P, _P, _P, _P, _P]),
     "siml_batch_run": (_I32, [_P, _P, _P, _P, _P]),
     "siml_batch_destroy": (_I32, [_P]),
     "siml_compile_width": (_I64, [_P, _P, _I64]),
@@ -73,6 +80,8 @@ _SIGNATURES = {
     "siml_synth_lengths": (_I32, [_U64, _I32, _I64, _I64, _P]),
     "siml_synth_smiles": (_I32, [_U64, _I32, _I64, _I64, _P, _I64, _P]),
     "siml_db_stats": (_I32, [_P, _P]),
+    "siml_set_tuning": (_I32, [_P, _I32, _I64]),
+    "siml_get_tuning": (_I32, [_P, _I32, ctypes.POINTER(_I64)]),
     "siml_launch_count": (_I64, [_P]),
     "siml_last_kernel_ms": (ctypes.c_double, [_P]),
 }

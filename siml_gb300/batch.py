@@ -57,11 +57,12 @@ class NeighborBatch:
         N.check(N.lib().siml_batch_create(gl._h, self.jobs.shape[0], self.jobs.ctypes.data,
                                           ctypes.c_float(lowerbound), ctypes.c_float(upperbound), self.pitch,
                                           int(tile_chunks), ctypes.byref(self._b)), "siml_batch_create")
-        r, n, t, sb = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        r, n, t, sb, ub = (ctypes.c_int64() for _ in range(5))
         N.check(N.lib().siml_batch_info(self._b, ctypes.byref(r), ctypes.byref(n), ctypes.byref(t),
-                                        ctypes.byref(sb)), "siml_batch_info")
+                                        ctypes.byref(sb), ctypes.byref(ub)), "siml_batch_info")
         self.rows_out, self.nitems, self.tile_chunks = int(r.value), int(n.value), int(t.value)
-        self.stream_bytes = int(sb.value)   # database bytes one run reads
+        self.stream_bytes = int(sb.value)   # database bytes one run streams (every work item)
+        self.unique_bytes = int(ub.value)   # every job's database range once
         self.pairs = int(sum(max(0, j[1] - j[0]) * max(0, j[3] - j[2]) for j in self.jobs.tolist()))
 
     def __del__(self):

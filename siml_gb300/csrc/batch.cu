@@ -31,6 +31,7 @@ struct siml_batch {
     int64_t pitch = 0;
     int64_t tile_chunks = 0;
     int64_t stream_bytes = 0;
+    int64_t unique_bytes = 0;
 };
 
 namespace siml {
@@ -168,18 +169,27 @@ int autotune_tile(siml_engine* h, const DbLayout* d, const std::vector<HostJob>&
     return rc;
 }
 
-// Algorithmic bytes one run streams: for every item, its chunks' entry
-// groups and per-lane metadata (the table and outputs are small beside them).
-int stream_bytes_of(siml_engine* h, const DbLayout* d, const std::vector<int4>& items, int64_t* out) {
+// Bytes one run reads: *streamed = every item's chunks (entry groups and
+// per-lane metadata), as the kernel reads them, mostly from L2; *unique =
+// every job's chunk range once, the least any schedule must bring from DRAM.
+int plan_bytes(siml_engine* h, const DbLayout* d, const std::vector<HostJob>& jobs, const std::vector<int4>& items,
+               int64_t* streamed, int64_t* unique) {
     std::vector<int64_t> off((size_t)d->nchunks + 1);
     SIML_CUDA(cudaMemcpyAsync(off.data(), d->off, off.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, h->stream));
     SIML_CUDA(cudaStreamSynchronize(h->stream));
-    int64_t b = 0;
-    for (size_t i = 1; i < items.size(); i += 2) {
-        const int64_t c0 = items[i].y, c1 = items[i].z;
-        b += (off[(size_t)c1] - off[(size_t)c0]) * 16 + (c1 - c0) * 32 * (int64_t)sizeof(int4);
+    auto range_bytes = [&](int64_t c0, int64_t c1) {
+        return (off[(size_t)c1] - off[(size_t)c0]) * 16 + (c1 - c0) * 32 * (int64_t)sizeof(int4);
+    };
+    int64_t b = 0, u = 0;
+    for (size_t i = 1; i < items.size(); i += 2) b += range_bytes(items[i].y, items[i].z);
+    for (const HostJob& j : jobs) {
+        if (j.re <= j.rb || j.ce <= j.cb) continue;
+        int64_t c0, c1;
+        sorted_chunk_range(d, j.cb, j.ce, c0, c1);
+        u += range_bytes(c0, c1);
     }
-    *out = b;
+    *streamed = b;
+    *unique = u;
     return SIML_OK;
 }
 
@@ -241,7 +251,7 @@ int siml_batch_create(siml_engine* h, int64_t njobs, const int64_t* jobs, float 
     std::vector<int4> items;
     make_items(d, hj, tile, items);
     b->nitems = (int64_t)items.size() / 2;
-    if ((rc = stream_bytes_of(h, d, items, &b->stream_bytes)) || (rc = upload_items(h, items, &b->items)) ||
+    if ((rc = plan_bytes(h, d, hj, items, &b->stream_bytes, &b->unique_bytes)) || (rc = upload_items(h, items, &b->items)) ||
         (rc = upload_items(h, rowinfo, &b->rowinfo))) {
         siml_batch_destroy(b);
         return rc;
@@ -256,13 +266,14 @@ int siml_batch_create(siml_engine* h, int64_t njobs, const int64_t* jobs, float 
 }
 
 int siml_batch_info(siml_batch* b, int64_t* rows_out, int64_t* nitems, int64_t* tile_chunks,
-                    int64_t* stream_bytes) {
+                    int64_t* stream_bytes, int64_t* unique_bytes) {
     clear_error();
     if (!b) return fail(SIML_ERR_INVALID, "siml_batch_info: NULL batch");
     if (rows_out) *rows_out = b->rows_out;
     if (nitems) *nitems = b->nitems;
     if (tile_chunks) *tile_chunks = b->tile_chunks;
     if (stream_bytes) *stream_bytes = b->stream_bytes;
+    if (unique_bytes) *unique_bytes = b->unique_bytes;
     return SIML_OK;
 }
 

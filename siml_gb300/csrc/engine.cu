@@ -280,18 +280,20 @@ __device__ __forceinline__ uint32_t vocab_lookup(const unsigned long long* __res
 }
 
 // One CTA of 256 threads per window: rank molecules by (entries, index).
-__global__ void k_window_sort(const int32_t* __restrict__ cmag, int64_t n, int32_t* perm) {
+__global__ void k_window_sort(const int32_t* __restrict__ cmag, int64_t n, int w, int32_t* perm) {
     __shared__ long long key[kWindow];
     const int64_t base = (int64_t)blockIdx.x * kWindow;
     const int t = threadIdx.x;
     const int64_t m = base + t;
-    // molecules past the end sort last
+    // molecules past the end sort last; ranks count only keys of the same
+    // w-molecule sub-window
     key[t] = m < n ? ((long long)cmag[m] << 20) | t : (0x7FFFFFFFll << 20) | t;
     __syncthreads();
     const long long mine = key[t];
+    const int w0 = t / w * w;
     int rank = 0;
-    for (int k = 0; k < kWindow; k++) rank += key[k] < mine;
-    perm[base + rank] = m < n ? (int32_t)m : -1;
+    for (int k = w0; k < w0 + w; k++) rank += key[k] < mine;
+    perm[base + w0 + rank] = m < n ? (int32_t)m : -1;
 }
 
 // Natural order: slot i holds molecule i.
@@ -327,7 +329,7 @@ __global__ void k_fill_entries(const int32_t* __restrict__ lingos, const int32_t
                                const int32_t* __restrict__ perm, const int64_t* __restrict__ off,
                                int64_t nchunks,
                                const unsigned long long* __restrict__ keys,
-                               const uint32_t* __restrict__ vid, int64_t cap,
+                               const uint32_t* __restrict__ vid, int64_t cap, int shift,
                                ET* __restrict__ entries) {
     constexpr int EPG = 16 / sizeof(ET);
     const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -345,7 +347,7 @@ __global__ void k_fill_entries(const int32_t* __restrict__ lingos, const int32_t
         for (int32_t lvl = 1; lvl <= cnt; lvl++, e++) {
             const uint32_t v = vocab_lookup(keys, vid, cap, code, lvl);
             const int64_t g = off[c] + (e / EPG) * 32 + lane;
-            entries[g * EPG + (e % EPG)] = (ET)v;
+            entries[g * EPG + (e % EPG)] = (ET)(v << shift);
         }
     }
 }
@@ -491,7 +493,14 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     cudaStream_t st = h->stream;
     d.n = q.n;
     d.sorted = sorted;
+    d.window = sorted ? kWindow : h->rows_window;
     d.entry_bytes = h->vocab.nvid < 65535 ? 2 : 4;
+    d.offsets = false;
+    if (!sorted && h->rows_entries == SIML_ENTRIES_U32) d.entry_bytes = 4;
+    if (!sorted && h->rows_entries == SIML_ENTRIES_OFFSETS) {
+        d.entry_bytes = 4;
+        d.offsets = true;
+    }
     const int64_t nwin = (q.n + kWindow - 1) / kWindow;
     d.nchunks = (q.n + kChunk - 1) / kChunk;
     const int64_t slots = nwin * kWindow;
@@ -501,7 +510,7 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     if ((rc = dev_alloc(&d.ng, (size_t)d.nchunks))) return rc;
     if ((rc = dev_alloc(&d.off, (size_t)d.nchunks + 1))) return rc;
     if (q.n == 0) return SIML_OK;
-    if (sorted) k_window_sort<<<(unsigned)nwin, kWindow, 0, st>>>(q.cmag, q.n, d.perm);
+    if (d.window > kChunk) k_window_sort<<<(unsigned)nwin, kWindow, 0, st>>>(q.cmag, q.n, d.window, d.perm);
     else k_identity_perm<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(q.n, slots, d.perm);
     h->launches++;
     const int epg = 16 / d.entry_bytes;
@@ -528,12 +537,12 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     const unsigned grid = (unsigned)((d.nchunks * 32 + 255) / 256);
     if (d.entry_bytes == 2)
         k_fill_entries<uint16_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.width, d.perm, d.off, d.nchunks,
-                                                       h->vocab.keys, h->vocab.vid, h->vocab.cap,
+                                                       h->vocab.keys, h->vocab.vid, h->vocab.cap, 0,
                                                        (uint16_t*)d.entries);
     else
         k_fill_entries<uint32_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.width, d.perm, d.off, d.nchunks,
                                                        h->vocab.keys, h->vocab.vid, h->vocab.cap,
-                                                       (uint32_t*)d.entries);
+                                                       d.offsets ? 2 : 0, (uint32_t*)d.entries);
     h->launches++;
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(cudaStreamSynchronize(st));
@@ -716,6 +725,44 @@ int siml_db_stats(siml_engine* h, int64_t out[8]) {
     out[6] = h->ref.max_entries;
     out[7] = h->qry.max_entries;
     return SIML_OK;
+}
+
+int siml_set_tuning(siml_engine* h, int key, int64_t value) {
+    SIML_GUARD(h);
+    switch (key) {
+    case SIML_TUNE_ROWS_WINDOW:
+        if (value != 32 && value != 64 && value != 128 && value != 256)
+            return fail(SIML_ERR_INVALID, "rows window must be 32, 64, 128 or 256 (got %lld)", (long long)value);
+        if (value != h->rows_window) {
+            SIML_CUDA(cudaStreamSynchronize(h->stream));
+            free_layout(h->db_nat);
+            h->nat_valid = false;
+            h->rows_window = (int)value;
+        }
+        return SIML_OK;
+    case SIML_TUNE_ROWS_ENTRIES:
+        if (value < SIML_ENTRIES_AUTO || value > SIML_ENTRIES_OFFSETS)
+            return fail(SIML_ERR_INVALID, "rows entry format must be 0..3 (got %lld)", (long long)value);
+        if (value != h->rows_entries) {
+            SIML_CUDA(cudaStreamSynchronize(h->stream));
+            free_layout(h->db_nat);
+            h->nat_valid = false;
+            h->rows_entries = (int)value;
+        }
+        return SIML_OK;
+    default:
+        return fail(SIML_ERR_INVALID, "unknown tuning key %d", key);
+    }
+}
+
+int siml_get_tuning(siml_engine* h, int key, int64_t* value) {
+    SIML_GUARD(h);
+    if (!value) return fail(SIML_ERR_INVALID, "siml_get_tuning: NULL output");
+    switch (key) {
+    case SIML_TUNE_ROWS_WINDOW: *value = h->rows_window; return SIML_OK;
+    case SIML_TUNE_ROWS_ENTRIES: *value = h->rows_entries; return SIML_OK;
+    default: return fail(SIML_ERR_INVALID, "unknown tuning key %d", key);
+    }
 }
 
 int64_t siml_launch_count(siml_engine* h) { return h ? h->launches : -1; }

@@ -58,6 +58,8 @@ struct DbLayout {
     int64_t ngroups_total = 0;
     int64_t max_ng = 0;
     bool sorted = false;
+    int window = kChunk;          // molecules are sorted by entry count inside windows of this size
+    bool offsets = false;         // 4-byte entries hold byte offsets (vid * 4) into the table
 };
 
 // Ref-set rows as vid lists (levels expanded, codes absent from the database
@@ -92,6 +94,8 @@ struct siml_engine {
     bool timed = false;
     int64_t launches = 0;
     uint64_t generation = 0;              // bumped whenever a set is replaced (plans made before are stale)
+    int rows_window = siml::kChunk;       // sort window of the full-matrix layout (kChunk: natural order)
+    int rows_entries = 0;                 // entry format of the full-matrix layout (SIML_TUNE_ROWS_ENTRIES)
 };
 
 namespace siml {

@@ -21,6 +21,7 @@
 // table would not fit in shared memory or counts exceed 16 bits.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 #include "engine.h"
 #include "lingo_core.cuh"
@@ -138,6 +139,19 @@ __device__ __forceinline__ void warp_range(const GroupParams& p, int64_t& wb, in
     we = cb + (ce - cb) * (warp + 1) / nwarps;
 }
 
+// Entry types of the database layout: 2-byte vids, 4-byte vids, or 4-byte
+// byte offsets into the table (off32_t: the lookup needs no index arithmetic).
+struct off32_t {
+    uint32_t v;
+};
+template <typename ET>
+__device__ __forceinline__ uint32_t tload(const uint32_t* T, uint32_t w) {
+    if constexpr (sizeof(ET) == 4 && !std::is_same<ET, uint32_t>::value)
+        return *reinterpret_cast<const uint32_t*>(reinterpret_cast<const char*>(T) + w);
+    else
+        return T[w];
+}
+
 // Streams the entries of chunks [wb, we) through the bit-sliced counter and
 // calls epi(chunk, meta, counter) at the end of each chunk.  All lanes of the
 // warp are in the same chunk at the same time.
@@ -196,7 +210,8 @@ __device__ __forceinline__ void stream_chunks(const uint32_t* __restrict__ T, co
             acc.add8(T[c0.x & 0xFFFFu], T[c0.x >> 16], T[c0.y & 0xFFFFu], T[c0.y >> 16],
                      T[c0.z & 0xFFFFu], T[c0.z >> 16], T[c0.w & 0xFFFFu], T[c0.w >> 16]);
         else
-            acc.add8(T[c0.x], T[c0.y], T[c0.z], T[c0.w], T[c1.x], T[c1.y], T[c1.z], T[c1.w]);
+            acc.add8(tload<ET>(T, c0.x), tload<ET>(T, c0.y), tload<ET>(T, c0.z), tload<ET>(T, c0.w),
+                     tload<ET>(T, c1.x), tload<ET>(T, c1.y), tload<ET>(T, c1.z), tload<ET>(T, c1.w));
         steps--;
     }
 }
@@ -1390,6 +1405,9 @@ int launch_rows(siml_engine* h, const RowsArgs& a) {
     size_t smem = 0;
     int np = 0;
     if (table_params(h, d, a.rowbase, rows, a.mode, p, smem, np)) {
+        if (d->offsets)
+            return np == 8 ? launch_rows_t<8, off32_t>(h, p, smem, a.out, a.ldo)
+                           : launch_rows_t<16, off32_t>(h, p, smem, a.out, a.ldo);
         if (np == 8)
             return d->entry_bytes == 2 ? launch_rows_t<8, uint16_t>(h, p, smem, a.out, a.ldo)
                                        : launch_rows_t<8, uint32_t>(h, p, smem, a.out, a.ldo);

@@ -192,3 +192,41 @@ def test_torch_device_inputs_and_outputs(native, oracle, set4096):
     got = buf.cpu().numpy()
     assert np.array_equal(got[:, :4096], want[:64]) and np.all(got[:, 4096:] == -5.0)
     assert gl.launchCount() > 0
+
+
+@pytest.mark.parametrize("window", [64, 128, 256])
+def test_rows_window_layouts_bit_exact(native, oracle, set4096, golden, window):
+    """Full-matrix results do not depend on the layout's sort window; the
+    single-row form neither."""
+    gl = _engine()
+    _load(gl, set4096, set4096)
+    gl.setRowsWindow(window)
+    assert gl.rowsWindow() == window
+    C = oracle.tanimoto_block(set4096, set4096, 0, 512)
+    assert np.array_equal(gl.getMultipleRows(0, 512), C)
+    q = (golden["lingos"], golden["counts"], golden["lengths"], golden["mags"])
+    rows = golden["rows"]
+    _load(gl, tuple(a[rows] for a in q), q)
+    assert np.array_equal(gl.getMultipleRows(0, len(rows)), golden["tanimoto"])
+    ref = tuple(a[rows] for a in q)
+    cm_r, cm_q = ref[1].sum(1).astype(np.int32), q[1].sum(1).astype(np.int32)
+    isct = oracle.isct_block(ref, q, 0, len(rows))
+    for r in (0, 3, len(rows) - 1):
+        u = (cm_r[r] + cm_q - isct[r]).astype(np.float32)
+        want = np.where((ref[2][r] == 0) | (q[2] == 0), np.float32(0), isct[r].astype(np.float32) / u)
+        assert np.array_equal(gl.getTanimotoRow(r)[0], want.astype(np.float32)), r
+    with pytest.raises(ValueError):
+        gl.setRowsWindow(48)
+
+
+@pytest.mark.parametrize("fmt", [2, 3])
+def test_rows_entry_formats_bit_exact(native, oracle, set4096, fmt):
+    """4-byte vid and 4-byte byte-offset entries give the same matrix."""
+    gl = _engine()
+    _load(gl, set4096, set4096)
+    gl.setRowsEntries(fmt)
+    assert gl.rowsEntries() == fmt
+    assert np.array_equal(gl.getMultipleRows(0, 300), oracle.tanimoto_block(set4096, set4096, 0, 300))
+    assert gl.dbStats()["entry_bytes"] == 4
+    with pytest.raises(ValueError):
+        gl.setRowsEntries(9)
