@@ -92,6 +92,7 @@ struct siml_engine {
     unsigned long long* d_counter = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed = false;
+    bool hold_timing = false;             // a multi-kernel call times itself as a whole
     int64_t launches = 0;
     uint64_t generation = 0;              // bumped whenever a set is replaced (plans made before are stale)
     int rows_window = siml::kChunk;       // sort window of the full-matrix layout (kChunk: natural order)

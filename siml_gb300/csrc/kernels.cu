@@ -74,6 +74,8 @@ struct GroupParams {
     int64_t chunk_begin, chunk_end;   // chunks this launch covers (a column range)
     int vt_words;
     int mode;
+    const float* row_lo;      // per output row lower bound (per-row threshold search) or null
+    const int* rows_dev;      // device row count bounding `rows` (row lists built on the device) or null
 };
 
 struct RowSmem {
@@ -83,7 +85,22 @@ struct RowSmem {
     __align__(16) float amagf[32];
     int allfast;
     int min_amag;
+    float lo[32];            // per-row lower bound (GroupParams.row_lo)
+    float coef[32];          // its integer-test coefficient (bound_coef)
+    float min_coef;          // lowest integer-test coefficient of the group's bounds
 };
+
+// Coefficient of the conservative integer test for a bound lo > 0:
+// t >= lo implies isct >= lo / (1 + lo) * (magA + magB); the factor
+// (1 - 2^-12) absorbs fp32 rounding of the test itself.
+__host__ __device__ __forceinline__ float bound_coef(float lo) {
+    return lo > 0.0f ? (float)((double)lo / (1.0 + (double)lo) * (1.0 - 1.0 / 4096.0)) : 0.0f;
+}
+
+// Rows this launch really has: p.rows, or fewer when a device counter says so.
+__device__ __forceinline__ int live_rows(const GroupParams& p) {
+    return p.rows_dev ? min(p.rows, *p.rows_dev) : p.rows;
+}
 
 // Clears T, sets bit r of T[vid] for the entries of row r, fills RowSmem.
 // Returns the number of rows of the group.
@@ -91,7 +108,7 @@ __device__ __forceinline__ int build_table(uint32_t* T, RowSmem& rs, const Group
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
     const int64_t row0 = (int64_t)blockIdx.x * 32;
-    const int nr = min(32, p.rows - (int)row0);
+    const int nr = min(32, live_rows(p) - (int)row0);
     for (int i = threadIdx.x * 4; i < p.vt_words; i += blockDim.x * 4)
         *reinterpret_cast<uint4*>(T + i) = make_uint4(0u, 0u, 0u, 0u);
     if (warp == 0) {
@@ -106,6 +123,14 @@ __device__ __forceinline__ int build_table(uint32_t* T, RowSmem& rs, const Group
         const unsigned all = __ballot_sync(0xFFFFFFFFu, f);
         int mn = r < nr ? am : 0x7FFFFFFF;
         for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
+        if (p.row_lo) {
+            const float lo = r < nr ? p.row_lo[gr - p.rowbase] : 3.0e38f;
+            rs.lo[r] = lo;
+            float c = r < nr ? bound_coef(lo) : 3.0e38f;
+            rs.coef[r] = r < nr ? c : 0.0f;
+            for (int o = 16; o > 0; o >>= 1) c = fminf(c, __shfl_xor_sync(0xFFFFFFFFu, c, o));
+            if (r == 0) rs.min_coef = c;
+        }
         if (r == 0) {
             rs.allfast = all == 0xFFFFFFFFu;
             rs.min_amag = mn;
@@ -303,7 +328,7 @@ NbrArgs nbr_args(float lo, float hi, int64_t pitch, int32_t* idx, float* sims, i
     if (std::isnan(lo)) a.thr_mode = 2;
     else if (lo <= 0.0f) a.thr_mode = 1;
     else a.thr_mode = 0;
-    a.thr_scale = a.thr_mode == 0 ? (float)((double)lo / (1.0 + (double)lo) * (1.0 - 1.0 / 4096.0)) : 0.0f;
+    a.thr_scale = a.thr_mode == 0 ? bound_coef(lo) : 0.0f;
     return a;
 }
 
@@ -318,6 +343,19 @@ __device__ __forceinline__ uint32_t sliced_ge(const SlicedCounter<NP>& acc, uint
         const uint32_t tb = 0u - ((th >> p) & 1u);   // all ones where the threshold bit is 1
         gt |= eq & acc.plane[p] & ~tb;
         eq &= ~(acc.plane[p] ^ tb);
+    }
+    return gt | eq;
+}
+
+// The same with a threshold per row, bit-sliced like the counts (bit r of
+// tp[p] = bit p of row r's threshold).
+template <int NP>
+__device__ __forceinline__ uint32_t sliced_ge_rows(const SlicedCounter<NP>& acc, const uint32_t (&tp)[NP]) {
+    uint32_t gt = 0u, eq = 0xFFFFFFFFu;
+#pragma unroll
+    for (int p = NP - 1; p >= 0; p--) {
+        gt |= eq & acc.plane[p] & ~tp[p];
+        eq &= ~(acc.plane[p] ^ tp[p]);
     }
     return gt | eq;
 }
@@ -348,10 +386,12 @@ struct NbrEpi {
 
     __device__ __forceinline__ void operator()(int64_t, const int4& meta, const SlicedCounter<NP>& acc) {
         const int32_t m = meta.x;
-        if (m < a.col_begin || m >= a.col_end || a.thr_mode == 2) return;
+        const bool valid = m >= a.col_begin && m < a.col_end;
         const int32_t mb = meta.y;
         uint32_t cand;
-        if (a.thr_mode == 1) {
+        if (!valid || a.thr_mode == 2) {
+            return;
+        } else if (a.thr_mode == 1) {
             cand = 0xFFFFFFFFu;
         } else {
             // exact t >= lo > 0 implies isct >= lo/(1+lo) * (ma + mb) >= th
@@ -381,11 +421,92 @@ template <int NP, typename ET>
 __global__ void __launch_bounds__(kThreads, 1) k_nbr(const GroupParams p, const NbrArgs a) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
+    if ((int64_t)blockIdx.x * 32 >= live_rows(p)) return;   // uniform over the CTA
     const int nr = build_table(T, rs, p);
     int64_t wb, we;
     warp_range(p, wb, we);
     NbrEpi<NP> epi{rs, nr, (int64_t)blockIdx.x * 32, a};
     stream_chunks<NP, ET>(T, p, wb, we, epi);
+}
+
+// ---------------------------------------------------------- k_collect ----
+// Top-k candidate collection: every pair with t >= its row's bound
+// (GroupParams.row_lo).  Lane r forms row r's integer threshold at the
+// chunk's smallest magnitude (valid for every lane of the chunk: the bound
+// grows with the magnitude) and ballots slice the 32 thresholds into
+// planes, so the bit-sliced compare is per row.  Positions come from
+// shared-memory counters: each (row, database split) owns a segment of
+// seg_cap entries of the candidate buffer [rows][splits][seg_cap], and the
+// per-segment counts (which may exceed seg_cap) go to seg_counts[rows][splits]
+// when the CTA ends.  No magnitude pre-filter here: a row or molecule with
+// no LINGOs scores 0 and still ranks.
+struct CollectArgs {
+    int64_t seg_cap;
+    int32_t* cand_i;
+    float* cand_t;
+    int32_t* seg_counts;
+};
+
+template <int NP>
+struct CollectEpi {
+    const RowSmem& rs;
+    int nr;
+    int* scount;        // shared, per group row
+    int32_t* cand_i;    // this CTA's segment of row 0: + row * splits * seg_cap
+    float* cand_t;
+    int64_t row_stride; // splits * seg_cap
+    int64_t seg_cap;
+
+    __device__ __forceinline__ void operator()(int64_t, const int4& meta, const SlicedCounter<NP>& acc) {
+        const int32_t m = meta.x, mb = meta.y;
+        const bool valid = m >= 0;
+        int mbm = valid ? mb : 0x7FFFFFFF;
+        for (int o = 16; o > 0; o >>= 1) mbm = min(mbm, __shfl_xor_sync(0xFFFFFFFFu, mbm, o));
+        if (mbm == 0x7FFFFFFF) return;   // padding-only chunk (uniform)
+        const int lane = threadIdx.x & 31;
+        const float thf = floorf(rs.coef[lane] * (rs.amagf[lane] + (float)mbm));
+        const bool never = lane >= nr || thf >= (float)(1u << NP);
+        const uint32_t thr = never || thf <= 0.0f ? 0u : (uint32_t)thf;
+        uint32_t tp[NP];
+#pragma unroll
+        for (int q = 0; q < NP; q++) tp[q] = __ballot_sync(0xFFFFFFFFu, (thr >> q) & 1u);
+        const uint32_t never_m = __ballot_sync(0xFFFFFFFFu, never);
+        if (!valid) return;
+        uint32_t cand = sliced_ge_rows<NP>(acc, tp) & ~never_m;
+        while (cand) {
+            const int r = __ffs(cand) - 1;
+            cand &= cand - 1u;
+            const int is = sliced_row<NP>(acc, r);
+            // the lane's own integer bound first, the exact similarity after
+            if ((float)is < floorf(rs.coef[r] * (rs.amagf[r] + (float)mb))) continue;
+            const float t = tanimoto_rows(is, rs.amag[r], mb);
+            if (!(t >= rs.lo[r])) continue;
+            const int pos = atomicAdd(scount + r, 1);
+            if (pos < seg_cap) {
+                const int64_t o = (int64_t)rs.orow[r] * row_stride + pos;
+                cand_i[o] = m;
+                cand_t[o] = t;
+            }
+        }
+    }
+};
+
+template <int NP, typename ET>
+__global__ void __launch_bounds__(kThreads, 1) k_collect(const GroupParams p, const CollectArgs c) {
+    extern __shared__ __align__(16) uint32_t T[];
+    __shared__ RowSmem rs;
+    __shared__ int scount[32];
+    if ((int64_t)blockIdx.x * 32 >= live_rows(p)) return;   // uniform over the CTA
+    if (threadIdx.x < 32) scount[threadIdx.x] = 0;
+    const int nr = build_table(T, rs, p);   // synchronizes the block
+    int64_t wb, we;
+    warp_range(p, wb, we);
+    const int64_t row_stride = (int64_t)gridDim.y * c.seg_cap;
+    CollectEpi<NP> epi{rs, nr, scount, c.cand_i + blockIdx.y * c.seg_cap, c.cand_t + blockIdx.y * c.seg_cap,
+                       row_stride, c.seg_cap};
+    stream_chunks<NP, ET>(T, p, wb, we, epi);
+    __syncthreads();
+    if (threadIdx.x < nr) c.seg_counts[(int64_t)rs.orow[threadIdx.x] * gridDim.y + blockIdx.y] = scount[threadIdx.x];
 }
 
 // ------------------------------------------------------------- k_hist ----
@@ -465,6 +586,81 @@ __global__ void __launch_bounds__(kThreads, 1) k_hist(const GroupParams p, void*
             const int r = i / kBins101, b = i - r * kBins101;
             if (H[i]) atomicAdd(o + (int64_t)rs.orow[r] * ldo + b, (int)H[i]);
         }
+    }
+}
+
+// ------------------------------------------------------------ k_loghist ----
+// Per-row histogram for the sample pass of top-k.  Bins follow the bits of
+// t: 64 per octave over [2^-8, 1), one below 2^-8 and one for t = 1, so every
+// bin is about 1.6% wide and its lower edge is an exact float.  Counts are
+// 16-bit halves of shared words; the launcher keeps each CTA's molecules per
+// row under 65,536 so no half carries into its neighbour.
+constexpr int kLogBins = 514;
+constexpr int kLogWords = (kLogBins + 1) / 2;
+
+__device__ __forceinline__ int log_bin(float t) {
+    if (!(t >= 0.00390625f)) return 0;
+    if (t >= 1.0f) return kLogBins - 1;
+    const uint32_t u = __float_as_uint(t);
+    const int e = (int)(u >> 23) - 127;   // -8 .. -1
+    return 1 + (e + 8) * 64 + (int)((u >> 17) & 63u);
+}
+
+// Lower edge of bin b: every t of bins >= b is >= it (-1 for bin 0).
+__device__ __forceinline__ float log_bin_floor(int b) {
+    if (b <= 0) return -1.0f;
+    if (b >= kLogBins - 1) return 1.0f;
+    const uint32_t e = (uint32_t)((b - 1) / 64 - 8 + 127), m = (uint32_t)((b - 1) % 64);
+    return __uint_as_float((e << 23) | (m << 17));
+}
+
+template <int NP>
+struct LogHistEpi {
+    const RowSmem& rs;
+    int nr;
+    uint32_t* H;   // shared: [32][kLogWords]
+
+    __device__ __forceinline__ void operator()(int64_t, const int4& meta, const SlicedCounter<NP>& acc) {
+        if (meta.x < 0) return;
+        const int32_t bmag = meta.y;
+        RowCounts<NP> rc;
+        counts_from_planes<NP>(acc, rc);
+        const bool fast = rs.allfast && fast_mag(bmag, meta.z);
+        const float bf = small_int_to_float((uint32_t)(bmag > 0 ? bmag : 0));
+#pragma unroll
+        for (int r = 0; r < 32; r++) {
+            if (r < nr) {
+                float t;
+                if (fast) {
+                    const float isf = small_int_to_float(row_count<NP>(rc, r));
+                    t = div_small(isf, __fsub_rn(__fadd_rn(rs.amagf[r], bf), isf));
+                } else {
+                    t = tanimoto_rows((int)row_count<NP>(rc, r), rs.amag[r], bmag);
+                }
+                const int b = log_bin(t);
+                atomicAdd(H + r * kLogWords + (b >> 1), 1u << ((b & 1) * 16));
+            }
+        }
+    }
+};
+
+// out: int32 [rows, kLogBins], accumulated (zeroed by the caller)
+template <int NP, typename ET>
+__global__ void __launch_bounds__(kThreads, 1) k_loghist(const GroupParams p, int32_t* out) {
+    extern __shared__ __align__(16) uint32_t T[];
+    __shared__ RowSmem rs;
+    __shared__ uint32_t H[32 * kLogWords];
+    for (int i = threadIdx.x; i < 32 * kLogWords; i += blockDim.x) H[i] = 0u;
+    const int nr = build_table(T, rs, p);   // synchronizes the block
+    int64_t wb, we;
+    warp_range(p, wb, we);
+    LogHistEpi<NP> epi{rs, nr, H};
+    stream_chunks<NP, ET>(T, p, wb, we, epi);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nr * kLogBins; i += blockDim.x) {
+        const int r = i / kLogBins, b = i - r * kLogBins;
+        const uint32_t v = (H[r * kLogWords + (b >> 1)] >> ((b & 1) * 16)) & 0xFFFFu;
+        if (v) atomicAdd(out + (int64_t)rs.orow[r] * kLogBins + b, (int)v);
     }
 }
 
@@ -779,7 +975,124 @@ __global__ void __launch_bounds__(512) k_topk_merge(const float* part_t, const i
 // with the sorted merge and keeps a k-heap in shared memory under the same
 // bounded lock, then sorts it.
 __global__ void __launch_bounds__(256) k_topk_rowscan(const struct RawArgs ra, int k, int32_t* idx, float* sims,
-                                                      int* err);
+                                                      int* err, const int* list, const int* list_count);
+
+// ---------------------------------------------- threshold-and-collect top-k ----
+// Exact top-k in three steps, for tables that fit in shared memory:
+//  1. per-row histograms of a sample (a prefix of the database's chunks,
+//     k_loghist) give each row a bound theta: the lower edge of the highest
+//     bin at which the sample already holds k molecules.  At least k database
+//     molecules reach theta, so the row's true k-th best is >= theta;
+//  2. k_collect gathers every pair with t >= theta into per-(row, split)
+//     segments of a candidate buffer;
+//  3. k_topk_select sorts each row's candidates by (similarity descending,
+//     index ascending) and writes the first k.  A row whose segments
+//     overflowed takes the k-th best of the candidates kept as its new bound
+//     (still at least k molecules above it) and goes on a device list for
+//     another collection pass; rows that overflow again are scanned by
+//     k_topk_rowscan.  No host synchronization is needed between the steps.
+constexpr int kSelectMax = 8192;
+
+__global__ void k_topk_theta(const int32_t* hist, int k, int64_t rows, float* row_lo, int* list_counts) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        list_counts[0] = 0;
+        list_counts[1] = 0;
+    }
+    if (i >= rows) return;
+    const int32_t* h = hist + i * kLogBins;
+    int64_t acc = 0;
+    int b = kLogBins - 1;
+    for (; b > 0; b--) {
+        acc += h[b];
+        if (acc >= k) break;
+    }
+    row_lo[i] = log_bin_floor(b);   // b == 0: fewer than k above bin 0, collect all
+}
+
+// One CTA per row (listed rows: absolute row ids, rowbase subtracted).
+// Candidates of row r: segments s = 0..splits-1 of seg_cap entries at
+// cand + (r * splits + s) * seg_cap, holding min(count, seg_cap) entries.
+__global__ void __launch_bounds__(512) k_topk_select(const int32_t* cand_i, const float* cand_t,
+                                                     const int32_t* seg_counts, int splits, int64_t seg_cap, int k,
+                                                     int64_t rowbase, const int* list, const int* list_count,
+                                                     float* row_lo, int* next, int* next_count, int32_t* idx,
+                                                     float* sims) {
+    extern __shared__ __align__(16) uint32_t sm[];
+    __shared__ int seg_off[1025];
+    __shared__ int s_over;
+    int64_t row;
+    if (list) {
+        if ((int)blockIdx.x >= *list_count) return;   // uniform over the CTA
+        row = list[blockIdx.x] - rowbase;
+    } else {
+        row = blockIdx.x;
+    }
+    if (threadIdx.x == 0) {
+        int acc = 0, over = 0;
+        for (int q = 0; q < splits; q++) {
+            const int c = seg_counts[row * splits + q];
+            seg_off[q] = acc;
+            acc += c < seg_cap ? c : (int)seg_cap;
+            over |= c > seg_cap;
+        }
+        seg_off[splits] = acc;
+        s_over = over;
+    }
+    __syncthreads();
+    const int n = seg_off[splits];
+    const bool over = s_over != 0;
+    int N = 1;
+    while (N < n) N <<= 1;
+    float* st = reinterpret_cast<float*>(sm);
+    int* si = reinterpret_cast<int*>(st + N);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        st[i] = -3.0e38f;
+        si[i] = -1;
+    }
+    __syncthreads();
+    for (int q = 0; q < splits; q++) {
+        const int c = seg_off[q + 1] - seg_off[q];
+        const int64_t base = (row * splits + q) * seg_cap;
+        for (int i = threadIdx.x; i < c; i += blockDim.x) {
+            st[seg_off[q] + i] = cand_t[base + i];
+            si[seg_off[q] + i] = cand_i[base + i];
+        }
+    }
+    __syncthreads();
+    for (int kk = 2; kk <= N; kk <<= 1) {
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < N; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const bool asc = (i & kk) == 0;
+                    const bool vi = si[i] >= 0, vj = si[ixj] >= 0;
+                    bool ji;
+                    if (vi != vj) ji = vj;
+                    else if (!vi) ji = false;
+                    else ji = worse(st[i], si[i], st[ixj], si[ixj]);
+                    if (ji == asc) {
+                        const float tt = st[i]; st[i] = st[ixj]; st[ixj] = tt;
+                        const int ti = si[i]; si[i] = si[ixj]; si[ixj] = ti;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (over) {
+        if (threadIdx.x == 0) {
+            row_lo[row] = st[k - 1];
+            next[atomicAdd(next_count, 1)] = (int)(row + rowbase);
+        }
+        return;
+    }
+    for (int j = threadIdx.x; j < k; j += blockDim.x) {
+        const bool ok = j < n;
+        idx[row * k + j] = ok ? si[j] : -1;
+        sims[row * k + j] = ok ? st[j] : -1.0f;
+    }
+}
 
 // -------------------------------------------------------- k_batch_nbr ----
 // Persistent batched neighbour search over ragged jobs (a job = a range of
@@ -998,15 +1311,17 @@ __global__ void k_rows_merge(const RawArgs ra, float* out, int64_t ldo, int mode
 }
 
 __global__ void __launch_bounds__(256) k_topk_rowscan(const RawArgs ra, int k, int32_t* idx, float* sims,
-                                                      int* err) {
+                                                      int* err, const int* list, const int* list_count) {
     extern __shared__ __align__(16) uint32_t sm[];
     float* ht = reinterpret_cast<float*>(sm);
     int* hi = reinterpret_cast<int*>(ht + k);
     __shared__ int lock, size, err_s;
     __shared__ unsigned long long root;   // published k-th best, 0 until the heap is full
+    if (list && (int)blockIdx.x >= *list_count) return;   // uniform over the CTA
     if (threadIdx.x == 0) { lock = 0; size = 0; err_s = 0; root = 0ull; }
     __syncthreads();
-    const int64_t r = ra.rowbase + blockIdx.x;
+    const int64_t r = list ? (int64_t)list[blockIdx.x] : ra.rowbase + blockIdx.x;   // absolute row
+    const int64_t orow = r - ra.rowbase;
     const int32_t* a = ra.rl + r * ra.rw;
     const int32_t* as = ra.rc + r * ra.rw;
     const int32_t alen = ra.rlen[r], ma = ra.rmag[r];
@@ -1055,8 +1370,8 @@ __global__ void __launch_bounds__(256) k_topk_rowscan(const RawArgs ra, int k, i
     __syncthreads();
     for (int j = threadIdx.x; j < k; j += blockDim.x) {
         const bool ok = j < size;
-        idx[(int64_t)blockIdx.x * k + j] = ok ? hi[j] : -1;
-        sims[(int64_t)blockIdx.x * k + j] = ok ? ht[j] : -1.0f;
+        idx[orow * k + j] = ok ? hi[j] : -1;
+        sims[orow * k + j] = ok ? ht[j] : -1.0f;
     }
 }
 
@@ -1153,7 +1468,15 @@ bool table_params(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t ro
     p.chunk_end = d->nchunks;
     p.vt_words = vt_words;
     p.mode = mode;
+    p.row_lo = nullptr;
+    p.rows_dev = nullptr;
     return true;
+}
+
+// Records a timing event on the engine's stream unless a multi-kernel call
+// holds the timing to bracket all of its launches itself.
+cudaError_t mark(siml_engine* h, cudaEvent_t ev) {
+    return h->hold_timing ? cudaSuccess : cudaEventRecord(ev, h->stream);
 }
 
 template <class K>
@@ -1169,10 +1492,10 @@ int launch_rows_t(siml_engine* h, const GroupParams& p, size_t smem, float* out,
     if (rc) return rc;
     const int s = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
     dim3 grid((unsigned)groups, (unsigned)s);
-    SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+    SIML_CUDA(mark(h, h->ev0));
     k_rows<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, out, ldo);
     SIML_CUDA(cudaGetLastError());
-    SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+    SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
     h->launches++;
     return SIML_OK;
@@ -1185,10 +1508,10 @@ int launch_nbr_t(siml_engine* h, const GroupParams& p, size_t smem, const NbrArg
     if (rc) return rc;
     const int s = choose_splits(groups, p.chunk_end - p.chunk_begin, h->num_sms, kThreads / 32);
     dim3 grid((unsigned)groups, (unsigned)s);
-    SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+    SIML_CUDA(mark(h, h->ev0));
     k_nbr<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, a);
     SIML_CUDA(cudaGetLastError());
-    SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+    SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
     h->launches++;
     return SIML_OK;
@@ -1201,10 +1524,10 @@ int launch_hist_t(siml_engine* h, const GroupParams& p, size_t smem, void* out, 
     if (rc) return rc;
     const int s = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
     dim3 grid((unsigned)groups, (unsigned)s);
-    SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+    SIML_CUDA(mark(h, h->ev0));
     k_hist<NP, ET, GLOBAL><<<grid, kThreads, smem, h->stream>>>(p, out, ldo);
     SIML_CUDA(cudaGetLastError());
-    SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+    SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
     h->launches++;
     return SIML_OK;
@@ -1216,10 +1539,10 @@ int launch_topk_t(siml_engine* h, const GroupParams& p, size_t smem, int k, int 
     int rc = set_smem(k_topk<NP, ET>, smem);
     if (rc) return rc;
     dim3 grid((unsigned)groups, (unsigned)splits);
-    SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+    SIML_CUDA(mark(h, h->ev0));
     k_topk<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, k, pt, pi, h->d_err);
     SIML_CUDA(cudaGetLastError());
-    SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+    SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
     h->launches++;
     return SIML_OK;
@@ -1325,14 +1648,134 @@ int launch_topk_core(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t
     }
     const size_t sm = (size_t)k * 8;
     if ((rc = set_smem(k_topk_rowscan, sm))) return rc;
-    SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
-    k_topk_rowscan<<<(unsigned)rows, 256, sm, h->stream>>>(raw_args(h, rowbase), k, idx, sims, h->d_err);
+    SIML_CUDA(mark(h, h->ev0));
+    k_topk_rowscan<<<(unsigned)rows, 256, sm, h->stream>>>(raw_args(h, rowbase), k, idx, sims, h->d_err, nullptr,
+                                                           nullptr);
     SIML_CUDA(cudaGetLastError());
-    SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+    SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
     h->launches++;
     return SIML_OK;
 }
+
+namespace {
+
+constexpr int64_t kTopkBlockRows = 8192;   // rows per pass of the threshold-and-collect path
+
+// The sample histogram kernel fits next to the table.
+bool smem_hist_ok(siml_engine* h, const DbLayout* d) {
+    GroupParams p;
+    size_t smem = 0;
+    int np = 0;
+    return table_params(h, d, 0, 1, kModeRows, p, smem, np) &&
+           smem + 32 * kLogWords * 4 + sizeof(RowSmem) + 64 <= h->smem_optin;
+}
+constexpr int64_t kSampleFraction = 8;     // the sample is 1/8 of the database's chunks
+
+// Holds the engine's per-launch timing so a multi-kernel call brackets all
+// of its launches with one event pair.
+struct TimingHold {
+    siml_engine* h;
+    explicit TimingHold(siml_engine* e) : h(e) { h->hold_timing = true; }
+    ~TimingHold() { h->hold_timing = false; }
+};
+
+template <int NP, typename ET>
+int launch_collect_t(siml_engine* h, const GroupParams& p, size_t smem, int splits, const CollectArgs& c) {
+    int rc = set_smem(k_collect<NP, ET>, smem);
+    if (rc) return rc;
+    dim3 grid((unsigned)((p.rows + 31) / 32), (unsigned)splits);
+    k_collect<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, c);
+    SIML_CUDA(cudaGetLastError());
+    h->launches++;
+    return SIML_OK;
+}
+
+// Database splits of the collection pass and the candidate segment size:
+// splits * seg_cap <= kSelectMax entries per row, seg_cap >= k.
+void collect_shape(siml_engine* h, const DbLayout* d, int64_t rows, int k, int& splits, int64_t& seg_cap) {
+    const int64_t groups = (rows + 31) / 32;
+    splits = choose_splits(groups, d->nchunks, h->num_sms, kThreads / 32);
+    while (splits > 1 && (int64_t)kSelectMax / splits < std::max<int64_t>(k, 64)) splits--;
+    seg_cap = kSelectMax / splits;
+}
+
+size_t topk_collect_bytes(int64_t rows, int splits, int64_t seg_cap) {
+    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+    return up((size_t)rows * kLogBins * 4) + up((size_t)rows * 4) + 2 * up((size_t)rows * splits * seg_cap * 4) +
+           up((size_t)rows * splits * 4) + 2 * up((size_t)rows * 4) + up(16);
+}
+
+template <int NP, typename ET>
+int topk_collect_block(siml_engine* h, const DbLayout* d, int64_t r0, int64_t rows, int k, int64_t sample,
+                       size_t smem, const int32_t* order, char* buf, int32_t* idx, float* sims) {
+    int splits = 1;
+    int64_t seg_cap = 0;
+    collect_shape(h, d, rows, k, splits, seg_cap);
+    auto carve = [&](size_t bytes) {
+        char* q = buf;
+        buf += (bytes + 255) / 256 * 256;
+        return q;
+    };
+    int32_t* hist = reinterpret_cast<int32_t*>(carve((size_t)rows * kLogBins * 4));
+    float* row_lo = reinterpret_cast<float*>(carve((size_t)rows * 4));
+    float* cand_t = reinterpret_cast<float*>(carve((size_t)rows * splits * seg_cap * 4));
+    int32_t* cand_i = reinterpret_cast<int32_t*>(carve((size_t)rows * splits * seg_cap * 4));
+    int32_t* seg_counts = reinterpret_cast<int32_t*>(carve((size_t)rows * splits * 4));
+    int* list_a = reinterpret_cast<int*>(carve((size_t)rows * 4));
+    int* list_b = reinterpret_cast<int*>(carve((size_t)rows * 4));
+    int* list_n = reinterpret_cast<int*>(carve(16));
+    int rc;
+    // 1. per-row histograms of the sample (chunks [0, sample)) and the bounds
+    GroupParams ps;
+    size_t sm0 = 0;
+    int np = 0;
+    table_params(h, d, r0, rows, kModeRows, ps, sm0, np);
+    ps.row_order = order;
+    ps.chunk_end = sample;
+    SIML_CUDA(cudaMemsetAsync(hist, 0, (size_t)rows * kLogBins * 4, h->stream));
+    {
+        const int64_t groups = (rows + 31) / 32;
+        int hs = choose_splits(groups, sample, h->num_sms, kThreads / 32);
+        hs = (int)std::max<int64_t>(hs, (sample * 32 + 65534) / 65535);   // <= 65,535 molecules per CTA
+        if ((rc = set_smem(k_loghist<NP, ET>, smem))) return rc;
+        dim3 grid((unsigned)groups, (unsigned)hs);
+        k_loghist<NP, ET><<<grid, kThreads, smem, h->stream>>>(ps, hist);
+        SIML_CUDA(cudaGetLastError());
+    }
+    k_topk_theta<<<(unsigned)((rows + 255) / 256), 256, 0, h->stream>>>(hist, k, rows, row_lo, list_n);
+    SIML_CUDA(cudaGetLastError());
+    // 2. collect every pair at or above its row's bound
+    GroupParams pc = ps;
+    pc.chunk_begin = 0;
+    pc.chunk_end = d->nchunks;
+    pc.row_lo = row_lo;
+    const CollectArgs ca{seg_cap, cand_i, cand_t, seg_counts};
+    if ((rc = launch_collect_t<NP, ET>(h, pc, smem, splits, ca))) return rc;
+    // 3. select; rows whose segments overflowed go to list a with a higher bound
+    const size_t ssm = (size_t)kSelectMax * 8;
+    if ((rc = set_smem(k_topk_select, ssm))) return rc;
+    k_topk_select<<<(unsigned)rows, 512, ssm, h->stream>>>(cand_i, cand_t, seg_counts, splits, seg_cap, k, r0,
+                                                          nullptr, nullptr, row_lo, list_a, list_n, idx, sims);
+    SIML_CUDA(cudaGetLastError());
+    // one more collection and selection for the listed rows
+    GroupParams pl = pc;
+    pl.row_order = list_a;
+    pl.rows_dev = list_n;
+    if ((rc = launch_collect_t<NP, ET>(h, pl, smem, splits, ca))) return rc;
+    k_topk_select<<<(unsigned)rows, 512, ssm, h->stream>>>(cand_i, cand_t, seg_counts, splits, seg_cap, k, r0,
+                                                          list_a, list_n, row_lo, list_b, list_n + 1, idx, sims);
+    SIML_CUDA(cudaGetLastError());
+    // rows that overflowed twice: exact scan
+    if ((rc = set_smem(k_topk_rowscan, (size_t)k * 8))) return rc;
+    k_topk_rowscan<<<(unsigned)rows, 256, (size_t)k * 8, h->stream>>>(raw_args(h, r0), k, idx, sims, h->d_err,
+                                                                     list_b, list_n + 1);
+    SIML_CUDA(cudaGetLastError());
+    h->launches += 4;
+    return SIML_OK;
+}
+
+}  // namespace
 
 int launch_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int k, int32_t* idx, float* sims) {
     const DbLayout* d = nullptr;
@@ -1340,6 +1783,40 @@ int launch_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int k, int32_
     if (rc) return rc;
     TopkPlan plan;
     if ((rc = topk_plan(h, d, rowbase, rowlimit, k, plan))) return rc;
+    const int64_t sample = std::max<int64_t>(d->nchunks / kSampleFraction, (4 * (int64_t)k + 31) / 32);
+    if (plan.splits > 0 && 32 * (int64_t)k <= kSelectMax && 2 * sample <= d->nchunks && smem_hist_ok(h, d)) {
+        GroupParams p;
+        size_t smem = 0;
+        int np = 0;
+        table_params(h, d, rowbase, 1, kModeRows, p, smem, np);
+        SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+        TimingHold hold(h);
+        SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+        for (int64_t r0 = rowbase; r0 < rowlimit; r0 += kTopkBlockRows) {
+            const int64_t r1 = std::min(rowlimit, r0 + kTopkBlockRows), rows = r1 - r0;
+            const int32_t* order = nullptr;
+            if ((rc = row_order_by_magnitude(h, r0, r1, &order))) return rc;
+            int splits = 1;
+            int64_t seg_cap = 0;
+            collect_shape(h, d, rows, k, splits, seg_cap);
+            void* buf = nullptr;
+            if ((rc = scratch_reserve(h, topk_collect_bytes(rows, splits, seg_cap), &buf, kSlotPartial))) return rc;
+            int32_t* oi = idx + (r0 - rowbase) * k;
+            float* os = sims + (r0 - rowbase) * k;
+            char* b = reinterpret_cast<char*>(buf);
+            const bool u16 = d->entry_bytes == 2;
+            if (np == 8)
+                rc = u16 ? topk_collect_block<8, uint16_t>(h, d, r0, rows, k, sample, smem, order, b, oi, os)
+                         : topk_collect_block<8, uint32_t>(h, d, r0, rows, k, sample, smem, order, b, oi, os);
+            else
+                rc = u16 ? topk_collect_block<16, uint16_t>(h, d, r0, rows, k, sample, smem, order, b, oi, os)
+                         : topk_collect_block<16, uint32_t>(h, d, r0, rows, k, sample, smem, order, b, oi, os);
+            if (rc) return rc;
+        }
+        SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+        h->timed = true;
+        return SIML_OK;
+    }
     const int32_t* order = nullptr;
     float* pt = nullptr;
     int* pi = nullptr;
@@ -1375,11 +1852,11 @@ int launch_hist(siml_engine* h, int64_t rowbase, int64_t rowlimit, bool global, 
     }
     if (rows > 65535) return fail(SIML_ERR_UNSUPPORTED, "merge path: more than 65535 rows per call");
     dim3 grid((unsigned)((h->qry.n + 255) / 256), (unsigned)rows);
-    SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+    SIML_CUDA(mark(h, h->ev0));
     if (global) k_hist_merge<true><<<grid, 256, 0, h->stream>>>(raw_args(h, rowbase), out, ldo);
     else k_hist_merge<false><<<grid, 256, 0, h->stream>>>(raw_args(h, rowbase), out, ldo);
     SIML_CUDA(cudaGetLastError());
-    SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+    SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
     h->launches++;
     return SIML_OK;
@@ -1416,10 +1893,10 @@ int launch_rows(siml_engine* h, const RowsArgs& a) {
     }
     if (rows > 65535) return fail(SIML_ERR_UNSUPPORTED, "merge path: more than 65535 rows per call");
     dim3 grid((unsigned)((h->qry.n + 255) / 256), (unsigned)rows);
-    SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
+    SIML_CUDA(mark(h, h->ev0));
     k_rows_merge<<<grid, 256, 0, h->stream>>>(raw_args(h, a.rowbase), a.out, a.ldo, a.mode);
     SIML_CUDA(cudaGetLastError());
-    SIML_CUDA(cudaEventRecord(h->ev1, h->stream));
+    SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
     h->launches++;
     return SIML_OK;
