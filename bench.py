@@ -607,6 +607,206 @@ def ragged_arm(args):
     return 0
 
 
+# ---------------------------------------------------------- serving ----
+SERVING_DB_N = 10_000_000
+SERVING_WORKLOAD = ("serving_10m: request loop over a resident 10,000,000-molecule database (uniform 20-90 chars); "
+                    "Poisson arrivals, each request 1-512 query SMILES (log-uniform), half asking top-50 and half "
+                    "every hit with T >= 0.75; continuous batching (1,024 query rows per batch, two slot regions)")
+
+
+def serving_requests(rate, seconds, first_mol, seed):
+    """Seeded arrival schedule: (arrival offset s, kind, SMILES list) per request."""
+    from siml_gb300 import synthetic as S
+    rng = np.random.default_rng(seed)
+    out, t, pos = [], 0.0, first_mol
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t >= seconds:
+            break
+        q = int(np.floor(np.exp(rng.uniform(0.0, np.log(513)))))
+        q = min(max(q, 1), 512)
+        kind = "topk" if rng.random() < 0.5 else "threshold"
+        out.append((t, kind, q, pos))
+        pos += q
+    buf_first, total = first_mol, pos - first_mol
+    smi = S.smiles_list(S.SEED_SERVING, S.UNIFORM_20_90, total, first=buf_first)
+    return [(t, kind, smi[p0 - first_mol:p0 - first_mol + q]) for t, kind, q, p0 in out]
+
+
+def run_arrivals(submit, schedule, t0):
+    """Submits each request at its arrival time (open loop); returns the requests."""
+    from siml_gb300.serving import Request
+    reqs = []
+    for i, (t, kind, smi) in enumerate(schedule):
+        now = time.perf_counter()
+        if t0 + t > now:
+            time.sleep(t0 + t - now)
+        r = Request(i, smi, kind=kind, k=50, lo=0.75, arrival=t0 + t)
+        reqs.append(r)
+        submit(r)
+    return reqs
+
+
+def serving_stats(reqs, nq):
+    from siml_gb300.serving import percentiles
+    lat = [r.latency() * 1e3 for r in reqs]
+    big = [r.latency() * 1e3 for r in reqs if r.rows >= 256]
+    t_first = min(r.arrival for r in reqs)
+    t_last = max(r.t_done for r in reqs)
+    pairs = sum(r.rows for r in reqs) * nq
+    st = {"requests": len(reqs), "queries": sum(r.rows for r in reqs), "pairs": pairs,
+          "gpairs_per_s": pairs / (t_last - t_first) / 1e9, "span_s": t_last - t_first}
+    st.update({k + "_ms": v for k, v in percentiles(lat, (50, 95, 99)).items()})
+    st.update({k + "_ms_ge256": v for k, v in percentiles(big, (50, 99)).items()})
+    st["errors"] = sum(r.error is not None for r in reqs)
+    return st
+
+
+def serving_arm(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from siml_gb300 import GPULingo
+    from siml_gb300 import synthetic as S
+    from siml_gb300.serving import LingoServer, ServerConfig, Request, serve_unbatched
+    t = time.time()
+    db = S.smiles_set(S.SEED_SERVING, S.UNIFORM_20_90, SERVING_DB_N)
+    log("generated + compiled %d molecules in %.1f s" % (SERVING_DB_N, time.time() - t))
+    dev = torch.device("cuda", local)
+    gl = GPULingo(local, stream=torch.cuda.Stream(device=dev))
+    t = time.time()
+    gl.set_qsmiles(*db)
+    cfg = ServerConfig(max_rows=1024, width=128, kmax=64, pitch=256, lo=0.75)
+    srv = LingoServer(gl, cfg)
+    # warm the layout, row lists and kernels with one small batch of each kind
+    warm = S.smiles_list(S.SEED_SERVING, S.UNIFORM_20_90, 64, first=SERVING_DB_N)
+    for kind in ("topk", "threshold"):
+        serve_unbatched(srv, Request(-1, warm, kind=kind, k=50))
+    torch.cuda.synchronize()
+    stats = gl.dbStats()
+    log("database resident in %.1f s: %s" % (time.time() - t, stats))
+    nq = SERVING_DB_N
+    rates = [float(x) for x in args.serving_rates.split(",")]
+    results = []
+    first = SERVING_DB_N + 64
+    clocks = ClockSampler(local)
+    clocks.start()
+    for ri, rate in enumerate(rates):
+        sched = serving_requests(rate, args.warmup + args.steps, first, S.SEED_SERVING + ri)
+        first += sum(len(x[2]) for x in sched)
+        # batched: open-loop arrivals into the running server
+        srv.start()
+        t0 = time.perf_counter() + 0.2
+        reqs = run_arrivals(srv.submit, sched, t0)
+        for r in reqs:
+            r.done.wait()
+        srv.stop()
+        timed = [r for r in reqs if r.arrival - t0 >= args.warmup]
+        b = serving_stats(timed, nq)
+        b["batches"] = srv.batches
+        # unbatched: the same arrivals served one request at a time, in order
+        pend = []
+        t0u = time.perf_counter() + 0.2
+        done_u = []
+
+        def worker():
+            while True:
+                with cvu:
+                    while not pend and not stop_u[0]:
+                        cvu.wait()
+                    if not pend:
+                        return
+                    r = pend.pop(0)
+                serve_unbatched(srv, r)
+                done_u.append(r)
+
+        import threading
+        cvu = threading.Condition()
+        stop_u = [False]
+
+        def submit_u(r):
+            with cvu:
+                pend.append(r)
+                cvu.notify()
+
+        th = threading.Thread(target=worker)
+        th.start()
+        ureqs = run_arrivals(submit_u, sched, t0u)
+        with cvu:
+            stop_u[0] = True
+            cvu.notify()
+        th.join()
+        utimed = [r for r in ureqs if r.arrival - t0u >= args.warmup]
+        u = serving_stats(utimed, nq)
+        # identical answers alone and in the mix (every request of the window)
+        same = all(_same_result(a.result, c.result) for a, c in zip(timed, utimed))
+        results.append({"rate_req_s": rate, "batched": b, "unbatched": u, "alone_equals_mix": same})
+        log("rate %g: batched p50/p99 %.1f/%.1f ms, %.1f Gpairs/s; unbatched p50/p99 %.1f/%.1f ms"
+            % (rate, b["p50_ms"], b["p99_ms"], b["gpairs_per_s"], u["p50_ms"], u["p99_ms"]))
+    clk = clocks.stop()
+    # saturated capacity: every request of the first schedule submitted at once
+    sched = serving_requests(rates[0], args.warmup + args.steps, SERVING_DB_N + 64, S.SEED_SERVING)
+    srv.start()
+    tb = time.perf_counter()
+    burst = [Request(i, smi, kind=kind, k=50, lo=0.75, arrival=tb) for i, (_, kind, smi) in enumerate(sched)]
+    for r in burst:
+        srv.submit(r)
+    for r in burst:
+        r.done.wait()
+    srv.stop()
+    cap = serving_stats(burst, nq)
+    # the per-request path on the same burst, one request after another
+    tu = time.perf_counter()
+    uburst = [Request(i, smi, kind=kind, k=50, lo=0.75, arrival=tu) for i, (_, kind, smi) in enumerate(sched)]
+    for r in uburst:
+        serve_unbatched(srv, r)
+    ucap = serving_stats(uburst, nq)
+    cap_same = all(_same_result(a.result, c.result) for a, c in zip(burst, uburst))
+    # oracle spot check: the smallest requests of each kind
+    from oracle import cpulingo as O
+    spot_ok = True
+    for kind in ("topk", "threshold"):
+        small = sorted((r for r in burst if r.kind == kind), key=lambda r: r.rows)[:2]
+        for r in small:
+            qs = O.compile_strings(r.smiles)
+            if kind == "topk":
+                oi, os_ = O.topk_block(qs, db, 0, r.rows, 50, nthreads=os.cpu_count() or 1)
+                want = [(oi[q], os_[q]) for q in range(r.rows)]
+            else:
+                oi, osm, oc = O.neighbors_block(qs, db, 0, r.rows, 0.75, 1.1, nq, nthreads=os.cpu_count() or 1)
+                want = [(oi[q, :oc[q]], osm[q, :oc[q]]) for q in range(r.rows)]
+            spot_ok &= _same_result(r.result, want)
+    head = results[0]["batched"]
+    line = {
+        "metric": METRIC, "value": cap["gpairs_per_s"], "unit": "Gpairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded SMILES-like strings)",
+        "config": {"workload": SERVING_WORKLOAD, "db_molecules": SERVING_DB_N, "rates_req_s": rates,
+                   "seconds_per_rate": args.warmup + args.steps, "timed_after_s": args.warmup,
+                   "server": vars(cfg), "db_layout": stats},
+        "value_note": "saturated capacity: the first rate's requests all submitted at once",
+        "serving": results, "capacity": cap, "capacity_unbatched": ucap,
+        "batched_over_unbatched_capacity": cap["gpairs_per_s"] / ucap["gpairs_per_s"],
+        "capacity_alone_equals_mix": cap_same,
+        "p50_ms": head["p50_ms"], "p95_ms": head["p95_ms"], "p99_ms": head["p99_ms"],
+        "e2e": {"value": head["gpairs_per_s"], "unit": "Gpairs/s", "note": "open-loop served rate at the first "
+                "rate, SMILES in, host results out", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+        "clocks": clk, "parity_spot_check": spot_ok,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _same_result(a, b):
+    if a is None or b is None or len(a) != len(b):
+        return False
+    for x, y in zip(a, b):
+        if not (np.array_equal(x[0], y[0]) and
+                np.array_equal(np.asarray(x[1], np.float32).view(np.uint32), np.asarray(y[1], np.float32).view(np.uint32))):
+            return False
+    return True
+
+
 def read_profile_traffic(name="k_rows_rows1m.md"):
     """DRAM bytes per launch of the dominant kernel from its committed ncu
     summary (a "traffic_bytes_per_launch:" line), if any."""
@@ -660,12 +860,14 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--rows-per-step", type=int, default=BLOCK,
                     help="rows per block (smaller blocks for profiler captures)")
-    ap.add_argument("--workload", choices=["rows_1m", "nbr_1m", "topk_1m", "hist_1m", "ragged_2m"],
+    ap.add_argument("--workload", choices=["rows_1m", "nbr_1m", "topk_1m", "hist_1m", "ragged_2m", "serving_10m"],
                     default="rows_1m",
                     help="rows_1m: getMultipleRows blocks (default); nbr_1m: getNeighbors at T >= 0.7; "
                          "topk_1m: top-100 per row; hist_1m: 1000-bin histogram of every pair; "
                          "ragged_2m: 4,096 batched neighbour jobs vs the plain per-job path")
     ap.add_argument("--ragged-jobs", type=int, default=RAGGED_JOBS, help="jobs of the ragged_2m workload")
+    ap.add_argument("--serving-rates", default="200,500,1000",
+                    help="serving_10m: request rates (req/s), each run for warmup + steps seconds")
     ap.add_argument("--rows-window", type=int, default=0,
                     help="sort window of the full-matrix layout (32, 64, 128, 256; 0: library default)")
     ap.add_argument("--rows-entries", type=int, default=-1,
@@ -678,6 +880,12 @@ def main():
     args = ap.parse_args()
     if args.workload == "ragged_2m":
         return ragged_reference_arm(args) if args.impl == "reference" else ragged_arm(args)
+    if args.workload == "serving_10m":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no request loop; its CPU "
+                              "path is timed by the rows_1m and ragged_2m reference arms"}), flush=True)
+            return 0
+        return serving_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
     return gpu_arm(args)

@@ -81,6 +81,17 @@ int siml_set_ref(siml_engine* h, const int32_t* lingos, const int32_t* counts,
 int siml_set_query(siml_engine* h, const int32_t* lingos, const int32_t* counts,
                    const int32_t* lengths, const int32_t* mags,
                    int64_t n, int64_t width, int64_t ld, int where);
+/* Overwrites ref rows [row0, row0 + n) in place (no reference counterpart;
+ * the reference replaces the whole set, pysiml/GPULingo.py:187-242): a
+ * request loop keeps a slot buffer of ref rows and writes each batch's query
+ * molecules into it.  Host arrays (row stride ld >= width, width <= the ref
+ * set's width); codes are validated on the host, the copies and the rows'
+ * device preparation are queued on the engine's stream, and the call
+ * returns without waiting for earlier work when the arrays are pinned.
+ * Rows with more entries than SIML_TUNE_ROW_STRIDE reserves make the next
+ * call rebuild every row's entry list. */
+int siml_write_ref_rows(siml_engine* h, int64_t row0, const int32_t* lingos, const int32_t* counts,
+                        const int32_t* lengths, const int32_t* mags, int64_t n, int64_t width, int64_t ld);
 /* Sizes of the current sets (-1 when unset). */
 int siml_set_sizes(siml_engine* h, int64_t* nref, int64_t* nquery);
 
@@ -230,6 +241,10 @@ int siml_db_stats(siml_engine* h, int64_t out[8]);
 #define SIML_ENTRIES_U16 1     /* as AUTO: 2-byte when the vocabulary allows */
 #define SIML_ENTRIES_U32 2
 #define SIML_ENTRIES_OFFSETS 3
+/* SIML_TUNE_ROW_STRIDE: least number of entries (sum of counts) reserved per
+ * ref row's entry list, so rows written later by siml_write_ref_rows up to
+ * that size need no rebuild. */
+#define SIML_TUNE_ROW_STRIDE 3
 int siml_set_tuning(siml_engine* h, int key, int64_t value);
 int siml_get_tuning(siml_engine* h, int key, int64_t* value);
 /* Number of kernel launches this engine has issued since creation. */

@@ -26,6 +26,7 @@ SIML_DEVICE = 1
 
 SIML_TUNE_ROWS_WINDOW = 1
 SIML_TUNE_ROWS_ENTRIES = 2
+SIML_TUNE_ROW_STRIDE = 3
 SIML_ENTRIES_AUTO = 0
 SIML_ENTRIES_U16 = 1
 SIML_ENTRIES_U32 = 2
@@ -60,6 +61,7 @@ _SIGNATURES = {
     "siml_query_done": (_I32, [_P, ctypes.POINTER(_I32)]),
     "siml_set_ref": (_I32, [_P, _P, _P, _P, _P, _I64, _I64, _I64, _I32]),
     "siml_set_query": (_I32, [_P, _P, _P, _P, _P, _I64, _I64, _I64, _I32]),
+    "siml_write_ref_rows": (_I32, [_P, _I64, _P, _P, _P, _P, _I64, _I64, _I64]),
     "siml_set_sizes": (_I32, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "siml_rows": (_I32, [_P, _I64, _I64, _P, _I64, _I32]),
     "siml_row_single": (_I32, [_P, _I64, _P, _I32]),

@@ -554,7 +554,7 @@ int build_rows(siml_engine* h) {
     const RawSet& r = h->ref;
     RowEntries& re = h->rows;
     re.n = r.n;
-    re.stride = std::max<int64_t>(1, r.max_entries);
+    re.stride = std::max<int64_t>(std::max<int64_t>(1, r.max_entries), h->row_stride_hint);
     int rc;
     if ((rc = dev_alloc(&re.vid, (size_t)(std::max<int64_t>(r.n, 1) * re.stride)))) return rc;
     if (r.n > 0) {
@@ -693,6 +693,73 @@ int siml_set_ref(siml_engine* h, const int32_t* lingos, const int32_t* counts, c
     return upload_set(h, h->ref, lingos, counts, lengths, mags, n, width, ld, "set_refsmiles");
 }
 
+int siml_write_ref_rows(siml_engine* h, int64_t row0, const int32_t* lingos, const int32_t* counts,
+                        const int32_t* lengths, const int32_t* mags, int64_t n, int64_t width, int64_t ld) {
+    SIML_GUARD(h);
+    RawSet& s = h->ref;
+    if (s.n < 0) return fail(SIML_ERR_STATE, "siml_write_ref_rows: no ref set (set_refsmiles first)");
+    if (row0 < 0 || n < 0 || row0 + n > s.n)
+        return fail(SIML_ERR_RANGE, "siml_write_ref_rows: rows [%lld, %lld) outside the ref set of %lld rows",
+                    (long long)row0, (long long)(row0 + n), (long long)s.n);
+    if (width < 0 || ld < width || width > s.width)
+        return fail(SIML_ERR_INVALID, "siml_write_ref_rows: width %lld (ld %lld) does not fit the ref set's %lld",
+                    (long long)width, (long long)ld, (long long)s.width);
+    if (n == 0) return SIML_OK;
+    if (!lengths || (width > 0 && (!lingos || !counts))) return fail(SIML_ERR_INVALID, "siml_write_ref_rows: NULL array");
+    // validate on the host, so the write needs no read-back and stays queued
+    int64_t mx = 0;
+    for (int64_t r = 0; r < n; r++) {
+        const int32_t L = lengths[r];
+        if (L < 0 || L > width)
+            return fail(SIML_ERR_INVALID, "siml_write_ref_rows: length %d of row %lld outside [0, %lld]", L,
+                        (long long)r, (long long)width);
+        long long sum = 0;
+        for (int32_t j = 0; j < L; j++) {
+            const int32_t c = counts[r * ld + j];
+            if (c < 0) return fail(SIML_ERR_UNSUPPORTED, "siml_write_ref_rows: negative LINGO count");
+            if (j > 0 && !(lingos[r * ld + j - 1] < lingos[r * ld + j]))
+                return fail(SIML_ERR_UNSUPPORTED, "siml_write_ref_rows: LINGO codes of a molecule are not strictly "
+                            "increasing (sorted unique codes are required, as the SMILES compiler produces)");
+            sum += c;
+        }
+        if (sum > 0x7FFFFFFFll) return fail(SIML_ERR_UNSUPPORTED, "siml_write_ref_rows: overflowing LINGO counts");
+        mx = std::max<int64_t>(mx, sum);
+    }
+    cudaStream_t st = h->stream;
+    int32_t* dl = s.lingos + row0 * s.width;
+    int32_t* dc = s.counts + row0 * s.width;
+    if (width < s.width) {
+        SIML_CUDA(cudaMemset2DAsync(dl, s.width * 4, 0, s.width * 4, n, st));
+        SIML_CUDA(cudaMemset2DAsync(dc, s.width * 4, 0, s.width * 4, n, st));
+    }
+    if (width > 0) {
+        SIML_CUDA(cudaMemcpy2DAsync(dl, s.width * 4, lingos, ld * 4, width * 4, n, cudaMemcpyHostToDevice, st));
+        SIML_CUDA(cudaMemcpy2DAsync(dc, s.width * 4, counts, ld * 4, width * 4, n, cudaMemcpyHostToDevice, st));
+    }
+    SIML_CUDA(cudaMemcpyAsync(s.len + row0, lengths, n * 4, cudaMemcpyHostToDevice, st));
+    // count sums on the device (the host copy above only validated them)
+    k_set_stats<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dl, dc, s.len + row0, n, s.width, s.cmag + row0,
+                                                            h->d_err, h->d_counter, h->d_counter + 1);
+    h->launches++;
+    SIML_CUDA(cudaGetLastError());
+    if (mags) SIML_CUDA(cudaMemcpyAsync(s.mag + row0, mags, n * 4, cudaMemcpyHostToDevice, st));
+    else SIML_CUDA(cudaMemcpyAsync(s.mag + row0, s.cmag + row0, n * 4, cudaMemcpyDeviceToDevice, st));
+    s.max_entries = std::max(s.max_entries, mx);
+    if (h->rows_valid) {
+        if (mx > h->rows.stride) {
+            h->rows_valid = false;   // rebuilt, wider, on next use
+        } else {
+            k_row_entries<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(dl, dc, s.len + row0, n, s.width,
+                                                                       h->vocab.keys, h->vocab.vid, h->vocab.cap,
+                                                                       h->rows.vid + row0 * h->rows.stride,
+                                                                       h->rows.stride);
+            h->launches++;
+            SIML_CUDA(cudaGetLastError());
+        }
+    }
+    return SIML_OK;
+}
+
 int siml_set_query(siml_engine* h, const int32_t* lingos, const int32_t* counts, const int32_t* lengths,
                    const int32_t* mags, int64_t n, int64_t width, int64_t ld, int where) {
     SIML_GUARD(h);
@@ -740,6 +807,12 @@ int siml_set_tuning(siml_engine* h, int key, int64_t value) {
             h->rows_window = (int)value;
         }
         return SIML_OK;
+    case SIML_TUNE_ROW_STRIDE:
+        if (value < 0 || value > (1 << 20))
+            return fail(SIML_ERR_INVALID, "row stride hint must be in [0, 2^20] (got %lld)", (long long)value);
+        if (value > h->row_stride_hint && h->rows_valid && value > h->rows.stride) h->rows_valid = false;
+        h->row_stride_hint = value;
+        return SIML_OK;
     case SIML_TUNE_ROWS_ENTRIES:
         if (value < SIML_ENTRIES_AUTO || value > SIML_ENTRIES_OFFSETS)
             return fail(SIML_ERR_INVALID, "rows entry format must be 0..3 (got %lld)", (long long)value);
@@ -761,6 +834,7 @@ int siml_get_tuning(siml_engine* h, int key, int64_t* value) {
     switch (key) {
     case SIML_TUNE_ROWS_WINDOW: *value = h->rows_window; return SIML_OK;
     case SIML_TUNE_ROWS_ENTRIES: *value = h->rows_entries; return SIML_OK;
+    case SIML_TUNE_ROW_STRIDE: *value = h->row_stride_hint; return SIML_OK;
     default: return fail(SIML_ERR_INVALID, "unknown tuning key %d", key);
     }
 }

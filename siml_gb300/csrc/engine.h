@@ -97,6 +97,7 @@ struct siml_engine {
     uint64_t generation = 0;              // bumped whenever a set is replaced (plans made before are stale)
     int rows_window = siml::kChunk;       // sort window of the full-matrix layout (kChunk: natural order)
     int rows_entries = 0;                 // entry format of the full-matrix layout (SIML_TUNE_ROWS_ENTRIES)
+    int64_t row_stride_hint = 0;          // least entries per ref row list (SIML_TUNE_ROW_STRIDE)
 };
 
 namespace siml {

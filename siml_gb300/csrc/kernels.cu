@@ -993,21 +993,32 @@ __global__ void __launch_bounds__(256) k_topk_rowscan(const struct RawArgs ra, i
 //     k_topk_rowscan.  No host synchronization is needed between the steps.
 constexpr int kSelectMax = 8192;
 
+// One warp per row: walks the bins from the top, 32 at a time, to the
+// highest bin at which k molecules have been seen.
 __global__ void k_topk_theta(const int32_t* hist, int k, int64_t rows, float* row_lo, int* list_counts) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) {
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         list_counts[0] = 0;
         list_counts[1] = 0;
     }
-    if (i >= rows) return;
+    if (i >= rows) return;   // uniform over the warp
     const int32_t* h = hist + i * kLogBins;
     int64_t acc = 0;
-    int b = kLogBins - 1;
-    for (; b > 0; b--) {
-        acc += h[b];
-        if (acc >= k) break;
+    int found = 0;   // bin index, 0 when fewer than k above bin 0
+    for (int top = kLogBins - 1; top > 0 && !found; top -= 32) {
+        const int b = top - lane;                       // lane 0 holds the highest bin of the slice
+        const int64_t v = b > 0 ? h[b] : 0;
+        int64_t incl = v;                               // inclusive prefix over lanes = count of bins >= b in slice
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        const unsigned hit = __ballot_sync(0xFFFFFFFFu, b > 0 && acc + incl >= k);
+        if (hit) found = top - (__ffs(hit) - 1);
+        acc += __shfl_sync(0xFFFFFFFFu, incl, 31);
     }
-    row_lo[i] = log_bin_floor(b);   // b == 0: fewer than k above bin 0, collect all
+    if (lane == 0) row_lo[i] = log_bin_floor(found);   // bin 0: collect all
 }
 
 // One CTA per row (listed rows: absolute row ids, rowbase subtracted).
@@ -1743,7 +1754,7 @@ int topk_collect_block(siml_engine* h, const DbLayout* d, int64_t r0, int64_t ro
         k_loghist<NP, ET><<<grid, kThreads, smem, h->stream>>>(ps, hist);
         SIML_CUDA(cudaGetLastError());
     }
-    k_topk_theta<<<(unsigned)((rows + 255) / 256), 256, 0, h->stream>>>(hist, k, rows, row_lo, list_n);
+    k_topk_theta<<<(unsigned)((rows + 7) / 8), 256, 0, h->stream>>>(hist, k, rows, row_lo, list_n);
     SIML_CUDA(cudaGetLastError());
     // 2. collect every pair at or above its row's bound
     GroupParams pc = ps;

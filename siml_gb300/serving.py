@@ -1,0 +1,378 @@
+"""Request loop over a resident database: continuous batching of similarity
+queries on one GPU.
+
+A request carries SMILES strings and asks either for the top-k most similar
+database molecules of each string (ties to the lower index) or for every
+database molecule with Tanimoto >= a threshold (getNeighbors' rule,
+pysiml/kernels.py:393-475).  The reference answers one call at a time
+(pysiml/GPULingo.py:467-534); here a batcher thread admits queued requests
+into the next batch while earlier batches run:
+
+* admission: a request joins the forming batch while the batch's query rows
+  fit one slot region of the ref buffer and its hit buffers fit the region's
+  device memory budget (FIFO: the first request that does not fit waits for
+  the next batch);
+* two slot regions alternate, so the next batch is compiled, written and
+  queued on the stream while the previous one computes and its results come
+  back; a region is reused only after its results have been handed out;
+* results are exact and independent of the batch a request lands in (the
+  kernels are deterministic and every ordering is total), which the tests
+  check alone against in a mix.
+
+The per-request path (`serve_unbatched`) runs the same steps one request at a
+time, as a caller of the reference's API would.
+"""
+from __future__ import annotations
+
+import collections
+import ctypes
+import math
+import threading
+import time
+
+import numpy as np
+
+from . import _native as N
+
+try:
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+TOPK = "topk"
+THRESHOLD = "threshold"
+
+
+class Request:
+    """One request: `smiles` (a list of bytes) and the kind of answer.
+
+    After completion `result` holds, per query string, either (indices,
+    similarities) of its top-k, or (indices, similarities) of every hit in
+    ascending index order; `t_done - arrival` is the latency in seconds."""
+
+    __slots__ = ("rid", "smiles", "kind", "k", "lo", "arrival", "t_admit", "t_done", "result", "error", "done",
+                 "rows")
+
+    def __init__(self, rid, smiles, kind=TOPK, k=50, lo=0.75, arrival=None):
+        if kind not in (TOPK, THRESHOLD):
+            raise ValueError("kind must be 'topk' or 'threshold'")
+        self.rid = rid
+        self.smiles = [s.encode() if isinstance(s, str) else bytes(s) for s in smiles]
+        self.kind = kind
+        self.k = int(k)
+        self.lo = float(lo)
+        self.arrival = time.perf_counter() if arrival is None else arrival
+        self.t_admit = None
+        self.t_done = None
+        self.result = None
+        self.error = None
+        self.done = threading.Event()
+        self.rows = len(self.smiles)
+
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.arrival
+
+
+def compile_into(smiles, L, C, ln, mg, width):
+    """Compiles SMILES into the first len(smiles) rows of preallocated
+    [*, width] arrays; returns the widest molecule's LINGO count."""
+    n = len(smiles)
+    off = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum([len(s) for s in smiles], out=off[1:])
+    buf = b"".join(smiles) or b"\0"
+    lib = N.lib()
+    w = lib.siml_compile_width(buf, off.ctypes.data, n)
+    if w < 0:
+        N.check(int(-w), "siml_compile_width")
+    if w > width:
+        raise ValueError("a query molecule has %d unique LINGOs, more than the server's width %d" % (w, width))
+    N.check(lib.siml_compile_smiles(buf, off.ctypes.data, n, L.ctypes.data, C.ctypes.data, ln.ctypes.data,
+                                    mg.ctypes.data, width), "siml_compile_smiles")
+    return w
+
+
+class _Region:
+    """One slot region: ref rows [base, base + max_rows) and its buffers."""
+
+    def __init__(self, base, cfg, dev):
+        self.base = base
+        pin = lambda shape, dt: torch.empty(shape, dtype=dt).pin_memory()
+        R, W = cfg.max_rows, cfg.width
+        self.hL, self.hC = pin((R, W), torch.int32), pin((R, W), torch.int32)
+        self.hlen, self.hmag = pin((R,), torch.int32), pin((R,), torch.int32)
+        self.k_idx = torch.empty((R, cfg.kmax), dtype=torch.int32, device=dev)
+        self.k_sims = torch.empty((R, cfg.kmax), dtype=torch.float32, device=dev)
+        self.n_idx = torch.empty((R, cfg.pitch), dtype=torch.int32, device=dev)
+        self.n_sims = torch.empty((R, cfg.pitch), dtype=torch.float32, device=dev)
+        self.n_cnt = torch.empty((R,), dtype=torch.int32, device=dev)
+        self.o_kidx, self.o_ksims = pin((R, cfg.kmax), torch.int32), pin((R, cfg.kmax), torch.float32)
+        self.o_nidx, self.o_nsims = pin((R, cfg.pitch), torch.int32), pin((R, cfg.pitch), torch.float32)
+        self.o_ncnt = pin((R,), torch.int32)
+        self.free = threading.Event()
+        self.free.set()
+
+
+class ServerConfig:
+    """max_rows: query rows per batch (one slot region); width: LINGO columns
+    per query row; kmax: largest k a top-k request may ask; pitch: hits per
+    row a threshold batch keeps before an overflowing row is re-run alone;
+    hit_budget: device bytes of hit buffers one batch may claim."""
+
+    def __init__(self, max_rows=1024, width=256, kmax=64, pitch=256, hit_budget=None, lo=0.75):
+        self.max_rows = int(max_rows)
+        self.width = int(width)
+        self.kmax = int(kmax)
+        self.pitch = int(pitch)
+        self.lo = float(lo)
+        self.hit_budget = int(hit_budget) if hit_budget else self.max_rows * max(self.pitch, self.kmax) * 8
+
+
+def _hit_bytes(req, cfg):
+    return req.rows * (cfg.pitch * 8 + 4 if req.kind == THRESHOLD else req.k * 8)
+
+
+class LingoServer:
+    """Continuous-batching request loop on a GPULingo object whose query set
+    (the database) is already set.  The object's ref set becomes the server's
+    slot buffer."""
+
+    def __init__(self, gl, cfg=None):
+        if torch is None:
+            raise RuntimeError("the request loop needs torch for pinned buffers and streams")
+        self.gl = gl
+        self.cfg = cfg or ServerConfig()
+        self.dev = gl._device()
+        R, W = self.cfg.max_rows, self.cfg.width
+        zeros = np.zeros((2 * R, W), dtype=np.int32)
+        gl.set_refsmiles(zeros, zeros, np.zeros(2 * R, dtype=np.int32))
+        N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_ROW_STRIDE, 4 * W), "siml_set_tuning")
+        self.regions = [_Region(0, self.cfg, self.dev), _Region(R, self.cfg, self.dev)]
+        self.queue = collections.deque()
+        self.cv = threading.Condition()
+        self.inflight = collections.deque()
+        self.icv = threading.Condition()
+        self.stop_flag = False
+        self.batcher_done = False
+        self.elock = threading.Lock()   # one host thread at a time on the engine handle
+        self.batches = 0
+        self.pairs = 0
+        self.batch_rows = []
+        self.threads = []
+
+    # ------------------------------------------------------------- control
+    def start(self):
+        self.stop_flag = False
+        self.batcher_done = False
+        self.threads = [threading.Thread(target=self._batcher, daemon=True),
+                        threading.Thread(target=self._completer, daemon=True)]
+        for t in self.threads:
+            t.start()
+        return self
+
+    def stop(self):
+        """Serves what is queued, then ends both threads."""
+        with self.cv:
+            self.stop_flag = True
+            self.cv.notify_all()
+        if self.threads:
+            self.threads[0].join()
+        with self.icv:
+            self.batcher_done = True
+            self.icv.notify_all()
+        if self.threads:
+            self.threads[1].join()
+        self.threads = []
+
+    def submit(self, req):
+        if req.rows > self.cfg.max_rows:
+            raise ValueError("request of %d queries exceeds the batch size %d" % (req.rows, self.cfg.max_rows))
+        if req.kind == TOPK and not 1 <= req.k <= self.cfg.kmax:
+            raise ValueError("k must be in [1, %d]" % self.cfg.kmax)
+        if req.kind == THRESHOLD and req.lo != self.cfg.lo:
+            raise ValueError("threshold requests use the server's bound %g" % self.cfg.lo)
+        with self.cv:
+            self.queue.append(req)
+            self.cv.notify()
+        return req
+
+    # ------------------------------------------------------------- batcher
+    def _take_batch(self):
+        cfg = self.cfg
+        with self.cv:
+            while not self.queue and not self.stop_flag:
+                self.cv.wait()
+            if self.stop_flag and not self.queue:
+                return None
+            batch, rows, hits = [], 0, 0
+            while self.queue:
+                r = self.queue[0]
+                need = _hit_bytes(r, cfg)
+                if batch and (rows + r.rows > cfg.max_rows or hits + need > cfg.hit_budget):
+                    break
+                self.queue.popleft()
+                batch.append(r)
+                rows += r.rows
+                hits += need
+            return batch
+
+    def _batcher(self):
+        seq = 0
+        while True:
+            region = self.regions[seq % 2]
+            region.free.wait()
+            batch = self._take_batch()
+            if batch is None:
+                return
+            region.free.clear()
+            try:
+                item = self._launch(batch, region)
+            except Exception as e:  # report the failure on every request of the batch
+                for r in batch:
+                    r.error = e
+                    r.t_done = time.perf_counter()
+                    r.done.set()
+                region.free.set()
+                continue
+            with self.icv:
+                self.inflight.append(item)
+                self.icv.notify()
+            seq += 1
+
+    def _launch(self, batch, region):
+        gl, cfg = self.gl, self.cfg
+        now = time.perf_counter()
+        thr = [r for r in batch if r.kind == THRESHOLD]
+        tk = [r for r in batch if r.kind == TOPK]
+        nt = sum(r.rows for r in thr)
+        nk = sum(r.rows for r in tk)
+        kmax = max([r.k for r in tk], default=1)
+        L, C = region.hL.numpy(), region.hC.numpy()
+        ln, mg = region.hlen.numpy(), region.hmag.numpy()
+        row = 0
+        for r in thr + tk:
+            r.t_admit = now
+            compile_into(r.smiles, L[row:], C[row:], ln[row:], mg[row:], cfg.width)
+            row += r.rows
+        with self.elock:
+            return self._queue(batch, thr, tk, nt, nk, kmax, region)
+
+    def _queue(self, batch, thr, tk, nt, nk, kmax, region):
+        gl, cfg = self.gl, self.cfg
+        L, C = region.hL.numpy(), region.hC.numpy()
+        ln, mg = region.hlen.numpy(), region.hmag.numpy()
+        lib = N.lib()
+        n = nt + nk
+        N.check(lib.siml_write_ref_rows(gl._h, region.base, L.ctypes.data, C.ctypes.data, ln.ctypes.data,
+                                        mg.ctypes.data, n, cfg.width, cfg.width), "siml_write_ref_rows")
+        st = gl.stream
+        b = region.base
+        if nt:
+            N.check(lib.siml_neighbors(gl._h, b, b + nt, ctypes.c_float(cfg.lo), ctypes.c_float(1.1), cfg.pitch,
+                                       region.n_idx.data_ptr(), region.n_sims.data_ptr(), region.n_cnt.data_ptr(),
+                                       N.SIML_DEVICE), "siml_neighbors")
+        if nk:
+            kidx = region.k_idx.view(-1)[:cfg.max_rows * kmax].view(cfg.max_rows, kmax)
+            ksims = region.k_sims.view(-1)[:cfg.max_rows * kmax].view(cfg.max_rows, kmax)
+            N.check(lib.siml_topk(gl._h, b + nt, b + nt + nk, kmax, kidx.data_ptr(), ksims.data_ptr(),
+                                  N.SIML_DEVICE), "siml_topk")
+        with torch.cuda.stream(st):
+            if nt:
+                region.o_ncnt[:nt].copy_(region.n_cnt[:nt], non_blocking=True)
+                region.o_nidx[:nt].copy_(region.n_idx[:nt], non_blocking=True)
+                region.o_nsims[:nt].copy_(region.n_sims[:nt], non_blocking=True)
+            if nk:
+                m = nk * kmax
+                region.o_kidx.view(-1)[:m].copy_(region.k_idx.view(-1)[:m], non_blocking=True)
+                region.o_ksims.view(-1)[:m].copy_(region.k_sims.view(-1)[:m], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(st)
+        self.batches += 1
+        self.pairs += n * gl.nquery
+        self.batch_rows.append(n)
+        return (batch, thr, tk, nt, nk, kmax, region, ev)
+
+    # ----------------------------------------------------------- completer
+    def _completer(self):
+        while True:
+            with self.icv:
+                while not self.inflight and not self.batcher_done:
+                    self.icv.wait()
+                if not self.inflight:
+                    return
+                item = self.inflight.popleft()
+            batch, thr, tk, nt, nk, kmax, region, ev = item
+            try:
+                ev.synchronize()
+                self._deliver(thr, tk, nt, nk, kmax, region)
+            except Exception as e:
+                for r in batch:
+                    r.error = e
+            t = time.perf_counter()
+            region.free.set()
+            for r in batch:
+                r.t_done = t
+                r.done.set()
+
+    def _deliver(self, thr, tk, nt, nk, kmax, region):
+        cfg = self.cfg
+        cnt = region.o_ncnt.numpy()
+        nidx, nsims = region.o_nidx.numpy(), region.o_nsims.numpy()
+        row = 0
+        for r in thr:
+            res = []
+            for q in range(r.rows):
+                c = int(cnt[row + q])
+                if c > cfg.pitch:
+                    res.append(self._rerun_row(region.base + row + q, c))
+                else:
+                    res.append((nidx[row + q, :c].copy(), nsims[row + q, :c].copy()))
+            r.result = res
+            row += r.rows
+        kid = region.o_kidx.numpy().reshape(-1)[:nk * kmax].reshape(nk, kmax) if nk else None
+        ksm = region.o_ksims.numpy().reshape(-1)[:nk * kmax].reshape(nk, kmax) if nk else None
+        row = 0
+        for r in tk:
+            r.result = [(kid[row + q, :r.k].copy(), ksm[row + q, :r.k].copy()) for q in range(r.rows)]
+            row += r.rows
+
+    def _rerun_row(self, ref_row, count):
+        """A threshold row with more hits than the batch pitch, searched
+        again alone with room for all of them (the region is still held)."""
+        pitch = 16 * ((count + 15) // 16)
+        idx = np.empty((1, pitch), dtype=np.int32)
+        sims = np.empty((1, pitch), dtype=np.float32)
+        cnt = np.empty(1, dtype=np.int32)
+        with self.elock:
+            N.check(N.lib().siml_neighbors(self.gl._h, ref_row, ref_row + 1, ctypes.c_float(self.cfg.lo),
+                                           ctypes.c_float(1.1), pitch, idx.ctypes.data, sims.ctypes.data,
+                                           cnt.ctypes.data, N.SIML_HOST), "siml_neighbors")
+        c = int(cnt[0])
+        return idx[0, :c].copy(), sims[0, :c].copy()
+
+
+def serve_unbatched(server, req):
+    """The per-request path: one request written, searched and read back on
+    its own, synchronously (uses the server's first region; do not mix with
+    a running batch loop)."""
+    region = server.regions[0]
+    req.t_admit = time.perf_counter()
+    thr = [req] if req.kind == THRESHOLD else []
+    tk = [req] if req.kind == TOPK else []
+    batch = server._launch([req], region)
+    _, _, _, nt, nk, kmax, _, ev = batch
+    ev.synchronize()
+    server._deliver(thr, tk, nt, nk, kmax, region)
+    req.t_done = time.perf_counter()
+    req.done.set()
+    return req
+
+
+def percentiles(values, ps=(50, 95, 99)):
+    if not values:
+        return {("p%d" % p): None for p in ps}
+    v = np.sort(np.asarray(values, dtype=np.float64))
+    out = {}
+    for p in ps:
+        i = min(len(v) - 1, max(0, int(math.ceil(p / 100.0 * len(v))) - 1))
+        out["p%d" % p] = float(v[i])
+    return out
