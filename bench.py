@@ -197,11 +197,10 @@ def reference_arm(args):
 # ------------------------------------------------------------- GPU arm ----
 def gpu_arm(args):
     import torch
+    from siml_gb300 import replicas
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    replicas.init("nccl", torch.device("cuda", local))
     from siml_gb300 import GPULingo
     db, q = make_sets()
     dev = torch.device("cuda", local)
@@ -223,7 +222,7 @@ def gpu_arm(args):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
 
     def block_of(k):
-        b = (k * world + rank) % nblocks
+        b = replicas.block_of(k, world, rank, nblocks)
         return b * rows_step, (b + 1) * rows_step
 
     wl = args.workload
@@ -254,8 +253,7 @@ def gpu_arm(args):
         r0, r1 = block_of(w)
         run_step(r0, r1)
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.5)
@@ -276,12 +274,8 @@ def gpu_arm(args):
     wall = time.time() - wall0
     launches = gl.launchCount() - launches0
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(step_ms)
-    if world > 1:
-        tt = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(tt.item())
-        torch.distributed.barrier()
+    total_ms = replicas.max_over_ranks(sum(step_ms), dev)
+    replicas.barrier()
     clk = clocks.stop()
     pairs_per_step = rows_step * DB_N
     value = world * args.steps * pairs_per_step / (total_ms / 1e3) / 1e9
@@ -347,8 +341,7 @@ def gpu_arm(args):
             "clocks": clk, "parity_spot_check": parity, "wall_s_timed": wall,
         }
         print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    replicas.finish()
     return 0
 
 
@@ -422,11 +415,10 @@ def ragged_arm(args):
     CUDA graph, against the plain path (one getNeighbors-over-a-range call per
     job) on the same GPU, outputs compared bit for bit."""
     import torch
+    from siml_gb300 import replicas
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    replicas.init("nccl", torch.device("cuda", local))
     from siml_gb300 import GPULingo
     db, jobs = ragged_sets_and_jobs(args.ragged_jobs)
     dev = torch.device("cuda", local)
@@ -460,8 +452,7 @@ def ragged_arm(args):
     for _ in range(args.warmup):
         graph.replay()
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    replicas.barrier()
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.5)
@@ -477,12 +468,8 @@ def ragged_arm(args):
     torch.cuda.synchronize()
     wall = time.time() - wall0
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(step_ms)
-    if world > 1:
-        tt = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(tt.item())
-        torch.distributed.barrier()
+    total_ms = replicas.max_over_ranks(sum(step_ms), dev)
+    replicas.barrier()
     clk = clocks.stop()
     value = world * args.steps * plan.pairs / (total_ms / 1e3) / 1e9
     ms_per_step = total_ms / args.steps
@@ -602,8 +589,7 @@ def ragged_arm(args):
             "parity_batched_equals_plain": same, "parity_spot_check": oracle_ok, "wall_s_timed": wall,
         }
         print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    replicas.finish()
     return 0
 
 
@@ -665,6 +651,8 @@ def serving_stats(reqs, nq):
 def serving_arm(args):
     import torch
     rank, world, local = dist_env()
+    if rank != 0:   # one request loop: the other ranks have nothing to serve
+        return 0
     torch.cuda.set_device(local)
     from siml_gb300 import GPULingo
     from siml_gb300 import synthetic as S
