@@ -245,6 +245,14 @@ int siml_db_stats(siml_engine* h, int64_t out[8]);
  * ref row's entry list, so rows written later by siml_write_ref_rows up to
  * that size need no rebuild. */
 #define SIML_TUNE_ROW_STRIDE 3
+/* SIML_TUNE_SORT_WINDOW: the layout of the fused kernels (neighbours,
+ * histograms, top-k, batched jobs) sorts database molecules by entry count
+ * inside windows of this many molecules (a power of two, 64..8192; default
+ * 2048).  Wider windows pad less and give chunks narrower magnitude ranges
+ * (more chunks skipped by threshold searches); column-range jobs are rounded
+ * out to whole windows.  Changing it drops the layout and invalidates
+ * batch plans. */
+#define SIML_TUNE_SORT_WINDOW 4
 int siml_set_tuning(siml_engine* h, int key, int64_t value);
 int siml_get_tuning(siml_engine* h, int key, int64_t* value);
 /* Number of kernel launches this engine has issued since creation. */

@@ -27,6 +27,7 @@ SIML_DEVICE = 1
 SIML_TUNE_ROWS_WINDOW = 1
 SIML_TUNE_ROWS_ENTRIES = 2
 SIML_TUNE_ROW_STRIDE = 3
+SIML_TUNE_SORT_WINDOW = 4
 SIML_ENTRIES_AUTO = 0
 SIML_ENTRIES_U16 = 1
 SIML_ENTRIES_U32 = 2

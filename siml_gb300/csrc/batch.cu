@@ -3,9 +3,9 @@
 // A job is a range of ref rows searched against a range of database columns
 // with getNeighbors' rule (pysiml/kernels.py:393-475).  The reference issues
 // one getNeighbors call per job (pysiml/GPULingo.py:467-513); here a plan
-// turns all jobs into work items of at most 32 rows x a chunk range of the
-// window-sorted layout, ordered largest first, and a persistent kernel pulls
-// them from a device queue.  siml_batch_run only enqueues work on the
+// turns all jobs into work items of at most 32 rows (each job's rows ordered
+// by magnitude) x a chunk range of the window-sorted layout, largest first,
+// and a persistent kernel pulls them from a device queue.  siml_batch_run only enqueues work on the
 // caller's stream (no host synchronization, no allocation), so it can be
 // captured in a CUDA graph and replayed.
 //
@@ -23,6 +23,7 @@ struct siml_batch {
     const siml::DbLayout* d = nullptr;
     uint64_t generation = 0;
     int4* items = nullptr;        // 2 per item
+    int32_t* order = nullptr;     // each job's ref rows, ordered by magnitude
     int64_t nitems = 0;
     int4* rowinfo = nullptr;      // per output row
     int64_t rows_out = 0;
@@ -41,22 +42,33 @@ struct HostJob {
     int64_t rb, re, cb, ce, out;
 };
 
-void make_items(const DbLayout* d, const std::vector<HostJob>& jobs, int64_t tile, std::vector<int4>& items) {
+// Orders each job's rows by magnitude into `order` (ref rows, stably) and
+// cuts each job into items of at most 32 consecutive ordered rows x `tile`
+// chunks, largest items first.  Rows of one item then have close
+// magnitudes, so whole chunks out of the bound's reach are skipped.
+void make_items(const DbLayout* d, const std::vector<HostJob>& jobs, const std::vector<int32_t>& mag, int64_t tile,
+                std::vector<int4>& items, std::vector<int32_t>& order) {
     struct It {
         int4 a, b;
         int64_t cost;
     };
     std::vector<It> v;
+    order.clear();
     for (const HostJob& j : jobs) {
         if (j.re <= j.rb || j.ce <= j.cb) continue;
+        const int64_t pos0 = (int64_t)order.size();
+        for (int64_t r = j.rb; r < j.re; r++) order.push_back((int32_t)r);
+        std::stable_sort(order.begin() + pos0, order.end(),
+                         [&](int32_t x, int32_t y) { return mag[(size_t)x] < mag[(size_t)y]; });
         int64_t c0, c1;
         sorted_chunk_range(d, j.cb, j.ce, c0, c1);
-        for (int64_t r = j.rb; r < j.re; r += 32) {
-            const int nr = (int)std::min<int64_t>(32, j.re - r);
+        const int64_t nrows = j.re - j.rb;
+        for (int64_t r = 0; r < nrows; r += 32) {
+            const int nr = (int)std::min<int64_t>(32, nrows - r);
             for (int64_t c = c0; c < c1; c += tile) {
                 const int64_t ce = std::min(c1, c + tile);
                 It it;
-                it.a = make_int4((int)r, nr, (int)(j.out + (r - j.rb)), (int)j.cb);
+                it.a = make_int4((int)(pos0 + r), nr, (int)(j.out - j.rb), (int)j.cb);
                 it.b = make_int4((int)j.ce, (int)c, (int)ce, 0);
                 it.cost = (int64_t)(ce - c) * (16 + nr);
                 v.push_back(it);
@@ -73,12 +85,22 @@ void make_items(const DbLayout* d, const std::vector<HostJob>& jobs, int64_t til
 
 // Copies on the engine's stream and waits, so kernels queued there later see
 // the data (the engine's stream need not synchronize with the legacy one).
-int upload_items(siml_engine* h, const std::vector<int4>& items, int4** out) {
+template <typename T>
+int upload_items(siml_engine* h, const std::vector<T>& items, T** out) {
     *out = nullptr;
-    SIML_CUDA(cudaMalloc((void**)out, std::max<size_t>(items.size(), 2) * sizeof(int4)));
+    SIML_CUDA(cudaMalloc((void**)out, std::max<size_t>(items.size(), 2) * sizeof(T)));
     if (!items.empty()) {
-        SIML_CUDA(cudaMemcpyAsync(*out, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice,
-                                  h->stream));
+        SIML_CUDA(cudaMemcpyAsync(*out, items.data(), items.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+        SIML_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    return SIML_OK;
+}
+
+// The ref set's magnitudes on the host (plans order each job's rows by them).
+int host_mags(siml_engine* h, std::vector<int32_t>& mag) {
+    mag.resize((size_t)std::max<int64_t>(h->ref.n, 0));
+    if (!mag.empty()) {
+        SIML_CUDA(cudaMemcpyAsync(mag.data(), h->ref.mag, mag.size() * 4, cudaMemcpyDeviceToHost, h->stream));
         SIML_CUDA(cudaStreamSynchronize(h->stream));
     }
     return SIML_OK;
@@ -90,9 +112,9 @@ int upload_items(siml_engine* h, const std::vector<int4>& items, int4** out) {
 // of a second whatever the batch size.
 constexpr double kTuneBudget = 1.0e10;
 
-int autotune_tile(siml_engine* h, const DbLayout* d, const std::vector<HostJob>& jobs, float lo, float hi,
-                  int64_t pitch, int64_t* best_tile) {
-    static const int64_t cand[] = {16, 32, 64, 128, 256, 512};
+int autotune_tile(siml_engine* h, const DbLayout* d, const std::vector<HostJob>& jobs,
+                  const std::vector<int32_t>& mag, float lo, float hi, int64_t pitch, int64_t* best_tile) {
+    static const int64_t cand[] = {32, 64, 128, 256, 512, 1024, 2048};
     std::vector<HostJob> sample;
     int64_t rows = 0;
     double pairs = 0.0;
@@ -114,11 +136,12 @@ int autotune_tile(siml_engine* h, const DbLayout* d, const std::vector<HostJob>&
         for (int64_t r = j.rb; r < j.re; r++)
             rowinfo[(size_t)(j.out + r - j.rb)] = make_int4((int)r, (int)j.cb, (int)j.ce, 0);
     int4* d_rowinfo = nullptr;
-    int32_t *d_idx = nullptr, *d_cnt = nullptr;
+    int32_t *d_idx = nullptr, *d_cnt = nullptr, *d_order = nullptr;
     unsigned int* d_head = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     int rc = SIML_OK;
     auto cleanup = [&]() {
+        if (d_order) cudaFree(d_order);
         if (d_rowinfo) cudaFree(d_rowinfo);
         if (d_idx) cudaFree(d_idx);
         if (d_cnt) cudaFree(d_cnt);
@@ -142,19 +165,21 @@ int autotune_tile(siml_engine* h, const DbLayout* d, const std::vector<HostJob>&
     bool warmed = false;
     for (int64_t t : cand) {
         std::vector<int4> items;
-        make_items(d, sample, t, items);
+        std::vector<int32_t> order;
+        make_items(d, sample, mag, t, items, order);
         int4* d_items = nullptr;
+        if (!d_order && (rc = upload_items(h, order, &d_order))) break;   // the same for every tile
         if ((rc = upload_items(h, items, &d_items))) break;
         const int64_t ni = (int64_t)items.size() / 2;
         if (!warmed) {   // first launch pays one-time costs; keep it out of the comparison
-            rc = launch_batch_neighbors(h, d, d_items, ni, d_head, d_rowinfo, rows, lo, hi, pitch, d_idx, nullptr,
-                                        d_cnt, h->stream);
+            rc = launch_batch_neighbors(h, d, d_items, ni, d_head, d_order, d_rowinfo, rows, lo, hi, pitch, d_idx,
+                                        nullptr, d_cnt, h->stream);
             warmed = true;
         }
         if (!rc) {
             cudaEventRecord(e0, h->stream);
-            rc = launch_batch_neighbors(h, d, d_items, ni, d_head, d_rowinfo, rows, lo, hi, pitch, d_idx, nullptr,
-                                        d_cnt, h->stream);
+            rc = launch_batch_neighbors(h, d, d_items, ni, d_head, d_order, d_rowinfo, rows, lo, hi, pitch, d_idx,
+                                        nullptr, d_cnt, h->stream);
             cudaEventRecord(e1, h->stream);
         }
         e = cudaEventSynchronize(e1);
@@ -231,10 +256,12 @@ int siml_batch_create(siml_engine* h, int64_t njobs, const int64_t* jobs, float 
                                        (long long)(x.out + r - x.rb));
             ri = make_int4((int)r, (int)x.cb, (int)x.ce, 0);
         }
+    std::vector<int32_t> mag;
+    if ((rc = host_mags(h, mag))) return rc;
     int64_t tile = tile_chunks;
     if (tile <= 0) {
         if (batch_nbr_usable(h, d)) {
-            if ((rc = autotune_tile(h, d, hj, lo, hi, pitch, &tile))) return rc;
+            if ((rc = autotune_tile(h, d, hj, mag, lo, hi, pitch, &tile))) return rc;
         } else {
             tile = 128;
         }
@@ -249,9 +276,11 @@ int siml_batch_create(siml_engine* h, int64_t njobs, const int64_t* jobs, float 
     b->tile_chunks = tile;
     b->rows_out = rows_out;
     std::vector<int4> items;
-    make_items(d, hj, tile, items);
+    std::vector<int32_t> order;
+    make_items(d, hj, mag, tile, items, order);
     b->nitems = (int64_t)items.size() / 2;
-    if ((rc = plan_bytes(h, d, hj, items, &b->stream_bytes, &b->unique_bytes)) || (rc = upload_items(h, items, &b->items)) ||
+    if ((rc = plan_bytes(h, d, hj, items, &b->stream_bytes, &b->unique_bytes)) ||
+        (rc = upload_items(h, items, &b->items)) || (rc = upload_items(h, order, &b->order)) ||
         (rc = upload_items(h, rowinfo, &b->rowinfo))) {
         siml_batch_destroy(b);
         return rc;
@@ -287,8 +316,8 @@ int siml_batch_run(siml_batch* b, int32_t* idx, float* sims, int32_t* counts, vo
     if (b->rows_out == 0) return SIML_OK;
     if (!counts || (b->pitch > 0 && !idx)) return fail(SIML_ERR_INVALID, "siml_batch_run: NULL output");
     cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
-    return launch_batch_neighbors(h, b->d, b->items, b->nitems, b->head, b->rowinfo, b->rows_out, b->lo, b->hi,
-                                  b->pitch, idx, sims, counts, st);
+    return launch_batch_neighbors(h, b->d, b->items, b->nitems, b->head, b->order, b->rowinfo, b->rows_out, b->lo,
+                                  b->hi, b->pitch, idx, sims, counts, st);
 }
 
 int siml_batch_destroy(siml_batch* b) {
@@ -296,6 +325,7 @@ int siml_batch_destroy(siml_batch* b) {
     if (!b) return SIML_OK;
     cudaSetDevice(b->h->device);
     if (b->items) cudaFree(b->items);
+    if (b->order) cudaFree(b->order);
     if (b->rowinfo) cudaFree(b->rowinfo);
     if (b->head) cudaFree(b->head);
     delete b;

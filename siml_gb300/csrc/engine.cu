@@ -126,6 +126,7 @@ void free_vocab(Vocab& v) { dev_free(v.keys); dev_free(v.vid); v = Vocab(); }
 void free_layout(DbLayout& d) {
     dev_free(d.perm); dev_free(d.meta);
     dev_free(d.ng); dev_free(d.off);
+    if (d.crange) cudaFree(d.crange);
     if (d.entries) cudaFree(d.entries);
     d = DbLayout();
 }
@@ -280,20 +281,37 @@ __device__ __forceinline__ uint32_t vocab_lookup(const unsigned long long* __res
 }
 
 // One CTA of 256 threads per window: rank molecules by (entries, index).
+// Sorts each window of w molecules (a power of two, 64..kMaxWindow) by entry
+// count: bitonic sort of (count << 32 | position) keys in shared memory;
+// positions past the end sort last.
 __global__ void k_window_sort(const int32_t* __restrict__ cmag, int64_t n, int w, int32_t* perm) {
-    __shared__ long long key[kWindow];
-    const int64_t base = (int64_t)blockIdx.x * kWindow;
-    const int t = threadIdx.x;
-    const int64_t m = base + t;
-    // molecules past the end sort last; ranks count only keys of the same
-    // w-molecule sub-window
-    key[t] = m < n ? ((long long)cmag[m] << 20) | t : (0x7FFFFFFFll << 20) | t;
+    extern __shared__ long long key[];
+    const int64_t base = (int64_t)blockIdx.x * w;
+    for (int i = threadIdx.x; i < w; i += blockDim.x) {
+        const int64_t m = base + i;
+        key[i] = m < n ? ((long long)cmag[m] << 32) | i : (0x7FFFFFFFll << 32) | i;
+    }
     __syncthreads();
-    const long long mine = key[t];
-    const int w0 = t / w * w;
-    int rank = 0;
-    for (int k = w0; k < w0 + w; k++) rank += key[k] < mine;
-    perm[base + w0 + rank] = m < n ? (int32_t)m : -1;
+    for (int k = 2; k <= w; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < w; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const bool asc = (i & k) == 0;
+                    const long long a = key[i], b = key[ixj];
+                    if ((a > b) == asc) {
+                        key[i] = b;
+                        key[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < w; i += blockDim.x) {
+        const int64_t m = base + (int)(key[i] & 0xFFFFFFFFll);
+        perm[base + i] = m < n ? (int32_t)m : -1;
+    }
 }
 
 // Natural order: slot i holds molecule i.
@@ -307,7 +325,7 @@ __global__ void k_identity_perm(int64_t n, int64_t slots, int32_t* perm) {
 __global__ void k_chunk_meta(const int32_t* __restrict__ perm, const int32_t* __restrict__ cmag,
                              const int32_t* __restrict__ mag, const int32_t* __restrict__ len,
                              int64_t nchunks, int entries_per_group,
-                             int32_t* __restrict__ ng, int4* __restrict__ meta) {
+                             int32_t* __restrict__ ng, int4* __restrict__ meta, int2* __restrict__ crange) {
     const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (c >= nchunks) return;
@@ -315,10 +333,16 @@ __global__ void k_chunk_meta(const int32_t* __restrict__ perm, const int32_t* __
     const int32_t e = m >= 0 ? cmag[m] : 0;
     meta[c * 32 + lane] = make_int4(m, m >= 0 ? mag[m] : 0, e, m >= 0 ? len[m] : 0);
     int32_t mx = e;
-    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+    int32_t mlo = m >= 0 ? mag[m] : 0x7FFFFFFF, mhi = m >= 0 ? mag[m] : -1;
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+        mlo = min(mlo, __shfl_xor_sync(0xFFFFFFFFu, mlo, o));
+        mhi = max(mhi, __shfl_xor_sync(0xFFFFFFFFu, mhi, o));
+    }
     if (lane == 0) {
         const int32_t steps = (mx + 7) / 8;                 // 8 entries per step
         ng[c] = steps * (8 / entries_per_group);
+        crange[c] = make_int2(mlo, mhi);                    // empty chunk: lo > hi
     }
 }
 
@@ -493,7 +517,7 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     cudaStream_t st = h->stream;
     d.n = q.n;
     d.sorted = sorted;
-    d.window = sorted ? kWindow : h->rows_window;
+    d.window = sorted ? h->sorted_window : h->rows_window;
     d.entry_bytes = h->vocab.nvid < 65535 ? 2 : 4;
     d.offsets = false;
     if (!sorted && h->rows_entries == SIML_ENTRIES_U32) d.entry_bytes = 4;
@@ -501,21 +525,27 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
         d.entry_bytes = 4;
         d.offsets = true;
     }
-    const int64_t nwin = (q.n + kWindow - 1) / kWindow;
+    const int64_t nwin = (q.n + d.window - 1) / d.window;
     d.nchunks = (q.n + kChunk - 1) / kChunk;
-    const int64_t slots = nwin * kWindow;
+    const int64_t slots = std::max<int64_t>(nwin, 1) * d.window;
     int rc;
     if ((rc = dev_alloc(&d.perm, (size_t)slots))) return rc;
     if ((rc = dev_alloc(&d.meta, (size_t)slots))) return rc;
     if ((rc = dev_alloc(&d.ng, (size_t)d.nchunks))) return rc;
     if ((rc = dev_alloc(&d.off, (size_t)d.nchunks + 1))) return rc;
     if (q.n == 0) return SIML_OK;
-    if (d.window > kChunk) k_window_sort<<<(unsigned)nwin, kWindow, 0, st>>>(q.cmag, q.n, d.window, d.perm);
-    else k_identity_perm<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(q.n, slots, d.perm);
+    SIML_CUDA(cudaMalloc((void**)&d.crange, (size_t)std::max<int64_t>(d.nchunks, 1) * sizeof(int2)));
+    if (d.window > kChunk) {
+        const size_t wsm = (size_t)d.window * 8;
+        SIML_CUDA(cudaFuncSetAttribute(k_window_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+        k_window_sort<<<(unsigned)nwin, std::min(d.window, 1024), wsm, st>>>(q.cmag, q.n, d.window, d.perm);
+    } else {
+        k_identity_perm<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(q.n, slots, d.perm);
+    }
     h->launches++;
     const int epg = 16 / d.entry_bytes;
     k_chunk_meta<<<(unsigned)((d.nchunks + 7) / 8), 256, 0, st>>>(d.perm, q.cmag, q.mag, q.len, d.nchunks, epg,
-                                                                  d.ng, d.meta);
+                                                                  d.ng, d.meta, d.crange);
     h->launches++;
     SIML_CUDA(cudaGetLastError());
     std::vector<int32_t> hng((size_t)d.nchunks);
@@ -807,6 +837,18 @@ int siml_set_tuning(siml_engine* h, int key, int64_t value) {
             h->rows_window = (int)value;
         }
         return SIML_OK;
+    case SIML_TUNE_SORT_WINDOW:
+        if (value < 64 || value > kMaxWindow || (value & (value - 1)))
+            return fail(SIML_ERR_INVALID, "sort window must be a power of two in [64, %d] (got %lld)", kMaxWindow,
+                        (long long)value);
+        if (value != h->sorted_window) {
+            SIML_CUDA(cudaStreamSynchronize(h->stream));
+            free_layout(h->db_sorted);
+            h->sorted_valid = false;
+            h->sorted_window = (int)value;
+            h->generation++;   // plans hold chunk ranges of the old layout
+        }
+        return SIML_OK;
     case SIML_TUNE_ROW_STRIDE:
         if (value < 0 || value > (1 << 20))
             return fail(SIML_ERR_INVALID, "row stride hint must be in [0, 2^20] (got %lld)", (long long)value);
@@ -835,6 +877,7 @@ int siml_get_tuning(siml_engine* h, int key, int64_t* value) {
     case SIML_TUNE_ROWS_WINDOW: *value = h->rows_window; return SIML_OK;
     case SIML_TUNE_ROWS_ENTRIES: *value = h->rows_entries; return SIML_OK;
     case SIML_TUNE_ROW_STRIDE: *value = h->row_stride_hint; return SIML_OK;
+    case SIML_TUNE_SORT_WINDOW: *value = h->sorted_window; return SIML_OK;
     default: return fail(SIML_ERR_INVALID, "unknown tuning key %d", key);
     }
 }

@@ -44,7 +44,7 @@ struct Vocab {
 // bytes per lane, interleaved [group][lane] so a warp's load of one group is
 // 512 contiguous bytes; an entry is a vid (uint16 when nvid < 65536, else
 // uint32), 0 padding a molecule's list to the chunk's length.
-constexpr int kWindow = 256;
+constexpr int kMaxWindow = 8192;   // largest sort window (one CTA sorts it in shared memory)
 constexpr int kChunk = 32;
 struct DbLayout {
     int64_t n = 0;
@@ -60,6 +60,7 @@ struct DbLayout {
     bool sorted = false;
     int window = kChunk;          // molecules are sorted by entry count inside windows of this size
     bool offsets = false;         // 4-byte entries hold byte offsets (vid * 4) into the table
+    int2* crange = nullptr;       // [nchunks] {smallest, largest} magnitude of the chunk's molecules
 };
 
 // Ref-set rows as vid lists (levels expanded, codes absent from the database
@@ -98,6 +99,7 @@ struct siml_engine {
     int rows_window = siml::kChunk;       // sort window of the full-matrix layout (kChunk: natural order)
     int rows_entries = 0;                 // entry format of the full-matrix layout (SIML_TUNE_ROWS_ENTRIES)
     int64_t row_stride_hint = 0;          // least entries per ref row list (SIML_TUNE_ROW_STRIDE)
+    int sorted_window = 2048;             // sort window of the fused-kernel layout (SIML_TUNE_SORT_WINDOW)
 };
 
 namespace siml {
@@ -142,12 +144,13 @@ struct NbrCall {
 };
 int launch_neighbors(siml_engine* h, const NbrCall& c);
 // Batched neighbour search: items (two int4 each) pulled by a persistent
-// kernel, then the per-output-row finish; rowinfo[rows_out] = {ref row,
-// col_begin, col_end, 0} (ref row -1: unused row).  Queued on st only.
+// kernel over ordered ref rows `order`, then the per-output-row finish;
+// rowinfo[rows_out] = {ref row, col_begin, col_end, 0} (ref row -1: unused
+// row).  Queued on st only.
 int batch_nbr_usable(siml_engine* h, const DbLayout* d);
 int launch_batch_neighbors(siml_engine* h, const DbLayout* d, const int4* items, int64_t nitems, unsigned int* head,
-                           const int4* rowinfo, int64_t rows_out, float lo, float hi, int64_t pitch,
-                           int32_t* idx, float* sims, int32_t* counts, cudaStream_t st);
+                           const int32_t* order, const int4* rowinfo, int64_t rows_out, float lo, float hi,
+                           int64_t pitch, int32_t* idx, float* sims, int32_t* counts, cudaStream_t st);
 // Chunks of the window-sorted layout that hold database columns [c0, c1).
 void sorted_chunk_range(const DbLayout* d, int64_t c0, int64_t c1, int64_t& chunk_begin, int64_t& chunk_end);
 // Per-row 101-bin int32 histograms (out [rows, ldo], zeroed here) or one

@@ -76,6 +76,7 @@ struct GroupParams {
     int mode;
     const float* row_lo;      // per output row lower bound (per-row threshold search) or null
     const int* rows_dev;      // device row count bounding `rows` (row lists built on the device) or null
+    const int2* crange;       // per chunk {smallest, largest} magnitude (the layout's), for chunk skipping
 };
 
 struct RowSmem {
@@ -85,6 +86,8 @@ struct RowSmem {
     __align__(16) float amagf[32];
     int allfast;
     int min_amag;
+    int max_amag;
+    float min_lo;            // lowest per-row bound of the group
     float lo[32];            // per-row lower bound (GroupParams.row_lo)
     float coef[32];          // its integer-test coefficient (bound_coef)
     float min_coef;          // lowest integer-test coefficient of the group's bounds
@@ -121,19 +124,30 @@ __device__ __forceinline__ int build_table(uint32_t* T, RowSmem& rs, const Group
         rs.alen[r] = r < nr ? p.row_len[gr] : 0;
         const bool f = r >= nr || (p.mode == kModeRows && fast_mag(am, p.row_cmag[gr]));
         const unsigned all = __ballot_sync(0xFFFFFFFFu, f);
-        int mn = r < nr ? am : 0x7FFFFFFF;
-        for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
+        int mn = r < nr ? am : 0x7FFFFFFF, mxa = r < nr ? am : -1;
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = min(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
+            mxa = max(mxa, __shfl_xor_sync(0xFFFFFFFFu, mxa, o));
+        }
         if (p.row_lo) {
             const float lo = r < nr ? p.row_lo[gr - p.rowbase] : 3.0e38f;
             rs.lo[r] = lo;
             float c = r < nr ? bound_coef(lo) : 3.0e38f;
             rs.coef[r] = r < nr ? c : 0.0f;
-            for (int o = 16; o > 0; o >>= 1) c = fminf(c, __shfl_xor_sync(0xFFFFFFFFu, c, o));
-            if (r == 0) rs.min_coef = c;
+            float ml = lo;
+            for (int o = 16; o > 0; o >>= 1) {
+                c = fminf(c, __shfl_xor_sync(0xFFFFFFFFu, c, o));
+                ml = fminf(ml, __shfl_xor_sync(0xFFFFFFFFu, ml, o));
+            }
+            if (r == 0) {
+                rs.min_coef = c;
+                rs.min_lo = ml;
+            }
         }
         if (r == 0) {
             rs.allfast = all == 0xFFFFFFFFu;
             rs.min_amag = mn;
+            rs.max_amag = mxa;
         }
     }
     __syncthreads();
@@ -154,14 +168,35 @@ __device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
     if (bytes) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// Chunks [wb, we) of this warp: the CTA's slice split contiguously.
-__device__ __forceinline__ void warp_range(const GroupParams& p, int64_t& wb, int64_t& we) {
+// First chunk c in [lo, hi] whose first entry group is at or past `target`
+// (the chunk offsets are non-decreasing).
+__device__ __forceinline__ int64_t chunk_at_volume(const int64_t* __restrict__ off, int64_t lo, int64_t hi,
+                                                   int64_t target) {
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) < target) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Splits chunks [cb, ce) among the CTA's warps by entry volume, so warps with
+// chunks of long molecules (the sorted layout orders sizes inside a window)
+// get fewer of them.
+__device__ __forceinline__ void warp_split(const int64_t* __restrict__ off, int64_t cb, int64_t ce,
+                                           int64_t& wb, int64_t& we) {
     const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int64_t g0 = __ldg(off + cb), g1 = __ldg(off + ce);
+    wb = warp == 0 ? cb : chunk_at_volume(off, cb, ce, g0 + (g1 - g0) * warp / nwarps);
+    we = warp == nwarps - 1 ? ce : chunk_at_volume(off, cb, ce, g0 + (g1 - g0) * (warp + 1) / nwarps);
+}
+
+// Chunks [wb, we) of this warp: the CTA's slice split by volume.
+__device__ __forceinline__ void warp_range(const GroupParams& p, int64_t& wb, int64_t& we) {
     const int64_t n = p.chunk_end - p.chunk_begin;
     const int64_t cb = p.chunk_begin + n * blockIdx.y / gridDim.y;
     const int64_t ce = p.chunk_begin + n * (blockIdx.y + 1) / gridDim.y;
-    wb = cb + (ce - cb) * warp / nwarps;
-    we = cb + (ce - cb) * (warp + 1) / nwarps;
+    warp_split(p.off, cb, ce, wb, we);
 }
 
 // Entry types of the database layout: 2-byte vids, 4-byte vids, or 4-byte
@@ -238,6 +273,42 @@ __device__ __forceinline__ void stream_chunks(const uint32_t* __restrict__ T, co
             acc.add8(tload<ET>(T, c0.x), tload<ET>(T, c0.y), tload<ET>(T, c0.z), tload<ET>(T, c0.w),
                      tload<ET>(T, c1.x), tload<ET>(T, c1.y), tload<ET>(T, c1.z), tload<ET>(T, c1.w));
         steps--;
+    }
+}
+
+// True when no pair of a chunk (magnitudes [r.x, r.y]) and the group's rows
+// (magnitudes [amin, amax]) can reach lo: t <= min(ma, mb) / max(ma, mb), and
+// the largest such bound over the two ranges sits at their nearest ends.  The
+// fp32 quotient is the reference's pre-filter (pysiml/kernels.py:437-448) and
+// rounding is monotone, so the corner value is the exact maximum.
+__device__ __forceinline__ bool chunk_out_of_reach(int2 r, int amin, int amax, float lo) {
+    if (r.x > r.y) return true;   // padding only
+    float b;
+    if (r.y < amin) b = __fdiv_rn(__int2float_rn(r.y), __int2float_rn(amin));
+    else if (r.x > amax) b = __fdiv_rn(__int2float_rn(amax), __int2float_rn(r.x));
+    else return false;
+    return !(b >= lo);
+}
+
+// stream_chunks over the chunks of [wb, we) that can hold a pair with
+// t >= lo for some row of the group (lo <= 0 or NaN: every chunk).  Chunks
+// are tested warp-uniformly; runs of reachable chunks are streamed whole.
+template <int NP, typename ET, class Epi>
+__device__ __forceinline__ void stream_chunks_within(const uint32_t* __restrict__ T, const GroupParams& p,
+                                                     const RowSmem& rs, int64_t wb, int64_t we, float lo,
+                                                     Epi& epi) {
+    if (!(lo > 0.0f) || p.crange == nullptr || rs.max_amag < 0) {
+        stream_chunks<NP, ET>(T, p, wb, we, epi);
+        return;
+    }
+    const int amin = rs.min_amag, amax = rs.max_amag;
+    int64_t c = wb;
+    while (c < we) {
+        while (c < we && chunk_out_of_reach(p.crange[c], amin, amax, lo)) c++;
+        int64_t e = c;
+        while (e < we && !chunk_out_of_reach(p.crange[e], amin, amax, lo)) e++;
+        if (e > c) stream_chunks<NP, ET>(T, p, c, e, epi);
+        c = e;
     }
 }
 
@@ -426,7 +497,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_nbr(const GroupParams p, const 
     int64_t wb, we;
     warp_range(p, wb, we);
     NbrEpi<NP> epi{rs, nr, (int64_t)blockIdx.x * 32, a};
-    stream_chunks<NP, ET>(T, p, wb, we, epi);
+    stream_chunks_within<NP, ET>(T, p, rs, wb, we, a.thr_mode == 0 ? a.lo : 0.0f, epi);
 }
 
 // ---------------------------------------------------------- k_collect ----
@@ -504,7 +575,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_collect(const GroupParams p, co
     const int64_t row_stride = (int64_t)gridDim.y * c.seg_cap;
     CollectEpi<NP> epi{rs, nr, scount, c.cand_i + blockIdx.y * c.seg_cap, c.cand_t + blockIdx.y * c.seg_cap,
                        row_stride, c.seg_cap};
-    stream_chunks<NP, ET>(T, p, wb, we, epi);
+    stream_chunks_within<NP, ET>(T, p, rs, wb, we, rs.min_lo, epi);
     __syncthreads();
     if (threadIdx.x < nr) c.seg_counts[(int64_t)rs.orow[threadIdx.x] * gridDim.y + blockIdx.y] = scount[threadIdx.x];
 }
@@ -1107,35 +1178,43 @@ __global__ void __launch_bounds__(512) k_topk_select(const int32_t* cand_i, cons
 
 // -------------------------------------------------------- k_batch_nbr ----
 // Persistent batched neighbour search over ragged jobs (a job = a range of
-// ref rows against a range of database columns).  The plan splits every job
-// into work items of at most 32 rows x a chunk range; one CTA per SM pulls
-// items from a device queue head.  The shared table is updated incrementally:
-// an item whose rows differ from the CTA's current rows first clears the
-// current rows' bits (their vid lists, not the whole table) and then sets its
-// own.  Lanes outside the job's columns are masked in the epilogue.
-// Item layout: two int4 {row0, nrows, out_row0, col_begin}, {col_end, c0, c1, 0}.
-__device__ __forceinline__ void set_rows(uint32_t* T, RowSmem& rs, const GroupParams& p, int64_t row0, int nr,
-                                         int64_t out0) {
+// ref rows against a range of database columns).  The plan orders each
+// job's rows by magnitude (GroupParams.row_order holds the ordered ref rows
+// of all jobs) and splits every job into work items of at most 32 of those
+// rows x a chunk range; one CTA per SM pulls items from a device queue head.
+// The shared table is updated incrementally: an item whose rows differ from
+// the CTA's current rows first clears the current rows' bits (their vid
+// lists, not the whole table) and then sets its own.  Lanes outside the
+// job's columns are masked in the epilogue; chunks whose magnitudes cannot
+// reach the bound against the item's rows are skipped.
+// Item layout: two int4 {first order position, rows, output row - ref row,
+// col_begin}, {col_end, c0, c1, 0}.
+__device__ __forceinline__ void set_rows(uint32_t* T, RowSmem& rs, const GroupParams& p, int64_t pos0, int nr,
+                                         int64_t bias) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     if (warp == 0) {
         const int r = lane;
-        const int64_t gr = r < nr ? row0 + r : row0;
+        const int64_t gr = p.row_order[pos0 + (r < nr ? r : 0)];
         const int am = r < nr ? p.row_mag[gr] : 0;
-        rs.orow[r] = (int)(out0 + r);
+        rs.orow[r] = (int)(gr + bias);
         rs.amag[r] = am;
         rs.amagf[r] = (float)am;
         rs.alen[r] = r < nr ? p.row_len[gr] : 0;
         const bool f = r >= nr || fast_mag(am, p.row_cmag[gr]);
         const unsigned all = __ballot_sync(0xFFFFFFFFu, f);
-        int mn = r < nr ? am : 0x7FFFFFFF;
-        for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
+        int mn = r < nr ? am : 0x7FFFFFFF, mxa = r < nr ? am : -1;
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = min(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
+            mxa = max(mxa, __shfl_xor_sync(0xFFFFFFFFu, mxa, o));
+        }
         if (r == 0) {
             rs.allfast = all == 0xFFFFFFFFu;
             rs.min_amag = mn;
+            rs.max_amag = mxa;
         }
     }
     for (int r = warp; r < nr; r += nwarps) {
-        const uint32_t* rv = p.row_vid + (row0 + r) * p.row_stride;
+        const uint32_t* rv = p.row_vid + (int64_t)p.row_order[pos0 + r] * p.row_stride;
         for (int64_t e = lane; e < p.row_stride; e += 32) {
             const uint32_t v = rv[e];
             if (v) atomicOr(&T[v], 1u << r);
@@ -1143,10 +1222,10 @@ __device__ __forceinline__ void set_rows(uint32_t* T, RowSmem& rs, const GroupPa
     }
 }
 
-__device__ __forceinline__ void clear_rows(uint32_t* T, const GroupParams& p, int64_t row0, int nr) {
+__device__ __forceinline__ void clear_rows(uint32_t* T, const GroupParams& p, int64_t pos0, int nr) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     for (int r = warp; r < nr; r += nwarps) {
-        const uint32_t* rv = p.row_vid + (row0 + r) * p.row_stride;
+        const uint32_t* rv = p.row_vid + (int64_t)p.row_order[pos0 + r] * p.row_stride;
         for (int64_t e = lane; e < p.row_stride; e += 32) {
             const uint32_t v = rv[e];
             if (v) T[v] = 0u;
@@ -1160,34 +1239,34 @@ __global__ void __launch_bounds__(kThreads, 1) k_batch_nbr(const GroupParams p, 
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
     __shared__ long long s_item;
-    __shared__ long long cur_row0, cur_out0;
+    __shared__ long long cur_pos, cur_bias;
     __shared__ int cur_nr;
     for (int i = threadIdx.x * 4; i < p.vt_words; i += blockDim.x * 4)
         *reinterpret_cast<uint4*>(T + i) = make_uint4(0u, 0u, 0u, 0u);
-    if (threadIdx.x == 0) { cur_row0 = -1; cur_out0 = -1; cur_nr = 0; }
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    if (threadIdx.x == 0) { cur_pos = -1; cur_bias = 0; cur_nr = 0; }
     for (;;) {
         if (threadIdx.x == 0) s_item = (long long)atomicAdd(head, 1u);
         __syncthreads();
         const long long w = s_item;
         if (w >= nitems) break;
         const int4 ia = items[2 * w], ib = items[2 * w + 1];
-        const int64_t row0 = ia.x, out0 = ia.z;
+        const int64_t pos0 = ia.x, bias = ia.z;
         const int nr = ia.y;
-        if (row0 != cur_row0 || nr != cur_nr || out0 != cur_out0) {
-            if (cur_nr > 0) clear_rows(T, p, cur_row0, cur_nr);
+        if (pos0 != cur_pos || nr != cur_nr || bias != cur_bias) {
+            if (cur_nr > 0) clear_rows(T, p, cur_pos, cur_nr);
             __syncthreads();
-            set_rows(T, rs, p, row0, nr, out0);
-            if (threadIdx.x == 0) { cur_row0 = row0; cur_nr = nr; cur_out0 = out0; }
+            set_rows(T, rs, p, pos0, nr, bias);
+            if (threadIdx.x == 0) { cur_pos = pos0; cur_nr = nr; cur_bias = bias; }
             __syncthreads();
         }
         NbrArgs ai = a;
         ai.col_begin = ia.w;
         ai.col_end = ib.x;
         const int64_t c0 = ib.y, c1 = ib.z;
-        const int64_t wb = c0 + (c1 - c0) * warp / nwarps, we = c0 + (c1 - c0) * (warp + 1) / nwarps;
-        NbrEpi<NP> epi{rs, nr, out0, ai};
-        stream_chunks<NP, ET>(T, p, wb, we, epi);
+        int64_t wb, we;
+        warp_split(p.off, c0, c1, wb, we);
+        NbrEpi<NP> epi{rs, nr, 0, ai};
+        stream_chunks_within<NP, ET>(T, p, rs, wb, we, ai.thr_mode == 0 ? ai.lo : 0.0f, epi);
         __syncthreads();
     }
 }
@@ -1481,6 +1560,7 @@ bool table_params(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t ro
     p.mode = mode;
     p.row_lo = nullptr;
     p.rows_dev = nullptr;
+    p.crange = d->crange;
     return true;
 }
 
@@ -1579,8 +1659,8 @@ int batch_nbr_usable(siml_engine* h, const DbLayout* d) {
 }
 
 int launch_batch_neighbors(siml_engine* h, const DbLayout* d, const int4* items, int64_t nitems, unsigned int* head,
-                           const int4* rowinfo, int64_t rows_out, float lo, float hi, int64_t pitch,
-                           int32_t* idx, float* sims, int32_t* counts, cudaStream_t st) {
+                           const int32_t* order, const int4* rowinfo, int64_t rows_out, float lo, float hi,
+                           int64_t pitch, int32_t* idx, float* sims, int32_t* counts, cudaStream_t st) {
     NbrArgs a = nbr_args(lo, hi, pitch, idx, sims, counts, 0, 0);
     a.rowinfo = rowinfo;
     SIML_CUDA(cudaMemsetAsync(counts, 0, rows_out * sizeof(int32_t), st));
@@ -1592,6 +1672,7 @@ int launch_batch_neighbors(siml_engine* h, const DbLayout* d, const int4* items,
     int rc;
     if (nitems > 0 && table_params(h, d, 0, 1, kModeRows, p, smem, np)) {
         force_ordered = 0;
+        p.row_order = order;
         if (np == 8)
             rc = d->entry_bytes == 2 ? launch_batch_t<8, uint16_t>(h, p, smem, items, nitems, head, a, st)
                                      : launch_batch_t<8, uint32_t>(h, p, smem, items, nitems, head, a, st);
@@ -1914,9 +1995,9 @@ int launch_rows(siml_engine* h, const RowsArgs& a) {
 }
 
 void sorted_chunk_range(const DbLayout* d, int64_t c0, int64_t c1, int64_t& chunk_begin, int64_t& chunk_end) {
-    const int64_t per_window = kWindow / kChunk;
-    chunk_begin = (c0 / kWindow) * per_window;
-    chunk_end = std::min<int64_t>(d->nchunks, ((c1 + kWindow - 1) / kWindow) * per_window);
+    const int64_t W = d->window, per_window = W / kChunk;
+    chunk_begin = (c0 / W) * per_window;
+    chunk_end = std::min<int64_t>(d->nchunks, ((c1 + W - 1) / W) * per_window);
     if (c1 <= c0) chunk_end = chunk_begin;
 }
 

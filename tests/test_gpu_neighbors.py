@@ -102,3 +102,20 @@ def test_neighbors_merge_path(native, oracle):
     gl = _engine(ref, qry)
     _check(gl, oracle, ref, qry, 0, 50, 0.3)
     _check(gl, oracle, ref, qry, 0, 50, 0.0, 1.1, 5)
+
+
+@pytest.mark.parametrize("window", [64, 256, 2048, 8192])
+def test_neighbors_mixed_lengths_sort_windows(native, oracle, window):
+    """A bimodal database (short and long molecules): threshold searches skip
+    whole chunks whose magnitudes cannot reach the bound, for every sort
+    window; results equal the oracle."""
+    from siml_gb300 import synthetic as S
+    db = S.smiles_set(S.SEED_RAGGED, S.BIMODAL_35_110, 12000)
+    q = tuple(a[:300] for a in db)
+    gl = _engine(q, db)
+    from siml_gb300 import _native as N
+    N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_SORT_WINDOW, window))
+    for lo, maxn in ((0.6, 64), (0.3, 200), (0.9, 16)):
+        _check(gl, oracle, q, db, 0, 300, lo, 1.1, maxn)
+    idx, cnt = gl.getNeighbors(0, 300, 0.6, 1.1, 64)
+    assert np.all(cnt >= 1)   # every row finds itself
