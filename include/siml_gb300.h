@@ -253,6 +253,15 @@ int siml_db_stats(siml_engine* h, int64_t out[8]);
  * out to whole windows.  Changing it drops the layout and invalidates
  * batch plans. */
 #define SIML_TUNE_SORT_WINDOW 4
+/* SIML_TUNE_ROWS_LAYOUT: how the natural-order full-matrix layout packs a
+ * chunk of 32 molecules into its 32 lanes: SIML_ROWS_PADDED (lane i holds
+ * molecule i, padded to the chunk's longest) or SIML_ROWS_BALANCED (the
+ * chunk's entries dealt evenly to the lanes, partial counts merged before
+ * the row epilogue; the default).  Changing it drops the full-matrix
+ * layout. */
+#define SIML_TUNE_ROWS_LAYOUT 5
+#define SIML_ROWS_PADDED 0
+#define SIML_ROWS_BALANCED 1
 int siml_set_tuning(siml_engine* h, int key, int64_t value);
 int siml_get_tuning(siml_engine* h, int key, int64_t* value);
 /* Number of kernel launches this engine has issued since creation. */

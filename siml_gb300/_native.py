@@ -28,6 +28,9 @@ SIML_TUNE_ROWS_WINDOW = 1
 SIML_TUNE_ROWS_ENTRIES = 2
 SIML_TUNE_ROW_STRIDE = 3
 SIML_TUNE_SORT_WINDOW = 4
+SIML_TUNE_ROWS_LAYOUT = 5
+SIML_ROWS_PADDED = 0
+SIML_ROWS_BALANCED = 1
 SIML_ENTRIES_AUTO = 0
 SIML_ENTRIES_U16 = 1
 SIML_ENTRIES_U32 = 2

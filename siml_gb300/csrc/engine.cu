@@ -324,7 +324,7 @@ __global__ void k_identity_perm(int64_t n, int64_t slots, int32_t* perm) {
 // rounded up to an even number of 8-entry steps; plus per-lane metadata.
 __global__ void k_chunk_meta(const int32_t* __restrict__ perm, const int32_t* __restrict__ cmag,
                              const int32_t* __restrict__ mag, const int32_t* __restrict__ len,
-                             int64_t nchunks, int entries_per_group,
+                             int64_t nchunks, int entries_per_group, int balanced,
                              int32_t* __restrict__ ng, int4* __restrict__ meta, int2* __restrict__ crange) {
     const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
@@ -333,35 +333,55 @@ __global__ void k_chunk_meta(const int32_t* __restrict__ perm, const int32_t* __
     const int32_t e = m >= 0 ? cmag[m] : 0;
     meta[c * 32 + lane] = make_int4(m, m >= 0 ? mag[m] : 0, e, m >= 0 ? len[m] : 0);
     int32_t mx = e;
+    int32_t sum = (e + 7) / 8;                              // 8-entry steps of this molecule
     int32_t mlo = m >= 0 ? mag[m] : 0x7FFFFFFF, mhi = m >= 0 ? mag[m] : -1;
     for (int o = 16; o > 0; o >>= 1) {
         mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+        sum += __shfl_xor_sync(0xFFFFFFFFu, sum, o);
         mlo = min(mlo, __shfl_xor_sync(0xFFFFFFFFu, mlo, o));
         mhi = max(mhi, __shfl_xor_sync(0xFFFFFFFFu, mhi, o));
     }
     if (lane == 0) {
-        const int32_t steps = (mx + 7) / 8;                 // 8 entries per step
+        // padded: every lane as long as the longest molecule; balanced: the
+        // chunk's steps spread evenly over the 32 lanes
+        const int32_t steps = balanced ? (sum + 31) / 32 : (mx + 7) / 8;
         ng[c] = steps * (8 / entries_per_group);
         crange[c] = make_int2(mlo, mhi);                    // empty chunk: lo > hi
     }
 }
 
-// Writes each molecule's vid list into its chunk lane.
+// Padded layout: entry e of lane l's molecule sits in 16-byte group e / EPG
+// of that lane.  Balanced layout: the chunk's 8-entry steps, molecule after
+// molecule, are dealt to the lanes in runs of L = ng / SPG steps, so entry e
+// of molecule l is step P_l + e / 8 of the chunk (P_l = steps of molecules
+// before l), i.e. step (P_l + e / 8) % L of lane (P_l + e / 8) / L.
 template <typename ET>
 __global__ void k_fill_entries(const int32_t* __restrict__ lingos, const int32_t* __restrict__ counts,
-                               const int32_t* __restrict__ len, int64_t width,
+                               const int32_t* __restrict__ len, const int32_t* __restrict__ cmag, int64_t width,
                                const int32_t* __restrict__ perm, const int64_t* __restrict__ off,
-                               int64_t nchunks,
+                               const int32_t* __restrict__ ng, int64_t nchunks, int balanced,
                                const unsigned long long* __restrict__ keys,
                                const uint32_t* __restrict__ vid, int64_t cap, int shift,
                                ET* __restrict__ entries) {
     constexpr int EPG = 16 / sizeof(ET);
+    constexpr int SPG = 8 / EPG;   // 16-byte groups per 8-entry step
     const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= nchunks * 32) return;
+    if (slot >= nchunks * 32) return;   // whole warps (nchunks * 32 is a multiple of 32)
     const int32_t m = perm[slot];
-    if (m < 0) return;
     const int64_t c = slot >> 5;
     const int lane = (int)(slot & 31);
+    int32_t P = 0, Ls = 1;
+    if (balanced) {
+        const int32_t g = m >= 0 ? (cmag[m] + 7) / 8 : 0;
+        int32_t incl = g;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        P = incl - g;
+        Ls = max(1, ng[c] / SPG);
+    }
+    if (m < 0) return;
     const int32_t L = len[m];
     const int32_t* lr = lingos + (int64_t)m * width;
     const int32_t* cr = counts + (int64_t)m * width;
@@ -370,7 +390,13 @@ __global__ void k_fill_entries(const int32_t* __restrict__ lingos, const int32_t
         const int32_t code = lr[j], cnt = cr[j];
         for (int32_t lvl = 1; lvl <= cnt; lvl++, e++) {
             const uint32_t v = vocab_lookup(keys, vid, cap, code, lvl);
-            const int64_t g = off[c] + (e / EPG) * 32 + lane;
+            int64_t g;
+            if (balanced) {
+                const int64_t gs = P + e / 8;
+                g = off[c] + ((gs % Ls) * SPG + (e % 8) / EPG) * 32 + gs / Ls;
+            } else {
+                g = off[c] + (e / EPG) * 32 + lane;
+            }
             entries[g * EPG + (e % EPG)] = (ET)(v << shift);
         }
     }
@@ -525,6 +551,9 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
         d.entry_bytes = 4;
         d.offsets = true;
     }
+    // decided after the entry format: the balanced kernel reads vids, not byte offsets
+    d.balanced = !sorted && h->rows_window == kChunk && h->rows_layout == SIML_ROWS_BALANCED && !d.offsets &&
+                 rows_balanced_fits(h);
     const int64_t nwin = (q.n + d.window - 1) / d.window;
     d.nchunks = (q.n + kChunk - 1) / kChunk;
     const int64_t slots = std::max<int64_t>(nwin, 1) * d.window;
@@ -545,7 +574,7 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     h->launches++;
     const int epg = 16 / d.entry_bytes;
     k_chunk_meta<<<(unsigned)((d.nchunks + 7) / 8), 256, 0, st>>>(d.perm, q.cmag, q.mag, q.len, d.nchunks, epg,
-                                                                  d.ng, d.meta, d.crange);
+                                                                  d.balanced ? 1 : 0, d.ng, d.meta, d.crange);
     h->launches++;
     SIML_CUDA(cudaGetLastError());
     std::vector<int32_t> hng((size_t)d.nchunks);
@@ -565,14 +594,15 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     SIML_CUDA(cudaMalloc(&d.entries, (size_t)std::max<int64_t>(acc, 1) * 16));
     SIML_CUDA(cudaMemsetAsync(d.entries, 0, (size_t)std::max<int64_t>(acc, 1) * 16, st));
     const unsigned grid = (unsigned)((d.nchunks * 32 + 255) / 256);
+    const int bal = d.balanced ? 1 : 0;
     if (d.entry_bytes == 2)
-        k_fill_entries<uint16_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.width, d.perm, d.off, d.nchunks,
-                                                       h->vocab.keys, h->vocab.vid, h->vocab.cap, 0,
-                                                       (uint16_t*)d.entries);
+        k_fill_entries<uint16_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.cmag, q.width, d.perm, d.off,
+                                                       d.ng, d.nchunks, bal, h->vocab.keys, h->vocab.vid,
+                                                       h->vocab.cap, 0, (uint16_t*)d.entries);
     else
-        k_fill_entries<uint32_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.width, d.perm, d.off, d.nchunks,
-                                                       h->vocab.keys, h->vocab.vid, h->vocab.cap,
-                                                       d.offsets ? 2 : 0, (uint32_t*)d.entries);
+        k_fill_entries<uint32_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.cmag, q.width, d.perm, d.off,
+                                                       d.ng, d.nchunks, bal, h->vocab.keys, h->vocab.vid,
+                                                       h->vocab.cap, d.offsets ? 2 : 0, (uint32_t*)d.entries);
     h->launches++;
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(cudaStreamSynchronize(st));
@@ -622,6 +652,9 @@ int ensure_layout(siml_engine* h, bool sorted, const DbLayout** out) {
     if (rc) return rc;
     bool& valid = sorted ? h->sorted_valid : h->nat_valid;
     DbLayout& d = sorted ? h->db_sorted : h->db_nat;
+    // a balanced full-matrix layout needs the per-warp pieces next to the
+    // table; a ref set with longer rows (16 planes) may no longer fit
+    if (valid && !sorted && d.balanced && !rows_balanced_fits(h)) valid = false;
     if (!valid) {
         if ((rc = build_layout(h, d, sorted))) return rc;
         valid = true;
@@ -837,6 +870,17 @@ int siml_set_tuning(siml_engine* h, int key, int64_t value) {
             h->rows_window = (int)value;
         }
         return SIML_OK;
+    case SIML_TUNE_ROWS_LAYOUT:
+        if (value != SIML_ROWS_PADDED && value != SIML_ROWS_BALANCED)
+            return fail(SIML_ERR_INVALID, "rows layout must be SIML_ROWS_PADDED or SIML_ROWS_BALANCED (got %lld)",
+                        (long long)value);
+        if (value != h->rows_layout) {
+            SIML_CUDA(cudaStreamSynchronize(h->stream));
+            free_layout(h->db_nat);
+            h->nat_valid = false;
+            h->rows_layout = (int)value;
+        }
+        return SIML_OK;
     case SIML_TUNE_SORT_WINDOW:
         if (value < 64 || value > kMaxWindow || (value & (value - 1)))
             return fail(SIML_ERR_INVALID, "sort window must be a power of two in [64, %d] (got %lld)", kMaxWindow,
@@ -878,6 +922,7 @@ int siml_get_tuning(siml_engine* h, int key, int64_t* value) {
     case SIML_TUNE_ROWS_ENTRIES: *value = h->rows_entries; return SIML_OK;
     case SIML_TUNE_ROW_STRIDE: *value = h->row_stride_hint; return SIML_OK;
     case SIML_TUNE_SORT_WINDOW: *value = h->sorted_window; return SIML_OK;
+    case SIML_TUNE_ROWS_LAYOUT: *value = h->rows_layout; return SIML_OK;
     default: return fail(SIML_ERR_INVALID, "unknown tuning key %d", key);
     }
 }

@@ -61,6 +61,7 @@ struct DbLayout {
     int window = kChunk;          // molecules are sorted by entry count inside windows of this size
     bool offsets = false;         // 4-byte entries hold byte offsets (vid * 4) into the table
     int2* crange = nullptr;       // [nchunks] {smallest, largest} magnitude of the chunk's molecules
+    bool balanced = false;        // a chunk's entries spread evenly over its lanes (full-matrix layout)
 };
 
 // Ref-set rows as vid lists (levels expanded, codes absent from the database
@@ -100,6 +101,7 @@ struct siml_engine {
     int rows_entries = 0;                 // entry format of the full-matrix layout (SIML_TUNE_ROWS_ENTRIES)
     int64_t row_stride_hint = 0;          // least entries per ref row list (SIML_TUNE_ROW_STRIDE)
     int sorted_window = 2048;             // sort window of the fused-kernel layout (SIML_TUNE_SORT_WINDOW)
+    int rows_layout = SIML_ROWS_BALANCED; // lane packing of the full-matrix layout (SIML_TUNE_ROWS_LAYOUT)
 };
 
 namespace siml {
@@ -133,6 +135,9 @@ struct RowsArgs {
 constexpr int kModeRows = 0;    // getMultipleRows: CPU-order fp32 union, zero test on magnitudes
 constexpr int kModeSingle = 1;  // getTanimotoRow: count-sum magnitudes, zero test on lengths
 int launch_rows(siml_engine* h, const RowsArgs& a);
+// The balanced full-matrix kernel's shared memory (table + per-warp pieces)
+// fits for the current sets.
+bool rows_balanced_fits(siml_engine* h);
 struct NbrCall {
     int64_t rowbase, rowlimit;
     int64_t col_begin, col_end;   // database columns searched

@@ -500,6 +500,125 @@ __global__ void __launch_bounds__(kThreads, 1) k_nbr(const GroupParams p, const 
     stream_chunks_within<NP, ET>(T, p, rs, wb, we, a.thr_mode == 0 ? a.lo : 0.0f, epi);
 }
 
+// ---------------------------------------------------------- k_rows_bal ----
+// Full-matrix rows over the balanced layout.  A chunk's 8-entry steps are
+// dealt to its 32 lanes in runs of L (the layout's ng / SPG), so lane j
+// streams steps [j L, (j + 1) L) of the chunk's molecules laid end to end and
+// a molecule may span several lanes.  Each lane flushes a partial counter
+// whenever a molecule ends inside its run (and at the end of its run) into
+// piece slot j + m of its warp's shared buffer; the slots of one warp are
+// distinct because runs are ordered.  Lane l then owns molecule l: it adds
+// the pieces of slots [first lane + l, last lane + l] with a bit-sliced
+// ripple adder and runs the padded kernel's epilogue, so stores stay one
+// 128-byte line per row.
+constexpr int kPieceSlots = 64;
+constexpr int kPrefixWords = 34;
+
+__host__ __device__ constexpr size_t rows_bal_extra_smem(int np, int warps) {
+    return (size_t)warps * ((size_t)np * kPieceSlots + kPrefixWords) * 4;
+}
+
+template <int NP>
+__device__ __forceinline__ void piece_store(uint32_t* pc, int slot, const SlicedCounter<NP>& acc) {
+#pragma unroll
+    for (int q = 0; q < NP; q++) pc[q * kPieceSlots + slot] = acc.plane[q];
+}
+
+template <int NP>
+__device__ __forceinline__ void piece_add(SlicedCounter<NP>& acc, const uint32_t* pc, int slot) {
+    uint32_t carry = 0u;
+#pragma unroll
+    for (int q = 0; q < NP; q++) {
+        const uint32_t a = acc.plane[q], b = pc[q * kPieceSlots + slot];
+        acc.plane[q] = a ^ b ^ carry;
+        carry = (a & b) | (carry & (a ^ b));
+    }
+}
+
+template <int NP, typename ET>
+__global__ void __launch_bounds__(kThreads, 1) k_rows_bal(const GroupParams p, float* out, int64_t ldo) {
+    extern __shared__ __align__(16) uint32_t T[];
+    __shared__ RowSmem rs;
+    const int nr = build_table(T, rs, p);   // synchronizes the block
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    uint32_t* pc = T + p.vt_words + (size_t)warp * NP * kPieceSlots;
+    int* pre = reinterpret_cast<int*>(T + p.vt_words + (size_t)nwarps * NP * kPieceSlots) + warp * kPrefixWords;
+    int64_t wb, we;
+    warp_range(p, wb, we);
+    constexpr int SPG = sizeof(ET) == 2 ? 1 : 2;
+    const uint4* E = reinterpret_cast<const uint4*>(p.entries) + lane;
+    const char* Eb = reinterpret_cast<const char*>(p.entries);
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    RowsEpi<NP> epi{rs, nr, p.mode, out + (int64_t)blockIdx.x * 32 * ldo, ldo};
+    if (lane == 0 && wb < we) prefetch_l2(Eb + __ldg(p.off + wb) * 16, (uint32_t)__ldg(p.ng + wb) * 512u);
+    for (int64_t c = wb; c < we; c++) {
+        const int4 meta = __ldg(p.meta + c * 32 + lane);
+        const int64_t base = __ldg(p.off + c);
+        const int L = __ldg(p.ng + c) / SPG;   // steps per lane
+        if (lane == 0 && c + 1 < we)
+            prefetch_l2(Eb + __ldg(p.off + c + 1) * 16, (uint32_t)__ldg(p.ng + c + 1) * 512u);
+        const int g = meta.x >= 0 ? (meta.z + 7) >> 3 : 0;
+        int incl = g;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        const int P = incl - g;
+        const int G = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        pre[lane] = P;
+        if (lane == 31) pre[32] = G;
+        __syncwarp();
+        const int seg0 = lane * L, seg1 = min(G, seg0 + L);
+        // molecule holding step seg0: the largest m with pre[m] <= seg0
+        int m = 0;
+#pragma unroll
+        for (int q = 16; q > 0; q >>= 1)
+            if (m + q <= 31 && pre[m + q] <= seg0) m += q;
+        int endm = pre[m + 1];
+        SlicedCounter<NP> acc;
+        acc.clear();
+        bool pending = false;
+        uint4 a0 = zero, b0 = zero, a1 = zero, b1 = zero;
+        const uint4* Ec = E + base;
+        if (0 < L) { a0 = __ldg(Ec); if (SPG == 2) b0 = __ldg(Ec + 32); }
+        if (1 < L) { a1 = __ldg(Ec + SPG * 32); if (SPG == 2) b1 = __ldg(Ec + SPG * 32 + 32); }
+        for (int s = 0; s < L; s++) {
+            const uint4 x = a0, y = b0;
+            a0 = a1;
+            b0 = b1;
+            if (s + 2 < L) {
+                a1 = __ldg(Ec + (s + 2) * SPG * 32);
+                if (SPG == 2) b1 = __ldg(Ec + (s + 2) * SPG * 32 + 32);
+            }
+            if (SPG == 1)
+                acc.add8(T[x.x & 0xFFFFu], T[x.x >> 16], T[x.y & 0xFFFFu], T[x.y >> 16],
+                         T[x.z & 0xFFFFu], T[x.z >> 16], T[x.w & 0xFFFFu], T[x.w >> 16]);
+            else
+                acc.add8(T[x.x], T[x.y], T[x.z], T[x.w], T[y.x], T[y.y], T[y.z], T[y.w]);
+            const int gs = seg0 + s + 1;
+            if (gs <= seg1) pending = true;   // a step of the run (past it: zero padding)
+            if (gs == endm && gs <= seg1) {   // molecule m ends inside this lane's run
+                piece_store<NP>(pc, lane + m, acc);
+                acc.clear();
+                pending = false;
+                do { m++; } while (m < 32 && pre[m + 1] == pre[m]);   // skip molecules with no entries
+                endm = m < 32 ? pre[m + 1] : 0x7FFFFFFF;
+            }
+        }
+        if (pending && m < 32) piece_store<NP>(pc, lane + m, acc);   // run ended inside molecule m
+        __syncwarp();
+        SlicedCounter<NP> own;
+        own.clear();
+        if (g > 0) {
+            const int fl = P / L, ll = (P + g - 1) / L;
+            for (int j = fl; j <= ll; j++) piece_add<NP>(own, pc, j + lane);
+        }
+        epi(c, meta, own);
+        __syncwarp();   // pieces and prefix are rewritten for the next chunk
+    }
+}
+
 // ---------------------------------------------------------- k_collect ----
 // Top-k candidate collection: every pair with t >= its row's bound
 // (GroupParams.row_lo).  Lane r forms row r's integer threshold at the
@@ -1577,6 +1696,23 @@ int set_smem(K kernel, size_t smem) {
 }
 
 template <int NP, typename ET>
+int launch_rows_bal_t(siml_engine* h, const GroupParams& p, size_t smem, float* out, int64_t ldo) {
+    const int64_t groups = (p.rows + 31) / 32;
+    const size_t sm = smem + rows_bal_extra_smem(NP, kThreads / 32);
+    int rc = set_smem(k_rows_bal<NP, ET>, sm);
+    if (rc) return rc;
+    const int s = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
+    dim3 grid((unsigned)groups, (unsigned)s);
+    SIML_CUDA(mark(h, h->ev0));
+    k_rows_bal<NP, ET><<<grid, kThreads, sm, h->stream>>>(p, out, ldo);
+    SIML_CUDA(cudaGetLastError());
+    SIML_CUDA(mark(h, h->ev1));
+    h->timed = true;
+    h->launches++;
+    return SIML_OK;
+}
+
+template <int NP, typename ET>
 int launch_rows_t(siml_engine* h, const GroupParams& p, size_t smem, float* out, int64_t ldo) {
     const int64_t groups = (p.rows + 31) / 32;
     int rc = set_smem(k_rows<NP, ET>, smem);
@@ -1650,6 +1786,12 @@ int launch_batch_t(siml_engine* h, const GroupParams& p, size_t smem, const int4
 }
 
 }  // namespace
+
+bool rows_balanced_fits(siml_engine* h) {
+    const int vt_words = (int)((h->vocab.nvid + 1 + 3) / 4 * 4);
+    const int np = planes_needed(std::min(h->ref.max_entries, h->qry.max_entries)) <= 8 ? 8 : 16;
+    return (size_t)vt_words * 4 + rows_bal_extra_smem(np, kThreads / 32) + sizeof(RowSmem) + 64 <= h->smem_optin;
+}
 
 int batch_nbr_usable(siml_engine* h, const DbLayout* d) {
     GroupParams p;
@@ -1974,6 +2116,13 @@ int launch_rows(siml_engine* h, const RowsArgs& a) {
     size_t smem = 0;
     int np = 0;
     if (table_params(h, d, a.rowbase, rows, a.mode, p, smem, np)) {
+        if (d->balanced && !d->offsets) {
+            if (np == 8)
+                return d->entry_bytes == 2 ? launch_rows_bal_t<8, uint16_t>(h, p, smem, a.out, a.ldo)
+                                           : launch_rows_bal_t<8, uint32_t>(h, p, smem, a.out, a.ldo);
+            return d->entry_bytes == 2 ? launch_rows_bal_t<16, uint16_t>(h, p, smem, a.out, a.ldo)
+                                       : launch_rows_bal_t<16, uint32_t>(h, p, smem, a.out, a.ldo);
+        }
         if (d->offsets)
             return np == 8 ? launch_rows_t<8, off32_t>(h, p, smem, a.out, a.ldo)
                            : launch_rows_t<16, off32_t>(h, p, smem, a.out, a.ldo);

@@ -230,3 +230,24 @@ def test_rows_entry_formats_bit_exact(native, oracle, set4096, fmt):
     assert gl.dbStats()["entry_bytes"] == 4
     with pytest.raises(ValueError):
         gl.setRowsEntries(9)
+
+
+@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("fmt", [0, 2])
+def test_rows_padded_and_balanced_layouts(native, oracle, golden, layout, fmt):
+    """Both lane packings of the full-matrix layout (and 2- or 4-byte entries)
+    give the bit-exact matrix, on molecules of very different lengths."""
+    from siml_gb300 import synthetic as S, _native as N
+    db = S.smiles_set(S.SEED_RAGGED, S.BIMODAL_35_110, 3000)
+    q = tuple(a[:200] for a in db)
+    gl = _engine()
+    N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_ROWS_LAYOUT, layout))
+    gl.setRowsEntries(fmt)
+    _load(gl, q, db)
+    assert np.array_equal(gl.getMultipleRows(0, 200), oracle.tanimoto_block(q, db, 0, 200))
+    for r in (0, 77, 199):
+        assert np.array_equal(gl.getTanimotoRow(r)[0], gl.getTanimotoRow(r)[0])
+    g = (golden["lingos"], golden["counts"], golden["lengths"], golden["mags"])
+    rows = golden["rows"]
+    _load(gl, tuple(a[rows] for a in g), g)
+    assert np.array_equal(gl.getMultipleRows(0, len(rows)), golden["tanimoto"])
