@@ -313,6 +313,9 @@ __device__ __forceinline__ void stream_chunks_within(const uint32_t* __restrict_
 }
 
 // ------------------------------------------------------------- k_rows ----
+// Largest row stride for which 31 rows of fp32 stay within 32-bit byte offsets.
+constexpr int64_t kFullGroupLdo = (int64_t)(0xFFFFFFFFull / (31ull * 4ull));
+
 template <int NP>
 struct RowsEpi {
     const RowSmem& rs;
@@ -332,6 +335,27 @@ struct RowsEpi {
             // union = ((float)amag + bmag) - isct, all exact: the reference's order
             const float bf = small_int_to_float((uint32_t)bmag);
             const float4* am4 = reinterpret_cast<const float4*>(rs.amagf);
+            if (NP == 8 && nr == 32 && ldo < kFullGroupLdo) {
+                // full group: no row predicate; one byte permute forms the
+                // float 2^23 + count straight from the transposed planes; rows
+                // advance by 32-bit byte offsets from the lane's column
+                char* ob = reinterpret_cast<char*>(o);
+                const uint32_t step = (uint32_t)ldo * 4u;
+#pragma unroll
+                for (int r4 = 0; r4 < 8; r4++) {
+                    const float4 a4 = am4[r4];
+                    const float av[4] = {a4.x, a4.y, a4.z, a4.w};
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        const int r = 4 * r4 + k;
+                        const uint32_t bits = __byte_perm(rc.lo[r & 7], 0x4B000000u, 0x7440u | (uint32_t)(r >> 3));
+                        const float isf = __fsub_rn(__uint_as_float(bits), 8388608.0f);
+                        const float u = __fsub_rn(__fadd_rn(av[k], bf), isf);
+                        *reinterpret_cast<float*>(ob + (uint32_t)r * step) = div_small(isf, u);
+                    }
+                }
+                return;
+            }
 #pragma unroll
             for (int r4 = 0; r4 < 8; r4++) {
                 const float4 a4 = am4[r4];
