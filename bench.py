@@ -315,7 +315,7 @@ def gpu_arm(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     traffic = read_profile_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": {"rows_1m": "k_rows", "nbr_1m": "k_nbr", "topk_1m": "k_topk",
+                "traffic": traffic, "kernel": {"rows_1m": "k_rows_bal", "nbr_1m": "k_nbr", "topk_1m": "k_loghist+k_collect+k_topk_select",
                                                "hist_1m": "k_hist"}[wl], "kernel_ms": kms,
                 "algorithmic_bytes_per_launch": alg_bytes,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback"}
