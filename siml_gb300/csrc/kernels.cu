@@ -312,6 +312,31 @@ __device__ __forceinline__ void stream_chunks_within(const uint32_t* __restrict_
     }
 }
 
+// The CTA's chunk slice [cb, ce) of this launch (blockIdx.y of gridDim.y).
+__device__ __forceinline__ void cta_range(const GroupParams& p, int64_t& cb, int64_t& ce) {
+    const int64_t n = p.chunk_end - p.chunk_begin;
+    cb = p.chunk_begin + n * blockIdx.y / gridDim.y;
+    ce = p.chunk_begin + n * (blockIdx.y + 1) / gridDim.y;
+}
+
+// Warps take the CTA's chunks from a shared counter, kGrab at a time, so a
+// warp slowed by candidates or skipped chunks does not hold the CTA back.
+// `next` starts at the slice's first chunk (set before the table build's
+// barrier).
+constexpr int kGrab = 4;
+template <int NP, typename ET, class Epi>
+__device__ __forceinline__ void stream_dynamic(const uint32_t* __restrict__ T, const GroupParams& p,
+                                               const RowSmem& rs, long long* next, int64_t ce, float lo, Epi& epi) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        long long c0 = 0;
+        if (lane == 0) c0 = atomicAdd(reinterpret_cast<unsigned long long*>(next), (unsigned long long)kGrab);
+        c0 = __shfl_sync(0xFFFFFFFFu, c0, 0);
+        if (c0 >= ce) break;
+        stream_chunks_within<NP, ET>(T, p, rs, c0, c0 + kGrab < ce ? c0 + kGrab : ce, lo, epi);
+    }
+}
+
 // ------------------------------------------------------------- k_rows ----
 // Largest row stride for which 31 rows of fp32 stay within 32-bit byte offsets.
 constexpr int64_t kFullGroupLdo = (int64_t)(0xFFFFFFFFull / (31ull * 4ull));
@@ -516,12 +541,14 @@ template <int NP, typename ET>
 __global__ void __launch_bounds__(kThreads, 1) k_nbr(const GroupParams p, const NbrArgs a) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
+    __shared__ long long next;
     if ((int64_t)blockIdx.x * 32 >= live_rows(p)) return;   // uniform over the CTA
-    const int nr = build_table(T, rs, p);
-    int64_t wb, we;
-    warp_range(p, wb, we);
+    int64_t cb, ce;
+    cta_range(p, cb, ce);
+    if (threadIdx.x == 0) next = cb;
+    const int nr = build_table(T, rs, p);   // synchronizes the block
     NbrEpi<NP> epi{rs, nr, (int64_t)blockIdx.x * 32, a};
-    stream_chunks_within<NP, ET>(T, p, rs, wb, we, a.thr_mode == 0 ? a.lo : 0.0f, epi);
+    stream_dynamic<NP, ET>(T, p, rs, &next, ce, a.thr_mode == 0 ? a.lo : 0.0f, epi);
 }
 
 // ---------------------------------------------------------- k_rows_bal ----
@@ -710,15 +737,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_collect(const GroupParams p, co
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
     __shared__ int scount[32];
+    __shared__ long long next;
     if ((int64_t)blockIdx.x * 32 >= live_rows(p)) return;   // uniform over the CTA
     if (threadIdx.x < 32) scount[threadIdx.x] = 0;
+    int64_t cb, ce;
+    cta_range(p, cb, ce);
+    if (threadIdx.x == 0) next = cb;
     const int nr = build_table(T, rs, p);   // synchronizes the block
-    int64_t wb, we;
-    warp_range(p, wb, we);
     const int64_t row_stride = (int64_t)gridDim.y * c.seg_cap;
     CollectEpi<NP> epi{rs, nr, scount, c.cand_i + blockIdx.y * c.seg_cap, c.cand_t + blockIdx.y * c.seg_cap,
                        row_stride, c.seg_cap};
-    stream_chunks_within<NP, ET>(T, p, rs, wb, we, rs.min_lo, epi);
+    stream_dynamic<NP, ET>(T, p, rs, &next, ce, rs.min_lo, epi);
     __syncthreads();
     if (threadIdx.x < nr) c.seg_counts[(int64_t)rs.orow[threadIdx.x] * gridDim.y + blockIdx.y] = scount[threadIdx.x];
 }
@@ -755,6 +784,17 @@ struct HistEpi {
         const uint32_t top = GLOBAL ? 999u : 100u;
         if (rs.allfast && fast_mag(bmag, meta.z)) {
             const float bf = small_int_to_float((uint32_t)bmag);
+            if (NP == 8 && nr == 32) {   // full group: as the fp32 block epilogue
+#pragma unroll
+                for (int r = 0; r < 32; r++) {
+                    const uint32_t bits = __byte_perm(rc.lo[r & 7], 0x4B000000u, 0x7440u | (uint32_t)(r >> 3));
+                    const float isf = __fsub_rn(__uint_as_float(bits), 8388608.0f);
+                    const float t = div_small(isf, __fsub_rn(__fadd_rn(rs.amagf[r], bf), isf));
+                    const uint32_t b = bin_fast(t, scale, top);
+                    atomicAdd(H + (GLOBAL ? b : r * kBins101 + b), 1u);
+                }
+                return;
+            }
 #pragma unroll
             for (int r = 0; r < 32; r++) {
                 if (r < nr) {
@@ -783,12 +823,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_hist(const GroupParams p, void*
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
     __shared__ uint32_t H[GLOBAL ? kBins1000 : 32 * kBins101];
+    __shared__ long long next;
     for (int i = threadIdx.x; i < (GLOBAL ? kBins1000 : 32 * kBins101); i += blockDim.x) H[i] = 0u;
+    int64_t cb, ce;
+    cta_range(p, cb, ce);
+    if (threadIdx.x == 0) next = cb;
     const int nr = build_table(T, rs, p);   // synchronizes the block
-    int64_t wb, we;
-    warp_range(p, wb, we);
     HistEpi<NP, GLOBAL> epi{rs, nr, H};
-    stream_chunks<NP, ET>(T, p, wb, we, epi);
+    stream_dynamic<NP, ET>(T, p, rs, &next, ce, 0.0f, epi);
     __syncthreads();
     if (GLOBAL) {
         unsigned long long* o = reinterpret_cast<unsigned long long*>(out);
@@ -841,6 +883,17 @@ struct LogHistEpi {
         counts_from_planes<NP>(acc, rc);
         const bool fast = rs.allfast && fast_mag(bmag, meta.z);
         const float bf = small_int_to_float((uint32_t)(bmag > 0 ? bmag : 0));
+        if (NP == 8 && fast && nr == 32) {   // full group: as the fp32 block epilogue
+#pragma unroll
+            for (int r = 0; r < 32; r++) {
+                const uint32_t bits = __byte_perm(rc.lo[r & 7], 0x4B000000u, 0x7440u | (uint32_t)(r >> 3));
+                const float isf = __fsub_rn(__uint_as_float(bits), 8388608.0f);
+                const float t = div_small(isf, __fsub_rn(__fadd_rn(rs.amagf[r], bf), isf));
+                const int b = log_bin(t);
+                atomicAdd(H + r * kLogWords + (b >> 1), 1u << ((b & 1) * 16));
+            }
+            return;
+        }
 #pragma unroll
         for (int r = 0; r < 32; r++) {
             if (r < nr) {
@@ -864,12 +917,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_loghist(const GroupParams p, in
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
     __shared__ uint32_t H[32 * kLogWords];
+    __shared__ long long next;
     for (int i = threadIdx.x; i < 32 * kLogWords; i += blockDim.x) H[i] = 0u;
+    int64_t cb, ce;
+    cta_range(p, cb, ce);
+    if (threadIdx.x == 0) next = cb;
     const int nr = build_table(T, rs, p);   // synchronizes the block
-    int64_t wb, we;
-    warp_range(p, wb, we);
     LogHistEpi<NP> epi{rs, nr, H};
-    stream_chunks<NP, ET>(T, p, wb, we, epi);
+    stream_dynamic<NP, ET>(T, p, rs, &next, ce, 0.0f, epi);
     __syncthreads();
     for (int i = threadIdx.x; i < nr * kLogBins; i += blockDim.x) {
         const int r = i / kLogBins, b = i - r * kLogBins;
