@@ -1439,11 +1439,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_batch_nbr(const GroupParams p, 
     __shared__ long long s_item;
     __shared__ long long cur_pos, cur_bias;
     __shared__ int cur_nr;
+    __shared__ long long next;
     for (int i = threadIdx.x * 4; i < p.vt_words; i += blockDim.x * 4)
         *reinterpret_cast<uint4*>(T + i) = make_uint4(0u, 0u, 0u, 0u);
     if (threadIdx.x == 0) { cur_pos = -1; cur_bias = 0; cur_nr = 0; }
     for (;;) {
-        if (threadIdx.x == 0) s_item = (long long)atomicAdd(head, 1u);
+        if (threadIdx.x == 0) {
+            s_item = (long long)atomicAdd(head, 1u);
+            if (s_item < nitems) next = items[2 * s_item + 1].y;   // the item's first chunk
+        }
         __syncthreads();
         const long long w = s_item;
         if (w >= nitems) break;
@@ -1460,11 +1464,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_batch_nbr(const GroupParams p, 
         NbrArgs ai = a;
         ai.col_begin = ia.w;
         ai.col_end = ib.x;
-        const int64_t c0 = ib.y, c1 = ib.z;
-        int64_t wb, we;
-        warp_split(p.off, c0, c1, wb, we);
         NbrEpi<NP> epi{rs, nr, 0, ai};
-        stream_chunks_within<NP, ET>(T, p, rs, wb, we, ai.thr_mode == 0 ? ai.lo : 0.0f, epi);
+        stream_dynamic<NP, ET>(T, p, rs, &next, ib.z, ai.thr_mode == 0 ? ai.lo : 0.0f, epi);
         __syncthreads();
     }
 }
