@@ -664,7 +664,8 @@ def serving_arm(args):
     gl = GPULingo(local, stream=torch.cuda.Stream(device=dev))
     t = time.time()
     gl.set_qsmiles(*db)
-    cfg = ServerConfig(max_rows=args.serving_max_rows, width=128, kmax=64, pitch=256, lo=0.75)
+    cfg = ServerConfig(max_rows=args.serving_max_rows, soft_rows=args.serving_soft_rows, width=128, kmax=64,
+                       pitch=256, lo=0.75)
     srv = LingoServer(gl, cfg)
     # warm the layout, row lists and kernels with one small batch of each kind
     warm = S.smiles_list(S.SEED_SERVING, S.UNIFORM_20_90, 64, first=SERVING_DB_N)
@@ -856,8 +857,10 @@ def main():
     ap.add_argument("--ragged-jobs", type=int, default=RAGGED_JOBS, help="jobs of the ragged_2m workload")
     ap.add_argument("--serving-rates", default="200,500,1000",
                     help="serving_10m: request rates (req/s), each run for warmup + steps seconds")
-    ap.add_argument("--serving-max-rows", type=int, default=512,
-                    help="serving_10m: query rows per batch (one slot region)")
+    ap.add_argument("--serving-max-rows", type=int, default=1024,
+                    help="serving_10m: most query rows per batch (one slot region), used under a backlog")
+    ap.add_argument("--serving-soft-rows", type=int, default=512,
+                    help="serving_10m: query rows per batch while the queue is short")
     ap.add_argument("--rows-window", type=int, default=0,
                     help="sort window of the full-matrix layout (32, 64, 128, 256; 0: library default)")
     ap.add_argument("--rows-entries", type=int, default=-1,

@@ -113,13 +113,19 @@ class _Region:
 
 
 class ServerConfig:
-    """max_rows: query rows per batch (one slot region); width: LINGO columns
-    per query row; kmax: largest k a top-k request may ask; pitch: hits per
-    row a threshold batch keeps before an overflowing row is re-run alone;
-    hit_budget: device bytes of hit buffers one batch may claim."""
+    """max_rows: query rows a batch may hold (one slot region); soft_rows: the
+    batch size while the queue is short (smaller batches, shorter waits);
+    backlog_rows: queued rows past which batches grow to max_rows for
+    throughput; width: LINGO columns per query row; kmax: largest k a top-k
+    request may ask; pitch: hits per row a threshold batch keeps before an
+    overflowing row is re-run alone; hit_budget: device bytes of hit buffers
+    one batch may claim."""
 
-    def __init__(self, max_rows=1024, width=256, kmax=64, pitch=256, hit_budget=None, lo=0.75):
+    def __init__(self, max_rows=1024, width=256, kmax=64, pitch=256, hit_budget=None, lo=0.75, soft_rows=None,
+                 backlog_rows=None):
         self.max_rows = int(max_rows)
+        self.soft_rows = int(soft_rows) if soft_rows else self.max_rows
+        self.backlog_rows = int(backlog_rows) if backlog_rows else 2 * self.max_rows
         self.width = int(width)
         self.kmax = int(kmax)
         self.pitch = int(pitch)
@@ -204,10 +210,12 @@ class LingoServer:
             if self.stop_flag and not self.queue:
                 return None
             batch, rows, hits = [], 0, 0
+            queued = sum(r.rows for r in self.queue)
+            limit = cfg.max_rows if queued > cfg.backlog_rows else cfg.soft_rows
             while self.queue:
                 r = self.queue[0]
                 need = _hit_bytes(r, cfg)
-                if batch and (rows + r.rows > cfg.max_rows or hits + need > cfg.hit_budget):
+                if batch and (rows + r.rows > limit or hits + need > cfg.hit_budget):
                     break
                 self.queue.popleft()
                 batch.append(r)

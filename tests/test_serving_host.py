@@ -57,3 +57,16 @@ def test_request_validation():
         Request(0, [b"CC"], kind="nearest")
     r = Request(1, ["CCO", b"CCN"], kind="threshold")
     assert r.rows == 2 and r.smiles == [b"CCO", b"CCN"]
+
+
+def test_batches_grow_under_a_backlog():
+    from siml_gb300.serving import ServerConfig
+    srv = _fake_server(max_rows=16, pitch=16, kmax=8, hit_budget=1 << 20)
+    srv.cfg = ServerConfig(max_rows=16, soft_rows=8, backlog_rows=20, width=64, kmax=8, pitch=16,
+                           hit_budget=1 << 20)
+    for i in range(3):
+        srv.queue.append(_req(i, 5))
+    assert [r.rid for r in srv._take_batch()] == [0]        # 15 queued rows: soft limit 8
+    for i in range(3, 8):
+        srv.queue.append(_req(i, 5))
+    assert [r.rid for r in srv._take_batch()] == [1, 2, 3]  # 35 queued rows > 20: up to 16
