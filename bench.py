@@ -684,6 +684,7 @@ def serving_arm(args):
         sched = serving_requests(rate, args.warmup + args.steps, first, S.SEED_SERVING + ri)
         first += sum(len(x[2]) for x in sched)
         # batched: open-loop arrivals into the running server
+        srv.gpu_ms, srv.launch_s, srv.deliver_s = 0.0, 0.0, 0.0
         srv.start()
         t0 = time.perf_counter() + 0.2
         reqs = run_arrivals(srv.submit, sched, t0)
@@ -693,6 +694,10 @@ def serving_arm(args):
         timed = [r for r in reqs if r.arrival - t0 >= args.warmup]
         b = serving_stats(timed, nq)
         b["batches"] = srv.batches
+        span_all = max(r.t_done for r in reqs) - min(r.arrival for r in reqs)
+        b["gpu_busy_frac"] = srv.gpu_ms / 1e3 / span_all
+        b["host_launch_frac"] = srv.launch_s / span_all
+        b["host_deliver_frac"] = srv.deliver_s / span_all
         # unbatched: the same arrivals served one request at a time, in order
         pend = []
         t0u = time.perf_counter() + 0.2
@@ -735,6 +740,7 @@ def serving_arm(args):
     clk = clocks.stop()
     # saturated capacity: every request of the first schedule submitted at once
     sched = serving_requests(rates[0], args.warmup + args.steps, SERVING_DB_N + 64, S.SEED_SERVING)
+    srv.gpu_ms, srv.launch_s, srv.deliver_s = 0.0, 0.0, 0.0
     srv.start()
     tb = time.perf_counter()
     burst = [Request(i, smi, kind=kind, k=50, lo=0.75, arrival=tb) for i, (_, kind, smi) in enumerate(sched)]
@@ -744,6 +750,9 @@ def serving_arm(args):
         r.done.wait()
     srv.stop()
     cap = serving_stats(burst, nq)
+    cap["gpu_busy_frac"] = srv.gpu_ms / 1e3 / cap["span_s"]
+    cap["host_launch_frac"] = srv.launch_s / cap["span_s"]
+    cap["host_deliver_frac"] = srv.deliver_s / cap["span_s"]
     # the per-request path on the same burst, one request after another
     tu = time.perf_counter()
     uburst = [Request(i, smi, kind=kind, k=50, lo=0.75, arrival=tu) for i, (_, kind, smi) in enumerate(sched)]

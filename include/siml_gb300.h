@@ -126,6 +126,13 @@ int siml_hist101(siml_engine* h, int64_t rowbase, int64_t rowlimit,
  * idx: int32 [rows, k], sims: fp32 [rows, k]. */
 int siml_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int64_t k,
               int32_t* idx, float* sims, int where);
+/* With SIML_DEVICE outputs siml_topk only queues work.  Its kernels' bounded
+ * lock waits (k > 256, or rows whose candidates overflow twice) record an
+ * expiry in a host-mapped word, which siml_sync reports as SIML_ERR_TIMEOUT.
+ * siml_async_status reports it without a stream synchronization, so the
+ * caller must know the work is done (an event it waited on); both clear the
+ * word. */
+int siml_async_status(siml_engine* h);
 /* siml_topk without any device allocation (no counterpart in the reference).
  * For callers that cannot allocate device memory on the request path (a
  * caller-owned memory pool, a strict memory budget, a service that must not

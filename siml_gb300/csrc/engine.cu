@@ -665,6 +665,20 @@ int ensure_layout(siml_engine* h, bool sorted, const DbLayout** out) {
 
 }  // namespace siml
 
+namespace siml {
+
+int take_async_error(siml_engine* h) {
+    volatile int* w = h->h_async_err;
+    if (w && *w) {
+        *w = 0;
+        return fail(SIML_ERR_TIMEOUT, "a top-k heap lock wait exceeded its bound in a queued call; that call's "
+                    "result is invalid");
+    }
+    return SIML_OK;
+}
+
+}  // namespace siml
+
 using namespace siml;
 
 #define SIML_GUARD(h)                                                   \
@@ -698,6 +712,9 @@ int siml_create(int device, siml_engine** out) {
     h->stream = h->own_stream;
     SIML_CUDA(cudaMalloc(&h->d_err, sizeof(int)));
     SIML_CUDA(cudaMalloc(&h->d_counter, 4 * sizeof(unsigned long long)));
+    SIML_CUDA(cudaHostAlloc((void**)&h->h_async_err, sizeof(int), cudaHostAllocMapped));
+    *h->h_async_err = 0;
+    SIML_CUDA(cudaHostGetDevicePointer((void**)&h->d_async_err, h->h_async_err, 0));
     SIML_CUDA(cudaEventCreate(&h->ev0));
     SIML_CUDA(cudaEventCreate(&h->ev1));
     *out = h;
@@ -718,6 +735,7 @@ int siml_destroy(siml_engine* h) {
     for (int i = 0; i < 4; i++)
         if (h->scratch[i]) cudaFree(h->scratch[i]);
     if (h->d_err) cudaFree(h->d_err);
+    if (h->h_async_err) cudaFreeHost(h->h_async_err);
     if (h->d_counter) cudaFree(h->d_counter);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
@@ -735,7 +753,12 @@ int siml_set_stream(siml_engine* h, void* stream) {
 int siml_sync(siml_engine* h) {
     SIML_GUARD(h);
     SIML_CUDA(cudaStreamSynchronize(h->stream));
-    return SIML_OK;
+    return take_async_error(h);
+}
+
+int siml_async_status(siml_engine* h) {
+    SIML_GUARD(h);
+    return take_async_error(h);
 }
 
 int siml_query_done(siml_engine* h, int* done) {
@@ -1097,19 +1120,16 @@ int siml_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int64_t k, int3
         ds = (float*)((char*)own + ob);
     }
     rc = launch_topk(h, rowbase, rowlimit, (int)k, di, ds);
-    int err = 0;
-    if (!rc) {
-        SIML_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-        if (where != SIML_DEVICE) {
-            SIML_CUDA(cudaMemcpyAsync(idx, di, ob, cudaMemcpyDefault, h->stream));
-            SIML_CUDA(cudaMemcpyAsync(sims, ds, ob, cudaMemcpyDefault, h->stream));
-        }
+    if (!rc && where != SIML_DEVICE) {
+        SIML_CUDA(cudaMemcpyAsync(idx, di, ob, cudaMemcpyDefault, h->stream));
+        SIML_CUDA(cudaMemcpyAsync(sims, ds, ob, cudaMemcpyDefault, h->stream));
         SIML_CUDA(cudaStreamSynchronize(h->stream));
     }
     if (own) cudaFreeAsync(own, h->stream);
     if (rc) return rc;
-    if (err) return fail(SIML_ERR_TIMEOUT, "siml_topk: a heap lock wait exceeded its bound; result discarded");
-    return SIML_OK;
+    // device outputs: queued only; a bounded lock wait that expired is
+    // reported by the next siml_sync / siml_async_status
+    return where == SIML_DEVICE ? SIML_OK : take_async_error(h);
 }
 
 int siml_row_single(siml_engine* h, int64_t row, float* out, int where) {

@@ -90,7 +90,12 @@ struct siml_engine {
     // device scratch reused across calls, one buffer per purpose (siml::kSlot*)
     void* scratch[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t scratch_bytes[4] = {0, 0, 0, 0};
-    int* d_err = nullptr;                 // device error word
+    int* d_err = nullptr;                 // device error word (calls that wait for their kernels)
+    // error word of kernels whose callers do not wait (top-k's bounded lock
+    // waits): host-mapped, so a waiting caller reads it with no copy; sticky
+    // until reported by siml_sync / siml_async_status or a waiting top-k call
+    int* h_async_err = nullptr;
+    int* d_async_err = nullptr;
     unsigned long long* d_counter = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed = false;
@@ -124,6 +129,9 @@ int row_order_by_magnitude(siml_engine* h, int64_t rowbase, int64_t rowlimit, co
 constexpr int kOrderBuckets = 4096;
 int row_order_into(siml_engine* h, int64_t rowbase, int64_t rowlimit, int32_t* order, int32_t* bucket);
 int cuda_fail(cudaError_t e, const char* what);
+// Reports (and clears) an expired top-k lock wait recorded by queued kernels;
+// call only once their work is known to be complete.
+int take_async_error(siml_engine* h);
 
 // kernels.cu — launchers; all queue work on h->stream and return a status.
 struct RowsArgs {

@@ -1847,7 +1847,7 @@ int launch_topk_t(siml_engine* h, const GroupParams& p, size_t smem, int k, int 
     if (rc) return rc;
     dim3 grid((unsigned)groups, (unsigned)splits);
     SIML_CUDA(mark(h, h->ev0));
-    k_topk<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, k, pt, pi, h->d_err);
+    k_topk<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, k, pt, pi, h->d_async_err);
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
@@ -1939,7 +1939,6 @@ int launch_topk_core(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t
                      float* sims) {
     const int64_t rows = rowlimit - rowbase;
     int rc;
-    SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
     if (plan.splits > 0) {
         GroupParams p;
         size_t smem = 0;
@@ -1963,7 +1962,7 @@ int launch_topk_core(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t
     const size_t sm = (size_t)k * 8;
     if ((rc = set_smem(k_topk_rowscan, sm))) return rc;
     SIML_CUDA(mark(h, h->ev0));
-    k_topk_rowscan<<<(unsigned)rows, 256, sm, h->stream>>>(raw_args(h, rowbase), k, idx, sims, h->d_err, nullptr,
+    k_topk_rowscan<<<(unsigned)rows, 256, sm, h->stream>>>(raw_args(h, rowbase), k, idx, sims, h->d_async_err, nullptr,
                                                            nullptr);
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(mark(h, h->ev1));
@@ -2082,7 +2081,7 @@ int topk_collect_block(siml_engine* h, const DbLayout* d, int64_t r0, int64_t ro
     SIML_CUDA(cudaGetLastError());
     // rows that overflowed twice: exact scan
     if ((rc = set_smem(k_topk_rowscan, (size_t)k * 8))) return rc;
-    k_topk_rowscan<<<(unsigned)rows, 256, (size_t)k * 8, h->stream>>>(raw_args(h, r0), k, idx, sims, h->d_err,
+    k_topk_rowscan<<<(unsigned)rows, 256, (size_t)k * 8, h->stream>>>(raw_args(h, r0), k, idx, sims, h->d_async_err,
                                                                      list_b, list_n + 1);
     SIML_CUDA(cudaGetLastError());
     h->launches += 4;
@@ -2103,7 +2102,6 @@ int launch_topk(siml_engine* h, int64_t rowbase, int64_t rowlimit, int k, int32_
         size_t smem = 0;
         int np = 0;
         table_params(h, d, rowbase, 1, kModeRows, p, smem, np);
-        SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
         TimingHold hold(h);
         SIML_CUDA(cudaEventRecord(h->ev0, h->stream));
         for (int64_t r0 = rowbase; r0 < rowlimit; r0 += kTopkBlockRows) {

@@ -94,9 +94,6 @@ extern "C" int siml_topk_noalloc(siml_engine* h, int64_t rowbase, int64_t rowlim
     int* pi = reinterpret_cast<int*>(pt + plan.partial_entries);
     if (plan.splits > 0 && (rc = row_order_into(h, rowbase, rowlimit, order, bucket))) return rc;
     if ((rc = launch_topk_core(h, d, rowbase, rowlimit, (int)k, plan, order, pt, pi, idx, sims))) return rc;
-    int err = 0;
-    SIML_CUDA(cudaMemcpyAsync(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     SIML_CUDA(cudaStreamSynchronize(h->stream));
-    if (err) return fail(SIML_ERR_TIMEOUT, "siml_topk_noalloc: a heap lock wait exceeded its bound; result discarded");
-    return SIML_OK;
+    return take_async_error(h);
 }

@@ -125,7 +125,7 @@ class ServerConfig:
                  backlog_rows=None):
         self.max_rows = int(max_rows)
         self.soft_rows = int(soft_rows) if soft_rows else self.max_rows
-        self.backlog_rows = int(backlog_rows) if backlog_rows else 2 * self.max_rows
+        self.backlog_rows = int(backlog_rows) if backlog_rows else 8 * self.max_rows
         self.width = int(width)
         self.kmax = int(kmax)
         self.pitch = int(pitch)
@@ -163,6 +163,9 @@ class LingoServer:
         self.batches = 0
         self.pairs = 0
         self.batch_rows = []
+        self.gpu_ms = 0.0       # device time of the batches (write, search, copy back)
+        self.launch_s = 0.0     # host time compiling, writing and queueing batches
+        self.deliver_s = 0.0    # host time handing results to requests
         self.threads = []
 
     # ------------------------------------------------------------- control
@@ -233,7 +236,9 @@ class LingoServer:
                 return
             region.free.clear()
             try:
+                t = time.perf_counter()
                 item = self._launch(batch, region)
+                self.launch_s += time.perf_counter() - t
             except Exception as e:  # report the failure on every request of the batch
                 for r in batch:
                     r.error = e
@@ -274,6 +279,8 @@ class LingoServer:
                                         mg.ctypes.data, n, cfg.width, cfg.width), "siml_write_ref_rows")
         st = gl.stream
         b = region.base
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev0.record(st)
         if nt:
             N.check(lib.siml_neighbors(gl._h, b, b + nt, ctypes.c_float(cfg.lo), ctypes.c_float(1.1), cfg.pitch,
                                        region.n_idx.data_ptr(), region.n_sims.data_ptr(), region.n_cnt.data_ptr(),
@@ -292,12 +299,12 @@ class LingoServer:
                 m = nk * kmax
                 region.o_kidx.view(-1)[:m].copy_(region.k_idx.view(-1)[:m], non_blocking=True)
                 region.o_ksims.view(-1)[:m].copy_(region.k_sims.view(-1)[:m], non_blocking=True)
-            ev = torch.cuda.Event()
+            ev = torch.cuda.Event(enable_timing=True)
             ev.record(st)
         self.batches += 1
         self.pairs += n * gl.nquery
         self.batch_rows.append(n)
-        return (batch, thr, tk, nt, nk, kmax, region, ev)
+        return (batch, thr, tk, nt, nk, kmax, region, (ev0, ev))
 
     # ----------------------------------------------------------- completer
     def _completer(self):
@@ -308,10 +315,15 @@ class LingoServer:
                 if not self.inflight:
                     return
                 item = self.inflight.popleft()
-            batch, thr, tk, nt, nk, kmax, region, ev = item
+            batch, thr, tk, nt, nk, kmax, region, (ev0, ev) = item
             try:
                 ev.synchronize()
+                with self.elock:   # a bounded top-k wait that expired in this batch
+                    N.check(N.lib().siml_async_status(self.gl._h), "siml_async_status")
+                self.gpu_ms += ev0.elapsed_time(ev)
+                t = time.perf_counter()
                 self._deliver(thr, tk, nt, nk, kmax, region)
+                self.deliver_s += time.perf_counter() - t
             except Exception as e:
                 for r in batch:
                     r.error = e
@@ -325,22 +337,25 @@ class LingoServer:
         cfg = self.cfg
         cnt = region.o_ncnt.numpy()
         nidx, nsims = region.o_nidx.numpy(), region.o_nsims.numpy()
+        # one block copy per request out of the region's pinned buffers (they
+        # are reused by a later batch); rows are views into it
         row = 0
         for r in thr:
+            c = cnt[row:row + r.rows]
+            w = int(min(int(c.max()), cfg.pitch)) if r.rows else 0
+            bi, bs = nidx[row:row + r.rows, :w].copy(), nsims[row:row + r.rows, :w].copy()
             res = []
             for q in range(r.rows):
-                c = int(cnt[row + q])
-                if c > cfg.pitch:
-                    res.append(self._rerun_row(region.base + row + q, c))
-                else:
-                    res.append((nidx[row + q, :c].copy(), nsims[row + q, :c].copy()))
+                cq = int(c[q])
+                res.append(self._rerun_row(region.base + row + q, cq) if cq > cfg.pitch else (bi[q, :cq], bs[q, :cq]))
             r.result = res
             row += r.rows
         kid = region.o_kidx.numpy().reshape(-1)[:nk * kmax].reshape(nk, kmax) if nk else None
         ksm = region.o_ksims.numpy().reshape(-1)[:nk * kmax].reshape(nk, kmax) if nk else None
         row = 0
         for r in tk:
-            r.result = [(kid[row + q, :r.k].copy(), ksm[row + q, :r.k].copy()) for q in range(r.rows)]
+            bi, bs = kid[row:row + r.rows, :r.k].copy(), ksm[row:row + r.rows, :r.k].copy()
+            r.result = list(zip(bi, bs))
             row += r.rows
 
     def _rerun_row(self, ref_row, count):
@@ -367,8 +382,9 @@ def serve_unbatched(server, req):
     thr = [req] if req.kind == THRESHOLD else []
     tk = [req] if req.kind == TOPK else []
     batch = server._launch([req], region)
-    _, _, _, nt, nk, kmax, _, ev = batch
+    _, _, _, nt, nk, kmax, _, (_, ev) = batch
     ev.synchronize()
+    N.check(N.lib().siml_async_status(server.gl._h), "siml_async_status")
     server._deliver(thr, tk, nt, nk, kmax, region)
     req.t_done = time.perf_counter()
     req.done.set()
