@@ -198,6 +198,15 @@ class GPULingo:
             self._enter()
             N.check(N.lib().siml_rows(self._h, int(rowbase), int(rowlimit), out.data_ptr(), max(nq, 1),
                                       N.SIML_DEVICE), "getMultipleRows")
+            # the block comes back into pinned host memory (reused by torch's
+            # host allocator), queued behind the kernel on the engine's stream
+            host = torch.empty((rows, max(nq, 1)), dtype=torch.float32, pin_memory=True)
+            with torch.cuda.stream(self._stream):
+                host.copy_(out, non_blocking=True)
+            out.record_stream(self._stream)
+            self.last_async_width = nq
+            self._pending = ("matrix", host, nq, out)
+            return
         else:
             out = np.empty((rows, max(nq, 1)), dtype=np.float32)
             N.check(N.lib().siml_rows(self._h, int(rowbase), int(rowlimit), out.ctypes.data, max(nq, 1),
@@ -405,8 +414,11 @@ class GPULingo:
         self._pending = None
         N.check(N.lib().siml_sync(self._h), "siml_sync")
         if kind == "matrix":
-            out, width = payload
-            host = out.cpu().numpy() if torch is not None and isinstance(out, torch.Tensor) else out
+            out, width = payload[0], payload[1]
+            if torch is not None and isinstance(out, torch.Tensor):
+                host = (out.cpu() if out.is_cuda else out).numpy()
+            else:
+                host = out
             return host[:, :width]
         if kind == "neighbors":
             idx, sims, cnt, pitch, rows = payload
