@@ -271,6 +271,11 @@ int siml_db_stats(siml_engine* h, int64_t out[8]);
 #define SIML_ROWS_BALANCED 1
 int siml_set_tuning(siml_engine* h, int key, int64_t value);
 int siml_get_tuning(siml_engine* h, int key, int64_t* value);
+/* Pairs the threshold kernels (neighbours, batched jobs, top-k collection,
+ * histograms) actually evaluated: 32 x group rows per streamed chunk, i.e.
+ * without the chunks skipped by the magnitude bound.  Waits for the engine's
+ * stream; reset != 0 zeroes the counter afterwards. */
+int siml_eval_pairs(siml_engine* h, uint64_t* out, int reset);
 /* Number of kernel launches this engine has issued since creation. */
 int64_t siml_launch_count(siml_engine* h);
 /* Average device time (ms) of the dominant kernel of the last call on this

@@ -468,6 +468,13 @@ class GPULingo:
         N.check(N.lib().siml_get_tuning(self._h, N.SIML_TUNE_ROWS_WINDOW, ctypes.byref(v)), "rowsWindow")
         return int(v.value)
 
+    def evaluatedPairs(self, reset=False):
+        """Pairs the threshold kernels evaluated since the last reset (chunks
+        skipped by the magnitude bound excluded)."""
+        v = ctypes.c_uint64()
+        N.check(N.lib().siml_eval_pairs(self._h, ctypes.byref(v), 1 if reset else 0), "siml_eval_pairs")
+        return int(v.value)
+
     def launchCount(self):
         """Kernel launches issued by this object so far."""
         return int(N.lib().siml_launch_count(self._h))

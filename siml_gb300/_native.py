@@ -73,6 +73,7 @@ _SIGNATURES = {
     "siml_hist101": (_I32, [_P, _I64, _I64, _P, _I64, _I32]),
     "siml_topk": (_I32, [_P, _I64, _I64, _I64, _P, _P, _I32]),
     "siml_async_status": (_I32, [_P]),
+    "siml_eval_pairs": (_I32, [_P, ctypes.POINTER(ctypes.c_uint64), _I32]),
     "siml_hist_global": (_I32, [_P, _I64, _I64, _P, _I32]),
     "siml_topk_noalloc": (_I32, [_P, _I64, _I64, _I64, _P, _P]),
     "siml_neighbors_range": (_I32, [_P, _I64, _I64, _I64, _I64, _F32, _F32, _I64, _P, _P, _P, _I32]),

@@ -712,6 +712,8 @@ int siml_create(int device, siml_engine** out) {
     h->stream = h->own_stream;
     SIML_CUDA(cudaMalloc(&h->d_err, sizeof(int)));
     SIML_CUDA(cudaMalloc(&h->d_counter, 4 * sizeof(unsigned long long)));
+    SIML_CUDA(cudaMalloc(&h->d_eval, sizeof(unsigned long long)));
+    SIML_CUDA(cudaMemset(h->d_eval, 0, sizeof(unsigned long long)));
     SIML_CUDA(cudaHostAlloc((void**)&h->h_async_err, sizeof(int), cudaHostAllocMapped));
     *h->h_async_err = 0;
     SIML_CUDA(cudaHostGetDevicePointer((void**)&h->d_async_err, h->h_async_err, 0));
@@ -736,6 +738,7 @@ int siml_destroy(siml_engine* h) {
         if (h->scratch[i]) cudaFree(h->scratch[i]);
     if (h->d_err) cudaFree(h->d_err);
     if (h->h_async_err) cudaFreeHost(h->h_async_err);
+    if (h->d_eval) cudaFree(h->d_eval);
     if (h->d_counter) cudaFree(h->d_counter);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
@@ -759,6 +762,17 @@ int siml_sync(siml_engine* h) {
 int siml_async_status(siml_engine* h) {
     SIML_GUARD(h);
     return take_async_error(h);
+}
+
+int siml_eval_pairs(siml_engine* h, uint64_t* out, int reset) {
+    SIML_GUARD(h);
+    if (!out) return fail(SIML_ERR_INVALID, "siml_eval_pairs: NULL output");
+    unsigned long long v = 0;
+    SIML_CUDA(cudaMemcpyAsync(&v, h->d_eval, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+    if (reset) SIML_CUDA(cudaMemsetAsync(h->d_eval, 0, sizeof(v), h->stream));
+    SIML_CUDA(cudaStreamSynchronize(h->stream));
+    *out = (uint64_t)v;
+    return SIML_OK;
 }
 
 int siml_query_done(siml_engine* h, int* done) {

@@ -96,6 +96,7 @@ struct siml_engine {
     // until reported by siml_sync / siml_async_status or a waiting top-k call
     int* h_async_err = nullptr;
     int* d_async_err = nullptr;
+    unsigned long long* d_eval = nullptr;  // pairs the threshold kernels evaluated (chunks not skipped)
     unsigned long long* d_counter = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed = false;

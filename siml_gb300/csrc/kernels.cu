@@ -77,6 +77,7 @@ struct GroupParams {
     const float* row_lo;      // per output row lower bound (per-row threshold search) or null
     const int* rows_dev;      // device row count bounding `rows` (row lists built on the device) or null
     const int2* crange;       // per chunk {smallest, largest} magnitude (the layout's), for chunk skipping
+    unsigned long long* eval; // counts the pairs of streamed (not skipped) chunks, or null
 };
 
 struct RowSmem {
@@ -293,23 +294,26 @@ __device__ __forceinline__ bool chunk_out_of_reach(int2 r, int amin, int amax, f
 // stream_chunks over the chunks of [wb, we) that can hold a pair with
 // t >= lo for some row of the group (lo <= 0 or NaN: every chunk).  Chunks
 // are tested warp-uniformly; runs of reachable chunks are streamed whole.
+// Returns the number of chunks streamed.
 template <int NP, typename ET, class Epi>
-__device__ __forceinline__ void stream_chunks_within(const uint32_t* __restrict__ T, const GroupParams& p,
-                                                     const RowSmem& rs, int64_t wb, int64_t we, float lo,
-                                                     Epi& epi) {
+__device__ __forceinline__ int64_t stream_chunks_within(const uint32_t* __restrict__ T, const GroupParams& p,
+                                                        const RowSmem& rs, int64_t wb, int64_t we, float lo,
+                                                        Epi& epi) {
     if (!(lo > 0.0f) || p.crange == nullptr || rs.max_amag < 0) {
         stream_chunks<NP, ET>(T, p, wb, we, epi);
-        return;
+        return we > wb ? we - wb : 0;
     }
     const int amin = rs.min_amag, amax = rs.max_amag;
-    int64_t c = wb;
+    int64_t c = wb, streamed = 0;
     while (c < we) {
         while (c < we && chunk_out_of_reach(p.crange[c], amin, amax, lo)) c++;
         int64_t e = c;
         while (e < we && !chunk_out_of_reach(p.crange[e], amin, amax, lo)) e++;
         if (e > c) stream_chunks<NP, ET>(T, p, c, e, epi);
+        streamed += e - c;
         c = e;
     }
+    return streamed;
 }
 
 // The CTA's chunk slice [cb, ce) of this launch (blockIdx.y of gridDim.y).
@@ -326,15 +330,19 @@ __device__ __forceinline__ void cta_range(const GroupParams& p, int64_t& cb, int
 constexpr int kGrab = 4;
 template <int NP, typename ET, class Epi>
 __device__ __forceinline__ void stream_dynamic(const uint32_t* __restrict__ T, const GroupParams& p,
-                                               const RowSmem& rs, long long* next, int64_t ce, float lo, Epi& epi) {
+                                               const RowSmem& rs, long long* next, int64_t ce, float lo, int nr,
+                                               Epi& epi) {
     const int lane = threadIdx.x & 31;
+    int64_t streamed = 0;
     for (;;) {
         long long c0 = 0;
         if (lane == 0) c0 = atomicAdd(reinterpret_cast<unsigned long long*>(next), (unsigned long long)kGrab);
         c0 = __shfl_sync(0xFFFFFFFFu, c0, 0);
         if (c0 >= ce) break;
-        stream_chunks_within<NP, ET>(T, p, rs, c0, c0 + kGrab < ce ? c0 + kGrab : ce, lo, epi);
+        streamed += stream_chunks_within<NP, ET>(T, p, rs, c0, c0 + kGrab < ce ? c0 + kGrab : ce, lo, epi);
     }
+    if (p.eval && lane == 0 && streamed > 0)
+        atomicAdd(p.eval, (unsigned long long)streamed * 32ull * (unsigned long long)(nr > 0 ? nr : 0));
 }
 
 // ------------------------------------------------------------- k_rows ----
@@ -548,7 +556,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_nbr(const GroupParams p, const 
     if (threadIdx.x == 0) next = cb;
     const int nr = build_table(T, rs, p);   // synchronizes the block
     NbrEpi<NP> epi{rs, nr, (int64_t)blockIdx.x * 32, a};
-    stream_dynamic<NP, ET>(T, p, rs, &next, ce, a.thr_mode == 0 ? a.lo : 0.0f, epi);
+    stream_dynamic<NP, ET>(T, p, rs, &next, ce, a.thr_mode == 0 ? a.lo : 0.0f, nr, epi);
 }
 
 // ---------------------------------------------------------- k_rows_bal ----
@@ -747,7 +755,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_collect(const GroupParams p, co
     const int64_t row_stride = (int64_t)gridDim.y * c.seg_cap;
     CollectEpi<NP> epi{rs, nr, scount, c.cand_i + blockIdx.y * c.seg_cap, c.cand_t + blockIdx.y * c.seg_cap,
                        row_stride, c.seg_cap};
-    stream_dynamic<NP, ET>(T, p, rs, &next, ce, rs.min_lo, epi);
+    stream_dynamic<NP, ET>(T, p, rs, &next, ce, rs.min_lo, nr, epi);
     __syncthreads();
     if (threadIdx.x < nr) c.seg_counts[(int64_t)rs.orow[threadIdx.x] * gridDim.y + blockIdx.y] = scount[threadIdx.x];
 }
@@ -830,7 +838,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_hist(const GroupParams p, void*
     if (threadIdx.x == 0) next = cb;
     const int nr = build_table(T, rs, p);   // synchronizes the block
     HistEpi<NP, GLOBAL> epi{rs, nr, H};
-    stream_dynamic<NP, ET>(T, p, rs, &next, ce, 0.0f, epi);
+    stream_dynamic<NP, ET>(T, p, rs, &next, ce, 0.0f, nr, epi);
     __syncthreads();
     if (GLOBAL) {
         unsigned long long* o = reinterpret_cast<unsigned long long*>(out);
@@ -924,7 +932,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_loghist(const GroupParams p, in
     if (threadIdx.x == 0) next = cb;
     const int nr = build_table(T, rs, p);   // synchronizes the block
     LogHistEpi<NP> epi{rs, nr, H};
-    stream_dynamic<NP, ET>(T, p, rs, &next, ce, 0.0f, epi);
+    stream_dynamic<NP, ET>(T, p, rs, &next, ce, 0.0f, nr, epi);
     __syncthreads();
     for (int i = threadIdx.x; i < nr * kLogBins; i += blockDim.x) {
         const int r = i / kLogBins, b = i - r * kLogBins;
@@ -1465,7 +1473,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_batch_nbr(const GroupParams p, 
         ai.col_begin = ia.w;
         ai.col_end = ib.x;
         NbrEpi<NP> epi{rs, nr, 0, ai};
-        stream_dynamic<NP, ET>(T, p, rs, &next, ib.z, ai.thr_mode == 0 ? ai.lo : 0.0f, epi);
+        stream_dynamic<NP, ET>(T, p, rs, &next, ib.z, ai.thr_mode == 0 ? ai.lo : 0.0f, nr, epi);
         __syncthreads();
     }
 }
@@ -1760,6 +1768,7 @@ bool table_params(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t ro
     p.row_lo = nullptr;
     p.rows_dev = nullptr;
     p.crange = d->crange;
+    p.eval = h->d_eval;
     return true;
 }
 

@@ -119,3 +119,21 @@ def test_neighbors_mixed_lengths_sort_windows(native, oracle, window):
         _check(gl, oracle, q, db, 0, 300, lo, 1.1, maxn)
     idx, cnt = gl.getNeighbors(0, 300, 0.6, 1.1, 64)
     assert np.all(cnt >= 1)   # every row finds itself
+
+
+def test_evaluated_pairs_counter(native, oracle):
+    """Threshold searches on a mixed-length database skip chunks: the
+    evaluated pairs are fewer than the logical pairs, and a bound of 0 skips
+    nothing."""
+    from siml_gb300 import synthetic as S
+    db = S.smiles_set(S.SEED_RAGGED, S.BIMODAL_35_110, 20000)
+    q = tuple(a[:256] for a in db)
+    gl = _engine(q, db)
+    gl.evaluatedPairs(reset=True)
+    gl.getNeighbors(0, 256, 0.8, 1.1, 64)
+    hi = gl.evaluatedPairs(reset=True)
+    gl.getNeighbors(0, 256, 0.0, 0.01, 64)
+    lo = gl.evaluatedPairs(reset=True)
+    assert 0 < hi < lo
+    assert lo >= 256 * 20000
+    assert gl.evaluatedPairs() == 0
