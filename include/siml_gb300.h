@@ -193,7 +193,10 @@ int siml_batch_info(siml_batch* b, int64_t* rows_out, int64_t* nitems, int64_t* 
  * device outputs idx, sims (may be NULL): [rows_out, pitch]; counts:
  * [rows_out], with siml_neighbors' meaning.  No host synchronization and
  * no allocation, so a run may be captured in a CUDA graph and replayed.
- * Runs of one plan must not overlap on the GPU (they share a queue head). */
+ * Runs of one plan must not overlap on the GPU (they share a queue head).
+ * The kernel checks every work item against the plan's extents; an item
+ * outside them is skipped and the next siml_sync / siml_async_status
+ * returns SIML_ERR_STATE. */
 int siml_batch_run(siml_batch* b, int32_t* idx, float* sims, int32_t* counts, void* stream);
 int siml_batch_destroy(siml_batch* b);
 

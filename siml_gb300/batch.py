@@ -101,6 +101,9 @@ class NeighborBatch:
         (matrix [rows, min(max count, pitch)], counts [rows]) — with the
         similarities as a middle element when ``sims`` is given."""
         torch.cuda.current_stream(self._gl._device()).synchronize()
+        # a work item outside the plan's extents is skipped by the kernel and
+        # reported here
+        N.check(N.lib().siml_async_status(self._gl._h), "siml_batch_run")
         hi = idx.cpu().numpy()
         hs = sims.cpu().numpy() if sims is not None else None
         hc = counts.cpu().numpy()

@@ -669,12 +669,14 @@ namespace siml {
 
 int take_async_error(siml_engine* h) {
     volatile int* w = h->h_async_err;
-    if (w && *w) {
-        *w = 0;
+    const int v = w ? *w : 0;
+    if (!v) return SIML_OK;
+    *w = 0;
+    if (v & 1)
         return fail(SIML_ERR_TIMEOUT, "a top-k heap lock wait exceeded its bound in a queued call; that call's "
                     "result is invalid");
-    }
-    return SIML_OK;
+    return fail(SIML_ERR_STATE, "a batched neighbour run met a work item outside its plan's extents and skipped "
+                "it; that run's result is invalid");
 }
 
 }  // namespace siml

@@ -160,11 +160,13 @@ int launch_neighbors(siml_engine* h, const NbrCall& c);
 // Batched neighbour search: items (two int4 each) pulled by a persistent
 // kernel over ordered ref rows `order`, then the per-output-row finish;
 // rowinfo[rows_out] = {ref row, col_begin, col_end, 0} (ref row -1: unused
-// row).  Queued on st only.
+// row).  Queued on st only.  Items that fail the kernel's extent checks
+// (order_len entries of order, rows_out output rows) are skipped and set
+// bit 2 of the asynchronous error word.
 int batch_nbr_usable(siml_engine* h, const DbLayout* d);
 int launch_batch_neighbors(siml_engine* h, const DbLayout* d, const int4* items, int64_t nitems, unsigned int* head,
-                           const int32_t* order, const int4* rowinfo, int64_t rows_out, float lo, float hi,
-                           int64_t pitch, int32_t* idx, float* sims, int32_t* counts, cudaStream_t st);
+                           const int32_t* order, int64_t order_len, const int4* rowinfo, int64_t rows_out, float lo,
+                           float hi, int64_t pitch, int32_t* idx, float* sims, int32_t* counts, cudaStream_t st);
 // Chunks of the window-sorted layout that hold database columns [c0, c1).
 void sorted_chunk_range(const DbLayout* d, int64_t c0, int64_t c1, int64_t& chunk_begin, int64_t& chunk_end);
 // Per-row 101-bin int32 histograms (out [rows, ldo], zeroed here) or one

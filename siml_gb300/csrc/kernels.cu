@@ -156,7 +156,7 @@ __device__ __forceinline__ int build_table(uint32_t* T, RowSmem& rs, const Group
         const uint32_t* rv = p.row_vid + (int64_t)(p.rowbase + rs.orow[r]) * p.row_stride;
         for (int64_t e = lane; e < p.row_stride; e += 32) {
             const uint32_t v = rv[e];
-            if (v) atomicOr(&T[v], 1u << r);
+            if (v && v < (uint32_t)p.vt_words) atomicOr(&T[v], 1u << r);
         }
     }
     __syncthreads();
@@ -1395,6 +1395,19 @@ __global__ void __launch_bounds__(512) k_topk_select(const int32_t* cand_i, cons
 // reach the bound against the item's rows are skipped.
 // Item layout: two int4 {first order position, rows, output row - ref row,
 // col_begin}, {col_end, c0, c1, 0}.
+//
+// Every item is checked against the plan's extents before it is used (its
+// order positions, chunk range, ref rows and output rows); an item that
+// fails sets bit 2 of the engine's asynchronous error word and is skipped,
+// so a damaged or stale plan cannot make the kernel touch memory outside
+// its buffers.
+struct BatchLimits {
+    int64_t order_len;   // entries of row_order
+    int64_t rows_out;    // output rows
+    int64_t nref;        // ref rows
+    int* err;            // asynchronous error word (bit 2: bad item)
+};
+
 __device__ __forceinline__ void set_rows(uint32_t* T, RowSmem& rs, const GroupParams& p, int64_t pos0, int nr,
                                          int64_t bias) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
@@ -1434,14 +1447,15 @@ __device__ __forceinline__ void clear_rows(uint32_t* T, const GroupParams& p, in
         const uint32_t* rv = p.row_vid + (int64_t)p.row_order[pos0 + r] * p.row_stride;
         for (int64_t e = lane; e < p.row_stride; e += 32) {
             const uint32_t v = rv[e];
-            if (v) T[v] = 0u;
+            if (v && v < (uint32_t)p.vt_words) T[v] = 0u;
         }
     }
 }
 
 template <int NP, typename ET>
 __global__ void __launch_bounds__(kThreads, 1) k_batch_nbr(const GroupParams p, const int4* __restrict__ items,
-                                                           int64_t nitems, unsigned int* head, NbrArgs a) {
+                                                           int64_t nitems, unsigned int* head, NbrArgs a,
+                                                           const BatchLimits lim) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
     __shared__ long long s_item;
@@ -1462,6 +1476,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_batch_nbr(const GroupParams p, 
         const int4 ia = items[2 * w], ib = items[2 * w + 1];
         const int64_t pos0 = ia.x, bias = ia.z;
         const int nr = ia.y;
+        bool bad = nr < 1 || nr > 32 || pos0 < 0 || pos0 + nr > lim.order_len || ib.y < 0 || ib.y > ib.z ||
+                   ib.z > p.nchunks;
+        if (!bad && threadIdx.x < nr) {
+            const int64_t gr = p.row_order[pos0 + threadIdx.x];
+            bad = gr < 0 || gr >= lim.nref || gr + bias < 0 || gr + bias >= lim.rows_out;
+        }
+        if (__syncthreads_or(bad)) {   // uniform: skip the item
+            if (threadIdx.x == 0) atomicOr(lim.err, 2);
+            continue;
+        }
         if (pos0 != cur_pos || nr != cur_nr || bias != cur_bias) {
             if (cur_nr > 0) clear_rows(T, p, cur_pos, cur_nr);
             __syncthreads();
@@ -1866,10 +1890,10 @@ int launch_topk_t(siml_engine* h, const GroupParams& p, size_t smem, int k, int 
 
 template <int NP, typename ET>
 int launch_batch_t(siml_engine* h, const GroupParams& p, size_t smem, const int4* items, int64_t nitems,
-                   unsigned int* head, const NbrArgs& a, cudaStream_t st) {
+                   unsigned int* head, const NbrArgs& a, const BatchLimits& lim, cudaStream_t st) {
     int rc = set_smem(k_batch_nbr<NP, ET>, smem);
     if (rc) return rc;
-    k_batch_nbr<NP, ET><<<(unsigned)h->num_sms, kThreads, smem, st>>>(p, items, nitems, head, a);
+    k_batch_nbr<NP, ET><<<(unsigned)h->num_sms, kThreads, smem, st>>>(p, items, nitems, head, a, lim);
     SIML_CUDA(cudaGetLastError());
     return SIML_OK;
 }
@@ -1890,10 +1914,11 @@ int batch_nbr_usable(siml_engine* h, const DbLayout* d) {
 }
 
 int launch_batch_neighbors(siml_engine* h, const DbLayout* d, const int4* items, int64_t nitems, unsigned int* head,
-                           const int32_t* order, const int4* rowinfo, int64_t rows_out, float lo, float hi,
-                           int64_t pitch, int32_t* idx, float* sims, int32_t* counts, cudaStream_t st) {
+                           const int32_t* order, int64_t order_len, const int4* rowinfo, int64_t rows_out, float lo,
+                           float hi, int64_t pitch, int32_t* idx, float* sims, int32_t* counts, cudaStream_t st) {
     NbrArgs a = nbr_args(lo, hi, pitch, idx, sims, counts, 0, 0);
     a.rowinfo = rowinfo;
+    const BatchLimits lim{order_len, rows_out, h->ref.n, h->d_async_err};
     SIML_CUDA(cudaMemsetAsync(counts, 0, rows_out * sizeof(int32_t), st));
     SIML_CUDA(cudaMemsetAsync(head, 0, sizeof(unsigned int), st));
     GroupParams p;
@@ -1905,11 +1930,11 @@ int launch_batch_neighbors(siml_engine* h, const DbLayout* d, const int4* items,
         force_ordered = 0;
         p.row_order = order;
         if (np == 8)
-            rc = d->entry_bytes == 2 ? launch_batch_t<8, uint16_t>(h, p, smem, items, nitems, head, a, st)
-                                     : launch_batch_t<8, uint32_t>(h, p, smem, items, nitems, head, a, st);
+            rc = d->entry_bytes == 2 ? launch_batch_t<8, uint16_t>(h, p, smem, items, nitems, head, a, lim, st)
+                                     : launch_batch_t<8, uint32_t>(h, p, smem, items, nitems, head, a, lim, st);
         else
-            rc = d->entry_bytes == 2 ? launch_batch_t<16, uint16_t>(h, p, smem, items, nitems, head, a, st)
-                                     : launch_batch_t<16, uint32_t>(h, p, smem, items, nitems, head, a, st);
+            rc = d->entry_bytes == 2 ? launch_batch_t<16, uint16_t>(h, p, smem, items, nitems, head, a, lim, st)
+                                     : launch_batch_t<16, uint32_t>(h, p, smem, items, nitems, head, a, lim, st);
         if (rc) return rc;
         h->launches++;
     }
