@@ -315,7 +315,8 @@ def gpu_arm(args):
     except (OSError, ValueError):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = read_profile_traffic()
+    traffic = read_profile_traffic({"rows_1m": "k_rows_rows1m.md", "nbr_1m": "k_nbr_nbr1m.md",
+                                    "topk_1m": "k_topk_topk1m.md", "hist_1m": "k_hist_hist1m.md"}[wl])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": {"rows_1m": "k_rows_bal", "nbr_1m": "k_nbr", "topk_1m": "k_loghist+k_collect+k_topk_select",
                                                "hist_1m": "k_hist"}[wl], "kernel_ms": kms,
