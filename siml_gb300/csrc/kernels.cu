@@ -1476,17 +1476,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_batch_nbr(const GroupParams p, 
         const int4 ia = items[2 * w], ib = items[2 * w + 1];
         const int64_t pos0 = ia.x, bias = ia.z;
         const int nr = ia.y;
-        bool bad = nr < 1 || nr > 32 || pos0 < 0 || pos0 + nr > lim.order_len || ib.y < 0 || ib.y > ib.z ||
-                   ib.z > p.nchunks;
-        if (!bad && threadIdx.x < nr) {
-            const int64_t gr = p.row_order[pos0 + threadIdx.x];
-            bad = gr < 0 || gr >= lim.nref || gr + bias < 0 || gr + bias >= lim.rows_out;
-        }
-        if (__syncthreads_or(bad)) {   // uniform: skip the item
+        if (nr < 1 || nr > 32 || pos0 < 0 || pos0 + nr > lim.order_len || ib.y < 0 || ib.y > ib.z ||
+            ib.z > p.nchunks) {   // uniform: skip the item
             if (threadIdx.x == 0) atomicOr(lim.err, 2);
+            __syncthreads();   // every thread has read s_item
             continue;
         }
         if (pos0 != cur_pos || nr != cur_nr || bias != cur_bias) {
+            // the item's rows are checked when they enter the table
+            bool bad = false;
+            if (threadIdx.x < nr) {
+                const int64_t gr = p.row_order[pos0 + threadIdx.x];
+                bad = gr < 0 || gr >= lim.nref || gr + bias < 0 || gr + bias >= lim.rows_out;
+            }
+            if (__syncthreads_or(bad)) {   // uniform: skip the item, keep the current rows
+                if (threadIdx.x == 0) atomicOr(lim.err, 2);
+                continue;
+            }
             if (cur_nr > 0) clear_rows(T, p, cur_pos, cur_nr);
             __syncthreads();
             set_rows(T, rs, p, pos0, nr, bias);
