@@ -919,8 +919,48 @@ struct LogHistEpi {
     }
 };
 
-// out: int32 [rows, kLogBins], accumulated (zeroed by the caller)
-template <int NP, typename ET>
+// The same histogram restricted to pairs with t >= the row's floor
+// (GroupParams.row_lo).  Pairs below the floor cost only CollectEpi's
+// pre-filter: per-row integer bounds at the chunk's smallest magnitude,
+// compared bit-sliced for all 32 rows at once.
+template <int NP>
+struct LogHistFloorEpi {
+    const RowSmem& rs;
+    int nr;
+    uint32_t* H;   // shared: [32][kLogWords]
+
+    __device__ __forceinline__ void operator()(int64_t, const int4& meta, const SlicedCounter<NP>& acc) {
+        const int32_t m = meta.x, mb = meta.y;
+        const bool valid = m >= 0;
+        int mbm = valid ? mb : 0x7FFFFFFF;
+        for (int o = 16; o > 0; o >>= 1) mbm = min(mbm, __shfl_xor_sync(0xFFFFFFFFu, mbm, o));
+        if (mbm == 0x7FFFFFFF) return;   // padding-only chunk (uniform)
+        const int lane = threadIdx.x & 31;
+        const float thf = floorf(rs.coef[lane] * (rs.amagf[lane] + (float)mbm));
+        const bool never = lane >= nr || thf >= (float)(1u << NP);
+        const uint32_t thr = never || thf <= 0.0f ? 0u : (uint32_t)thf;
+        uint32_t tp[NP];
+#pragma unroll
+        for (int q = 0; q < NP; q++) tp[q] = __ballot_sync(0xFFFFFFFFu, (thr >> q) & 1u);
+        const uint32_t never_m = __ballot_sync(0xFFFFFFFFu, never);
+        if (!valid) return;
+        uint32_t cand = sliced_ge_rows<NP>(acc, tp) & ~never_m;
+        while (cand) {
+            const int r = __ffs(cand) - 1;
+            cand &= cand - 1u;
+            const int is = sliced_row<NP>(acc, r);
+            if ((float)is < floorf(rs.coef[r] * (rs.amagf[r] + (float)mb))) continue;
+            const float t = tanimoto_rows(is, rs.amag[r], mb);
+            if (!(t >= rs.lo[r])) continue;
+            const int b = log_bin(t);
+            atomicAdd(H + r * kLogWords + (b >> 1), 1u << ((b & 1) * 16));
+        }
+    }
+};
+
+// out: int32 [rows, kLogBins], accumulated (zeroed by the caller).  FLOOR:
+// only pairs at or above the rows' floors (LogHistFloorEpi).
+template <int NP, typename ET, bool FLOOR>
 __global__ void __launch_bounds__(kThreads, 1) k_loghist(const GroupParams p, int32_t* out) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
@@ -931,8 +971,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_loghist(const GroupParams p, in
     cta_range(p, cb, ce);
     if (threadIdx.x == 0) next = cb;
     const int nr = build_table(T, rs, p);   // synchronizes the block
-    LogHistEpi<NP> epi{rs, nr, H};
-    stream_dynamic<NP, ET>(T, p, rs, &next, ce, 0.0f, nr, epi);
+    if constexpr (FLOOR) {
+        LogHistFloorEpi<NP> epi{rs, nr, H};
+        stream_dynamic<NP, ET>(T, p, rs, &next, ce, rs.min_lo, nr, epi);
+    } else {
+        LogHistEpi<NP> epi{rs, nr, H};
+        stream_dynamic<NP, ET>(T, p, rs, &next, ce, 0.0f, nr, epi);
+    }
     __syncthreads();
     for (int i = threadIdx.x; i < nr * kLogBins; i += blockDim.x) {
         const int r = i / kLogBins, b = i - r * kLogBins;
@@ -1259,7 +1304,10 @@ __global__ void __launch_bounds__(256) k_topk_rowscan(const struct RawArgs ra, i
 //  1. per-row histograms of a sample (a prefix of the database's chunks,
 //     k_loghist) give each row a bound theta: the lower edge of the highest
 //     bin at which the sample already holds k molecules.  At least k database
-//     molecules reach theta, so the row's true k-th best is >= theta;
+//     molecules reach theta, so the row's true k-th best is >= theta.  The
+//     sample's histogram is taken above floors from a smaller prefix (the
+//     same rule on 1/8 of the sample), which skips most of its pairs with
+//     the bit-sliced integer compare and leaves theta unchanged;
 //  2. k_collect gathers every pair with t >= theta into per-(row, split)
 //     segments of a candidate buffer;
 //  3. k_topk_select sorts each row's candidates by (similarity descending,
@@ -2079,25 +2127,51 @@ int topk_collect_block(siml_engine* h, const DbLayout* d, int64_t r0, int64_t ro
     int* list_b = reinterpret_cast<int*>(carve((size_t)rows * 4));
     int* list_n = reinterpret_cast<int*>(carve(16));
     int rc;
-    // 1. per-row histograms of the sample (chunks [0, sample)) and the bounds
+    // 1. per-row histograms of the sample (chunks [0, sample)) and the bounds.
+    // With a large enough sample this takes two stages: the first 1/8 of the
+    // sample gives floors (its k-th largest similarity or less, so the whole
+    // sample holds at least k pairs at or above them), and the sample's
+    // histogram is then taken above those floors only.  Its bins from the
+    // floor up are complete, so the bound equals the one-stage bound.
     GroupParams ps;
     size_t sm0 = 0;
     int np = 0;
     table_params(h, d, r0, rows, kModeRows, ps, sm0, np);
     ps.row_order = order;
-    ps.chunk_end = sample;
-    SIML_CUDA(cudaMemsetAsync(hist, 0, (size_t)rows * kLogBins * 4, h->stream));
-    {
+    auto sample_bounds = [&](const GroupParams& g, int64_t nch, bool floor) -> int {
+        SIML_CUDA(cudaMemsetAsync(hist, 0, (size_t)rows * kLogBins * 4, h->stream));
         const int64_t groups = (rows + 31) / 32;
-        int hs = choose_splits(groups, sample, h->num_sms, kThreads / 32);
-        hs = (int)std::max<int64_t>(hs, (sample * 32 + 65534) / 65535);   // <= 65,535 molecules per CTA
-        if ((rc = set_smem(k_loghist<NP, ET>, smem))) return rc;
+        int hs = choose_splits(groups, nch, h->num_sms, kThreads / 32);
+        hs = (int)std::max<int64_t>(hs, (nch * 32 + 65534) / 65535);   // <= 65,535 molecules per CTA
         dim3 grid((unsigned)groups, (unsigned)hs);
-        k_loghist<NP, ET><<<grid, kThreads, smem, h->stream>>>(ps, hist);
+        int rc2;
+        if (floor) {
+            if ((rc2 = set_smem(k_loghist<NP, ET, true>, smem))) return rc2;
+            k_loghist<NP, ET, true><<<grid, kThreads, smem, h->stream>>>(g, hist);
+        } else {
+            if ((rc2 = set_smem(k_loghist<NP, ET, false>, smem))) return rc2;
+            k_loghist<NP, ET, false><<<grid, kThreads, smem, h->stream>>>(g, hist);
+        }
         SIML_CUDA(cudaGetLastError());
+        k_topk_theta<<<(unsigned)((rows + 7) / 8), 256, 0, h->stream>>>(hist, k, rows, row_lo, list_n);
+        SIML_CUDA(cudaGetLastError());
+        h->launches += 2;
+        return SIML_OK;
+    };
+    const int64_t sample1 = sample / kSampleFraction;
+    if (sample1 * 32 >= 4 * (int64_t)k) {
+        GroupParams p1 = ps;
+        p1.chunk_end = sample1;
+        if ((rc = sample_bounds(p1, sample1, false))) return rc;
+        GroupParams p2 = ps;
+        p2.chunk_end = sample;
+        p2.row_lo = row_lo;   // read when each CTA starts, rewritten by the bound kernel after it
+        if ((rc = sample_bounds(p2, sample, true))) return rc;
+    } else {
+        GroupParams p1 = ps;
+        p1.chunk_end = sample;
+        if ((rc = sample_bounds(p1, sample, false))) return rc;
     }
-    k_topk_theta<<<(unsigned)((rows + 7) / 8), 256, 0, h->stream>>>(hist, k, rows, row_lo, list_n);
-    SIML_CUDA(cudaGetLastError());
     // 2. collect every pair at or above its row's bound
     GroupParams pc = ps;
     pc.chunk_begin = 0;
@@ -2124,7 +2198,7 @@ int topk_collect_block(siml_engine* h, const DbLayout* d, int64_t r0, int64_t ro
     k_topk_rowscan<<<(unsigned)rows, 256, (size_t)k * 8, h->stream>>>(raw_args(h, r0), k, idx, sims, h->d_async_err,
                                                                      list_b, list_n + 1);
     SIML_CUDA(cudaGetLastError());
-    h->launches += 4;
+    h->launches += 3;
     return SIML_OK;
 }
 
