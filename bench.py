@@ -340,7 +340,10 @@ def gpu_arm(args):
                        "rows_window": gl.rowsWindow(), "rows_entries": gl.rowsEntries(),
                        "l2": "flushed between steps by a 256 MB write; each step also writes a 4 GB block",
                        "db_layout": stats},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "roofline": roofline,
+            "int_roofline": int_roofline(value / world, np.mean(q[2]), np.mean(db[2]),
+                                         clk.get("sm_mhz") or 2070.0, local),
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk, "parity_spot_check": parity, "wall_s_timed": wall,
             "evaluated_pairs_per_step": evaluated,
             "evaluated_fraction": None if evaluated is None else evaluated / pairs_per_step,
@@ -368,6 +371,18 @@ def ragged_sets_and_jobs(njobs):
     jobs = S.ragged_jobs(S.SEED_RAGGED, RAGGED_DB_N, njobs)
     log("generated + compiled %d molecules and %d jobs in %.1f s" % (RAGGED_DB_N, njobs, time.time() - t))
     return db, jobs
+
+
+def job_mean_lengths(lengths, jobs):
+    """Pair-weighted mean unique LINGOs of the row and column molecules of a
+    job list (one set on both sides)."""
+    s = np.concatenate([[0], np.cumsum(np.asarray(lengths, dtype=np.float64).reshape(-1))])
+    j = np.asarray(jobs, dtype=np.int64).reshape(-1, 4)
+    nr, nc = j[:, 1] - j[:, 0], j[:, 3] - j[:, 2]
+    pairs = float((nr * nc).sum())
+    la = float((nc * (s[j[:, 1]] - s[j[:, 0]])).sum()) / pairs
+    lb = float((nr * (s[j[:, 3]] - s[j[:, 2]])).sum()) / pairs
+    return la, lb
 
 
 def ragged_cpu_rate(db, jobs, target_s=10.0):
@@ -591,7 +606,10 @@ def ragged_arm(args):
             "plain": {"value": plain_value, "unit": "Gpairs/s", "ms": plain_ms, "launches": plain_launches,
                       "path": "one neighborsRangeDevice call per job (siml_neighbors_range)"},
             "batched_over_plain": value / plain_value,
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roofline,
+            "int_roofline": int_roofline(value / world, *job_mean_lengths(db[2], jobs),
+                                         clk.get("sm_mhz") or 2070.0, local),
+            "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": args.steps * kernels_per_run, "clocks": clk,
             "parity_batched_equals_plain": same, "parity_spot_check": oracle_ok, "wall_s_timed": wall,
             "evaluated_pairs_per_step": evaluated, "evaluated_fraction": evaluated / plan.pairs,
@@ -825,6 +843,44 @@ def _same_result(a, b):
                 np.array_equal(np.asarray(x[1], np.float32).view(np.uint32), np.asarray(y[1], np.float32).view(np.uint32))):
             return False
     return True
+
+
+_INT_PEAK = {}
+
+
+def int_peak(device):
+    """Measured 32-bit integer instruction rates of this GPU (siml_int_peak:
+    rings of LOP3, IADD3 and IMNMX), once per process."""
+    if device not in _INT_PEAK:
+        import ctypes
+        from siml_gb300 import _native as N
+        out = (ctypes.c_double * 3)()
+        N.check(N.lib().siml_int_peak(int(device), out), "siml_int_peak")
+        _INT_PEAK[device] = {"lop3": out[0], "iadd3": out[1], "imnmx": out[2]}
+    return _INT_PEAK[device]
+
+
+def int_roofline(gpairs_per_s, la, lb, sm_mhz, device):
+    """The integer roofline of the reference's merge for the same pairs:
+    3 ops per merge step (compare, select/advance, min-accumulate) over
+    La + Lb steps plus 4 for the epilogue (pysiml/_CPULingo.c:53-71; La, Lb
+    the pair-weighted mean unique LINGOs of the row and database molecules), against
+    SMs x 128 lanes x the SM clock under load, and against the measured
+    instruction rates.  The bit-sliced kernels do less work per pair than the
+    merge, so the fraction can exceed 1: it says how far past the merge's
+    integer ceiling the path runs."""
+    import torch
+    la, lb = float(la), float(lb)
+    ops_pair = 3.0 * (la + lb) + 4.0
+    achieved = gpairs_per_s * 1e9 * ops_pair
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    nominal = sms * 128.0 * float(sm_mhz) * 1e6
+    meas = int_peak(device)
+    best = max(meas.values())
+    return {"ops_per_pair": ops_pair, "La": la, "Lb": lb, "achieved_ops_per_s": achieved,
+            "peak_nominal_ops_per_s": nominal, "frac_nominal": achieved / nominal,
+            "peak_measured_ops_per_s": meas, "frac_measured": achieved / best,
+            "formula": "3*(La+Lb)+4 ops per pair; nominal peak = SMs x 128 x SM clock under load"}
 
 
 def read_profile_traffic(name="k_rows_rows1m.md"):

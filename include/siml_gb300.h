@@ -284,6 +284,13 @@ int64_t siml_launch_count(siml_engine* h);
 /* Average device time (ms) of the dominant kernel of the last call on this
  * engine, measured with CUDA events on the engine's stream (0 if none). */
 double siml_last_kernel_ms(siml_engine* h);
+/* Measurement support (no counterpart in the reference): the measured rate
+ * of 32-bit integer instructions on `device`, out[0..2] = LOP3, IADD3 and
+ * IMNMX instructions per second (eight independent ring chains per thread,
+ * eight 256-thread CTAs per SM, best of three ~ms launches).  It is the
+ * measured peak beside the nominal SMs x 128 x clock used for the integer
+ * roofline of the reference's merge (pysiml/_CPULingo.c:53-71). */
+int siml_int_peak(int device, double out[3]);
 
 #ifdef __cplusplus
 }
