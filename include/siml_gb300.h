@@ -211,6 +211,18 @@ int64_t siml_compile_width(const char* buf, const int64_t* offsets, int64_t n);
 int siml_compile_smiles(const char* buf, const int64_t* offsets, int64_t n,
                         int32_t* lingos, int32_t* counts, int32_t* lengths,
                         int32_t* mags, int64_t width);
+/* The same compiler on the GPU (the reference compiles on the CPU only;
+ * same rules and output bytes as siml_compile_smiles).  buf (offsets[n]
+ * bytes) and offsets (n+1 int64) are device memory, as are the outputs;
+ * work is queued on the engine's stream.  siml_compile_width_gpu returns
+ * the width (waits for the stream) or a negative status;
+ * siml_compile_smiles_gpu fills [n, width] rows (width >= 1) and returns
+ * once they are written.  Strings longer than 1,024 bytes are compiled by a
+ * second kernel over device scratch sized for them. */
+int64_t siml_compile_width_gpu(siml_engine* h, const char* buf, const int64_t* offsets, int64_t n);
+int siml_compile_smiles_gpu(siml_engine* h, const char* buf, const int64_t* offsets, int64_t n,
+                            int32_t* lingos, int32_t* counts, int32_t* lengths,
+                            int32_t* mags, int64_t width);
 
 /* ---- utilities ---------------------------------------------------------- */
 /* rowHistogram101 — pysiml/utilities.py:44-55, pysiml/_cpuutil.cpp:52-126:

@@ -2,7 +2,9 @@
 
 ``cSMILEStoMatrices`` runs the native multithreaded compiler
 (siml_gb300/csrc/lingo_compiler.cpp), which produces exactly the reference C
-compiler's output (pysiml/_ccompiler.cpp).  ``SMILEStoMatrices``,
+compiler's output (pysiml/_ccompiler.cpp).  ``compile_buffer_gpu`` produces
+the same arrays on the GPU (siml_gb300/csrc/compile_gpu.cu, sharing the
+rules of siml_gb300/csrc/lingo_compile_core.h).  ``SMILEStoMatrices``,
 ``SMILEStoMultiset`` and ``preprocessNumbers`` restate the reference's pure
 Python variants (pysiml/compiler.py:98-194) for Python 3.
 
@@ -10,6 +12,8 @@ Strings may be ``str`` (encoded as UTF-8) or ``bytes``; a file object works
 as an iterable of lines.
 """
 from __future__ import annotations
+
+import ctypes
 
 import numpy as np
 
@@ -46,6 +50,51 @@ def compile_buffer(buf: bytes, offsets: np.ndarray):
     mags = np.empty(n, dtype=np.int32)
     N.check(L.siml_compile_smiles(cbuf, offsets.ctypes.data, n, lingos.ctypes.data, counts.ctypes.data,
                                   lengths.ctypes.data, mags.ctypes.data, w), "siml_compile_smiles")
+    return lingos, counts, lengths, mags
+
+
+def compile_buffer_gpu(buf, offsets, device: int = 0):
+    """compile_buffer on the GPU: the same four arrays, as int32 CUDA tensors
+    on cuda:device (queued on torch's current stream).  buf is bytes or a
+    uint8 CUDA tensor holding offsets[-1] bytes; offsets an int64 array or
+    tensor of n+1 entries.  The result can go straight to set_qsmiles /
+    set_refsmiles without a host round trip."""
+    import torch
+    from .utilities import _engine
+    dev = torch.device("cuda", device)
+    off_h = offsets.cpu().numpy() if isinstance(offsets, torch.Tensor) else np.asarray(offsets)
+    off_h = np.ascontiguousarray(off_h, dtype=np.int64).reshape(-1)
+    n = off_h.shape[0] - 1
+    if n < 0:
+        raise ValueError("offsets needs at least one entry")
+    total = int(off_h[-1]) if n >= 0 else 0
+    if isinstance(buf, torch.Tensor):
+        if not buf.is_cuda or buf.dtype != torch.uint8:
+            raise ValueError("a tensor buffer must be a uint8 CUDA tensor")
+        text = buf.contiguous()
+        if text.numel() < total:
+            raise ValueError("buffer holds %d bytes, offsets need %d" % (text.numel(), total))
+    else:
+        raw = bytes(buf)
+        if len(raw) < total:
+            raise ValueError("buffer holds %d bytes, offsets need %d" % (len(raw), total))
+        host = torch.frombuffer(bytearray(raw[:total] or b"\0"), dtype=torch.uint8)
+        text = host.pin_memory().to(dev, non_blocking=True)
+    off_d = torch.from_numpy(off_h).to(dev)
+    L = N.lib()
+    h = _engine(device)
+    N.check(L.siml_set_stream(h, ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)), "siml_set_stream")
+    w = L.siml_compile_width_gpu(h, text.data_ptr(), off_d.data_ptr(), n)
+    if w < 0:
+        N.check(int(-w), "siml_compile_width_gpu")
+    lingos = torch.zeros((n, w), dtype=torch.int32, device=dev)
+    counts = torch.zeros((n, w), dtype=torch.int32, device=dev)
+    lengths = torch.zeros(n, dtype=torch.int32, device=dev)
+    mags = torch.zeros(n, dtype=torch.int32, device=dev)
+    if w > 0:
+        N.check(L.siml_compile_smiles_gpu(h, text.data_ptr(), off_d.data_ptr(), n, lingos.data_ptr(),
+                                          counts.data_ptr(), lengths.data_ptr(), mags.data_ptr(), w),
+                "siml_compile_smiles_gpu")
     return lingos, counts, lengths, mags
 
 
