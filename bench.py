@@ -683,20 +683,40 @@ def serving_arm(args):
     from siml_gb300 import GPULingo
     from siml_gb300 import synthetic as S
     from siml_gb300.serving import LingoServer, ServerConfig, Request, serve_unbatched
-    from siml_gb300.compiler import compile_buffer
+    from siml_gb300.compiler import compile_buffer, compile_buffer_gpu
     t = time.time()
     buf, off = S.smiles_buffer(S.SEED_SERVING, S.UNIFORM_20_90, SERVING_DB_N)
     t_gen = time.time() - t
     t = time.time()
-    db = compile_buffer(buf, off)
+    db = compile_buffer(buf, off)        # host arrays: the oracle's spot checks read them
     t_compile = time.time() - t
-    del buf, off
-    log("generated %d molecules in %.1f s, compiled in %.1f s" % (SERVING_DB_N, t_gen, t_compile))
     dev = torch.device("cuda", local)
+    # the database is made resident from the GPU compiler's output: SMILES
+    # bytes up, compiled on the device, no host arrays
+    torch.cuda.synchronize()
+    t = time.time()
+    db_dev = compile_buffer_gpu(buf, off, device=local)
+    torch.cuda.synchronize()
+    t_compile_gpu = time.time() - t
+    # the kernels alone: the same bytes already on the device
+    text_dev = torch.from_numpy(np.frombuffer(buf, dtype=np.uint8).copy()).to(dev)
+    torch.cuda.synchronize()
+    t = time.time()
+    again = compile_buffer_gpu(text_dev, off, device=local)
+    torch.cuda.synchronize()
+    t_compile_kernels = time.time() - t
+    del again, text_dev
+    spot = slice(0, min(SERVING_DB_N, 200_000))
+    gpu_equals_host = all(torch.equal(torch.from_numpy(np.ascontiguousarray(a[spot])).to(dev), b[spot])
+                          for a, b in zip(db, db_dev)) and tuple(db_dev[0].shape) == db[0].shape
+    del buf, off
+    log("generated %d molecules in %.1f s, compiled in %.1f s (host), %.3f s (GPU)" %
+        (SERVING_DB_N, t_gen, t_compile, t_compile_gpu))
     gl = GPULingo(local, stream=torch.cuda.Stream(device=dev))
     t = time.time()
-    gl.set_qsmiles(*db)
+    gl.set_qsmiles(*db_dev)
     torch.cuda.synchronize()
+    del db_dev
     t_upload = time.time() - t
     cfg = ServerConfig(max_rows=args.serving_max_rows, soft_rows=args.serving_soft_rows, width=128, kmax=64,
                        pitch=256, lo=0.75)
@@ -711,9 +731,13 @@ def serving_arm(args):
     log("database resident in %.1f s: %s" % (t_resident, stats))
     ingest = {"molecules": SERVING_DB_N, "compile_s": t_compile,
               "compile_molecules_per_s": SERVING_DB_N / t_compile, "compile_threads": os.cpu_count(),
+              "compile_gpu_s": t_compile_gpu, "compile_gpu_molecules_per_s": SERVING_DB_N / t_compile_gpu,
+              "compile_gpu_device_input_s": t_compile_kernels,
+              "compile_gpu_equals_host_first_200k": bool(gpu_equals_host),
               "upload_s": t_upload, "resident_s": t_resident,
-              "note": "compile: native multithreaded SMILES->LINGO compiler; resident: upload, vocabulary, "
-                      "layouts and the warm-up batches"}
+              "note": "compile: the host's multithreaded SMILES->LINGO compiler, timed for comparison; "
+                      "compile_gpu: the GPU compiler (SMILES bytes copied up included), whose device arrays "
+                      "the database is set from; resident: set-up, vocabulary, layouts and the warm-up batches"}
     nq = SERVING_DB_N
     rates = [float(x) for x in args.serving_rates.split(",")]
     results = []

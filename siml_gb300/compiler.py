@@ -75,11 +75,17 @@ def compile_buffer_gpu(buf, offsets, device: int = 0):
         if text.numel() < total:
             raise ValueError("buffer holds %d bytes, offsets need %d" % (text.numel(), total))
     else:
-        raw = bytes(buf)
-        if len(raw) < total:
-            raise ValueError("buffer holds %d bytes, offsets need %d" % (len(raw), total))
-        host = torch.frombuffer(bytearray(raw[:total] or b"\0"), dtype=torch.uint8)
-        text = host.pin_memory().to(dev, non_blocking=True)
+        raw = memoryview(buf).cast("B")
+        if raw.nbytes < total:
+            raise ValueError("buffer holds %d bytes, offsets need %d" % (raw.nbytes, total))
+        if total == 0:
+            text = torch.zeros(1, dtype=torch.uint8, device=dev)
+        else:
+            import warnings
+            with warnings.catch_warnings():   # read-only host bytes, only ever read
+                warnings.simplefilter("ignore")
+                host = torch.from_numpy(np.frombuffer(raw[:total], dtype=np.uint8))
+            text = host.to(dev)
     off_d = torch.from_numpy(off_h).to(dev)
     L = N.lib()
     h = _engine(device)
