@@ -247,6 +247,15 @@ int siml_synth_smiles(uint64_t seed, int dist, int64_t first, int64_t n,
  * molecules, out[4] = largest chunk in groups per lane, out[5] = database
  * molecules, out[6] / out[7] = largest count sum in the ref / query set. */
 int siml_db_stats(siml_engine* h, int64_t out[8]);
+/* Vocabulary split (no counterpart in the reference).  When the table of
+ * all (code, level) pairs does not fit in shared memory, the pairs are
+ * renumbered by database frequency: the first out[1] ("common") keep the
+ * shared-memory table, the rest are "rare" and are looked up per row group
+ * in a small hash of the ref rows' rare pairs.  out[0] = pairs, out[1] =
+ * common pairs (== out[0] without a split), out[2] = rare entries of the
+ * database (window-sorted layout), out[3] = most rare entries in one ref row
+ * (table kernels run while it is at most 96; otherwise the per-pair merge). */
+int siml_vocab_stats(siml_engine* h, int64_t out[4]);
 /* Layout tuning (no reference counterpart).  SIML_TUNE_ROWS_WINDOW: the
  * full-matrix layout (siml_rows, siml_row_single) sorts database molecules by
  * entry count inside windows of 32 (natural order), 64, 128 or 256 molecules;

@@ -448,6 +448,14 @@ class GPULingo:
         keys = ["nvid", "entry_bytes", "ngroups_total", "nchunks", "max_ng", "n", "ref_max_entries", "qry_max_entries"]
         return dict(zip(keys, [int(x) for x in a]))
 
+    def vocabStats(self):
+        """Vocabulary split of the resident database (dict): pairs, common
+        pairs (shared-memory table), rare database entries, most rare entries
+        in one ref row."""
+        a = (ctypes.c_int64 * 4)()
+        N.check(N.lib().siml_vocab_stats(self._h, a), "siml_vocab_stats")
+        return dict(zip(["nvid", "ncommon", "nrare", "row_max_rare"], [int(x) for x in a]))
+
     def setRowsWindow(self, window):
         """Sort window (32 = natural order, 64, 128 or 256) of the layout the
         full-matrix calls stream; see SIML_TUNE_ROWS_WINDOW."""

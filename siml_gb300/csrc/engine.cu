@@ -126,6 +126,7 @@ void free_vocab(Vocab& v) { dev_free(v.keys); dev_free(v.vid); v = Vocab(); }
 void free_layout(DbLayout& d) {
     dev_free(d.perm); dev_free(d.meta);
     dev_free(d.ng); dev_free(d.off);
+    dev_free(d.rare_off); dev_free(d.rare_vid);
     if (d.crange) cudaFree(d.crange);
     if (d.entries) cudaFree(d.entries);
     d = DbLayout();
@@ -280,6 +281,82 @@ __device__ __forceinline__ uint32_t vocab_lookup(const unsigned long long* __res
     return 0u;
 }
 
+// Database frequency of every (code, level) pair: the number of molecules
+// holding the code with count >= level, i.e. how often its vid appears in
+// the entry stream.  Used to renumber a vocabulary that has to be split.
+__global__ void k_vocab_freq(const int32_t* __restrict__ lingos, const int32_t* __restrict__ counts,
+                             const int32_t* __restrict__ len, int64_t n, int64_t width,
+                             const unsigned long long* __restrict__ keys, int64_t cap, uint32_t* freq) {
+    const int64_t total = n * width;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t m = i / width;
+        const int32_t j = (int32_t)(i - m * width);
+        if (j >= len[m]) continue;
+        const int32_t code = lingos[i], c = counts[i];
+        for (int32_t lvl = 1; lvl <= c; lvl++) {
+            const unsigned long long k = vkey(code, lvl);
+            unsigned long long slot = mix64(k) & (unsigned long long)(cap - 1);
+            for (int64_t probes = 0; probes < cap; probes++) {
+                const unsigned long long cur = keys[slot];
+                if (cur == k) { atomicAdd(&freq[slot], 1u); break; }
+                if (cur == kEmptyKey) break;
+                slot = (slot + 1) & (unsigned long long)(cap - 1);
+            }
+        }
+    }
+}
+
+// Split vocabulary: per molecule the entries that stay in the stream
+// (vid <= ncommon) and the rare ones.
+__global__ void k_split_count(const int32_t* __restrict__ lingos, const int32_t* __restrict__ counts,
+                              const int32_t* __restrict__ len, int64_t n, int64_t width,
+                              const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ vid,
+                              int64_t cap, int64_t ncommon, int32_t* ccount, int32_t* rcount) {
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    const int32_t L = len[m];
+    int32_t nc = 0, nrare = 0;
+    for (int32_t j = 0; j < L; j++) {
+        const int32_t code = lingos[m * width + j], cnt = counts[m * width + j];
+        for (int32_t lvl = 1; lvl <= cnt; lvl++) {
+            const uint32_t v = vocab_lookup(keys, vid, cap, code, lvl);
+            if ((int64_t)v <= ncommon) nc++;
+            else nrare++;
+        }
+    }
+    ccount[m] = nc;
+    rcount[m] = nrare;
+}
+
+// Rare entries per chunk of the layout (slot order).
+__global__ void k_rare_chunk(const int32_t* __restrict__ perm, const int32_t* __restrict__ rcount, int64_t nchunks,
+                             int64_t* chunk_sum) {
+    const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    if (c >= nchunks) return;
+    const int32_t m = perm[c * 32 + (threadIdx.x & 31)];
+    int64_t v = m >= 0 ? rcount[m] : 0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    if ((threadIdx.x & 31) == 0) chunk_sum[c] = v;
+}
+
+// rare_off[slot] = chunk base + rare entries of the chunk's earlier lanes.
+__global__ void k_rare_off(const int32_t* __restrict__ perm, const int32_t* __restrict__ rcount, int64_t nchunks,
+                           const int64_t* __restrict__ chunk_base, int64_t* rare_off) {
+    const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= nchunks) return;
+    const int32_t m = perm[c * 32 + lane];
+    const int64_t v = m >= 0 ? rcount[m] : 0;
+    int64_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int64_t u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    rare_off[c * 32 + lane] = chunk_base[c] + incl - v;
+    if (c == nchunks - 1 && lane == 31) rare_off[nchunks * 32] = chunk_base[c] + incl;
+}
+
 // One CTA of 256 threads per window: rank molecules by (entries, index).
 // Sorts each window of w molecules (a power of two, 64..kMaxWindow) by entry
 // count: bitonic sort of (count << 32 | position) keys in shared memory;
@@ -323,15 +400,16 @@ __global__ void k_identity_perm(int64_t n, int64_t slots, int32_t* perm) {
 // Per chunk: 16-byte groups per lane = ceil(max entries / entries-per-group),
 // rounded up to an even number of 8-entry steps; plus per-lane metadata.
 __global__ void k_chunk_meta(const int32_t* __restrict__ perm, const int32_t* __restrict__ cmag,
-                             const int32_t* __restrict__ mag, const int32_t* __restrict__ len,
-                             int64_t nchunks, int entries_per_group, int balanced,
-                             int32_t* __restrict__ ng, int4* __restrict__ meta, int2* __restrict__ crange) {
+                             const int32_t* __restrict__ scount, const int32_t* __restrict__ mag,
+                             const int32_t* __restrict__ len, int64_t nchunks, int entries_per_group,
+                             int balanced, int32_t* __restrict__ ng, int4* __restrict__ meta,
+                             int2* __restrict__ crange) {
     const int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (c >= nchunks) return;
     const int32_t m = perm[c * 32 + lane];
-    const int32_t e = m >= 0 ? cmag[m] : 0;
-    meta[c * 32 + lane] = make_int4(m, m >= 0 ? mag[m] : 0, e, m >= 0 ? len[m] : 0);
+    meta[c * 32 + lane] = make_int4(m, m >= 0 ? mag[m] : 0, m >= 0 ? cmag[m] : 0, m >= 0 ? len[m] : 0);
+    const int32_t e = m >= 0 ? scount[m] : 0;               // streamed entries (all, or the common ones)
     int32_t mx = e;
     int32_t sum = (e + 7) / 8;                              // 8-entry steps of this molecule
     int32_t mlo = m >= 0 ? mag[m] : 0x7FFFFFFF, mhi = m >= 0 ? mag[m] : -1;
@@ -362,7 +440,8 @@ __global__ void k_fill_entries(const int32_t* __restrict__ lingos, const int32_t
                                const int32_t* __restrict__ ng, int64_t nchunks, int balanced,
                                const unsigned long long* __restrict__ keys,
                                const uint32_t* __restrict__ vid, int64_t cap, int shift,
-                               ET* __restrict__ entries) {
+                               ET* __restrict__ entries, int64_t ncommon, const int64_t* __restrict__ rare_off,
+                               uint32_t* __restrict__ rare_vid) {
     constexpr int EPG = 16 / sizeof(ET);
     constexpr int SPG = 8 / EPG;   // 16-byte groups per 8-entry step
     const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -371,7 +450,7 @@ __global__ void k_fill_entries(const int32_t* __restrict__ lingos, const int32_t
     const int64_t c = slot >> 5;
     const int lane = (int)(slot & 31);
     int32_t P = 0, Ls = 1;
-    if (balanced) {
+    if (balanced) {   // never with a split vocabulary
         const int32_t g = m >= 0 ? (cmag[m] + 7) / 8 : 0;
         int32_t incl = g;
         for (int o = 1; o < 32; o <<= 1) {
@@ -385,11 +464,15 @@ __global__ void k_fill_entries(const int32_t* __restrict__ lingos, const int32_t
     const int32_t L = len[m];
     const int32_t* lr = lingos + (int64_t)m * width;
     const int32_t* cr = counts + (int64_t)m * width;
-    int64_t e = 0;
+    int64_t e = 0, er = 0;   // streamed and rare entries so far
     for (int32_t j = 0; j < L; j++) {
         const int32_t code = lr[j], cnt = cr[j];
-        for (int32_t lvl = 1; lvl <= cnt; lvl++, e++) {
+        for (int32_t lvl = 1; lvl <= cnt; lvl++) {
             const uint32_t v = vocab_lookup(keys, vid, cap, code, lvl);
+            if (rare_off && (int64_t)v > ncommon) {
+                rare_vid[rare_off[slot] + er++] = v;
+                continue;
+            }
             int64_t g;
             if (balanced) {
                 const int64_t gs = P + e / 8;
@@ -398,6 +481,7 @@ __global__ void k_fill_entries(const int32_t* __restrict__ lingos, const int32_t
                 g = off[c] + (e / EPG) * 32 + lane;
             }
             entries[g * EPG + (e % EPG)] = (ET)(v << shift);
+            e++;
         }
     }
 }
@@ -407,9 +491,10 @@ __global__ void k_row_entries(const int32_t* __restrict__ lingos, const int32_t*
                               const int32_t* __restrict__ len, int64_t n, int64_t width,
                               const unsigned long long* __restrict__ keys,
                               const uint32_t* __restrict__ vid, int64_t cap,
-                              uint32_t* __restrict__ out, int64_t stride) {
+                              uint32_t* __restrict__ out, int64_t stride, int64_t ncommon, int* max_rare) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
+    int nrare = 0;
     const int32_t L = len[r];
     const int32_t* lr = lingos + r * width;
     const int32_t* cr = counts + r * width;
@@ -421,9 +506,11 @@ __global__ void k_row_entries(const int32_t* __restrict__ lingos, const int32_t*
             const uint32_t v = vocab_lookup(keys, vid, cap, code, lvl);
             if (v == 0u) break;   // higher levels of an absent pair are absent too
             o[e++] = v;
+            nrare += (int64_t)v > ncommon;
         }
     }
     for (; e < stride; e++) o[e] = 0u;
+    if (nrare) atomicMax(max_rare, nrare);
 }
 
 // ------------------------------------------------------------ host helpers --
@@ -481,6 +568,8 @@ int upload_set(siml_engine* h, RawSet& s, const int32_t* lingos, const int32_t* 
     return SIML_OK;
 }
 
+int split_vocab(siml_engine* h, int64_t ncommon);
+
 int build_vocab(siml_engine* h) {
     free_vocab(h->vocab);
     const RawSet& q = h->qry;
@@ -532,28 +621,84 @@ int build_vocab(siml_engine* h) {
         SIML_CUDA(cudaStreamSynchronize(st));
         dev_free(bcount);
         v.nvid = acc;
+        v.ncommon = acc;
+        v.split = false;
+        if (!direct_table_fits(h, acc)) return split_vocab(h, split_table_capacity(h));
         return SIML_OK;
     }
     return fail(SIML_ERR_NOMEM, "vocabulary hash could not be sized");
 }
 
+// Renumbers the vocabulary by falling database frequency (ties: slot order)
+// so that vids 1..ncommon are the most frequent pairs, and marks it split.
+int split_vocab(siml_engine* h, int64_t ncommon) {
+    Vocab& v = h->vocab;
+    const RawSet& q = h->qry;
+    cudaStream_t st = h->stream;
+    ncommon = std::max<int64_t>(0, std::min<int64_t>(ncommon, v.nvid));
+    uint32_t* freq = nullptr;
+    int rc;
+    if ((rc = dev_alloc(&freq, (size_t)v.cap))) return rc;
+    std::vector<uint32_t> hf((size_t)v.cap);
+    cudaError_t e = cudaMemsetAsync(freq, 0, (size_t)v.cap * 4, st);
+    if (e == cudaSuccess && q.n > 0) {
+        const int64_t total = q.n * q.width;
+        const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, 65535LL * 8);
+        k_vocab_freq<<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.n, q.width, v.keys, v.cap, freq);
+        h->launches++;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hf.data(), freq, (size_t)v.cap * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dev_free(freq);
+    if (e != cudaSuccess) return cuda_fail(e, "vocabulary frequencies");
+    std::vector<int64_t> occ;
+    occ.reserve((size_t)v.nvid);
+    for (int64_t s = 0; s < v.cap; s++)
+        if (hf[(size_t)s]) occ.push_back(s);
+    if ((int64_t)occ.size() != v.nvid) return fail(SIML_ERR_CUDA, "vocabulary frequencies do not cover the vocabulary");
+    auto more = [&](int64_t a, int64_t b) {
+        return hf[(size_t)a] != hf[(size_t)b] ? hf[(size_t)a] > hf[(size_t)b] : a < b;
+    };
+    std::nth_element(occ.begin(), occ.begin() + ncommon, occ.end(), more);
+    std::sort(occ.begin(), occ.begin() + ncommon, more);
+    std::vector<uint32_t> hv((size_t)v.cap, 0u);
+    for (int64_t i = 0; i < ncommon; i++) hv[(size_t)occ[(size_t)i]] = (uint32_t)(i + 1);
+    uint32_t next = (uint32_t)ncommon + 1u;
+    for (int64_t s = 0; s < v.cap; s++)
+        if (hf[(size_t)s] && !hv[(size_t)s]) hv[(size_t)s] = next++;
+    SIML_CUDA(cudaMemcpyAsync(v.vid, hv.data(), (size_t)v.cap * 4, cudaMemcpyHostToDevice, st));
+    SIML_CUDA(cudaStreamSynchronize(st));
+    v.ncommon = ncommon;
+    v.split = ncommon < v.nvid;
+    return SIML_OK;
+}
+
+// Device scratch freed when the scope ends (layout builds only).
+struct DevTemp {
+    void* p = nullptr;
+    ~DevTemp() { if (p) cudaFree(p); }
+};
+
 int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     free_layout(d);
     const RawSet& q = h->qry;
     cudaStream_t st = h->stream;
+    const bool split = h->vocab.split;
     d.n = q.n;
     d.sorted = sorted;
     d.window = sorted ? h->sorted_window : h->rows_window;
-    d.entry_bytes = h->vocab.nvid < 65535 ? 2 : 4;
+    d.entry_bytes = h->vocab.ncommon < 65535 ? 2 : 4;
     d.offsets = false;
-    if (!sorted && h->rows_entries == SIML_ENTRIES_U32) d.entry_bytes = 4;
-    if (!sorted && h->rows_entries == SIML_ENTRIES_OFFSETS) {
+    if (!split && !sorted && h->rows_entries == SIML_ENTRIES_U32) d.entry_bytes = 4;
+    if (!split && !sorted && h->rows_entries == SIML_ENTRIES_OFFSETS) {
         d.entry_bytes = 4;
         d.offsets = true;
     }
-    // decided after the entry format: the balanced kernel reads vids, not byte offsets
-    d.balanced = !sorted && h->rows_window == kChunk && h->rows_layout == SIML_ROWS_BALANCED && !d.offsets &&
-                 rows_balanced_fits(h);
+    // decided after the entry format: the balanced kernel reads vids, not byte
+    // offsets, and has no rare-entry pass
+    d.balanced = !split && !sorted && h->rows_window == kChunk && h->rows_layout == SIML_ROWS_BALANCED &&
+                 !d.offsets && rows_balanced_fits(h);
     const int64_t nwin = (q.n + d.window - 1) / d.window;
     d.nchunks = (q.n + kChunk - 1) / kChunk;
     const int64_t slots = std::max<int64_t>(nwin, 1) * d.window;
@@ -564,17 +709,33 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     if ((rc = dev_alloc(&d.off, (size_t)d.nchunks + 1))) return rc;
     if (q.n == 0) return SIML_OK;
     SIML_CUDA(cudaMalloc((void**)&d.crange, (size_t)std::max<int64_t>(d.nchunks, 1) * sizeof(int2)));
+    // streamed entries per molecule: all of them, or the common ones of a
+    // split vocabulary (the rare ones go to per-slot lists)
+    DevTemp t_cc, t_rc;
+    const int32_t* scount = q.cmag;
+    int32_t* rcount = nullptr;
+    if (split) {
+        SIML_CUDA(cudaMalloc(&t_cc.p, (size_t)q.n * 4));
+        SIML_CUDA(cudaMalloc(&t_rc.p, (size_t)q.n * 4));
+        k_split_count<<<(unsigned)((q.n + 255) / 256), 256, 0, st>>>(
+            q.lingos, q.counts, q.len, q.n, q.width, h->vocab.keys, h->vocab.vid, h->vocab.cap, h->vocab.ncommon,
+            (int32_t*)t_cc.p, (int32_t*)t_rc.p);
+        h->launches++;
+        SIML_CUDA(cudaGetLastError());
+        scount = (const int32_t*)t_cc.p;
+        rcount = (int32_t*)t_rc.p;
+    }
     if (d.window > kChunk) {
         const size_t wsm = (size_t)d.window * 8;
         SIML_CUDA(cudaFuncSetAttribute(k_window_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-        k_window_sort<<<(unsigned)nwin, std::min(d.window, 1024), wsm, st>>>(q.cmag, q.n, d.window, d.perm);
+        k_window_sort<<<(unsigned)nwin, std::min(d.window, 1024), wsm, st>>>(scount, q.n, d.window, d.perm);
     } else {
         k_identity_perm<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(q.n, slots, d.perm);
     }
     h->launches++;
     const int epg = 16 / d.entry_bytes;
-    k_chunk_meta<<<(unsigned)((d.nchunks + 7) / 8), 256, 0, st>>>(d.perm, q.cmag, q.mag, q.len, d.nchunks, epg,
-                                                                  d.balanced ? 1 : 0, d.ng, d.meta, d.crange);
+    k_chunk_meta<<<(unsigned)((d.nchunks + 7) / 8), 256, 0, st>>>(d.perm, q.cmag, scount, q.mag, q.len, d.nchunks,
+                                                                  epg, d.balanced ? 1 : 0, d.ng, d.meta, d.crange);
     h->launches++;
     SIML_CUDA(cudaGetLastError());
     std::vector<int32_t> hng((size_t)d.nchunks);
@@ -591,18 +752,46 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     d.ngroups_total = acc;
     d.max_ng = mx;
     SIML_CUDA(cudaMemcpyAsync(d.off, hoff.data(), (d.nchunks + 1) * 8, cudaMemcpyHostToDevice, st));
+    if (split) {
+        // slot s's rare vids at rare_off[s]: chunk sums, a host scan over
+        // chunks, lane offsets inside each chunk
+        DevTemp t_sum, t_base;
+        SIML_CUDA(cudaMalloc(&t_sum.p, (size_t)d.nchunks * 8));
+        SIML_CUDA(cudaMalloc(&t_base.p, (size_t)d.nchunks * 8));
+        k_rare_chunk<<<(unsigned)((d.nchunks + 7) / 8), 256, 0, st>>>(d.perm, rcount, d.nchunks,
+                                                                      (int64_t*)t_sum.p);
+        h->launches++;
+        SIML_CUDA(cudaGetLastError());
+        std::vector<int64_t> hs((size_t)d.nchunks);
+        SIML_CUDA(cudaMemcpyAsync(hs.data(), t_sum.p, (size_t)d.nchunks * 8, cudaMemcpyDeviceToHost, st));
+        SIML_CUDA(cudaStreamSynchronize(st));
+        int64_t tot = 0;
+        for (auto& x : hs) { const int64_t t = x; x = tot; tot += t; }
+        SIML_CUDA(cudaMemcpyAsync(t_base.p, hs.data(), (size_t)d.nchunks * 8, cudaMemcpyHostToDevice, st));
+        if ((rc = dev_alloc(&d.rare_off, (size_t)d.nchunks * 32 + 1))) return rc;
+        if ((rc = dev_alloc(&d.rare_vid, (size_t)std::max<int64_t>(tot, 1)))) return rc;
+        d.nrare = tot;
+        k_rare_off<<<(unsigned)((d.nchunks + 7) / 8), 256, 0, st>>>(d.perm, rcount, d.nchunks,
+                                                                    (const int64_t*)t_base.p, d.rare_off);
+        h->launches++;
+        SIML_CUDA(cudaGetLastError());
+        SIML_CUDA(cudaStreamSynchronize(st));   // t_base is freed at scope end
+    }
     SIML_CUDA(cudaMalloc(&d.entries, (size_t)std::max<int64_t>(acc, 1) * 16));
     SIML_CUDA(cudaMemsetAsync(d.entries, 0, (size_t)std::max<int64_t>(acc, 1) * 16, st));
     const unsigned grid = (unsigned)((d.nchunks * 32 + 255) / 256);
     const int bal = d.balanced ? 1 : 0;
+    const int64_t ncommon = h->vocab.ncommon;
     if (d.entry_bytes == 2)
         k_fill_entries<uint16_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.cmag, q.width, d.perm, d.off,
                                                        d.ng, d.nchunks, bal, h->vocab.keys, h->vocab.vid,
-                                                       h->vocab.cap, 0, (uint16_t*)d.entries);
+                                                       h->vocab.cap, 0, (uint16_t*)d.entries, ncommon,
+                                                       d.rare_off, d.rare_vid);
     else
         k_fill_entries<uint32_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.cmag, q.width, d.perm, d.off,
                                                        d.ng, d.nchunks, bal, h->vocab.keys, h->vocab.vid,
-                                                       h->vocab.cap, d.offsets ? 2 : 0, (uint32_t*)d.entries);
+                                                       h->vocab.cap, d.offsets ? 2 : 0, (uint32_t*)d.entries,
+                                                       ncommon, d.rare_off, d.rare_vid);
     h->launches++;
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(cudaStreamSynchronize(st));
@@ -617,13 +806,18 @@ int build_rows(siml_engine* h) {
     re.stride = std::max<int64_t>(std::max<int64_t>(1, r.max_entries), h->row_stride_hint);
     int rc;
     if ((rc = dev_alloc(&re.vid, (size_t)(std::max<int64_t>(r.n, 1) * re.stride)))) return rc;
+    int max_rare = 0;
     if (r.n > 0) {
+        SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
         k_row_entries<<<(unsigned)((r.n + 127) / 128), 128, 0, h->stream>>>(
-            r.lingos, r.counts, r.len, r.n, r.width, h->vocab.keys, h->vocab.vid, h->vocab.cap, re.vid, re.stride);
+            r.lingos, r.counts, r.len, r.n, r.width, h->vocab.keys, h->vocab.vid, h->vocab.cap, re.vid, re.stride,
+            h->vocab.ncommon, h->d_err);
         h->launches++;
         SIML_CUDA(cudaGetLastError());
+        SIML_CUDA(cudaMemcpyAsync(&max_rare, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     }
     SIML_CUDA(cudaStreamSynchronize(h->stream));
+    re.max_rare = max_rare;
     return SIML_OK;
 }
 
@@ -851,12 +1045,22 @@ int siml_write_ref_rows(siml_engine* h, int64_t row0, const int32_t* lingos, con
         if (mx > h->rows.stride) {
             h->rows_valid = false;   // rebuilt, wider, on next use
         } else {
+            // with a split vocabulary the rows' rare-entry maximum decides
+            // whether the table kernels may run, so it is read back (a
+            // stream synchronization only for split vocabularies)
+            if (h->vocab.split) SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), st));
             k_row_entries<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(dl, dc, s.len + row0, n, s.width,
                                                                        h->vocab.keys, h->vocab.vid, h->vocab.cap,
                                                                        h->rows.vid + row0 * h->rows.stride,
-                                                                       h->rows.stride);
+                                                                       h->rows.stride, h->vocab.ncommon, h->d_err);
             h->launches++;
             SIML_CUDA(cudaGetLastError());
+            if (h->vocab.split) {
+                int mr = 0;
+                SIML_CUDA(cudaMemcpyAsync(&mr, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+                SIML_CUDA(cudaStreamSynchronize(st));
+                h->rows.max_rare = std::max<int64_t>(h->rows.max_rare, mr);
+            }
         }
     }
     return SIML_OK;
@@ -893,6 +1097,19 @@ int siml_db_stats(siml_engine* h, int64_t out[8]) {
     out[5] = d->n;
     out[6] = h->ref.max_entries;
     out[7] = h->qry.max_entries;
+    return SIML_OK;
+}
+
+int siml_vocab_stats(siml_engine* h, int64_t out[4]) {
+    SIML_GUARD(h);
+    if (!out) return fail(SIML_ERR_INVALID, "siml_vocab_stats: NULL output");
+    const DbLayout* d = nullptr;
+    int rc = ensure_layout(h, true, &d);
+    if (rc) return rc;
+    out[0] = h->vocab.nvid;
+    out[1] = h->vocab.ncommon;
+    out[2] = d->nrare;
+    out[3] = h->rows.max_rare;
     return SIML_OK;
 }
 

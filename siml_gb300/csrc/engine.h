@@ -29,11 +29,23 @@ struct RawSet {
 // (level << 32) | (uint32)code, empty slots hold kEmptyKey; vid[slot] is the
 // dense virtual id (1..nvid) of an occupied slot.
 constexpr unsigned long long kEmptyKey = 0xFFFFFFFFFFFFFFFFull;
+//
+// When the table of all vids does not fit in shared memory the vocabulary
+// is split: vids are renumbered by falling database frequency, vids
+// 1..ncommon are "common" and keep the direct shared-memory table, and the
+// rest are "rare": a database molecule's rare entries are kept in a separate
+// list per molecule and looked up in a small per-row-group hash of the rows'
+// rare vids.  Without a split ncommon == nvid.
+constexpr int kRareSlotsLog2 = 12;
+constexpr int kRareSlots = 1 << kRareSlotsLog2;   // per-group hash of the rows' rare vids
+constexpr int kRareRowMax = 96;                    // 32 rows x 96 <= 3/4 of the hash
 struct Vocab {
     unsigned long long* keys = nullptr;
     uint32_t* vid = nullptr;
     int64_t cap = 0;      // power of two
     int64_t nvid = 0;     // number of (code, level) pairs; vids are 1..nvid
+    int64_t ncommon = 0;  // vids 1..ncommon go to the shared-memory table
+    bool split = false;   // ncommon < nvid
 };
 
 // Database (query set) layout.  Molecules are cut into chunks of 32 (one
@@ -62,6 +74,11 @@ struct DbLayout {
     bool offsets = false;         // 4-byte entries hold byte offsets (vid * 4) into the table
     int2* crange = nullptr;       // [nchunks] {smallest, largest} magnitude of the chunk's molecules
     bool balanced = false;        // a chunk's entries spread evenly over its lanes (full-matrix layout)
+    // split vocabulary: the streamed entries are the common ones; slot s's
+    // rare vids are rare_vid[rare_off[s] .. rare_off[s + 1])
+    int64_t* rare_off = nullptr;  // [nchunks*32 + 1]
+    uint32_t* rare_vid = nullptr;
+    int64_t nrare = 0;
 };
 
 // Ref-set rows as vid lists (levels expanded, codes absent from the database
@@ -70,6 +87,7 @@ struct RowEntries {
     int64_t n = 0;
     int64_t stride = 0;
     uint32_t* vid = nullptr;
+    int64_t max_rare = 0;   // most rare-vid entries in one row (split vocabulary)
 };
 
 }  // namespace siml
@@ -164,6 +182,11 @@ int launch_neighbors(siml_engine* h, const NbrCall& c);
 // (order_len entries of order, rows_out output rows) are skipped and set
 // bit 2 of the asynchronous error word.
 int batch_nbr_usable(siml_engine* h, const DbLayout* d);
+// Whether a direct table of nvid vids fits in shared memory, and the number
+// of common vids a split vocabulary keeps (its table, the rare-vid hash and
+// the largest kernel extras then fit).
+bool direct_table_fits(siml_engine* h, int64_t nvid);
+int64_t split_table_capacity(siml_engine* h);
 int launch_batch_neighbors(siml_engine* h, const DbLayout* d, const int4* items, int64_t nitems, unsigned int* head,
                            const int32_t* order, int64_t order_len, const int4* rowinfo, int64_t rows_out, float lo,
                            float hi, int64_t pitch, int32_t* idx, float* sims, int32_t* counts, cudaStream_t st);

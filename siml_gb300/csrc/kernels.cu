@@ -72,7 +72,12 @@ struct GroupParams {
     const int4* meta;
     int64_t nchunks;
     int64_t chunk_begin, chunk_end;   // chunks this launch covers (a column range)
-    int vt_words;
+    int vt_words;             // words of the direct table (vids 0..ncommon)
+    int tab_words;            // vt_words + the rare-vid hash (2 * rare_slots words)
+    int64_t ncommon;          // vids above it are rare (split vocabulary)
+    int rare_slots;           // 0, or kRareSlots with a split vocabulary
+    const int64_t* rare_off;  // split vocabulary: slot s's rare vids are rare_vid[rare_off[s] ..
+    const uint32_t* rare_vid; //   rare_off[s + 1])
     int mode;
     const float* row_lo;      // per output row lower bound (per-row threshold search) or null
     const int* rows_dev;      // device row count bounding `rows` (row lists built on the device) or null
@@ -106,6 +111,54 @@ __device__ __forceinline__ int live_rows(const GroupParams& p) {
     return p.rows_dev ? min(p.rows, *p.rows_dev) : p.rows;
 }
 
+// Rare-vid hash of a row group (split vocabulary): kRareSlots keys (0 =
+// empty) after the direct table, then their 32-row masks.  Linear probing;
+// at most 32 x kRareRowMax keys, so it is never more than 3/4 full and every
+// probe sequence ends.
+__device__ __forceinline__ uint32_t rare_hash(uint32_t v) { return (v * 0x9E3779B1u) >> (32 - kRareSlotsLog2); }
+
+__device__ __forceinline__ void rare_insert(uint32_t* keys, uint32_t v, uint32_t bit) {
+    uint32_t h = rare_hash(v);
+    for (int probe = 0; probe < kRareSlots; probe++) {
+        const uint32_t prev = atomicCAS(&keys[h], 0u, v);
+        if (prev == 0u || prev == v) {
+            atomicOr(&keys[kRareSlots + h], bit);
+            return;
+        }
+        h = (h + 1) & (kRareSlots - 1);
+    }
+}
+
+__device__ __forceinline__ uint32_t rare_lookup(const uint32_t* keys, uint32_t v) {
+    uint32_t h = rare_hash(v);
+    for (int probe = 0; probe < kRareSlots; probe++) {
+        const uint32_t k = keys[h];
+        if (k == v) return keys[kRareSlots + h];
+        if (k == 0u) return 0u;
+        h = (h + 1) & (kRareSlots - 1);
+    }
+    return 0u;
+}
+
+// Sets a row's bit for one of its vids: the direct table, or the rare hash.
+__device__ __forceinline__ void table_set(uint32_t* T, const GroupParams& p, uint32_t v, uint32_t bit) {
+    if (v == 0u) return;
+    if ((int64_t)v <= p.ncommon) atomicOr(&T[v], bit);
+    else if (p.rare_slots) rare_insert(T + p.vt_words, v, bit);
+}
+
+// Adds the rare entries of layout slot `slot` (split vocabulary) to acc.
+template <int NP>
+__device__ __forceinline__ void rare_add(const uint32_t* T, const GroupParams& p, int64_t slot,
+                                         SlicedCounter<NP>& acc) {
+    const int64_t b = __ldg(p.rare_off + slot), e = __ldg(p.rare_off + slot + 1);
+    const uint32_t* keys = T + p.vt_words;
+    for (int64_t i = b; i < e; i++) {
+        const uint32_t m = rare_lookup(keys, __ldg(p.rare_vid + i));
+        if (m) acc.add1(m);
+    }
+}
+
 // Clears T, sets bit r of T[vid] for the entries of row r, fills RowSmem.
 // Returns the number of rows of the group.
 __device__ __forceinline__ int build_table(uint32_t* T, RowSmem& rs, const GroupParams& p) {
@@ -113,7 +166,7 @@ __device__ __forceinline__ int build_table(uint32_t* T, RowSmem& rs, const Group
     const int nwarps = blockDim.x >> 5;
     const int64_t row0 = (int64_t)blockIdx.x * 32;
     const int nr = min(32, live_rows(p) - (int)row0);
-    for (int i = threadIdx.x * 4; i < p.vt_words; i += blockDim.x * 4)
+    for (int i = threadIdx.x * 4; i < p.tab_words; i += blockDim.x * 4)
         *reinterpret_cast<uint4*>(T + i) = make_uint4(0u, 0u, 0u, 0u);
     if (warp == 0) {
         const int r = lane;
@@ -154,10 +207,7 @@ __device__ __forceinline__ int build_table(uint32_t* T, RowSmem& rs, const Group
     __syncthreads();
     for (int r = warp; r < nr; r += nwarps) {
         const uint32_t* rv = p.row_vid + (int64_t)(p.rowbase + rs.orow[r]) * p.row_stride;
-        for (int64_t e = lane; e < p.row_stride; e += 32) {
-            const uint32_t v = rv[e];
-            if (v && v < (uint32_t)p.vt_words) atomicOr(&T[v], 1u << r);
-        }
+        for (int64_t e = lane; e < p.row_stride; e += 32) table_set(T, p, rv[e], 1u << r);
     }
     __syncthreads();
     return nr;
@@ -216,7 +266,7 @@ __device__ __forceinline__ uint32_t tload(const uint32_t* T, uint32_t w) {
 // Streams the entries of chunks [wb, we) through the bit-sliced counter and
 // calls epi(chunk, meta, counter) at the end of each chunk.  All lanes of the
 // warp are in the same chunk at the same time.
-template <int NP, typename ET, class Epi>
+template <int NP, typename ET, bool RARE = false, class Epi>
 __device__ __forceinline__ void stream_chunks(const uint32_t* __restrict__ T, const GroupParams& p,
                                               int64_t wb, int64_t we, Epi& epi) {
     if (wb >= we) return;
@@ -248,6 +298,7 @@ __device__ __forceinline__ void stream_chunks(const uint32_t* __restrict__ T, co
     acc.clear();
     for (;;) {
         while (steps == 0) {
+            if constexpr (RARE) rare_add<NP>(T, p, c * 32 + lane, acc);
             epi(c, meta, acc);
             acc.clear();
             if (++c >= we) return;
@@ -295,12 +346,12 @@ __device__ __forceinline__ bool chunk_out_of_reach(int2 r, int amin, int amax, f
 // t >= lo for some row of the group (lo <= 0 or NaN: every chunk).  Chunks
 // are tested warp-uniformly; runs of reachable chunks are streamed whole.
 // Returns the number of chunks streamed.
-template <int NP, typename ET, class Epi>
+template <int NP, typename ET, bool RARE = false, class Epi>
 __device__ __forceinline__ int64_t stream_chunks_within(const uint32_t* __restrict__ T, const GroupParams& p,
                                                         const RowSmem& rs, int64_t wb, int64_t we, float lo,
                                                         Epi& epi) {
     if (!(lo > 0.0f) || p.crange == nullptr || rs.max_amag < 0) {
-        stream_chunks<NP, ET>(T, p, wb, we, epi);
+        stream_chunks<NP, ET, RARE>(T, p, wb, we, epi);
         return we > wb ? we - wb : 0;
     }
     const int amin = rs.min_amag, amax = rs.max_amag;
@@ -309,7 +360,7 @@ __device__ __forceinline__ int64_t stream_chunks_within(const uint32_t* __restri
         while (c < we && chunk_out_of_reach(p.crange[c], amin, amax, lo)) c++;
         int64_t e = c;
         while (e < we && !chunk_out_of_reach(p.crange[e], amin, amax, lo)) e++;
-        if (e > c) stream_chunks<NP, ET>(T, p, c, e, epi);
+        if (e > c) stream_chunks<NP, ET, RARE>(T, p, c, e, epi);
         streamed += e - c;
         c = e;
     }
@@ -328,7 +379,7 @@ __device__ __forceinline__ void cta_range(const GroupParams& p, int64_t& cb, int
 // `next` starts at the slice's first chunk (set before the table build's
 // barrier).
 constexpr int kGrab = 4;
-template <int NP, typename ET, class Epi>
+template <int NP, typename ET, bool RARE = false, class Epi>
 __device__ __forceinline__ void stream_dynamic(const uint32_t* __restrict__ T, const GroupParams& p,
                                                const RowSmem& rs, long long* next, int64_t ce, float lo, int nr,
                                                Epi& epi) {
@@ -339,7 +390,7 @@ __device__ __forceinline__ void stream_dynamic(const uint32_t* __restrict__ T, c
         if (lane == 0) c0 = atomicAdd(reinterpret_cast<unsigned long long*>(next), (unsigned long long)kGrab);
         c0 = __shfl_sync(0xFFFFFFFFu, c0, 0);
         if (c0 >= ce) break;
-        streamed += stream_chunks_within<NP, ET>(T, p, rs, c0, c0 + kGrab < ce ? c0 + kGrab : ce, lo, epi);
+        streamed += stream_chunks_within<NP, ET, RARE>(T, p, rs, c0, c0 + kGrab < ce ? c0 + kGrab : ce, lo, epi);
     }
     if (p.eval && lane == 0 && streamed > 0)
         atomicAdd(p.eval, (unsigned long long)streamed * 32ull * (unsigned long long)(nr > 0 ? nr : 0));
@@ -417,7 +468,7 @@ struct RowsEpi {
     }
 };
 
-template <int NP, typename ET>
+template <int NP, typename ET, bool RARE = false>
 __global__ void __launch_bounds__(kThreads, 1) k_rows(const GroupParams p, float* out, int64_t ldo) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
@@ -425,7 +476,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_rows(const GroupParams p, float
     int64_t wb, we;
     warp_range(p, wb, we);
     RowsEpi<NP> epi{rs, nr, p.mode, out + (int64_t)blockIdx.x * 32 * ldo, ldo};
-    stream_chunks<NP, ET>(T, p, wb, we, epi);
+    stream_chunks<NP, ET, RARE>(T, p, wb, we, epi);
 }
 
 // -------------------------------------------------------------- k_nbr ----
@@ -545,7 +596,7 @@ struct NbrEpi {
     }
 };
 
-template <int NP, typename ET>
+template <int NP, typename ET, bool RARE = false>
 __global__ void __launch_bounds__(kThreads, 1) k_nbr(const GroupParams p, const NbrArgs a) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
@@ -556,7 +607,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_nbr(const GroupParams p, const 
     if (threadIdx.x == 0) next = cb;
     const int nr = build_table(T, rs, p);   // synchronizes the block
     NbrEpi<NP> epi{rs, nr, (int64_t)blockIdx.x * 32, a};
-    stream_dynamic<NP, ET>(T, p, rs, &next, ce, a.thr_mode == 0 ? a.lo : 0.0f, nr, epi);
+    stream_dynamic<NP, ET, RARE>(T, p, rs, &next, ce, a.thr_mode == 0 ? a.lo : 0.0f, nr, epi);
 }
 
 // ---------------------------------------------------------- k_rows_bal ----
@@ -600,8 +651,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_rows_bal(const GroupParams p, f
     __shared__ RowSmem rs;
     const int nr = build_table(T, rs, p);   // synchronizes the block
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    uint32_t* pc = T + p.vt_words + (size_t)warp * NP * kPieceSlots;
-    int* pre = reinterpret_cast<int*>(T + p.vt_words + (size_t)nwarps * NP * kPieceSlots) + warp * kPrefixWords;
+    uint32_t* pc = T + p.tab_words + (size_t)warp * NP * kPieceSlots;
+    int* pre = reinterpret_cast<int*>(T + p.tab_words + (size_t)nwarps * NP * kPieceSlots) + warp * kPrefixWords;
     int64_t wb, we;
     warp_range(p, wb, we);
     constexpr int SPG = sizeof(ET) == 2 ? 1 : 2;
@@ -740,7 +791,7 @@ struct CollectEpi {
     }
 };
 
-template <int NP, typename ET>
+template <int NP, typename ET, bool RARE = false>
 __global__ void __launch_bounds__(kThreads, 1) k_collect(const GroupParams p, const CollectArgs c) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
@@ -755,7 +806,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_collect(const GroupParams p, co
     const int64_t row_stride = (int64_t)gridDim.y * c.seg_cap;
     CollectEpi<NP> epi{rs, nr, scount, c.cand_i + blockIdx.y * c.seg_cap, c.cand_t + blockIdx.y * c.seg_cap,
                        row_stride, c.seg_cap};
-    stream_dynamic<NP, ET>(T, p, rs, &next, ce, rs.min_lo, nr, epi);
+    stream_dynamic<NP, ET, RARE>(T, p, rs, &next, ce, rs.min_lo, nr, epi);
     __syncthreads();
     if (threadIdx.x < nr) c.seg_counts[(int64_t)rs.orow[threadIdx.x] * gridDim.y + blockIdx.y] = scount[threadIdx.x];
 }
@@ -826,7 +877,7 @@ struct HistEpi {
 };
 
 // out: GLOBAL ? uint64 [1000] (accumulated) : int32 [rows, ldo] (zeroed first)
-template <int NP, typename ET, bool GLOBAL>
+template <int NP, typename ET, bool GLOBAL, bool RARE = false>
 __global__ void __launch_bounds__(kThreads, 1) k_hist(const GroupParams p, void* out, int64_t ldo) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
@@ -838,7 +889,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_hist(const GroupParams p, void*
     if (threadIdx.x == 0) next = cb;
     const int nr = build_table(T, rs, p);   // synchronizes the block
     HistEpi<NP, GLOBAL> epi{rs, nr, H};
-    stream_dynamic<NP, ET>(T, p, rs, &next, ce, 0.0f, nr, epi);
+    stream_dynamic<NP, ET, RARE>(T, p, rs, &next, ce, 0.0f, nr, epi);
     __syncthreads();
     if (GLOBAL) {
         unsigned long long* o = reinterpret_cast<unsigned long long*>(out);
@@ -960,7 +1011,7 @@ struct LogHistFloorEpi {
 
 // out: int32 [rows, kLogBins], accumulated (zeroed by the caller).  FLOOR:
 // only pairs at or above the rows' floors (LogHistFloorEpi).
-template <int NP, typename ET, bool FLOOR>
+template <int NP, typename ET, bool FLOOR, bool RARE = false>
 __global__ void __launch_bounds__(kThreads, 1) k_loghist(const GroupParams p, int32_t* out) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
@@ -973,10 +1024,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_loghist(const GroupParams p, in
     const int nr = build_table(T, rs, p);   // synchronizes the block
     if constexpr (FLOOR) {
         LogHistFloorEpi<NP> epi{rs, nr, H};
-        stream_dynamic<NP, ET>(T, p, rs, &next, ce, rs.min_lo, nr, epi);
+        stream_dynamic<NP, ET, RARE>(T, p, rs, &next, ce, rs.min_lo, nr, epi);
     } else {
         LogHistEpi<NP> epi{rs, nr, H};
-        stream_dynamic<NP, ET>(T, p, rs, &next, ce, 0.0f, nr, epi);
+        stream_dynamic<NP, ET, RARE>(T, p, rs, &next, ce, 0.0f, nr, epi);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nr * kLogBins; i += blockDim.x) {
@@ -1200,13 +1251,13 @@ struct TopkEpi {
 };
 
 // scratch: float t[rows][splits][k] followed by int idx[rows][splits][k]
-template <int NP, typename ET>
+template <int NP, typename ET, bool RARE = false>
 __global__ void __launch_bounds__(kThreads, 1) k_topk(const GroupParams p, int k, float* part_t, int* part_i,
                                                       int* err) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
     __shared__ TopkSmem ts;
-    float* ht = reinterpret_cast<float*>(T + p.vt_words);
+    float* ht = reinterpret_cast<float*>(T + p.tab_words);
     int* hi = reinterpret_cast<int*>(ht + 32 * k);
     if (threadIdx.x < 32) {
         ts.lock[threadIdx.x] = 0;
@@ -1225,7 +1276,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_topk(const GroupParams p, int k
     const int64_t warm = (ce - cb) < want_warm ? (ce - cb) : want_warm;
     if ((threadIdx.x >> 5) == 0) {
         TopkWarmEpi<NP> we{rs, ts, ht, hi, nr, k};
-        stream_chunks<NP, ET>(T, p, cb, cb + warm, we);
+        stream_chunks<NP, ET, RARE>(T, p, cb, cb + warm, we);
         __syncwarp();
         if (threadIdx.x == 0) update_coef_min(ts, nr);
     }
@@ -1234,7 +1285,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_topk(const GroupParams p, int k
     const int64_t rb = cb + warm;
     const int64_t wb = rb + (ce - rb) * warp / nwarps, wend = rb + (ce - rb) * (warp + 1) / nwarps;
     TopkEpi<NP> epi{rs, ts, ht, hi, nr, k};
-    stream_chunks<NP, ET>(T, p, wb, wend, epi);
+    stream_chunks<NP, ET, RARE>(T, p, wb, wend, epi);
     __syncthreads();
     const int splits = gridDim.y;
     for (int i = threadIdx.x; i < nr * k; i += blockDim.x) {
@@ -1482,10 +1533,7 @@ __device__ __forceinline__ void set_rows(uint32_t* T, RowSmem& rs, const GroupPa
     }
     for (int r = warp; r < nr; r += nwarps) {
         const uint32_t* rv = p.row_vid + (int64_t)p.row_order[pos0 + r] * p.row_stride;
-        for (int64_t e = lane; e < p.row_stride; e += 32) {
-            const uint32_t v = rv[e];
-            if (v) atomicOr(&T[v], 1u << r);
-        }
+        for (int64_t e = lane; e < p.row_stride; e += 32) table_set(T, p, rv[e], 1u << r);
     }
 }
 
@@ -1495,12 +1543,15 @@ __device__ __forceinline__ void clear_rows(uint32_t* T, const GroupParams& p, in
         const uint32_t* rv = p.row_vid + (int64_t)p.row_order[pos0 + r] * p.row_stride;
         for (int64_t e = lane; e < p.row_stride; e += 32) {
             const uint32_t v = rv[e];
-            if (v && v < (uint32_t)p.vt_words) T[v] = 0u;
+            if (v && (int64_t)v <= p.ncommon) T[v] = 0u;
         }
     }
+    // the rare-vid hash is cleared whole
+    for (int i = p.vt_words + threadIdx.x * 4; i < p.tab_words; i += blockDim.x * 4)
+        *reinterpret_cast<uint4*>(T + i) = make_uint4(0u, 0u, 0u, 0u);
 }
 
-template <int NP, typename ET>
+template <int NP, typename ET, bool RARE = false>
 __global__ void __launch_bounds__(kThreads, 1) k_batch_nbr(const GroupParams p, const int4* __restrict__ items,
                                                            int64_t nitems, unsigned int* head, NbrArgs a,
                                                            const BatchLimits lim) {
@@ -1510,7 +1561,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_batch_nbr(const GroupParams p, 
     __shared__ long long cur_pos, cur_bias;
     __shared__ int cur_nr;
     __shared__ long long next;
-    for (int i = threadIdx.x * 4; i < p.vt_words; i += blockDim.x * 4)
+    for (int i = threadIdx.x * 4; i < p.tab_words; i += blockDim.x * 4)
         *reinterpret_cast<uint4*>(T + i) = make_uint4(0u, 0u, 0u, 0u);
     if (threadIdx.x == 0) { cur_pos = -1; cur_bias = 0; cur_nr = 0; }
     for (;;) {
@@ -1551,7 +1602,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_batch_nbr(const GroupParams p, 
         ai.col_begin = ia.w;
         ai.col_end = ib.x;
         NbrEpi<NP> epi{rs, nr, 0, ai};
-        stream_dynamic<NP, ET>(T, p, rs, &next, ib.z, ai.thr_mode == 0 ? ai.lo : 0.0f, nr, epi);
+        stream_dynamic<NP, ET, RARE>(T, p, rs, &next, ib.z, ai.thr_mode == 0 ? ai.lo : 0.0f, nr, epi);
         __syncthreads();
     }
 }
@@ -1817,12 +1868,18 @@ RawArgs raw_args(siml_engine* h, int64_t rowbase) {
     return m;
 }
 
-// Table kernels are usable when T fits in shared memory and 16-bit counters
-// suffice; fills p and the dynamic shared-memory size.
+// Table kernels are usable when T (and, with a split vocabulary, the rare-vid
+// hash) fits in shared memory, no ref row holds more rare entries than the
+// hash allows, and 16-bit counters suffice; fills p and the dynamic
+// shared-memory size.
 bool table_params(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t rows, int mode,
                   GroupParams& p, size_t& smem, int& np) {
-    const int vt_words = (int)((h->vocab.nvid + 1 + 3) / 4 * 4);
-    smem = (size_t)vt_words * 4;
+    const bool split = h->vocab.split;
+    if (split && (h->rows.max_rare > kRareRowMax || !d->rare_off)) return false;
+    const int vt_words = (int)((h->vocab.ncommon + 1 + 3) / 4 * 4);
+    const int rare_slots = split ? kRareSlots : 0;
+    const int tab_words = vt_words + 2 * rare_slots;
+    smem = (size_t)tab_words * 4;
     np = planes_needed(std::min(h->ref.max_entries, h->qry.max_entries));
     if (smem + sizeof(RowSmem) + 64 > h->smem_optin || np > 16) return false;
     np = np <= 8 ? 8 : 16;
@@ -1842,6 +1899,11 @@ bool table_params(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t ro
     p.chunk_begin = 0;
     p.chunk_end = d->nchunks;
     p.vt_words = vt_words;
+    p.tab_words = tab_words;
+    p.ncommon = h->vocab.ncommon;
+    p.rare_slots = rare_slots;
+    p.rare_off = split ? d->rare_off : nullptr;
+    p.rare_vid = split ? d->rare_vid : nullptr;
     p.mode = mode;
     p.row_lo = nullptr;
     p.rows_dev = nullptr;
@@ -1882,12 +1944,17 @@ int launch_rows_bal_t(siml_engine* h, const GroupParams& p, size_t smem, float* 
 template <int NP, typename ET>
 int launch_rows_t(siml_engine* h, const GroupParams& p, size_t smem, float* out, int64_t ldo) {
     const int64_t groups = (p.rows + 31) / 32;
-    int rc = set_smem(k_rows<NP, ET>, smem);
+    auto kern = k_rows<NP, ET, false>;
+    if (p.rare_slots) {
+        if constexpr (std::is_same<ET, uint16_t>::value) kern = k_rows<NP, ET, true>;
+        else return fail(SIML_ERR_UNSUPPORTED, "a split vocabulary needs 16-bit entries");
+    }
+    int rc = set_smem(kern, smem);
     if (rc) return rc;
     const int s = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
     dim3 grid((unsigned)groups, (unsigned)s);
     SIML_CUDA(mark(h, h->ev0));
-    k_rows<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, out, ldo);
+    kern<<<grid, kThreads, smem, h->stream>>>(p, out, ldo);
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
@@ -1898,12 +1965,17 @@ int launch_rows_t(siml_engine* h, const GroupParams& p, size_t smem, float* out,
 template <int NP, typename ET>
 int launch_nbr_t(siml_engine* h, const GroupParams& p, size_t smem, const NbrArgs& a) {
     const int64_t groups = (p.rows + 31) / 32;
-    int rc = set_smem(k_nbr<NP, ET>, smem);
+    auto kern = k_nbr<NP, ET, false>;
+    if (p.rare_slots) {
+        if constexpr (std::is_same<ET, uint16_t>::value) kern = k_nbr<NP, ET, true>;
+        else return fail(SIML_ERR_UNSUPPORTED, "a split vocabulary needs 16-bit entries");
+    }
+    int rc = set_smem(kern, smem);
     if (rc) return rc;
     const int s = choose_splits(groups, p.chunk_end - p.chunk_begin, h->num_sms, kThreads / 32);
     dim3 grid((unsigned)groups, (unsigned)s);
     SIML_CUDA(mark(h, h->ev0));
-    k_nbr<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, a);
+    kern<<<grid, kThreads, smem, h->stream>>>(p, a);
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
@@ -1914,12 +1986,17 @@ int launch_nbr_t(siml_engine* h, const GroupParams& p, size_t smem, const NbrArg
 template <int NP, typename ET, bool GLOBAL>
 int launch_hist_t(siml_engine* h, const GroupParams& p, size_t smem, void* out, int64_t ldo) {
     const int64_t groups = (p.rows + 31) / 32;
-    int rc = set_smem(k_hist<NP, ET, GLOBAL>, smem);
+    auto kern = k_hist<NP, ET, GLOBAL, false>;
+    if (p.rare_slots) {
+        if constexpr (std::is_same<ET, uint16_t>::value) kern = k_hist<NP, ET, GLOBAL, true>;
+        else return fail(SIML_ERR_UNSUPPORTED, "a split vocabulary needs 16-bit entries");
+    }
+    int rc = set_smem(kern, smem);
     if (rc) return rc;
     const int s = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
     dim3 grid((unsigned)groups, (unsigned)s);
     SIML_CUDA(mark(h, h->ev0));
-    k_hist<NP, ET, GLOBAL><<<grid, kThreads, smem, h->stream>>>(p, out, ldo);
+    kern<<<grid, kThreads, smem, h->stream>>>(p, out, ldo);
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
@@ -1930,11 +2007,16 @@ int launch_hist_t(siml_engine* h, const GroupParams& p, size_t smem, void* out, 
 template <int NP, typename ET>
 int launch_topk_t(siml_engine* h, const GroupParams& p, size_t smem, int k, int splits, float* pt, int* pi) {
     const int64_t groups = (p.rows + 31) / 32;
-    int rc = set_smem(k_topk<NP, ET>, smem);
+    auto kern = k_topk<NP, ET, false>;
+    if (p.rare_slots) {
+        if constexpr (std::is_same<ET, uint16_t>::value) kern = k_topk<NP, ET, true>;
+        else return fail(SIML_ERR_UNSUPPORTED, "a split vocabulary needs 16-bit entries");
+    }
+    int rc = set_smem(kern, smem);
     if (rc) return rc;
     dim3 grid((unsigned)groups, (unsigned)splits);
     SIML_CUDA(mark(h, h->ev0));
-    k_topk<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, k, pt, pi, h->d_async_err);
+    kern<<<grid, kThreads, smem, h->stream>>>(p, k, pt, pi, h->d_async_err);
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
@@ -1945,17 +2027,35 @@ int launch_topk_t(siml_engine* h, const GroupParams& p, size_t smem, int k, int 
 template <int NP, typename ET>
 int launch_batch_t(siml_engine* h, const GroupParams& p, size_t smem, const int4* items, int64_t nitems,
                    unsigned int* head, const NbrArgs& a, const BatchLimits& lim, cudaStream_t st) {
-    int rc = set_smem(k_batch_nbr<NP, ET>, smem);
+    auto kern = k_batch_nbr<NP, ET, false>;
+    if (p.rare_slots) {
+        if constexpr (std::is_same<ET, uint16_t>::value) kern = k_batch_nbr<NP, ET, true>;
+        else return fail(SIML_ERR_UNSUPPORTED, "a split vocabulary needs 16-bit entries");
+    }
+    int rc = set_smem(kern, smem);
     if (rc) return rc;
-    k_batch_nbr<NP, ET><<<(unsigned)h->num_sms, kThreads, smem, st>>>(p, items, nitems, head, a, lim);
+    kern<<<(unsigned)h->num_sms, kThreads, smem, st>>>(p, items, nitems, head, a, lim);
     SIML_CUDA(cudaGetLastError());
     return SIML_OK;
 }
 
 }  // namespace
 
+bool direct_table_fits(siml_engine* h, int64_t nvid) {
+    return (size_t)((nvid + 1 + 3) / 4 * 4) * 4 + sizeof(RowSmem) + 64 <= h->smem_optin;
+}
+
+int64_t split_table_capacity(siml_engine* h) {
+    // room for the rare-vid hash and the largest per-kernel extra (the
+    // sample histogram of top-k), with a margin for static shared memory
+    const int64_t extra = (int64_t)kRareSlots * 8 + 32 * kLogWords * 4 + (int64_t)sizeof(RowSmem) + 2048;
+    const int64_t words = ((int64_t)h->smem_optin - extra) / 4;
+    return std::max<int64_t>(0, words / 4 * 4 - 4);   // (ncommon + 1) rounded up to 4 stays <= words
+}
+
 bool rows_balanced_fits(siml_engine* h) {
-    const int vt_words = (int)((h->vocab.nvid + 1 + 3) / 4 * 4);
+    if (h->vocab.split) return false;
+    const int vt_words = (int)((h->vocab.ncommon + 1 + 3) / 4 * 4);
     const int np = planes_needed(std::min(h->ref.max_entries, h->qry.max_entries)) <= 8 ? 8 : 16;
     return (size_t)vt_words * 4 + rows_bal_extra_smem(np, kThreads / 32) + sizeof(RowSmem) + 64 <= h->smem_optin;
 }
@@ -2083,10 +2183,15 @@ struct TimingHold {
 
 template <int NP, typename ET>
 int launch_collect_t(siml_engine* h, const GroupParams& p, size_t smem, int splits, const CollectArgs& c) {
-    int rc = set_smem(k_collect<NP, ET>, smem);
+    auto kern = k_collect<NP, ET, false>;
+    if (p.rare_slots) {
+        if constexpr (std::is_same<ET, uint16_t>::value) kern = k_collect<NP, ET, true>;
+        else return fail(SIML_ERR_UNSUPPORTED, "a split vocabulary needs 16-bit entries");
+    }
+    int rc = set_smem(kern, smem);
     if (rc) return rc;
     dim3 grid((unsigned)((p.rows + 31) / 32), (unsigned)splits);
-    k_collect<NP, ET><<<grid, kThreads, smem, h->stream>>>(p, c);
+    kern<<<grid, kThreads, smem, h->stream>>>(p, c);
     SIML_CUDA(cudaGetLastError());
     h->launches++;
     return SIML_OK;
@@ -2144,14 +2249,16 @@ int topk_collect_block(siml_engine* h, const DbLayout* d, int64_t r0, int64_t ro
         int hs = choose_splits(groups, nch, h->num_sms, kThreads / 32);
         hs = (int)std::max<int64_t>(hs, (nch * 32 + 65534) / 65535);   // <= 65,535 molecules per CTA
         dim3 grid((unsigned)groups, (unsigned)hs);
-        int rc2;
-        if (floor) {
-            if ((rc2 = set_smem(k_loghist<NP, ET, true>, smem))) return rc2;
-            k_loghist<NP, ET, true><<<grid, kThreads, smem, h->stream>>>(g, hist);
-        } else {
-            if ((rc2 = set_smem(k_loghist<NP, ET, false>, smem))) return rc2;
-            k_loghist<NP, ET, false><<<grid, kThreads, smem, h->stream>>>(g, hist);
+        auto kern = floor ? k_loghist<NP, ET, true, false> : k_loghist<NP, ET, false, false>;
+        if (g.rare_slots) {
+            if constexpr (std::is_same<ET, uint16_t>::value)
+                kern = floor ? k_loghist<NP, ET, true, true> : k_loghist<NP, ET, false, true>;
+            else
+                return fail(SIML_ERR_UNSUPPORTED, "a split vocabulary needs 16-bit entries");
         }
+        int rc2;
+        if ((rc2 = set_smem(kern, smem))) return rc2;
+        kern<<<grid, kThreads, smem, h->stream>>>(g, hist);
         SIML_CUDA(cudaGetLastError());
         k_topk_theta<<<(unsigned)((rows + 7) / 8), 256, 0, h->stream>>>(hist, k, rows, row_lo, list_n);
         SIML_CUDA(cudaGetLastError());

@@ -55,6 +55,16 @@ struct SlicedCounter {
         }
     }
 
+    // add one 32-row mask
+    SIML_HD void add1(uint32_t m) {
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            const uint32_t t = plane[p] & m;
+            plane[p] ^= m;
+            m = t;
+        }
+    }
+
     // add eight 32-row masks (each contributes 1 to every row whose bit is set)
     SIML_HD void add8(uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3,
                       uint32_t m4, uint32_t m5, uint32_t m6, uint32_t m7) {
