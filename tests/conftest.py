@@ -1,5 +1,5 @@
 """Shared fixtures.  Tests marked ``gpu`` need a CUDA GPU (GB300); everything
-else runs on the CPU.  The oracle (oracle/) is used only as the checker."""
+else runs on the CPU.  The oracle (oracle/) only computes the expected results."""
 import os
 import sys
 
