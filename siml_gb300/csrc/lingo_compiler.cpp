@@ -64,6 +64,14 @@ bool check_args(const char* buf, const int64_t* offsets, int64_t n) {
     return true;
 }
 
+// Strings per task: large batches in 1,024-string tasks; small ones (a
+// request of a few hundred SMILES) split over a few threads, each with at
+// least 128 strings so thread start-up stays small against the work.
+int64_t chunk_of(int64_t n) {
+    const int64_t per = (n + 2 * siml::host_threads() - 1) / (2 * siml::host_threads());
+    return std::max<int64_t>(128, std::min<int64_t>(1024, per));
+}
+
 }  // namespace
 
 extern "C" {
@@ -72,7 +80,7 @@ int64_t siml_compile_width(const char* buf, const int64_t* offsets, int64_t n) {
     siml::clear_error();
     if (!check_args(buf, offsets, n)) return -siml::fail(SIML_ERR_INVALID, "siml_compile_width: bad offsets");
     // chunked so each thread keeps one Bag
-    const int64_t chunk = 1024;
+    const int64_t chunk = chunk_of(n);
     const int64_t nchunks = (n + chunk - 1) / chunk;
     std::vector<int64_t> chunk_max((size_t)nchunks, 0);
     siml::parallel_for(nchunks, [&](int64_t c) {
@@ -97,7 +105,7 @@ int siml_compile_smiles(const char* buf, const int64_t* offsets, int64_t n,
     if (!check_args(buf, offsets, n) || width < 0 ||
         (n > 0 && (!lingos || !counts || !lengths || !mags)))
         return siml::fail(SIML_ERR_INVALID, "siml_compile_smiles: bad arguments");
-    const int64_t chunk = 1024;
+    const int64_t chunk = chunk_of(n);
     const int64_t nchunks = (n + chunk - 1) / chunk;
     std::atomic<int> overflow{0};
     siml::parallel_for(nchunks, [&](int64_t c) {

@@ -51,7 +51,7 @@ class Request:
     ascending index order; `t_done - arrival` is the latency in seconds."""
 
     __slots__ = ("rid", "smiles", "kind", "k", "lo", "arrival", "t_admit", "t_done", "result", "error", "done",
-                 "rows")
+                 "rows", "compiled")
 
     def __init__(self, rid, smiles, kind=TOPK, k=50, lo=0.75, arrival=None):
         if kind not in (TOPK, THRESHOLD):
@@ -68,6 +68,7 @@ class Request:
         self.error = None
         self.done = threading.Event()
         self.rows = len(self.smiles)
+        self.compiled = None   # (lingos, counts, lengths, mags) once compiled
 
     def latency(self):
         return None if self.t_done is None else self.t_done - self.arrival
@@ -75,20 +76,21 @@ class Request:
 
 def compile_into(smiles, L, C, ln, mg, width):
     """Compiles SMILES into the first len(smiles) rows of preallocated
-    [*, width] arrays; returns the widest molecule's LINGO count."""
+    [*, width] arrays in one pass (ValueError when a molecule has more unique
+    LINGOs than width)."""
     n = len(smiles)
     off = np.zeros(n + 1, dtype=np.int64)
     np.cumsum([len(s) for s in smiles], out=off[1:])
     buf = b"".join(smiles) or b"\0"
     lib = N.lib()
-    w = lib.siml_compile_width(buf, off.ctypes.data, n)
-    if w < 0:
-        N.check(int(-w), "siml_compile_width")
-    if w > width:
-        raise ValueError("a query molecule has %d unique LINGOs, more than the server's width %d" % (w, width))
-    N.check(lib.siml_compile_smiles(buf, off.ctypes.data, n, L.ctypes.data, C.ctypes.data, ln.ctypes.data,
-                                    mg.ctypes.data, width), "siml_compile_smiles")
-    return w
+    rc = lib.siml_compile_smiles(buf, off.ctypes.data, n, L.ctypes.data, C.ctypes.data, ln.ctypes.data,
+                                 mg.ctypes.data, width)
+    if rc != N.SIML_OK:
+        msg = N.last_error()
+        w = lib.siml_compile_width(buf, off.ctypes.data, n)
+        if w > width:
+            raise ValueError("a query molecule has %d unique LINGOs, more than the server's width %d" % (w, width))
+        raise ValueError(msg or "siml_compile_smiles failed")
 
 
 class _Region:
@@ -199,10 +201,21 @@ class LingoServer:
             raise ValueError("k must be in [1, %d]" % self.cfg.kmax)
         if req.kind == THRESHOLD and req.lo != self.cfg.lo:
             raise ValueError("threshold requests use the server's bound %g" % self.cfg.lo)
+        # compiled in the caller's thread: a malformed request is refused here
+        # and never reaches a batch, and the batcher only copies rows
+        self._compile(req)
         with self.cv:
             self.queue.append(req)
             self.cv.notify()
         return req
+
+    def _compile(self, req):
+        if req.compiled is None:
+            W = self.cfg.width
+            arrays = (np.empty((req.rows, W), np.int32), np.empty((req.rows, W), np.int32),
+                      np.empty(req.rows, np.int32), np.empty(req.rows, np.int32))
+            compile_into(req.smiles, *arrays, W)
+            req.compiled = arrays
 
     # ------------------------------------------------------------- batcher
     def _take_batch(self):
@@ -264,7 +277,13 @@ class LingoServer:
         row = 0
         for r in thr + tk:
             r.t_admit = now
-            compile_into(r.smiles, L[row:], C[row:], ln[row:], mg[row:], cfg.width)
+            self._compile(r)
+            cL, cC, cln, cmg = r.compiled
+            L[row:row + r.rows] = cL
+            C[row:row + r.rows] = cC
+            ln[row:row + r.rows] = cln
+            mg[row:row + r.rows] = cmg
+            r.compiled = None
             row += r.rows
         with self.elock:
             return self._queue(batch, thr, tk, nt, nk, kmax, region)
