@@ -103,6 +103,9 @@ def test_serving_admission_limits(native):
         srv.submit(Request(0, smi, kind="topk", k=8))        # more rows than a batch
     with pytest.raises(ValueError):
         srv.submit(Request(1, smi[:3], kind="topk", k=9))    # k above kmax
+    wide = bytes(np.random.default_rng(4).choice(np.frombuffer(b"CNOSPFcnosp()=#[]", np.uint8), 400))
+    with pytest.raises(ValueError):
+        srv.submit(Request(2, [smi[0], wide], kind="topk", k=8))   # more unique LINGOs than the rows hold
     reqs = [Request(i, smi[i:i + 5], kind="topk", k=8) for i in range(6)]
     srv.start()
     for r in reqs:
