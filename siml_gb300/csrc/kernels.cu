@@ -378,7 +378,11 @@ __device__ __forceinline__ void cta_range(const GroupParams& p, int64_t& cb, int
 // warp slowed by candidates or skipped chunks does not hold the CTA back.
 // `next` starts at the slice's first chunk (set before the table build's
 // barrier).
+// Near the end of the range (fewer than kGrabTail chunks left, read without
+// synchronization as a hint) warps take one chunk at a time, so they reach
+// the CTA's next barrier at nearly the same time.
 constexpr int kGrab = 4;
+constexpr long long kGrabTail = kGrab * (kThreads / 32);
 template <int NP, typename ET, bool RARE = false, class Epi>
 __device__ __forceinline__ void stream_dynamic(const uint32_t* __restrict__ T, const GroupParams& p,
                                                const RowSmem& rs, long long* next, int64_t ce, float lo, int nr,
@@ -386,11 +390,15 @@ __device__ __forceinline__ void stream_dynamic(const uint32_t* __restrict__ T, c
     const int lane = threadIdx.x & 31;
     int64_t streamed = 0;
     for (;;) {
-        long long c0 = 0;
-        if (lane == 0) c0 = atomicAdd(reinterpret_cast<unsigned long long*>(next), (unsigned long long)kGrab);
+        long long c0 = 0, g = kGrab;
+        if (lane == 0) {
+            g = ce - *reinterpret_cast<volatile long long*>(next) > kGrabTail ? kGrab : 1;
+            c0 = atomicAdd(reinterpret_cast<unsigned long long*>(next), (unsigned long long)g);
+        }
         c0 = __shfl_sync(0xFFFFFFFFu, c0, 0);
+        g = __shfl_sync(0xFFFFFFFFu, g, 0);
         if (c0 >= ce) break;
-        streamed += stream_chunks_within<NP, ET, RARE>(T, p, rs, c0, c0 + kGrab < ce ? c0 + kGrab : ce, lo, epi);
+        streamed += stream_chunks_within<NP, ET, RARE>(T, p, rs, c0, c0 + g < ce ? c0 + g : ce, lo, epi);
     }
     if (p.eval && lane == 0 && streamed > 0)
         atomicAdd(p.eval, (unsigned long long)streamed * 32ull * (unsigned long long)(nr > 0 ? nr : 0));
