@@ -450,7 +450,7 @@ __global__ void k_fill_entries(const int32_t* __restrict__ lingos, const int32_t
     const int64_t c = slot >> 5;
     const int lane = (int)(slot & 31);
     int32_t P = 0, Ls = 1;
-    if (balanced) {   // never with a split vocabulary
+    if (balanced) {   // cmag: the streamed entries of each molecule
         const int32_t g = m >= 0 ? (cmag[m] + 7) / 8 : 0;
         int32_t incl = g;
         for (int o = 1; o < 32; o <<= 1) {
@@ -491,10 +491,11 @@ __global__ void k_row_entries(const int32_t* __restrict__ lingos, const int32_t*
                               const int32_t* __restrict__ len, int64_t n, int64_t width,
                               const unsigned long long* __restrict__ keys,
                               const uint32_t* __restrict__ vid, int64_t cap,
-                              uint32_t* __restrict__ out, int64_t stride, int64_t ncommon, int* max_rare) {
+                              uint32_t* __restrict__ out, int64_t stride, int64_t ncommon, int64_t ncommon_bal,
+                              int* max_rare) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
-    int nrare = 0;
+    int nrare = 0, nrare_bal = 0;
     const int32_t L = len[r];
     const int32_t* lr = lingos + r * width;
     const int32_t* cr = counts + r * width;
@@ -507,10 +508,12 @@ __global__ void k_row_entries(const int32_t* __restrict__ lingos, const int32_t*
             if (v == 0u) break;   // higher levels of an absent pair are absent too
             o[e++] = v;
             nrare += (int64_t)v > ncommon;
+            nrare_bal += (int64_t)v > ncommon_bal;
         }
     }
     for (; e < stride; e++) o[e] = 0u;
     if (nrare) atomicMax(max_rare, nrare);
+    if (nrare_bal) atomicMax(max_rare + 1, nrare_bal);
 }
 
 // ------------------------------------------------------------ host helpers --
@@ -569,6 +572,12 @@ int upload_set(siml_engine* h, RawSet& s, const int32_t* lingos, const int32_t* 
 }
 
 int split_vocab(siml_engine* h, int64_t ncommon);
+
+// Common vids of the balanced full-matrix layout: the vocabulary's, or
+// fewer with a split vocabulary (room for the piece buffers).
+int64_t balanced_ncommon(siml_engine* h) {
+    return h->vocab.split ? std::min<int64_t>(h->vocab.ncommon, split_balanced_capacity(h)) : h->vocab.ncommon;
+}
 
 int build_vocab(siml_engine* h) {
     free_vocab(h->vocab);
@@ -684,21 +693,19 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     free_layout(d);
     const RawSet& q = h->qry;
     cudaStream_t st = h->stream;
-    const bool split = h->vocab.split;
+    const bool vsplit = h->vocab.split;
     d.n = q.n;
     d.sorted = sorted;
     d.window = sorted ? h->sorted_window : h->rows_window;
-    d.entry_bytes = h->vocab.ncommon < 65535 ? 2 : 4;
-    d.offsets = false;
-    if (!split && !sorted && h->rows_entries == SIML_ENTRIES_U32) d.entry_bytes = 4;
-    if (!split && !sorted && h->rows_entries == SIML_ENTRIES_OFFSETS) {
-        d.entry_bytes = 4;
-        d.offsets = true;
-    }
-    // decided after the entry format: the balanced kernel reads vids, not byte
-    // offsets, and has no rare-entry pass
-    d.balanced = !split && !sorted && h->rows_window == kChunk && h->rows_layout == SIML_ROWS_BALANCED &&
-                 !d.offsets && rows_balanced_fits(h);
+    d.offsets = !vsplit && !sorted && h->rows_entries == SIML_ENTRIES_OFFSETS;
+    // the balanced kernel reads vids, not byte offsets; with a split
+    // vocabulary its piece buffers leave room for fewer common vids
+    d.balanced = !sorted && h->rows_window == kChunk && h->rows_layout == SIML_ROWS_BALANCED && !d.offsets &&
+                 rows_balanced_fits(h);
+    d.ncommon = vsplit && d.balanced ? balanced_ncommon(h) : h->vocab.ncommon;
+    const bool split = d.ncommon < h->vocab.nvid;
+    d.entry_bytes = d.ncommon < 65535 ? 2 : 4;
+    if (!vsplit && !sorted && (h->rows_entries == SIML_ENTRIES_U32 || d.offsets)) d.entry_bytes = 4;
     const int64_t nwin = (q.n + d.window - 1) / d.window;
     d.nchunks = (q.n + kChunk - 1) / kChunk;
     const int64_t slots = std::max<int64_t>(nwin, 1) * d.window;
@@ -718,7 +725,7 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
         SIML_CUDA(cudaMalloc(&t_cc.p, (size_t)q.n * 4));
         SIML_CUDA(cudaMalloc(&t_rc.p, (size_t)q.n * 4));
         k_split_count<<<(unsigned)((q.n + 255) / 256), 256, 0, st>>>(
-            q.lingos, q.counts, q.len, q.n, q.width, h->vocab.keys, h->vocab.vid, h->vocab.cap, h->vocab.ncommon,
+            q.lingos, q.counts, q.len, q.n, q.width, h->vocab.keys, h->vocab.vid, h->vocab.cap, d.ncommon,
             (int32_t*)t_cc.p, (int32_t*)t_rc.p);
         h->launches++;
         SIML_CUDA(cudaGetLastError());
@@ -781,14 +788,14 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     SIML_CUDA(cudaMemsetAsync(d.entries, 0, (size_t)std::max<int64_t>(acc, 1) * 16, st));
     const unsigned grid = (unsigned)((d.nchunks * 32 + 255) / 256);
     const int bal = d.balanced ? 1 : 0;
-    const int64_t ncommon = h->vocab.ncommon;
+    const int64_t ncommon = d.ncommon;
     if (d.entry_bytes == 2)
-        k_fill_entries<uint16_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.cmag, q.width, d.perm, d.off,
+        k_fill_entries<uint16_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, scount, q.width, d.perm, d.off,
                                                        d.ng, d.nchunks, bal, h->vocab.keys, h->vocab.vid,
                                                        h->vocab.cap, 0, (uint16_t*)d.entries, ncommon,
                                                        d.rare_off, d.rare_vid);
     else
-        k_fill_entries<uint32_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, q.cmag, q.width, d.perm, d.off,
+        k_fill_entries<uint32_t><<<grid, 256, 0, st>>>(q.lingos, q.counts, q.len, scount, q.width, d.perm, d.off,
                                                        d.ng, d.nchunks, bal, h->vocab.keys, h->vocab.vid,
                                                        h->vocab.cap, d.offsets ? 2 : 0, (uint32_t*)d.entries,
                                                        ncommon, d.rare_off, d.rare_vid);
@@ -806,18 +813,20 @@ int build_rows(siml_engine* h) {
     re.stride = std::max<int64_t>(std::max<int64_t>(1, r.max_entries), h->row_stride_hint);
     int rc;
     if ((rc = dev_alloc(&re.vid, (size_t)(std::max<int64_t>(r.n, 1) * re.stride)))) return rc;
-    int max_rare = 0;
+    int max_rare[2] = {0, 0};   // against the vocabulary's common set and the balanced layout's
+    int* d_max = reinterpret_cast<int*>(h->d_counter);
     if (r.n > 0) {
-        SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+        SIML_CUDA(cudaMemsetAsync(d_max, 0, 2 * sizeof(int), h->stream));
         k_row_entries<<<(unsigned)((r.n + 127) / 128), 128, 0, h->stream>>>(
             r.lingos, r.counts, r.len, r.n, r.width, h->vocab.keys, h->vocab.vid, h->vocab.cap, re.vid, re.stride,
-            h->vocab.ncommon, h->d_err);
+            h->vocab.ncommon, balanced_ncommon(h), d_max);
         h->launches++;
         SIML_CUDA(cudaGetLastError());
-        SIML_CUDA(cudaMemcpyAsync(&max_rare, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        SIML_CUDA(cudaMemcpyAsync(max_rare, d_max, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     }
     SIML_CUDA(cudaStreamSynchronize(h->stream));
-    re.max_rare = max_rare;
+    re.max_rare = max_rare[0];
+    re.max_rare_bal = max_rare[1];
     return SIML_OK;
 }
 
@@ -1048,18 +1057,21 @@ int siml_write_ref_rows(siml_engine* h, int64_t row0, const int32_t* lingos, con
             // with a split vocabulary the rows' rare-entry maximum decides
             // whether the table kernels may run, so it is read back (a
             // stream synchronization only for split vocabularies)
-            if (h->vocab.split) SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), st));
+            int* d_max = reinterpret_cast<int*>(h->d_counter);
+            if (h->vocab.split) SIML_CUDA(cudaMemsetAsync(d_max, 0, 2 * sizeof(int), st));
             k_row_entries<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(dl, dc, s.len + row0, n, s.width,
                                                                        h->vocab.keys, h->vocab.vid, h->vocab.cap,
                                                                        h->rows.vid + row0 * h->rows.stride,
-                                                                       h->rows.stride, h->vocab.ncommon, h->d_err);
+                                                                       h->rows.stride, h->vocab.ncommon,
+                                                                       balanced_ncommon(h), d_max);
             h->launches++;
             SIML_CUDA(cudaGetLastError());
             if (h->vocab.split) {
-                int mr = 0;
-                SIML_CUDA(cudaMemcpyAsync(&mr, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+                int mr[2] = {0, 0};
+                SIML_CUDA(cudaMemcpyAsync(mr, d_max, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
                 SIML_CUDA(cudaStreamSynchronize(st));
-                h->rows.max_rare = std::max<int64_t>(h->rows.max_rare, mr);
+                h->rows.max_rare = std::max<int64_t>(h->rows.max_rare, mr[0]);
+                h->rows.max_rare_bal = std::max<int64_t>(h->rows.max_rare_bal, mr[1]);
             }
         }
     }

@@ -79,6 +79,7 @@ struct DbLayout {
     int64_t* rare_off = nullptr;  // [nchunks*32 + 1]
     uint32_t* rare_vid = nullptr;
     int64_t nrare = 0;
+    int64_t ncommon = 0;          // vids the layout streams (<= the vocabulary's ncommon)
 };
 
 // Ref-set rows as vid lists (levels expanded, codes absent from the database
@@ -87,7 +88,8 @@ struct RowEntries {
     int64_t n = 0;
     int64_t stride = 0;
     uint32_t* vid = nullptr;
-    int64_t max_rare = 0;   // most rare-vid entries in one row (split vocabulary)
+    int64_t max_rare = 0;      // most rare-vid entries in one row (split vocabulary)
+    int64_t max_rare_bal = 0;  // the same against the balanced layout's smaller common set
 };
 
 }  // namespace siml
@@ -187,6 +189,9 @@ int batch_nbr_usable(siml_engine* h, const DbLayout* d);
 // the largest kernel extras then fit).
 bool direct_table_fits(siml_engine* h, int64_t nvid);
 int64_t split_table_capacity(siml_engine* h);
+// Common vids of the balanced full-matrix layout with a split vocabulary
+// (its table, the rare-vid hash and the per-warp piece buffers fit).
+int64_t split_balanced_capacity(siml_engine* h);
 int launch_batch_neighbors(siml_engine* h, const DbLayout* d, const int4* items, int64_t nitems, unsigned int* head,
                            const int32_t* order, int64_t order_len, const int4* rowinfo, int64_t rows_out, float lo,
                            float hi, int64_t pitch, int32_t* idx, float* sims, int32_t* counts, cudaStream_t st);

@@ -653,7 +653,7 @@ __device__ __forceinline__ void piece_add(SlicedCounter<NP>& acc, const uint32_t
     }
 }
 
-template <int NP, typename ET>
+template <int NP, typename ET, bool RARE = false>
 __global__ void __launch_bounds__(kThreads, 1) k_rows_bal(const GroupParams p, float* out, int64_t ldo) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
@@ -675,7 +675,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_rows_bal(const GroupParams p, f
         const int L = __ldg(p.ng + c) / SPG;   // steps per lane
         if (lane == 0 && c + 1 < we)
             prefetch_l2(Eb + __ldg(p.off + c + 1) * 16, (uint32_t)__ldg(p.ng + c + 1) * 512u);
-        const int g = meta.x >= 0 ? (meta.z + 7) >> 3 : 0;
+        int es = meta.z;   // streamed entries: all, or the common ones (split vocabulary)
+        if constexpr (RARE) {
+            if (meta.x >= 0) es -= (int)(__ldg(p.rare_off + c * 32 + lane + 1) - __ldg(p.rare_off + c * 32 + lane));
+        }
+        const int g = meta.x >= 0 ? (es + 7) >> 3 : 0;
         int incl = g;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -732,6 +736,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_rows_bal(const GroupParams p, f
             const int fl = P / L, ll = (P + g - 1) / L;
             for (int j = fl; j <= ll; j++) piece_add<NP>(own, pc, j + lane);
         }
+        if constexpr (RARE) rare_add<NP>(T, p, c * 32 + lane, own);
         epi(c, meta, own);
         __syncwarp();   // pieces and prefix are rewritten for the next chunk
     }
@@ -1882,9 +1887,10 @@ RawArgs raw_args(siml_engine* h, int64_t rowbase) {
 // shared-memory size.
 bool table_params(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t rows, int mode,
                   GroupParams& p, size_t& smem, int& np) {
-    const bool split = h->vocab.split;
-    if (split && (h->rows.max_rare > kRareRowMax || !d->rare_off)) return false;
-    const int vt_words = (int)((h->vocab.ncommon + 1 + 3) / 4 * 4);
+    const bool split = d->ncommon < h->vocab.nvid;
+    const int64_t max_rare = d->ncommon < h->vocab.ncommon ? h->rows.max_rare_bal : h->rows.max_rare;
+    if (split && (max_rare > kRareRowMax || !d->rare_off)) return false;
+    const int vt_words = (int)((d->ncommon + 1 + 3) / 4 * 4);
     const int rare_slots = split ? kRareSlots : 0;
     const int tab_words = vt_words + 2 * rare_slots;
     smem = (size_t)tab_words * 4;
@@ -1908,7 +1914,7 @@ bool table_params(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t ro
     p.chunk_end = d->nchunks;
     p.vt_words = vt_words;
     p.tab_words = tab_words;
-    p.ncommon = h->vocab.ncommon;
+    p.ncommon = d->ncommon;
     p.rare_slots = rare_slots;
     p.rare_off = split ? d->rare_off : nullptr;
     p.rare_vid = split ? d->rare_vid : nullptr;
@@ -1936,12 +1942,17 @@ template <int NP, typename ET>
 int launch_rows_bal_t(siml_engine* h, const GroupParams& p, size_t smem, float* out, int64_t ldo) {
     const int64_t groups = (p.rows + 31) / 32;
     const size_t sm = smem + rows_bal_extra_smem(NP, kThreads / 32);
-    int rc = set_smem(k_rows_bal<NP, ET>, sm);
+    auto kern = k_rows_bal<NP, ET, false>;
+    if (p.rare_slots) {
+        if constexpr (std::is_same<ET, uint16_t>::value) kern = k_rows_bal<NP, ET, true>;
+        else return fail(SIML_ERR_UNSUPPORTED, "a split vocabulary needs 16-bit entries");
+    }
+    int rc = set_smem(kern, sm);
     if (rc) return rc;
     const int s = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
     dim3 grid((unsigned)groups, (unsigned)s);
     SIML_CUDA(mark(h, h->ev0));
-    k_rows_bal<NP, ET><<<grid, kThreads, sm, h->stream>>>(p, out, ldo);
+    kern<<<grid, kThreads, sm, h->stream>>>(p, out, ldo);
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
@@ -2061,8 +2072,18 @@ int64_t split_table_capacity(siml_engine* h) {
     return std::max<int64_t>(0, words / 4 * 4 - 4);   // (ncommon + 1) rounded up to 4 stays <= words
 }
 
+int64_t split_balanced_capacity(siml_engine* h) {
+    const int64_t extra = (int64_t)kRareSlots * 8 + (int64_t)rows_bal_extra_smem(8, kThreads / 32) +
+                          (int64_t)sizeof(RowSmem) + 2048;
+    const int64_t words = ((int64_t)h->smem_optin - extra) / 4;
+    return std::max<int64_t>(0, words / 4 * 4 - 4);
+}
+
 bool rows_balanced_fits(siml_engine* h) {
-    if (h->vocab.split) return false;
+    if (h->vocab.split) {   // 8 planes only; the layout keeps split_balanced_capacity common vids
+        const int np = planes_needed(std::min(h->ref.max_entries, h->qry.max_entries));
+        return np <= 8 && split_balanced_capacity(h) > 0;
+    }
     const int vt_words = (int)((h->vocab.ncommon + 1 + 3) / 4 * 4);
     const int np = planes_needed(std::min(h->ref.max_entries, h->qry.max_entries)) <= 8 ? 8 : 16;
     return (size_t)vt_words * 4 + rows_bal_extra_smem(np, kThreads / 32) + sizeof(RowSmem) + 64 <= h->smem_optin;
