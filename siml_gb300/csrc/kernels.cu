@@ -629,6 +629,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_nbr(const GroupParams p, const 
 // the pieces of slots [first lane + l, last lane + l] with a bit-sliced
 // ripple adder and runs the padded kernel's epilogue, so stores stay one
 // 128-byte line per row.
+//
+// MASKED (layouts whose runs are all at most 32 steps: every chunk of a
+// database whose molecules hold fewer than about 256 entries): lanes know
+// their flush steps before streaming.  The owner of each molecule sets bit
+// (end % L) of lane end / L's mask, and a lane's next molecule after a flush
+// is the next set bit of the warp's ballot of non-empty molecules, so a step
+// costs one bit test besides the flush itself.  Otherwise lanes walk the
+// prefix array.
 constexpr int kPieceSlots = 64;
 constexpr int kPrefixWords = 34;
 
@@ -653,7 +661,14 @@ __device__ __forceinline__ void piece_add(SlicedCounter<NP>& acc, const uint32_t
     }
 }
 
-template <int NP, typename ET, bool RARE = false>
+// floor(x / L) for 0 <= x <= 64 L and 1 <= L <= 1024, from rl ~ 1 / L (the
+// hardware reciprocal estimate, relative error below 2^-22): (x + 0.5) / L
+// lies at least 0.5 / L from an integer, far beyond the product's error.
+__device__ __forceinline__ int div_run(int x, float rl) {
+    return (int)__fmul_rz(__int2float_rn(x) + 0.5f, rl);
+}
+
+template <int NP, typename ET, bool RARE, bool MASKED>
 __global__ void __launch_bounds__(kThreads, 1) k_rows_bal(const GroupParams p, float* out, int64_t ldo) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
@@ -688,24 +703,37 @@ __global__ void __launch_bounds__(kThreads, 1) k_rows_bal(const GroupParams p, f
         }
         const int P = incl - g;
         const int G = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        float rl = 0.0f;
+        if constexpr (MASKED) {
+            asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rl) : "f"(__int2float_rn(max(L, 1))));
+            pc[lane] = 0u;   // flush masks, in the piece buffer until the first flush
+        }
         pre[lane] = P;
         if (lane == 31) pre[32] = G;
         __syncwarp();
+        uint32_t fmask = 0u;
+        if constexpr (MASKED) {
+            if (g > 0) {
+                const int e = incl - 1;   // the molecule's last step
+                const int j = div_run(e, rl);
+                atomicOr(pc + j, 1u << (e - j * L));
+            }
+            __syncwarp();
+            fmask = pc[lane];
+        }
         const int seg0 = lane * L, seg1 = min(G, seg0 + L);
         // molecule holding step seg0: the largest m with pre[m] <= seg0
         int m = 0;
 #pragma unroll
         for (int q = 16; q > 0; q >>= 1)
             if (m + q <= 31 && pre[m + q] <= seg0) m += q;
-        int endm = pre[m + 1];
         SlicedCounter<NP> acc;
         acc.clear();
-        bool pending = false;
         uint4 a0 = zero, b0 = zero, a1 = zero, b1 = zero;
         const uint4* Ec = E + base;
         if (0 < L) { a0 = __ldg(Ec); if (SPG == 2) b0 = __ldg(Ec + 32); }
         if (1 < L) { a1 = __ldg(Ec + SPG * 32); if (SPG == 2) b1 = __ldg(Ec + SPG * 32 + 32); }
-        for (int s = 0; s < L; s++) {
+        auto step = [&](int s) {
             const uint4 x = a0, y = b0;
             a0 = a1;
             b0 = b1;
@@ -718,22 +746,53 @@ __global__ void __launch_bounds__(kThreads, 1) k_rows_bal(const GroupParams p, f
                          T[x.z & 0xFFFFu], T[x.z >> 16], T[x.w & 0xFFFFu], T[x.w >> 16]);
             else
                 acc.add8(T[x.x], T[x.y], T[x.z], T[x.w], T[y.x], T[y.y], T[y.z], T[y.w]);
-            const int gs = seg0 + s + 1;
-            if (gs <= seg1) pending = true;   // a step of the run (past it: zero padding)
-            if (gs == endm && gs <= seg1) {   // molecule m ends inside this lane's run
-                piece_store<NP>(pc, lane + m, acc);
-                acc.clear();
-                pending = false;
-                do { m++; } while (m < 32 && pre[m + 1] == pre[m]);   // skip molecules with no entries
-                endm = m < 32 ? pre[m + 1] : 0x7FFFFFFF;
+        };
+        if constexpr (MASKED) {
+            const uint32_t nz = __ballot_sync(0xFFFFFFFFu, g > 0);
+            // the run ends inside a molecule (its last step ends none)
+            const bool open_end = seg1 > seg0 && !((fmask >> (seg1 - seg0 - 1)) & 1u);
+            __syncwarp();   // every mask is read before pieces overwrite them
+            uint32_t f = fmask;
+            for (int s = 0; s < L; s++) {
+                step(s);
+                if (f & 1u) {   // molecule m ends at this step
+                    piece_store<NP>(pc, lane + m, acc);
+                    acc.clear();
+                    m = __ffs(nz & (0xFFFFFFFEu << m)) - 1;   // next molecule with entries
+                }
+                f >>= 1;
             }
+            if (open_end) piece_store<NP>(pc, lane + m, acc);
+        } else {
+            int endm = pre[m + 1];
+            bool pending = false;
+            for (int s = 0; s < L; s++) {
+                step(s);
+                const int gs = seg0 + s + 1;
+                if (gs <= seg1) pending = true;   // a step of the run (past it: zero padding)
+                if (gs == endm && gs <= seg1) {   // molecule m ends inside this lane's run
+                    piece_store<NP>(pc, lane + m, acc);
+                    acc.clear();
+                    pending = false;
+                    do { m++; } while (m < 32 && pre[m + 1] == pre[m]);   // skip molecules with no entries
+                    endm = m < 32 ? pre[m + 1] : 0x7FFFFFFF;
+                }
+            }
+            if (pending && m < 32) piece_store<NP>(pc, lane + m, acc);   // run ended inside molecule m
         }
-        if (pending && m < 32) piece_store<NP>(pc, lane + m, acc);   // run ended inside molecule m
         __syncwarp();
         SlicedCounter<NP> own;
         own.clear();
         if (g > 0) {
-            const int fl = P / L, ll = (P + g - 1) / L;
+            int fl, ll;
+            if constexpr (MASKED) {
+                asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rl) : "f"(__int2float_rn(L)));
+                fl = div_run(P, rl);
+                ll = div_run(P + g - 1, rl);
+            } else {
+                fl = P / L;
+                ll = (P + g - 1) / L;
+            }
             for (int j = fl; j <= ll; j++) piece_add<NP>(own, pc, j + lane);
         }
         if constexpr (RARE) rare_add<NP>(T, p, c * 32 + lane, own);
@@ -1939,12 +1998,15 @@ int set_smem(K kernel, size_t smem) {
 }
 
 template <int NP, typename ET>
-int launch_rows_bal_t(siml_engine* h, const GroupParams& p, size_t smem, float* out, int64_t ldo) {
+int launch_rows_bal_t(siml_engine* h, const GroupParams& p, size_t smem, float* out, int64_t ldo, int64_t max_ng) {
     const int64_t groups = (p.rows + 31) / 32;
     const size_t sm = smem + rows_bal_extra_smem(NP, kThreads / 32);
-    auto kern = k_rows_bal<NP, ET, false>;
+    constexpr int SPG = sizeof(ET) == 2 ? 1 : 2;
+    const bool masked = max_ng / SPG <= 32;   // every run fits a 32-bit flush mask
+    auto kern = masked ? k_rows_bal<NP, ET, false, true> : k_rows_bal<NP, ET, false, false>;
     if (p.rare_slots) {
-        if constexpr (std::is_same<ET, uint16_t>::value) kern = k_rows_bal<NP, ET, true>;
+        if constexpr (std::is_same<ET, uint16_t>::value)
+            kern = masked ? k_rows_bal<NP, ET, true, true> : k_rows_bal<NP, ET, true, false>;
         else return fail(SIML_ERR_UNSUPPORTED, "a split vocabulary needs 16-bit entries");
     }
     int rc = set_smem(kern, sm);
@@ -2446,10 +2508,10 @@ int launch_rows(siml_engine* h, const RowsArgs& a) {
     if (table_params(h, d, a.rowbase, rows, a.mode, p, smem, np)) {
         if (d->balanced && !d->offsets) {
             if (np == 8)
-                return d->entry_bytes == 2 ? launch_rows_bal_t<8, uint16_t>(h, p, smem, a.out, a.ldo)
-                                           : launch_rows_bal_t<8, uint32_t>(h, p, smem, a.out, a.ldo);
-            return d->entry_bytes == 2 ? launch_rows_bal_t<16, uint16_t>(h, p, smem, a.out, a.ldo)
-                                       : launch_rows_bal_t<16, uint32_t>(h, p, smem, a.out, a.ldo);
+                return d->entry_bytes == 2 ? launch_rows_bal_t<8, uint16_t>(h, p, smem, a.out, a.ldo, d->max_ng)
+                                           : launch_rows_bal_t<8, uint32_t>(h, p, smem, a.out, a.ldo, d->max_ng);
+            return d->entry_bytes == 2 ? launch_rows_bal_t<16, uint16_t>(h, p, smem, a.out, a.ldo, d->max_ng)
+                                       : launch_rows_bal_t<16, uint32_t>(h, p, smem, a.out, a.ldo, d->max_ng);
         }
         if (d->offsets)
             return np == 8 ? launch_rows_t<8, off32_t>(h, p, smem, a.out, a.ldo)

@@ -116,10 +116,16 @@ def _random_sets(rng, n, width, code_range, max_count, p_empty=0.05):
     return L, C, ln, mg
 
 
-@pytest.mark.parametrize("case", ["small_vocab", "negative_codes", "high_counts", "zero_mags"])
+@pytest.mark.parametrize("case", ["small_vocab", "negative_codes", "high_counts", "zero_mags", "long_db_molecules"])
 def test_rows_random_sets(native, oracle, case):
-    rng = np.random.default_rng({"small_vocab": 1, "negative_codes": 2, "high_counts": 3, "zero_mags": 4}[case])
-    if case == "small_vocab":
+    rng = np.random.default_rng({"small_vocab": 1, "negative_codes": 2, "high_counts": 3, "zero_mags": 4,
+                                 "long_db_molecules": 5}[case])
+    if case == "long_db_molecules":
+        # short ref rows (8-plane counters) against database molecules of up
+        # to 800 entries: lanes' runs of the balanced layout exceed 32 steps
+        ref = _random_sets(rng, 70, 30, (0, 3000), 2)
+        qry = _random_sets(rng, 800, 400, (0, 3000), 2)
+    elif case == "small_vocab":
         ref = _random_sets(rng, 77, 30, (0, 200), 3)
         qry = _random_sets(rng, 1500, 30, (0, 200), 3)
     elif case == "negative_codes":
@@ -140,6 +146,9 @@ def test_rows_random_sets(native, oracle, case):
     _load(gl, ref, qry)
     got = gl.getMultipleRows(0, ref[0].shape[0])
     assert np.array_equal(got, oracle.tanimoto_block(ref, qry, 0, ref[0].shape[0]))
+    if case == "long_db_molecules":
+        st = gl.dbStats()
+        assert st["max_ng"] > 32 and st["ref_max_entries"] <= 255, st
 
 
 def test_large_vocabulary_uses_merge_path(native, oracle):
