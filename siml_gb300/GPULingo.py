@@ -434,6 +434,40 @@ class GPULingo:
             return payload[0]
         raise RuntimeError("unknown pending result")
 
+    # The reference rebinds retrieveAsyncResult to one of these per call
+    # kind; they are public names there, so they are kept for callers that
+    # use them directly.
+    def retrieveAsyncMatrixResult(self):
+        """Matrix result of a pending getTanimotoRow_async, getMultipleRows_async
+        or getMultipleHistogrammedRows_async (pysiml/GPULingo.py:536-555)."""
+        self._expect_pending("matrix")
+        return self.retrieveAsyncResult()
+
+    def retrieveAsyncMatrixVectorResult(self):
+        """(indices, counts) of a pending getNeighbors_async
+        (pysiml/GPULingo.py:558-583).  Here both forms return the columns up to
+        the largest count, as retrieveAsyncResult does."""
+        self._expect_pending("neighbors")
+        return self.retrieveAsyncResult()
+
+    def retrieveAsyncMatrixVectorResult_trimmed(self):
+        """(indices, counts) of a pending getNeighbors_async, trimmed to the
+        largest count (pysiml/GPULingo.py:585-622)."""
+        self._expect_pending("neighbors")
+        return self.retrieveAsyncResult()
+
+    def retrieveAsyncResultBase(self):
+        """What retrieveAsyncResult is reset to after a retrieval
+        (pysiml/GPULingo.py:624-628): always an error."""
+        raise RuntimeError("Error: tried to call retrieveAsyncResult without a pending asynchronous result")
+
+    def _expect_pending(self, kind):
+        if self._pending is None:
+            self.retrieveAsyncResultBase()
+        if self._pending[0] != kind:
+            raise RuntimeError("the pending asynchronous result is a %s result, not a %s result"
+                               % (self._pending[0], kind))
+
     def asyncOperationsDone(self):
         """True once all queued work of this object has finished (pysiml/GPULingo.py:642-647)."""
         done = ctypes.c_int(0)

@@ -55,6 +55,21 @@ def test_async_protocol(native, oracle, set4096):
     assert np.array_equal(got, oracle.tanimoto_block(set4096, set4096, 100, 164))
     with pytest.raises(RuntimeError):
         gl.retrieveAsyncResult()
+    # the reference's per-kind retrievers
+    gl.getMultipleRows_async(5, 9)
+    with pytest.raises(RuntimeError):
+        gl.retrieveAsyncMatrixVectorResult()
+    assert np.array_equal(gl.retrieveAsyncMatrixResult(), oracle.tanimoto_block(set4096, set4096, 5, 9))
+    with pytest.raises(RuntimeError):
+        gl.retrieveAsyncMatrixResult()
+    with pytest.raises(RuntimeError):
+        gl.retrieveAsyncResultBase()
+    gl.getNeighbors_async(0, 3, 0.5)
+    idx, cnt = gl.retrieveAsyncMatrixVectorResult_trimmed()
+    assert idx.shape[0] == 3 and cnt.shape == (3,) and idx.shape[1] <= int(cnt.max())
+    gl.getNeighbors_async(0, 3, 0.5)
+    idx2, cnt2 = gl.retrieveAsyncMatrixVectorResult()
+    assert np.array_equal(idx, idx2) and np.array_equal(cnt, cnt2)
 
 
 def test_row_ranges(native, set4096):
