@@ -639,6 +639,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_nbr(const GroupParams p, const 
 // prefix array.
 constexpr int kPieceSlots = 64;
 constexpr int kPrefixWords = 34;
+constexpr int kRowsBalThreads = 1024;   // threads of a k_rows_bal CTA (one CTA per SM beside the table)
 
 __host__ __device__ constexpr size_t rows_bal_extra_smem(int np, int warps) {
     return (size_t)warps * ((size_t)np * kPieceSlots + kPrefixWords) * 4;
@@ -669,7 +670,7 @@ __device__ __forceinline__ int div_run(int x, float rl) {
 }
 
 template <int NP, typename ET, bool RARE, bool MASKED>
-__global__ void __launch_bounds__(kThreads, 1) k_rows_bal(const GroupParams p, float* out, int64_t ldo) {
+__global__ void __launch_bounds__(kRowsBalThreads, 1) k_rows_bal(const GroupParams p, float* out, int64_t ldo) {
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
     const int nr = build_table(T, rs, p);   // synchronizes the block
@@ -2000,7 +2001,7 @@ int set_smem(K kernel, size_t smem) {
 template <int NP, typename ET>
 int launch_rows_bal_t(siml_engine* h, const GroupParams& p, size_t smem, float* out, int64_t ldo, int64_t max_ng) {
     const int64_t groups = (p.rows + 31) / 32;
-    const size_t sm = smem + rows_bal_extra_smem(NP, kThreads / 32);
+    const size_t sm = smem + rows_bal_extra_smem(NP, kRowsBalThreads / 32);
     constexpr int SPG = sizeof(ET) == 2 ? 1 : 2;
     const bool masked = max_ng / SPG <= 32;   // every run fits a 32-bit flush mask
     auto kern = masked ? k_rows_bal<NP, ET, false, true> : k_rows_bal<NP, ET, false, false>;
@@ -2011,10 +2012,10 @@ int launch_rows_bal_t(siml_engine* h, const GroupParams& p, size_t smem, float* 
     }
     int rc = set_smem(kern, sm);
     if (rc) return rc;
-    const int s = choose_splits(groups, p.nchunks, h->num_sms, kThreads / 32);
+    const int s = choose_splits(groups, p.nchunks, h->num_sms, kRowsBalThreads / 32);
     dim3 grid((unsigned)groups, (unsigned)s);
     SIML_CUDA(mark(h, h->ev0));
-    kern<<<grid, kThreads, sm, h->stream>>>(p, out, ldo);
+    kern<<<grid, kRowsBalThreads, sm, h->stream>>>(p, out, ldo);
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
@@ -2135,7 +2136,7 @@ int64_t split_table_capacity(siml_engine* h) {
 }
 
 int64_t split_balanced_capacity(siml_engine* h) {
-    const int64_t extra = (int64_t)kRareSlots * 8 + (int64_t)rows_bal_extra_smem(8, kThreads / 32) +
+    const int64_t extra = (int64_t)kRareSlots * 8 + (int64_t)rows_bal_extra_smem(8, kRowsBalThreads / 32) +
                           (int64_t)sizeof(RowSmem) + 2048;
     const int64_t words = ((int64_t)h->smem_optin - extra) / 4;
     return std::max<int64_t>(0, words / 4 * 4 - 4);
@@ -2148,7 +2149,7 @@ bool rows_balanced_fits(siml_engine* h) {
     }
     const int vt_words = (int)((h->vocab.ncommon + 1 + 3) / 4 * 4);
     const int np = planes_needed(std::min(h->ref.max_entries, h->qry.max_entries)) <= 8 ? 8 : 16;
-    return (size_t)vt_words * 4 + rows_bal_extra_smem(np, kThreads / 32) + sizeof(RowSmem) + 64 <= h->smem_optin;
+    return (size_t)vt_words * 4 + rows_bal_extra_smem(np, kRowsBalThreads / 32) + sizeof(RowSmem) + 64 <= h->smem_optin;
 }
 
 int batch_nbr_usable(siml_engine* h, const DbLayout* d) {
