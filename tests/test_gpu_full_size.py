@@ -1,0 +1,125 @@
+"""Full-size checks on the 1,000,000-molecule database of the row-block and
+fused-search workloads (lognormal lengths, median 45 chars).
+
+The oracle computes a few complete rows bit for bit. Over the whole
+1,024 x 1,000,000 block the tests check properties that hold at any size:
+- a molecule's similarity with itself is 1;
+- the block is symmetric where the ref rows are database molecules;
+- getNeighbors, top-k and both histograms, each computed by its own fused
+  kernel, are derived exactly from the rows block, with the rules the
+  reference states: the fp32 magnitude bound, then lo <= t < hi, indices
+  ascending (pysiml/kernels.py:437-448); bins (unsigned)(t*100) capped at 100
+  (pysiml/kernels.py:660-661); top-k ties to the lower index; 1000 bins of
+  min((unsigned)(t*1000), 999)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROWS = 1024
+DB_N = 1_000_000
+
+
+@pytest.fixture(scope="module")
+def full(native):
+    torch = pytest.importorskip("torch")
+    from siml_gb300 import GPULingo, synthetic as S
+    db = S.smiles_set(S.SEED_DB_1M, S.LOGNORMAL_45, DB_N)
+    ref = tuple(a[:ROWS] for a in db)   # database molecules 0..1023 as the ref rows
+    gl = GPULingo(0)
+    gl.set_qsmiles(*db)
+    gl.set_refsmiles(*ref)
+    block = gl.getMultipleRowsDevice(0, ROWS)
+    torch.cuda.synchronize()
+    yield gl, db, ref, block
+    del block
+    torch.cuda.empty_cache()
+
+
+def test_rows_block_full_size(full, oracle):
+    import torch
+    gl, db, ref, block = full
+    assert block.shape == (ROWS, DB_N)
+    # self-similarity and symmetry over the ref molecules' own columns
+    assert bool((torch.diagonal(block[:, :ROWS]) == 1.0).all())
+    sq = block[:, :ROWS].view(torch.int32)
+    assert torch.equal(sq, sq.t())
+    # complete rows against the oracle, bit for bit (rows in different 32-row groups)
+    rows = [0, 7, 31, 32, 511, 1023]
+    sub = tuple(a[rows] for a in ref)
+    want = oracle.tanimoto_block(sub, db, 0, len(rows))
+    got = block[rows].cpu().numpy()
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.parametrize("lo", [0.2, 0.7])
+def test_neighbors_full_size_equal_the_rows_block(full, lo):
+    import torch
+    gl, db, ref, block = full
+    dev = block.device
+    amag = torch.from_numpy(ref[3].astype(np.int32)).to(dev)
+    bmag = torch.from_numpy(db[3].astype(np.int32)).to(dev)
+    # the kernel compares with the fp32 bounds (0.7f < 0.7)
+    lo32 = torch.tensor(lo, dtype=torch.float32, device=dev)
+    hi32 = torch.tensor(1.1, dtype=torch.float32, device=dev)
+    counts, cols, vals = [], [], []
+    for r0 in range(0, ROWS, 128):
+        b = block[r0:r0 + 128]
+        a = amag[r0:r0 + 128, None]
+        bound = torch.minimum(a, bmag[None, :]).float() / torch.maximum(a, bmag[None, :]).float()
+        m = (bound >= lo32) & (b >= lo32) & (b < hi32)
+        counts.append(m.sum(1, dtype=torch.int32))
+        nz = m.nonzero()
+        cols.append(nz[:, 1].to(torch.int32))
+        vals.append(b[nz[:, 0], nz[:, 1]])
+        del bound, m
+    want_cnt = torch.cat(counts)
+    want_cols = torch.cat(cols)
+    want_vals = torch.cat(vals)
+    assert int(want_cnt.min()) >= 1   # every ref molecule finds itself
+    pitch = 16 * ((int(want_cnt.max()) + 15) // 16)
+    idx = torch.empty((ROWS, pitch), dtype=torch.int32, device=dev)
+    sims = torch.empty((ROWS, pitch), dtype=torch.float32, device=dev)
+    cnt = torch.empty(ROWS, dtype=torch.int32, device=dev)
+    gl.neighborsDevice(0, ROWS, lo, 1.1, pitch, idx, sims, cnt)
+    torch.cuda.synchronize()
+    assert torch.equal(cnt, want_cnt)
+    listed = torch.arange(pitch, device=dev)[None, :] < cnt[:, None]
+    assert torch.equal(idx[listed], want_cols)   # row-major: ascending indices per row
+    assert torch.equal(sims[listed].view(torch.int32), want_vals.view(torch.int32))
+
+
+def test_topk_full_size_equals_the_rows_block(full):
+    import torch
+    gl, db, ref, block = full
+    k = 100
+    dev = block.device
+    idx = torch.empty((ROWS, k), dtype=torch.int32, device=dev)
+    sims = torch.empty((ROWS, k), dtype=torch.float32, device=dev)
+    gl.topKDevice(0, ROWS, k, idx, sims)
+    torch.cuda.synchronize()
+    for r0 in range(0, ROWS, 128):
+        # a stable descending sort keeps the lower index first among equal similarities
+        v, i = torch.sort(block[r0:r0 + 128], dim=1, descending=True, stable=True)
+        assert torch.equal(idx[r0:r0 + 128], i[:, :k].to(torch.int32))
+        assert torch.equal(sims[r0:r0 + 128].view(torch.int32), v[:, :k].contiguous().view(torch.int32))
+        del v, i
+
+
+def test_histograms_full_size_equal_the_rows_block(full):
+    import torch
+    gl, db, ref, block = full
+    dev = block.device
+    h1000 = torch.zeros(1000, dtype=torch.int64, device=dev)
+    h101 = torch.zeros((ROWS, 101), dtype=torch.int64, device=dev)
+    for r0 in range(0, ROWS, 128):
+        b = block[r0:r0 + 128]
+        h1000 += torch.bincount((b * 1000.0).to(torch.int32).clamp(max=999).view(-1), minlength=1000)
+        bins = (b * 100.0).to(torch.int64).clamp(max=100) + 101 * torch.arange(b.shape[0], device=dev)[:, None]
+        h101[r0:r0 + 128] = torch.bincount(bins.view(-1), minlength=101 * b.shape[0]).view(-1, 101)
+        del bins
+    got1000 = gl.getSimilarityHistogram(0, ROWS)
+    assert int(got1000.sum()) == ROWS * DB_N
+    assert np.array_equal(got1000.astype(np.int64), h1000.cpu().numpy())
+    got101 = gl.getMultipleHistogrammedRows(0, ROWS)
+    assert np.array_equal(np.asarray(got101)[:, :101].astype(np.int64), h101.cpu().numpy())
