@@ -1,5 +1,6 @@
 """Full-size checks on the 1,000,000-molecule database of the row-block and
-fused-search workloads (lognormal lengths, median 45 chars).
+fused-search workloads (lognormal lengths, median 45 chars), and on the
+2,000,000-molecule database of the ragged batched jobs.
 
 The oracle computes a few complete rows bit for bit. Over the whole
 1,024 x 1,000,000 block the tests check properties that hold at any size:
@@ -123,3 +124,74 @@ def test_histograms_full_size_equal_the_rows_block(full):
     assert np.array_equal(got1000.astype(np.int64), h1000.cpu().numpy())
     got101 = gl.getMultipleHistogrammedRows(0, ROWS)
     assert np.array_equal(np.asarray(got101)[:, :101].astype(np.int64), h101.cpu().numpy())
+
+
+RAGGED_DB_N = 2_000_000
+
+
+@pytest.fixture(scope="module")
+def ragged(native):
+    torch = pytest.importorskip("torch")
+    from siml_gb300 import GPULingo, synthetic as S
+    db = S.smiles_set(S.SEED_RAGGED, S.BIMODAL_35_110, RAGGED_DB_N)
+    gl = GPULingo(0)
+    gl.set_qsmiles(*db)
+    gl.set_refsmiles(*db)
+    jobs = S.ragged_jobs(S.SEED_RAGGED, RAGGED_DB_N, 512)
+    yield gl, db, jobs
+    torch.cuda.empty_cache()
+
+
+def test_ragged_jobs_full_size(ragged, oracle):
+    """512 jobs of the ragged workload on its full 2M-molecule bimodal
+    database (rows log-uniform 1-2,048, columns log-uniform 1,000-200,000,
+    T >= 0.6, pitch 128): one batched run (autotuned tile), its CUDA-graph
+    replay and the plain one-call-per-job path give identical results, and
+    the two smallest jobs equal the oracle."""
+    import torch
+    from siml_gb300 import _native as N
+    gl, db, jobs = ragged
+    lo, maxn = 0.6, 128
+    plan = gl.planNeighborBatch(jobs, lo, 1.1, maxn)
+    idx, sims, cnt = plan.buffers(with_sims=True)
+    plan.run(idx, sims, cnt)
+    # the same plan captured in a CUDA graph and replayed into other buffers
+    g_idx, g_sims, g_cnt = plan.buffers(with_sims=True)
+    cap = torch.cuda.Stream()
+    cap.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(cap):
+        plan.run(g_idx, g_sims, g_cnt, stream=cap)
+    torch.cuda.current_stream().wait_stream(cap)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        plan.run(g_idx, g_sims, g_cnt, stream=torch.cuda.current_stream())
+    g_idx.fill_(-1)
+    g_sims.fill_(-1.0)
+    g_cnt.fill_(-1)
+    graph.replay()
+    # plain path: one range search per job
+    p_idx, p_sims, p_cnt = plan.buffers(with_sims=True)
+    J = plan.jobs.tolist()
+    for rb, re, cb, ce, o in J:
+        if re > rb:
+            gl.neighborsRangeDevice(rb, re, cb, ce, lo, 1.1, plan.pitch, p_idx[o:o + re - rb],
+                                    p_sims[o:o + re - rb], p_cnt[o:o + re - rb])
+    torch.cuda.synchronize()
+    N.check(N.lib().siml_async_status(gl._h), "siml_async_status")
+    n = plan.rows_out
+    listed = torch.arange(plan.pitch, device=cnt.device)[None, :] < torch.clamp(cnt[:n], max=plan.pitch)[:, None]
+    for oi, os_, oc in ((g_idx, g_sims, g_cnt), (p_idx, p_sims, p_cnt)):
+        assert torch.equal(oc[:n], cnt[:n])
+        assert torch.equal(oi[:n][listed], idx[:n][listed])
+        assert torch.equal(os_[:n][listed].view(torch.int32), sims[:n][listed].view(torch.int32))
+    res = plan.split(idx, sims, cnt)
+    pairs = (jobs[:, 1] - jobs[:, 0]) * (jobs[:, 3] - jobs[:, 2])
+    for i in [int(x) for x in np.argsort(pairs, kind="stable")[:2]]:
+        rb, re, cb, ce = (int(v) for v in jobs[i])
+        m, s, c = res[i]
+        om, os_, oc = oracle.neighbors_range_block(db, db, rb, re, cb, ce, lo, 1.1, maxn)
+        assert np.array_equal(c, oc)
+        for r in range(re - rb):
+            k = min(int(c[r]), plan.pitch)
+            assert np.array_equal(m[r, :k], om[r, :k])
+            assert np.array_equal(s[r, :k].view(np.uint32), os_[r, :k].view(np.uint32))
