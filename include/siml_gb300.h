@@ -59,7 +59,9 @@ const char* siml_last_error(void);
 /* GPULingo(deviceID) — pysiml/GPULingo.py:162-173 (context + stream per object). */
 int siml_create(int device, siml_engine** out);
 int siml_destroy(siml_engine* h);
-/* Run subsequent work on a caller-owned cudaStream_t (NULL: the engine's own). */
+/* Run subsequent work on a caller-owned cudaStream_t (NULL: the engine's own,
+ * a non-blocking stream).  For the legacy default stream pass cudaStreamLegacy
+ * ((void*)1), not NULL. */
 int siml_set_stream(siml_engine* h, void* cuda_stream);
 /* stream.synchronize() inside retrieveAsyncResult — pysiml/GPULingo.py:546. */
 int siml_sync(siml_engine* h);
@@ -189,7 +191,8 @@ int siml_batch_create(siml_engine* h, int64_t njobs, const int64_t* jobs,
  * skips an output. */
 int siml_batch_info(siml_batch* b, int64_t* rows_out, int64_t* nitems, int64_t* tile_chunks,
                     int64_t* stream_bytes, int64_t* unique_bytes);
-/* Queues the plan on stream (a cudaStream_t; NULL: the engine's stream):
+/* Queues the plan on stream (a cudaStream_t; NULL: the engine's stream;
+ * cudaStreamLegacy for the legacy default stream):
  * device outputs idx, sims (may be NULL): [rows_out, pitch]; counts:
  * [rows_out], with siml_neighbors' meaning.  No host synchronization and
  * no allocation, so a run may be captured in a CUDA graph and replayed.

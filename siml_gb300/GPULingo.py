@@ -91,7 +91,7 @@ class GPULingo:
             stream = torch.cuda.Stream(device=torch.device("cuda", deviceID))
         self._stream = stream
         if stream is not None:
-            N.check(L.siml_set_stream(self._h, ctypes.c_void_p(stream.cuda_stream)), "siml_set_stream")
+            N.check(L.siml_set_stream(self._h, N.stream_arg(stream)), "siml_set_stream")
 
     @property
     def stream(self):

@@ -135,6 +135,19 @@ def check(rc: int, what: str = "") -> None:
     raise SimlError(rc, msg)
 
 
+# CUDA's handle for the legacy default stream (cudaStreamLegacy).  A NULL
+# stream given to siml_set_stream selects the engine's own stream instead.
+CUDA_STREAM_LEGACY = 1
+
+
+def stream_arg(stream) -> ctypes.c_void_p:
+    """siml_set_stream argument for a torch stream.  Torch's default stream has
+    handle 0, which is the legacy default stream: it is passed as
+    cudaStreamLegacy, so the engine's work is ordered with torch's."""
+    h = int(stream.cuda_stream)
+    return ctypes.c_void_p(h if h != 0 else CUDA_STREAM_LEGACY)
+
+
 def ptr(a) -> int | None:
     """Address of a numpy array or torch tensor (None for None)."""
     if a is None:

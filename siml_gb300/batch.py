@@ -89,7 +89,7 @@ class NeighborBatch:
         L = N.lib()
         if stream is not None:
             N.check(L.siml_batch_run(self._b, idx.data_ptr(), N.ptr(sims), counts.data_ptr(),
-                                     ctypes.c_void_p(stream.cuda_stream)), "siml_batch_run")
+                                     N.stream_arg(stream)), "siml_batch_run")
             return
         gl = self._gl
         gl._enter()

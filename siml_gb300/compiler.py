@@ -13,7 +13,6 @@ as an iterable of lines.
 """
 from __future__ import annotations
 
-import ctypes
 
 import numpy as np
 
@@ -89,7 +88,7 @@ def compile_buffer_gpu(buf, offsets, device: int = 0):
     off_d = torch.from_numpy(off_h).to(dev)
     L = N.lib()
     h = _engine(device)
-    N.check(L.siml_set_stream(h, ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)), "siml_set_stream")
+    N.check(L.siml_set_stream(h, N.stream_arg(torch.cuda.current_stream(dev))), "siml_set_stream")
     w = L.siml_compile_width_gpu(h, text.data_ptr(), off_d.data_ptr(), n)
     if w < 0:
         N.check(int(-w), "siml_compile_width_gpu")

@@ -43,8 +43,7 @@ def rowHistogram101(datamatrix, device: int = 0):
         d = datamatrix if datamatrix.stride(1) == 1 else datamatrix.contiguous()
         out = torch.empty((d.shape[0], 101), dtype=torch.int32, device=d.device)
         h = _engine(d.device.index)
-        N.check(L.siml_set_stream(h, ctypes.c_void_p(torch.cuda.current_stream(d.device).cuda_stream)),
-                "siml_set_stream")
+        N.check(L.siml_set_stream(h, N.stream_arg(torch.cuda.current_stream(d.device))), "siml_set_stream")
         fn = L.siml_row_histogram101_f64 if d.dtype == torch.float64 else L.siml_row_histogram101
         N.check(fn(h, d.data_ptr(), d.shape[0], d.shape[1], d.stride(0), out.data_ptr(), N.SIML_DEVICE),
                 "rowHistogram101")

@@ -101,3 +101,20 @@ def test_gpu_compiled_set_gives_the_same_rows(native):
     b.set_qsmiles(*gpu)
     torch.cuda.synchronize()
     assert np.array_equal(a.getMultipleRows(0, 64).view(np.uint32), b.getMultipleRows(0, 64).view(np.uint32))
+
+
+def test_gpu_compiler_is_ordered_after_torch_default_stream(native):
+    """The compiler runs on torch's current stream.  With torch's default
+    stream (handle 0, the legacy default stream) busy for ~0.1 s when the
+    call is made, the byte upload and the output arrays' zero fill queue
+    behind that work; the compile must wait for them rather than run on a
+    stream of its own."""
+    import torch
+    from siml_gb300 import synthetic as S
+    buf, off = S.smiles_buffer(S.SEED_SERVING, S.UNIFORM_20_90, 50000)
+    want, _, _ = _cpu([buf[off[i]:off[i + 1]] for i in range(len(off) - 1)])
+    assert torch.cuda.current_stream().cuda_stream == 0
+    for _ in range(2):
+        torch.cuda._sleep(200_000_000)   # bounded spin on the default stream
+        got = _gpu(buf, off)
+        _same(got, want)

@@ -1,6 +1,7 @@
 """Full-size checks on the 1,000,000-molecule database of the row-block and
-fused-search workloads (lognormal lengths, median 45 chars), and on the
-2,000,000-molecule database of the ragged batched jobs.
+fused-search workloads (lognormal lengths, median 45 chars), on the
+2,000,000-molecule database of the ragged batched jobs and on the
+10,000,000-molecule serving database.
 
 The oracle computes a few complete rows bit for bit. Over the whole
 1,024 x 1,000,000 block the tests check properties that hold at any size:
@@ -195,3 +196,68 @@ def test_ragged_jobs_full_size(ragged, oracle):
             k = min(int(c[r]), plan.pitch)
             assert np.array_equal(m[r, :k], om[r, :k])
             assert np.array_equal(s[r, :k].view(np.uint32), os_[r, :k].view(np.uint32))
+
+
+SERVING_DB_N = 10_000_000
+
+
+def test_serving_full_size(native, oracle):
+    """The serving workload's 10M-molecule database made resident from the
+    GPU compiler: requests of 1-512 query SMILES (log-uniform), half top-50
+    and half T >= 0.75, are queued together for the server; each answer
+    equals the same request served alone, and the two smallest equal the
+    oracle."""
+    import torch
+    from siml_gb300 import GPULingo, synthetic as S
+    from siml_gb300.compiler import compile_buffer, compile_buffer_gpu
+    from siml_gb300.serving import LingoServer, Request, ServerConfig, serve_unbatched
+    buf, off = S.smiles_buffer(S.SEED_SERVING, S.UNIFORM_20_90, SERVING_DB_N)
+    db = compile_buffer(buf, off)
+    db_dev = compile_buffer_gpu(buf, off)
+    del buf, off
+    # the GPU compiler's arrays equal the host compiler's, molecule for molecule
+    for a, b in zip(db, db_dev):
+        assert tuple(b.shape) == a.shape
+        for i0 in range(0, SERVING_DB_N, 1_000_000):
+            assert torch.equal(torch.from_numpy(np.ascontiguousarray(a[i0:i0 + 1_000_000])).to(b.device),
+                               b[i0:i0 + 1_000_000]), i0
+    gl = GPULingo(0)
+    gl.set_qsmiles(*db_dev)
+    del db_dev
+    srv = LingoServer(gl, ServerConfig(max_rows=512, width=128, kmax=64, pitch=256, lo=0.75))
+    rng = np.random.default_rng(20260005)
+    reqs, pos = [], SERVING_DB_N
+    for i in range(16):
+        q = int(np.floor(np.exp(rng.uniform(0.0, np.log(513.0)))))
+        smi = S.smiles_list(S.SEED_SERVING, S.UNIFORM_20_90, q, first=pos)
+        pos += q
+        reqs.append(Request(i, smi, kind="topk" if i % 2 == 0 else "threshold", k=50, lo=0.75))
+    for r in reqs:   # all queued before the loop starts: batches take as many as fit
+        srv.submit(r)
+    srv.start()
+    for r in reqs:
+        assert r.done.wait(300), r.rid
+    srv.stop()
+    assert srv.batches < len(reqs)
+    for r in reqs:
+        assert r.error is None, r.error
+        a = Request(r.rid, r.smiles, kind=r.kind, k=r.k, lo=r.lo)
+        serve_unbatched(srv, a)
+        assert len(a.result) == len(r.result) == r.rows
+        for x, y in zip(a.result, r.result):
+            assert np.array_equal(x[0], y[0]) and np.array_equal(np.asarray(x[1]).view(np.uint32),
+                                                                 np.asarray(y[1]).view(np.uint32)), r.rid
+    for r in sorted(reqs, key=lambda q: q.rows)[:2]:
+        qs = oracle.compile_strings(r.smiles)
+        if r.kind == "topk":
+            oi, os_ = oracle.topk_block(qs, db, 0, r.rows, r.k)
+            want = [(oi[q], os_[q]) for q in range(r.rows)]
+        else:
+            oi, osm, oc = oracle.neighbors_block(qs, db, 0, r.rows, 0.75, 1.1, 4096)
+            assert int(oc.max()) <= 4096
+            want = [(oi[q, :oc[q]], osm[q, :oc[q]]) for q in range(r.rows)]
+        for x, y in zip(r.result, want):
+            assert np.array_equal(x[0], y[0]) and np.array_equal(np.asarray(x[1]).view(np.uint32),
+                                                                 np.asarray(y[1]).view(np.uint32)), r.rid
+    del srv, gl
+    torch.cuda.empty_cache()

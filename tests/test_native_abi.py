@@ -60,3 +60,16 @@ def test_sliced_counter_host_unit(tmp_path):
                     os.path.join(REPO, "tests", "native", "sliced_counter_test.cpp"), "-o", exe], check=True)
     r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_stream_argument_maps_torch_default_stream_to_legacy():
+    """siml_set_stream(NULL) selects the engine's own (non-blocking) stream,
+    so torch's default stream (handle 0) is passed as cudaStreamLegacy."""
+    from siml_gb300 import _native as N
+
+    class _S:
+        def __init__(self, h):
+            self.cuda_stream = h
+
+    assert N.stream_arg(_S(0)).value == N.CUDA_STREAM_LEGACY == 1
+    assert N.stream_arg(_S(0x7F001234)).value == 0x7F001234
