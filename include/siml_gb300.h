@@ -61,7 +61,8 @@ int siml_create(int device, siml_engine** out);
 int siml_destroy(siml_engine* h);
 /* Run subsequent work on a caller-owned cudaStream_t (NULL: the engine's own,
  * a non-blocking stream).  For the legacy default stream pass cudaStreamLegacy
- * ((void*)1), not NULL. */
+ * ((void*)1), not NULL.  Work on the engine's own stream is not ordered after
+ * other streams: device inputs written there must be complete first. */
 int siml_set_stream(siml_engine* h, void* cuda_stream);
 /* stream.synchronize() inside retrieveAsyncResult — pysiml/GPULingo.py:546. */
 int siml_sync(siml_engine* h);
