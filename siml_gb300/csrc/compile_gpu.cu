@@ -3,13 +3,15 @@
 // (pysiml/_ccompiler.cpp:276-381), for strings already in device memory, so
 // a database can be compiled and made resident without a host round trip.
 //
-// One warp per string.  Lane 0 runs the preprocessing state machine in
-// place over the string's bytes (each input byte yields at most one output
-// byte, so the writes trail the reads); the lanes then form the windows in
-// parallel, sort them with a bitonic network, and mark run starts with
-// ballots: the unique codes and their counts go straight to the string's
-// output row.  Strings of up to kCompileCap bytes work in shared memory;
-// longer ones are listed and compiled by the same code over global scratch.
+// One warp per string.  A string free of the bytes that carry state (see
+// lingo::stateful_byte) is preprocessed by all lanes at once; otherwise lane
+// 0 runs the preprocessing state machine in place over the string's bytes
+// (each input byte yields at most one output byte, so the writes trail the
+// reads).  The lanes then form the windows in parallel, sort them with a
+// bitonic network, and mark run starts with ballots: the unique codes and
+// their counts go straight to the string's output row.  Strings of up to
+// kCompileCap bytes work in shared memory; longer ones are listed and
+// compiled by the same code over global scratch.
 #include <algorithm>
 #include <vector>
 
@@ -31,11 +33,22 @@ constexpr int kCompileWarps = 8;        // warps (strings in flight) per CTA
 __device__ void compile_one(const unsigned char* __restrict__ raw, int64_t inlen, unsigned char* buf, int32_t* codes,
                             int64_t width, int32_t* lrow, int32_t* crow, int32_t* length, int32_t* mag, int* maxw) {
     const int lane = threadIdx.x & 31;
-    for (int64_t i = lane; i < inlen; i += 32) buf[i] = raw[i];
-    __syncwarp();
-    int32_t len = 0;
-    if (lane == 0) len = lingo::preprocess(buf, inlen, buf);
-    len = __shfl_sync(0xFFFFFFFFu, len, 0);
+    bool stateful = false;
+    for (int64_t i = lane; i < inlen; i += 32) {
+        const unsigned char c = raw[i];
+        buf[i] = c;
+        stateful |= lingo::stateful_byte(c);
+    }
+    int32_t len = (int32_t)inlen;
+    if (__ballot_sync(0xFFFFFFFFu, stateful) == 0u) {
+        // digits become '0', every other byte stays: each lane maps its own bytes
+        for (int64_t i = lane; i < inlen; i += 32)
+            if (lingo::is_digit(buf[i])) buf[i] = '0';
+    } else {
+        __syncwarp();
+        if (lane == 0) len = lingo::preprocess(buf, inlen, buf);
+        len = __shfl_sync(0xFFFFFFFFu, len, 0);
+    }
     __syncwarp();
     int32_t m = 0;
     if (len >= 4) {

@@ -36,6 +36,14 @@ namespace lingo {
 
 SIML_CHD bool is_digit(unsigned char c) { return c >= '0' && c <= '9'; }
 
+// Bytes that make preprocessing depend on state: the '+', '-', 'H', '['
+// and '%' rules and the terminators.  A string with none of them is
+// preprocessed by mapping each digit to '0' and keeping every other byte.
+SIML_CHD bool stateful_byte(unsigned char c) {
+    return c == '+' || c == '-' || c == 'H' || c == '[' || c == '%' || c == ' ' || c == '\n' || c == '\r' ||
+           c == 0;
+}
+
 // Returns the processed length; out needs inlen bytes.
 SIML_CHD int32_t preprocess(const unsigned char* in, int64_t inlen, unsigned char* out) {
     enum State { kNormal, kSwallow, kAfterDigit, kVerbatimDigits };

@@ -198,6 +198,25 @@ def test_invalid_sets_are_rejected(native):
         gl.getMultipleRows(0, 1)
 
 
+def test_engine_on_torch_default_stream(native, oracle, set4096):
+    """A GPULingo object given torch's default stream (handle 0, the legacy
+    default stream) is ordered with torch's work there: device inputs whose
+    upload queues behind ~0.1 s of other work are read only once written,
+    and the rows are ready for torch's next operation."""
+    torch = pytest.importorskip("torch")
+    from siml_gb300 import GPULingo
+    gl = GPULingo(0, stream=torch.cuda.default_stream())
+    for _ in range(2):
+        torch.cuda._sleep(200_000_000)   # bounded spin on the default stream
+        L, C, ln, mg = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in set4096)
+        gl.set_qsmiles(L, C, ln, mg)
+        gl.set_refsmiles(L[:256], C[:256], ln[:256], mg[:256])
+        torch.cuda._sleep(200_000_000)
+        out = gl.getMultipleRowsDevice(0, 256)
+        got = out.cpu().numpy()
+        assert np.array_equal(got, oracle.tanimoto_block(set4096, set4096, 0, 256))
+
+
 def test_torch_device_inputs_and_outputs(native, oracle, set4096):
     torch = pytest.importorskip("torch")
     from siml_gb300 import GPULingo
