@@ -59,7 +59,7 @@ def compile_buffer_gpu(buf, offsets, device: int = 0):
     tensor of n+1 entries.  The result can go straight to set_qsmiles /
     set_refsmiles without a host round trip."""
     import torch
-    from .utilities import _engine
+    from .utilities import _shared
     dev = torch.device("cuda", device)
     off_h = offsets.cpu().numpy() if isinstance(offsets, torch.Tensor) else np.asarray(offsets)
     off_h = np.ascontiguousarray(off_h, dtype=np.int64).reshape(-1)
@@ -87,19 +87,21 @@ def compile_buffer_gpu(buf, offsets, device: int = 0):
             text = host.to(dev)
     off_d = torch.from_numpy(off_h).to(dev)
     L = N.lib()
-    h = _engine(device)
-    N.check(L.siml_set_stream(h, N.stream_arg(torch.cuda.current_stream(dev))), "siml_set_stream")
-    w = L.siml_compile_width_gpu(h, text.data_ptr(), off_d.data_ptr(), n)
-    if w < 0:
-        N.check(int(-w), "siml_compile_width_gpu")
-    lingos = torch.zeros((n, w), dtype=torch.int32, device=dev)
-    counts = torch.zeros((n, w), dtype=torch.int32, device=dev)
-    lengths = torch.zeros(n, dtype=torch.int32, device=dev)
-    mags = torch.zeros(n, dtype=torch.int32, device=dev)
-    if w > 0:
-        N.check(L.siml_compile_smiles_gpu(h, text.data_ptr(), off_d.data_ptr(), n, lingos.data_ptr(),
-                                          counts.data_ptr(), lengths.data_ptr(), mags.data_ptr(), w),
-                "siml_compile_smiles_gpu")
+    e = _shared(device)
+    with e.lock:
+        h = e.h
+        N.check(L.siml_set_stream(h, N.stream_arg(torch.cuda.current_stream(dev))), "siml_set_stream")
+        w = L.siml_compile_width_gpu(h, text.data_ptr(), off_d.data_ptr(), n)
+        if w < 0:
+            N.check(int(-w), "siml_compile_width_gpu")
+        lingos = torch.zeros((n, w), dtype=torch.int32, device=dev)
+        counts = torch.zeros((n, w), dtype=torch.int32, device=dev)
+        lengths = torch.zeros(n, dtype=torch.int32, device=dev)
+        mags = torch.zeros(n, dtype=torch.int32, device=dev)
+        if w > 0:
+            N.check(L.siml_compile_smiles_gpu(h, text.data_ptr(), off_d.data_ptr(), n, lingos.data_ptr(),
+                                              counts.data_ptr(), lengths.data_ptr(), mags.data_ptr(), w),
+                    "siml_compile_smiles_gpu")
     return lingos, counts, lengths, mags
 
 

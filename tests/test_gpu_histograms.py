@@ -73,3 +73,38 @@ def test_row_histogram101_utility(native, golden):
     assert np.array_equal(rowHistogram101(D), want)
     with pytest.raises(ValueError):
         rowHistogram101(np.zeros((3, 3), np.int32))
+
+
+def test_shared_engine_users_from_two_threads(native):
+    """rowHistogram101 and the GPU compiler share one engine per device; two
+    host threads using them at once get the single-thread results."""
+    import threading
+    import torch
+    from siml_gb300 import synthetic as S, utilities as U
+    from siml_gb300.compiler import compile_buffer, compile_buffer_gpu
+    rng = np.random.default_rng(11)
+    mats = [torch.from_numpy(rng.random((300, 2000), dtype=np.float32)).cuda() for _ in range(2)]
+    want_h = [U.rowHistogram101(m.cpu().numpy()) for m in mats]
+    buf, off = S.smiles_buffer(S.SEED_ALLPAIRS, S.UNIFORM_20_90, 3000)
+    want_c = compile_buffer(buf, off)
+    errors = []
+
+    def work(i):
+        try:
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                for _ in range(10):
+                    h = U.rowHistogram101(mats[i])
+                    c = compile_buffer_gpu(buf, off)
+                    s.synchronize()
+                    assert np.array_equal(h.cpu().numpy().astype(np.uint32), want_h[i])
+                    assert all(np.array_equal(a.cpu().numpy(), b) for a, b in zip(c, want_c))
+        except Exception as e:  # reported in the main thread
+            errors.append(e)
+
+    ts = [threading.Thread(target=work, args=(i,)) for i in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors, errors
