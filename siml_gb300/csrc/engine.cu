@@ -13,6 +13,9 @@
 //                         the database are dropped; they cannot match).
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "engine.h"
@@ -23,6 +26,37 @@ namespace siml {
 int cuda_fail(cudaError_t e, const char* what) {
     int code = (e == cudaErrorMemoryAllocation) ? SIML_ERR_NOMEM : SIML_ERR_CUDA;
     return fail(code, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+}
+
+namespace {
+std::mutex g_smem_mu;
+std::map<std::pair<const void*, int>, size_t> g_smem_limit;   // (kernel, device) -> dynamic limit set
+}  // namespace
+
+int raise_smem_limit(const void* kernel, size_t need) {
+    int dev = 0;
+    SIML_CUDA(cudaGetDevice(&dev));
+    const std::pair<const void*, int> key(kernel, dev);
+    size_t limit = 0;
+    {
+        std::lock_guard<std::mutex> lk(g_smem_mu);
+        auto it = g_smem_limit.find(key);
+        if (it != g_smem_limit.end()) limit = it->second;
+    }
+    if (limit == 0) {
+        cudaFuncAttributes a;
+        SIML_CUDA(cudaFuncGetAttributes(&a, kernel));
+        int optin = 0;
+        SIML_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        limit = (size_t)std::max(0, optin - (int)a.sharedSizeBytes);
+        SIML_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
+        std::lock_guard<std::mutex> lk(g_smem_mu);
+        g_smem_limit[key] = limit;
+    }
+    if (need > limit)
+        return fail(SIML_ERR_UNSUPPORTED, "a kernel launch needs %zu bytes of dynamic shared memory, more than the "
+                    "%zu this GPU allows it", need, limit);
+    return SIML_OK;
 }
 
 int scratch_reserve(siml_engine* h, size_t bytes, void** out, int slot) {
@@ -734,7 +768,8 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     }
     if (d.window > kChunk) {
         const size_t wsm = (size_t)d.window * 8;
-        SIML_CUDA(cudaFuncSetAttribute(k_window_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+        rc = raise_smem_limit(reinterpret_cast<const void*>(k_window_sort), wsm);
+        if (rc) return rc;
         k_window_sort<<<(unsigned)nwin, std::min(d.window, 1024), wsm, st>>>(scount, q.n, d.window, d.perm);
     } else {
         k_identity_perm<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(q.n, slots, d.perm);

@@ -150,6 +150,13 @@ int row_order_by_magnitude(siml_engine* h, int64_t rowbase, int64_t rowlimit, co
 constexpr int kOrderBuckets = 4096;
 int row_order_into(siml_engine* h, int64_t rowbase, int64_t rowlimit, int32_t* order, int32_t* bucket);
 int cuda_fail(cudaError_t e, const char* what);
+// Lets `kernel` launch with up to `need` bytes of dynamic shared memory on
+// the current device.  The limit is an attribute of the function, shared by
+// every engine and host thread, so it is raised once per kernel and device
+// to the most the kernel can use (the opt-in limit less its static shared
+// memory) and never set per launch: a smaller value set for one engine
+// would make another thread's larger launch of the same kernel fail.
+int raise_smem_limit(const void* kernel, size_t need);
 // Reports (and clears) an expired top-k lock wait recorded by queued kernels;
 // call only once their work is known to be complete.
 int take_async_error(siml_engine* h);

@@ -1994,8 +1994,7 @@ cudaError_t mark(siml_engine* h, cudaEvent_t ev) {
 
 template <class K>
 int set_smem(K kernel, size_t smem) {
-    SIML_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    return SIML_OK;
+    return raise_smem_limit(reinterpret_cast<const void*>(kernel), smem);
 }
 
 template <int NP, typename ET>

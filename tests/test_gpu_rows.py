@@ -294,3 +294,39 @@ def test_rows_padded_and_balanced_layouts(native, oracle, golden, layout, fmt):
     rows = golden["rows"]
     _load(gl, tuple(a[rows] for a in g), g)
     assert np.array_equal(gl.getMultipleRows(0, len(rows)), golden["tanimoto"])
+
+
+def test_two_engines_in_two_threads(native, set4096):
+    """Two engines with different shared-memory tables (about 120 KB and 75 KB,
+    both on the balanced layout) launch the same row kernel from
+    two host threads at once; every launch succeeds and gives the
+    single-thread result."""
+    import threading
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    big = _random_sets(rng, 1500, 40, (0, 2 ** 31 - 1), 1, p_empty=0.0)   # ~30K distinct pairs
+    sets = [(big, big), (set4096, set4096)]
+    engines, want = [], []
+    for ref, qry in sets:
+        gl = _engine()
+        _load(gl, tuple(a[:64] for a in ref), qry)
+        want.append(gl.getMultipleRowsDevice(0, 64).cpu())
+        engines.append(gl)
+    va, vb = engines[0].vocabStats(), engines[1].vocabStats()
+    assert 25000 < va["nvid"] == va["ncommon"] < 38000 and vb["nvid"] < va["nvid"] - 10000
+    errors = []
+
+    def work(i):
+        try:
+            for _ in range(200):
+                out = engines[i].getMultipleRowsDevice(0, 64)
+                assert torch.equal(out.cpu(), want[i])
+        except Exception as e:  # reported in the main thread
+            errors.append(e)
+
+    ts = [threading.Thread(target=work, args=(i,)) for i in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors, errors
