@@ -692,7 +692,10 @@ def serving_arm(args):
     t_compile = time.time() - t
     dev = torch.device("cuda", local)
     # the database is made resident from the GPU compiler's output: SMILES
-    # bytes up, compiled on the device, no host arrays
+    # bytes up, compiled on the device, no host arrays.  A few strings are
+    # compiled first so that one-time set-up (the compiler's engine, loading
+    # its kernels) stays out of the ingest time.
+    compile_buffer_gpu(buf[:off[64]], off[:65], device=local)
     torch.cuda.synchronize()
     t = time.time()
     db_dev = compile_buffer_gpu(buf, off, device=local)
