@@ -227,6 +227,22 @@ int64_t siml_compile_width_gpu(siml_engine* h, const char* buf, const int64_t* o
 int siml_compile_smiles_gpu(siml_engine* h, const char* buf, const int64_t* offsets, int64_t n,
                             int32_t* lingos, int32_t* counts, int32_t* lengths,
                             int32_t* mags, int64_t width);
+/* One-pass form of the GPU compiler (no reference counterpart; the same
+ * output as the two calls above, each string compiled once).
+ * siml_compile_stage_gpu compiles every string into device staging arrays of
+ * offsets[n] int32 each (string s's unique codes and counts, unpadded, at
+ * [offsets[s], offsets[s] + lengths[s])), writes lengths and mags [n], and
+ * returns the width (waits for the stream) or a negative status.
+ * siml_compile_scatter_gpu then writes the zero-padded [n, width] rows
+ * (width >= the returned width, else SIML_ERR_INVALID) and returns once they
+ * are written. */
+int64_t siml_compile_stage_gpu(siml_engine* h, const char* buf, const int64_t* offsets, int64_t n,
+                               int32_t* stage_codes, int32_t* stage_counts, int32_t* lengths,
+                               int32_t* mags);
+int siml_compile_scatter_gpu(siml_engine* h, const int64_t* offsets, int64_t n,
+                             const int32_t* stage_codes, const int32_t* stage_counts,
+                             const int32_t* lengths, int32_t* lingos, int32_t* counts,
+                             int64_t width);
 
 /* ---- utilities ---------------------------------------------------------- */
 /* rowHistogram101 — pysiml/utilities.py:44-55, pysiml/_cpuutil.cpp:52-126:

@@ -95,6 +95,8 @@ _SIGNATURES = {
     "siml_vocab_stats": (_I32, [_P, _P]),
     "siml_compile_width_gpu": (_I64, [_P, _P, _P, _I64]),
     "siml_compile_smiles_gpu": (_I32, [_P, _P, _P, _I64, _P, _P, _P, _P, _I64]),
+    "siml_compile_stage_gpu": (_I64, [_P, _P, _P, _I64, _P, _P, _P, _P]),
+    "siml_compile_scatter_gpu": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _I64]),
     "siml_last_kernel_ms": (ctypes.c_double, [_P]),
 }
 

@@ -91,17 +91,23 @@ def compile_buffer_gpu(buf, offsets, device: int = 0):
     with e.lock:
         h = e.h
         N.check(L.siml_set_stream(h, N.stream_arg(torch.cuda.current_stream(dev))), "siml_set_stream")
-        w = L.siml_compile_width_gpu(h, text.data_ptr(), off_d.data_ptr(), n)
+        # one pass: every string compiled once into staging (its stretch of
+        # the byte range holds its unique codes), then scattered into rows
+        stage_codes = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+        stage_counts = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+        lengths = torch.empty(max(n, 1), dtype=torch.int32, device=dev)[:n]
+        mags = torch.empty(max(n, 1), dtype=torch.int32, device=dev)[:n]
+        w = L.siml_compile_stage_gpu(h, text.data_ptr(), off_d.data_ptr(), n, stage_codes.data_ptr(),
+                                     stage_counts.data_ptr(), lengths.data_ptr(), mags.data_ptr())
         if w < 0:
-            N.check(int(-w), "siml_compile_width_gpu")
-        lingos = torch.zeros((n, w), dtype=torch.int32, device=dev)
-        counts = torch.zeros((n, w), dtype=torch.int32, device=dev)
-        lengths = torch.zeros(n, dtype=torch.int32, device=dev)
-        mags = torch.zeros(n, dtype=torch.int32, device=dev)
-        if w > 0:
-            N.check(L.siml_compile_smiles_gpu(h, text.data_ptr(), off_d.data_ptr(), n, lingos.data_ptr(),
-                                              counts.data_ptr(), lengths.data_ptr(), mags.data_ptr(), w),
-                    "siml_compile_smiles_gpu")
+            N.check(int(-w), "siml_compile_stage_gpu")
+        lingos = torch.empty((n, w), dtype=torch.int32, device=dev)
+        counts = torch.empty((n, w), dtype=torch.int32, device=dev)
+        if w > 0 and n > 0:
+            N.check(L.siml_compile_scatter_gpu(h, off_d.data_ptr(), n, stage_codes.data_ptr(), stage_counts.data_ptr(),
+                                               lengths.data_ptr(), lingos.data_ptr(), counts.data_ptr(), w),
+                    "siml_compile_scatter_gpu")
+        del stage_codes, stage_counts   # the scatter has returned: its reads are done
     return lingos, counts, lengths, mags
 
 

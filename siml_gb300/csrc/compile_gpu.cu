@@ -27,11 +27,12 @@ constexpr int kCompileWarps = 8;        // warps (strings in flight) per CTA
 // Compiles one string with the calling warp.  buf holds >= inlen + 8 bytes
 // and codes >= max(next power of two >= inlen, 32) words of scratch.
 // Always raises *maxw to the number of unique codes.  width > 0: also
-// writes the row (zero padded to width), length and magnitude, unless the
-// string has more unique codes than width (the caller then reports it).
-// No write leaves the row.
+// writes the row (zero padded to width when pad), length and magnitude,
+// unless the string has more unique codes than width (the caller then
+// reports it).  No write leaves the row.
 __device__ void compile_one(const unsigned char* __restrict__ raw, int64_t inlen, unsigned char* buf, int32_t* codes,
-                            int64_t width, int32_t* lrow, int32_t* crow, int32_t* length, int32_t* mag, int* maxw) {
+                            int64_t width, int32_t* lrow, int32_t* crow, int32_t* length, int32_t* mag, int* maxw,
+                            bool pad = true) {
     const int lane = threadIdx.x & 31;
     bool stateful = false;
     for (int64_t i = lane; i < inlen; i += 32) {
@@ -121,9 +122,11 @@ __device__ void compile_one(const unsigned char* __restrict__ raw, int64_t inlen
         if (r < nu) crow[r] = b - a;
         __syncwarp();
     }
-    for (int64_t j = nu + lane; j < width; j += 32) {
-        lrow[j] = 0;
-        crow[j] = 0;
+    if (pad) {
+        for (int64_t j = nu + lane; j < width; j += 32) {
+            lrow[j] = 0;
+            crow[j] = 0;
+        }
     }
     if (lane == 0) {
         *length = nu;
@@ -131,7 +134,22 @@ __device__ void compile_one(const unsigned char* __restrict__ raw, int64_t inlen
     }
 }
 
+// Output row of string s: row s of [n, width] (zero padded), or with STAGED
+// its stretch [off[s], off[s+1]) of the staging arrays, which holds its
+// unique codes unpadded (a string has at most as many unique windows as
+// bytes).
+struct RowOut {
+    int64_t row;
+    int64_t width;
+};
+template <bool STAGED>
+__device__ __forceinline__ RowOut row_out(int64_t s, int64_t b, int64_t inlen, int64_t width) {
+    if (STAGED) return {b, inlen > 0 ? inlen : 1};
+    return {s * width, width};
+}
+
 // Strings of at most kCompileCap bytes; longer ones are appended to `longs`.
+template <bool STAGED>
 __global__ void __launch_bounds__(kCompileWarps * 32) k_compile(const unsigned char* __restrict__ text,
                                                                 const int64_t* __restrict__ off, int64_t n,
                                                                 int64_t width, int32_t* lingos, int32_t* counts,
@@ -147,14 +165,16 @@ __global__ void __launch_bounds__(kCompileWarps * 32) k_compile(const unsigned c
             if (lane == 0) longs[atomicAdd(nlong, 1)] = s;
             continue;
         }
-        compile_one(text + b, inlen, sbuf[warp], scodes[warp], width, lingos + s * width, counts + s * width,
-                    lengths + s, mags + s, maxw);
+        const RowOut o = row_out<STAGED>(s, b, inlen, width);
+        compile_one(text + b, inlen, sbuf[warp], scodes[warp], o.width, lingos + o.row, counts + o.row, lengths + s,
+                    mags + s, maxw, !STAGED);
         __syncwarp();
     }
 }
 
 // The listed long strings, one warp each, over global scratch at
 // scratch_off[i] bytes (bytes first, then the code words, 16-byte aligned).
+template <bool STAGED>
 __global__ void __launch_bounds__(32) k_compile_long(const unsigned char* __restrict__ text,
                                                      const int64_t* __restrict__ off, const int64_t* __restrict__ longs,
                                                      const int64_t* __restrict__ scratch_off, char* scratch,
@@ -165,8 +185,31 @@ __global__ void __launch_bounds__(32) k_compile_long(const unsigned char* __rest
     char* base = scratch + scratch_off[blockIdx.x];
     unsigned char* buf = reinterpret_cast<unsigned char*>(base);
     int32_t* codes = reinterpret_cast<int32_t*>(base + ((inlen + 16 + 15) / 16) * 16);
-    compile_one(text + b, inlen, buf, codes, width, lingos + s * width, counts + s * width, lengths + s, mags + s,
-                maxw);
+    const RowOut o = row_out<STAGED>(s, b, inlen, width);
+    compile_one(text + b, inlen, buf, codes, o.width, lingos + o.row, counts + o.row, lengths + s, mags + s, maxw,
+                !STAGED);
+}
+
+// Staged rows into [n, width]: warp per string, zero padded past its unique
+// codes.  A string's count is bounded by its staging stretch, so no read
+// leaves it; *bad is set when a string has more codes than width.
+__global__ void k_compile_scatter(const int64_t* __restrict__ off, int64_t n, const int32_t* __restrict__ sc,
+                                  const int32_t* __restrict__ sn, const int32_t* __restrict__ lengths, int64_t width,
+                                  int32_t* __restrict__ lingos, int32_t* __restrict__ counts, int* bad) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t s = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); s < n; s += nwarps) {
+        const int64_t b = off[s];
+        const int64_t nu = min((int64_t)max(lengths[s], 0), off[s + 1] - b);
+        if (lane == 0 && nu > width) atomicOr(bad, 1);
+        int32_t* lr = lingos + s * width;
+        int32_t* cr = counts + s * width;
+        for (int64_t j = lane; j < width; j += 32) {
+            const bool in = j < nu;
+            lr[j] = in ? sc[b + j] : 0;
+            cr[j] = in ? sn[b + j] : 0;
+        }
+    }
 }
 
 int64_t pow2_at_least(int64_t v) {
@@ -175,9 +218,11 @@ int64_t pow2_at_least(int64_t v) {
     return p;
 }
 
-// Runs both kernels; width == 0 computes the width into *maxw_out.
+// Runs both kernels; width == 0 computes the width into *maxw_out.  staged:
+// lingos/counts are staging arrays of off[n] words (width is ignored) and
+// every string's row, length and magnitude are written.
 int compile_gpu(siml_engine* h, const char* text, const int64_t* off, int64_t n, int64_t width, int32_t* lingos,
-                int32_t* counts, int32_t* lengths, int32_t* mags, int64_t* maxw_out) {
+                int32_t* counts, int32_t* lengths, int32_t* mags, int64_t* maxw_out, bool staged = false) {
     cudaStream_t st = h->stream;
     if (n == 0) {
         if (maxw_out) *maxw_out = 0;
@@ -199,8 +244,9 @@ int compile_gpu(siml_engine* h, const char* text, const int64_t* off, int64_t n,
     if ((e = cudaMemsetAsync(d_small, 0, 2 * sizeof(int), st)) != cudaSuccess) return done(cuda_fail(e, "memset"));
     const int64_t per_cta = kCompileWarps;
     const int64_t grid = std::min<int64_t>((n + per_cta - 1) / per_cta, (int64_t)h->num_sms * 16);
-    k_compile<<<(unsigned)grid, kCompileWarps * 32, 0, st>>>((const unsigned char*)text, off, n, width, lingos,
-                                                             counts, lengths, mags, d_small, d_longs, d_small + 1);
+    auto kc = staged ? k_compile<true> : k_compile<false>;
+    kc<<<(unsigned)grid, kCompileWarps * 32, 0, st>>>((const unsigned char*)text, off, n, width, lingos, counts,
+                                                      lengths, mags, d_small, d_longs, d_small + 1);
     if ((e = cudaGetLastError()) != cudaSuccess) return done(cuda_fail(e, "k_compile"));
     h->launches++;
     int hs[2] = {0, 0};
@@ -231,8 +277,9 @@ int compile_gpu(siml_engine* h, const char* text, const int64_t* off, int64_t n,
             cudaFreeAsync(scratch, st);
             return done(cuda_fail(e, "long-string scratch"));
         }
-        k_compile_long<<<(unsigned)nlong, 32, 0, st>>>((const unsigned char*)text, off, d_longs, d_soff, scratch,
-                                                       width, lingos, counts, lengths, mags, d_small);
+        auto kl = staged ? k_compile_long<true> : k_compile_long<false>;
+        kl<<<(unsigned)nlong, 32, 0, st>>>((const unsigned char*)text, off, d_longs, d_soff, scratch, width, lingos,
+                                           counts, lengths, mags, d_small);
         e = cudaGetLastError();
         h->launches++;
         if (e == cudaSuccess) e = cudaMemcpyAsync(hs, d_small, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -304,6 +351,43 @@ int siml_compile_smiles_gpu(siml_engine* h, const char* buf, const int64_t* offs
     if ((rc = compile_gpu(h, buf, offsets, n, width, lingos, counts, lengths, mags, &w))) return rc;
     if (w > width)
         return fail(SIML_ERR_INVALID, "siml_compile_smiles_gpu: width smaller than a string's unique LINGO count");
+    return SIML_OK;
+}
+
+int64_t siml_compile_stage_gpu(siml_engine* h, const char* buf, const int64_t* offsets, int64_t n,
+                               int32_t* stage_codes, int32_t* stage_counts, int32_t* lengths, int32_t* mags) {
+    clear_error();
+    if (!h) return -fail(SIML_ERR_INVALID, "siml_compile_stage_gpu: NULL engine");
+    if (n < 0 || (n > 0 && (!buf || !offsets || !stage_codes || !stage_counts || !lengths || !mags)))
+        return -fail(SIML_ERR_INVALID, "siml_compile_stage_gpu: bad arguments");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return -cuda_fail(e, "cudaSetDevice");
+    int rc = check_offsets_gpu(h, offsets, n);
+    if (rc) return -rc;
+    int64_t w = 0;
+    rc = compile_gpu(h, buf, offsets, n, 0, stage_codes, stage_counts, lengths, mags, &w, true);
+    return rc ? -rc : w;
+}
+
+int siml_compile_scatter_gpu(siml_engine* h, const int64_t* offsets, int64_t n, const int32_t* stage_codes,
+                             const int32_t* stage_counts, const int32_t* lengths, int32_t* lingos, int32_t* counts,
+                             int64_t width) {
+    clear_error();
+    if (!h) return fail(SIML_ERR_INVALID, "siml_compile_scatter_gpu: NULL engine");
+    if (n < 0 || width < 1 || (n > 0 && (!offsets || !stage_codes || !stage_counts || !lengths || !lingos || !counts)))
+        return fail(SIML_ERR_INVALID, "siml_compile_scatter_gpu: bad arguments");
+    if (n == 0) return SIML_OK;
+    SIML_CUDA(cudaSetDevice(h->device));
+    SIML_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+    const int64_t grid = std::min<int64_t>((n + 7) / 8, (int64_t)h->num_sms * 16);
+    k_compile_scatter<<<(unsigned)grid, 256, 0, h->stream>>>(offsets, n, stage_codes, stage_counts, lengths, width,
+                                                            lingos, counts, h->d_err);
+    SIML_CUDA(cudaGetLastError());
+    h->launches++;
+    int bad = 0;
+    SIML_CUDA(cudaMemcpyAsync(&bad, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    SIML_CUDA(cudaStreamSynchronize(h->stream));
+    if (bad) return fail(SIML_ERR_INVALID, "siml_compile_scatter_gpu: width smaller than a string's unique LINGO count");
     return SIML_OK;
 }
 

@@ -118,3 +118,42 @@ def test_gpu_compiler_is_ordered_after_torch_default_stream(native):
         torch.cuda._sleep(200_000_000)   # bounded spin on the default stream
         got = _gpu(buf, off)
         _same(got, want)
+
+
+def test_gpu_compiler_two_pass_entries_and_scatter_width(native):
+    """The two-pass C entries (width, then fill) give what the one-pass
+    staging path of compile_buffer_gpu gives, and the scatter refuses a
+    width below the widest string."""
+    import torch
+    from siml_gb300 import _native as N, synthetic as S
+    from siml_gb300.compiler import compile_buffer_gpu
+    buf, off = S.smiles_buffer(S.SEED_RAGGED, S.BIMODAL_35_110, 5000)
+    one = compile_buffer_gpu(buf, off)
+    dev = one[0].device
+    text = torch.from_numpy(np.frombuffer(buf, dtype=np.uint8).copy()).to(dev)
+    off_d = torch.from_numpy(off).to(dev)
+    L = N.lib()
+    from siml_gb300.utilities import _shared
+    e = _shared(0)
+    with e.lock:
+        h = e.h
+        N.check(L.siml_set_stream(h, N.stream_arg(torch.cuda.current_stream())), "siml_set_stream")
+        w = L.siml_compile_width_gpu(h, text.data_ptr(), off_d.data_ptr(), len(off) - 1)
+        assert w == one[0].shape[1]
+        n = len(off) - 1
+        got = [torch.zeros((n, w), dtype=torch.int32, device=dev) for _ in range(2)]
+        got += [torch.zeros(n, dtype=torch.int32, device=dev) for _ in range(2)]
+        N.check(L.siml_compile_smiles_gpu(h, text.data_ptr(), off_d.data_ptr(), n, *(t.data_ptr() for t in got), w))
+        # the scatter with a width one short of the widest string
+        sc = torch.empty(int(off[-1]), dtype=torch.int32, device=dev)
+        sn = torch.empty_like(sc)
+        ln = torch.empty(n, dtype=torch.int32, device=dev)
+        mg = torch.empty(n, dtype=torch.int32, device=dev)
+        assert L.siml_compile_stage_gpu(h, text.data_ptr(), off_d.data_ptr(), n, sc.data_ptr(), sn.data_ptr(),
+                                        ln.data_ptr(), mg.data_ptr()) == w
+        narrow = torch.empty((n, w - 1), dtype=torch.int32, device=dev)
+        rc = L.siml_compile_scatter_gpu(h, off_d.data_ptr(), n, sc.data_ptr(), sn.data_ptr(), ln.data_ptr(),
+                                        narrow.data_ptr(), narrow.clone().data_ptr(), w - 1)
+        assert rc == N.SIML_ERR_INVALID
+    for a, b in zip(got, one):
+        assert torch.equal(a, b)
