@@ -322,6 +322,13 @@ int siml_get_tuning(siml_engine* h, int key, int64_t* value);
 int siml_eval_pairs(siml_engine* h, uint64_t* out, int reset);
 /* Number of kernel launches this engine has issued since creation. */
 int64_t siml_launch_count(siml_engine* h);
+/* Fault injection for tests (no counterpart in the reference): the nth
+ * device allocation from now through the engines' array allocator, in any
+ * engine of the process, returns SIML_ERR_NOMEM without calling cudaMalloc,
+ * as an out-of-memory GPU would; 0 disarms.  Nothing is faulted on the GPU:
+ * the refusal is made on the host.  The engine stays usable, and the next
+ * call rebuilds whatever the failed one left unbuilt. */
+int siml_debug_fail_alloc(int64_t nth);
 /* Average device time (ms) of the dominant kernel of the last call on this
  * engine, measured with CUDA events on the engine's stream (0 if none). */
 double siml_last_kernel_ms(siml_engine* h);

@@ -96,6 +96,7 @@ _SIGNATURES = {
     "siml_compile_width_gpu": (_I64, [_P, _P, _P, _I64]),
     "siml_compile_smiles_gpu": (_I32, [_P, _P, _P, _I64, _P, _P, _P, _P, _I64]),
     "siml_compile_stage_gpu": (_I64, [_P, _P, _P, _I64, _P, _P, _P, _P]),
+    "siml_debug_fail_alloc": (_I32, [_I64]),
     "siml_compile_scatter_gpu": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _I64]),
     "siml_last_kernel_ms": (ctypes.c_double, [_P]),
 }

@@ -12,6 +12,7 @@
 //   ref-row entries       each ref row as its list of vids (pairs absent from
 //                         the database are dropped; they cannot match).
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -139,10 +140,19 @@ int row_order_by_magnitude(siml_engine* h, int64_t rowbase, int64_t rowlimit, co
 
 namespace {
 
+// siml_debug_fail_alloc: allocations left before one is refused (0: none).
+std::atomic<int64_t> g_fail_alloc{0};
+
 template <class T>
 int dev_alloc(T** p, size_t count) {
     *p = nullptr;
     if (count == 0) count = 1;
+    int64_t left = g_fail_alloc.load();
+    while (left > 0 && !g_fail_alloc.compare_exchange_weak(left, left - 1)) {
+    }
+    if (left == 1)
+        return fail(SIML_ERR_NOMEM, "device allocation of %zu bytes refused (siml_debug_fail_alloc)",
+                    count * sizeof(T));
     SIML_CUDA(cudaMalloc((void**)p, count * sizeof(T)));
     return SIML_OK;
 }
@@ -1231,6 +1241,13 @@ int siml_get_tuning(siml_engine* h, int key, int64_t* value) {
 }
 
 int64_t siml_launch_count(siml_engine* h) { return h ? h->launches : -1; }
+
+int siml_debug_fail_alloc(int64_t nth) {
+    clear_error();
+    if (nth < 0) return fail(SIML_ERR_INVALID, "siml_debug_fail_alloc: nth must be >= 0");
+    siml::g_fail_alloc.store(nth);
+    return SIML_OK;
+}
 
 double siml_last_kernel_ms(siml_engine* h) {
     if (!h || !h->timed) return 0.0;

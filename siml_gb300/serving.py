@@ -43,6 +43,11 @@ TOPK = "topk"
 THRESHOLD = "threshold"
 
 
+class RequestCancelled(RuntimeError):
+    """The error of a request withdrawn by LingoServer.cancel before it
+    joined a batch."""
+
+
 class Request:
     """One request: `smiles` (a list of bytes) and the kind of answer.
 
@@ -208,6 +213,22 @@ class LingoServer:
             self.queue.append(req)
             self.cv.notify()
         return req
+
+    def cancel(self, req):
+        """Withdraws a request that is still queued: it completes at once with
+        a RequestCancelled error and never joins a batch.  Returns False when
+        it has already joined one (its answer still arrives) or is not queued
+        here."""
+        with self.cv:
+            try:
+                self.queue.remove(req)
+            except ValueError:
+                return False
+        req.compiled = None
+        req.error = RequestCancelled("request %r was cancelled before it joined a batch" % (req.rid,))
+        req.t_done = time.perf_counter()
+        req.done.set()
+        return True
 
     def _compile(self, req):
         if req.compiled is None:

@@ -70,3 +70,19 @@ def test_batches_grow_under_a_backlog():
     for i in range(3, 8):
         srv.queue.append(_req(i, 5))
     assert [r.rid for r in srv._take_batch()] == [1, 2, 3]  # 35 queued rows > 20: up to 16
+
+
+def test_cancel_before_admission():
+    """A cancelled request leaves the queue at once with a RequestCancelled
+    error; one already taken into a batch cannot be cancelled."""
+    from siml_gb300.serving import RequestCancelled
+    srv = _fake_server(max_rows=8, pitch=16, kmax=8, hit_budget=1 << 20)
+    reqs = [_req(i, 3) for i in range(4)]
+    srv.queue.extend(reqs)
+    b1 = srv._take_batch()
+    assert [r.rid for r in b1] == [0, 1]
+    assert not srv.cancel(reqs[0])                 # already in a batch
+    assert srv.cancel(reqs[2])
+    assert reqs[2].done.is_set() and isinstance(reqs[2].error, RequestCancelled)
+    assert not srv.cancel(reqs[2])                 # no longer queued
+    assert [r.rid for r in srv._take_batch()] == [3]
