@@ -630,13 +630,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_nbr(const GroupParams p, const 
 // ripple adder and runs the padded kernel's epilogue, so stores stay one
 // 128-byte line per row.
 //
-// MASKED (layouts whose runs are all at most 32 steps: every chunk of a
+// MODE >= 1 (layouts whose runs are all at most 32 steps: every chunk of a
 // database whose molecules hold fewer than about 256 entries): lanes know
 // their flush steps before streaming.  The owner of each molecule sets bit
 // (end % L) of lane end / L's mask, and a lane's next molecule after a flush
 // is the next set bit of the warp's ballot of non-empty molecules, so a step
-// costs one bit test besides the flush itself.  Otherwise lanes walk the
-// prefix array.
+// costs one bit test besides the flush itself.  MODE 0: lanes walk the
+// prefix array.  MODE 2 (runs of at most 15 steps, with 8-plane counts): a
+// run holds at most 120 entries, so the lane's running counter and its
+// pieces need 7 planes; the ripple of each step's weight-8 carry is one
+// plane shorter and a flush stores one word less.  The molecule's counter,
+// made of the pieces, keeps NP planes.
 constexpr int kPieceSlots = 64;
 constexpr int kPrefixWords = 34;
 constexpr int kRowsBalThreads = 1024;   // threads of a k_rows_bal CTA (one CTA per SM beside the table)
@@ -645,20 +649,27 @@ __host__ __device__ constexpr size_t rows_bal_extra_smem(int np, int warps) {
     return (size_t)warps * ((size_t)np * kPieceSlots + kPrefixWords) * 4;
 }
 
-template <int NP>
-__device__ __forceinline__ void piece_store(uint32_t* pc, int slot, const SlicedCounter<NP>& acc) {
+template <int NPR>
+__device__ __forceinline__ void piece_store(uint32_t* pc, int slot, const SlicedCounter<NPR>& acc) {
 #pragma unroll
-    for (int q = 0; q < NP; q++) pc[q * kPieceSlots + slot] = acc.plane[q];
+    for (int q = 0; q < NPR; q++) pc[q * kPieceSlots + slot] = acc.plane[q];
 }
 
-template <int NP>
+// Adds an NPR-plane piece into an NP-plane counter (NPR <= NP).
+template <int NP, int NPR>
 __device__ __forceinline__ void piece_add(SlicedCounter<NP>& acc, const uint32_t* pc, int slot) {
     uint32_t carry = 0u;
 #pragma unroll
-    for (int q = 0; q < NP; q++) {
+    for (int q = 0; q < NPR; q++) {
         const uint32_t a = acc.plane[q], b = pc[q * kPieceSlots + slot];
         acc.plane[q] = a ^ b ^ carry;
         carry = (a & b) | (carry & (a ^ b));
+    }
+#pragma unroll
+    for (int q = NPR; q < NP; q++) {
+        const uint32_t a = acc.plane[q];
+        acc.plane[q] = a ^ carry;
+        carry = a & carry;
     }
 }
 
@@ -669,8 +680,10 @@ __device__ __forceinline__ int div_run(int x, float rl) {
     return (int)__fmul_rz(__int2float_rn(x) + 0.5f, rl);
 }
 
-template <int NP, typename ET, bool RARE, bool MASKED>
+template <int NP, typename ET, bool RARE, int MODE>
 __global__ void __launch_bounds__(kRowsBalThreads, 1) k_rows_bal(const GroupParams p, float* out, int64_t ldo) {
+    constexpr bool MASKED = MODE >= 1;
+    constexpr int NPR = (MODE == 2 && NP == 8) ? 7 : NP;   // planes of a lane's running counter
     extern __shared__ __align__(16) uint32_t T[];
     __shared__ RowSmem rs;
     const int nr = build_table(T, rs, p);   // synchronizes the block
@@ -728,7 +741,7 @@ __global__ void __launch_bounds__(kRowsBalThreads, 1) k_rows_bal(const GroupPara
 #pragma unroll
         for (int q = 16; q > 0; q >>= 1)
             if (m + q <= 31 && pre[m + q] <= seg0) m += q;
-        SlicedCounter<NP> acc;
+        SlicedCounter<NPR> acc;
         acc.clear();
         uint4 a0 = zero, b0 = zero, a1 = zero, b1 = zero;
         const uint4* Ec = E + base;
@@ -757,13 +770,13 @@ __global__ void __launch_bounds__(kRowsBalThreads, 1) k_rows_bal(const GroupPara
             for (int s = 0; s < L; s++) {
                 step(s);
                 if (f & 1u) {   // molecule m ends at this step
-                    piece_store<NP>(pc, lane + m, acc);
+                    piece_store<NPR>(pc, lane + m, acc);
                     acc.clear();
                     m = __ffs(nz & (0xFFFFFFFEu << m)) - 1;   // next molecule with entries
                 }
                 f >>= 1;
             }
-            if (open_end) piece_store<NP>(pc, lane + m, acc);
+            if (open_end) piece_store<NPR>(pc, lane + m, acc);
         } else {
             int endm = pre[m + 1];
             bool pending = false;
@@ -772,14 +785,14 @@ __global__ void __launch_bounds__(kRowsBalThreads, 1) k_rows_bal(const GroupPara
                 const int gs = seg0 + s + 1;
                 if (gs <= seg1) pending = true;   // a step of the run (past it: zero padding)
                 if (gs == endm && gs <= seg1) {   // molecule m ends inside this lane's run
-                    piece_store<NP>(pc, lane + m, acc);
+                    piece_store<NPR>(pc, lane + m, acc);
                     acc.clear();
                     pending = false;
                     do { m++; } while (m < 32 && pre[m + 1] == pre[m]);   // skip molecules with no entries
                     endm = m < 32 ? pre[m + 1] : 0x7FFFFFFF;
                 }
             }
-            if (pending && m < 32) piece_store<NP>(pc, lane + m, acc);   // run ended inside molecule m
+            if (pending && m < 32) piece_store<NPR>(pc, lane + m, acc);   // run ended inside molecule m
         }
         __syncwarp();
         SlicedCounter<NP> own;
@@ -794,7 +807,7 @@ __global__ void __launch_bounds__(kRowsBalThreads, 1) k_rows_bal(const GroupPara
                 fl = P / L;
                 ll = (P + g - 1) / L;
             }
-            for (int j = fl; j <= ll; j++) piece_add<NP>(own, pc, j + lane);
+            for (int j = fl; j <= ll; j++) piece_add<NP, NPR>(own, pc, j + lane);
         }
         if constexpr (RARE) rare_add<NP>(T, p, c * 32 + lane, own);
         epi(c, meta, own);
@@ -2002,12 +2015,22 @@ int launch_rows_bal_t(siml_engine* h, const GroupParams& p, size_t smem, float* 
     const int64_t groups = (p.rows + 31) / 32;
     const size_t sm = smem + rows_bal_extra_smem(NP, kRowsBalThreads / 32);
     constexpr int SPG = sizeof(ET) == 2 ? 1 : 2;
-    const bool masked = max_ng / SPG <= 32;   // every run fits a 32-bit flush mask
-    auto kern = masked ? k_rows_bal<NP, ET, false, true> : k_rows_bal<NP, ET, false, false>;
+    const int64_t run = max_ng / SPG;   // longest run of steps of a lane
+    // 1: every run fits a 32-bit flush mask; 2: and its counts fit 7 planes
+    const int mode = run > 32 ? 0 : (NP == 8 && run * 8 <= 127 ? 2 : 1);
+    auto kern = mode == 0 ? k_rows_bal<NP, ET, false, 0> : k_rows_bal<NP, ET, false, 1>;
+    if constexpr (NP == 8) {
+        if (mode == 2) kern = k_rows_bal<NP, ET, false, 2>;
+    }
     if (p.rare_slots) {
-        if constexpr (std::is_same<ET, uint16_t>::value)
-            kern = masked ? k_rows_bal<NP, ET, true, true> : k_rows_bal<NP, ET, true, false>;
-        else return fail(SIML_ERR_UNSUPPORTED, "a split vocabulary needs 16-bit entries");
+        if constexpr (std::is_same<ET, uint16_t>::value) {
+            kern = mode == 0 ? k_rows_bal<NP, ET, true, 0> : k_rows_bal<NP, ET, true, 1>;
+            if constexpr (NP == 8) {
+                if (mode == 2) kern = k_rows_bal<NP, ET, true, 2>;
+            }
+        } else {
+            return fail(SIML_ERR_UNSUPPORTED, "a split vocabulary needs 16-bit entries");
+        }
     }
     int rc = set_smem(kern, sm);
     if (rc) return rc;

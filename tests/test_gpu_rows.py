@@ -131,11 +131,16 @@ def _random_sets(rng, n, width, code_range, max_count, p_empty=0.05):
     return L, C, ln, mg
 
 
-@pytest.mark.parametrize("case", ["small_vocab", "negative_codes", "high_counts", "zero_mags", "long_db_molecules"])
+@pytest.mark.parametrize("case", ["small_vocab", "negative_codes", "high_counts", "zero_mags", "long_db_molecules",
+                                  "mid_db_molecules"])
 def test_rows_random_sets(native, oracle, case):
     rng = np.random.default_rng({"small_vocab": 1, "negative_codes": 2, "high_counts": 3, "zero_mags": 4,
-                                 "long_db_molecules": 5}[case])
-    if case == "long_db_molecules":
+                                 "long_db_molecules": 5, "mid_db_molecules": 6}[case])
+    if case == "mid_db_molecules":
+        # runs of 16-32 steps: flush masks, but counts past 7 planes
+        ref = _random_sets(rng, 70, 30, (0, 3000), 2)
+        qry = _random_sets(rng, 800, 250, (0, 3000), 1)
+    elif case == "long_db_molecules":
         # short ref rows (8-plane counters) against database molecules of up
         # to 800 entries: lanes' runs of the balanced layout exceed 32 steps
         ref = _random_sets(rng, 70, 30, (0, 3000), 2)
@@ -164,6 +169,9 @@ def test_rows_random_sets(native, oracle, case):
     if case == "long_db_molecules":
         st = gl.dbStats()
         assert st["max_ng"] > 32 and st["ref_max_entries"] <= 255, st
+    if case == "mid_db_molecules":
+        st = gl.dbStats()
+        assert 15 < st["max_ng"] <= 32 and st["ref_max_entries"] <= 255, st
 
 
 def test_large_vocabulary_uses_merge_path(native, oracle):
