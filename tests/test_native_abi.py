@@ -1,10 +1,8 @@
 """The C-ABI library: loads, exports every entry point include/siml_gb300.h
 declares, and reports errors through status codes (no GPU needed)."""
-import ctypes
 import os
 import re
 
-import numpy as np
 import pytest
 
 from tests.conftest import REPO

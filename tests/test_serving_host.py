@@ -3,7 +3,6 @@ latency percentiles."""
 import collections
 import threading
 
-import numpy as np
 import pytest
 
 

@@ -3,7 +3,6 @@ device memory on the request path (it takes all scratch from the library's
 static 16 MiB device array), checked through the C ABI against siml_topk on
 two calls in a row.  Collected last on purpose: it only adds to what the
 other tests cover."""
-import ctypes
 
 import numpy as np
 import pytest
