@@ -215,6 +215,19 @@ int64_t siml_compile_width(const char* buf, const int64_t* offsets, int64_t n);
 int siml_compile_smiles(const char* buf, const int64_t* offsets, int64_t n,
                         int32_t* lingos, int32_t* counts, int32_t* lengths,
                         int32_t* mags, int64_t width);
+/* One-pass form of the two calls above (no reference counterpart; the same
+ * output, each string compiled once).  siml_compile_stage writes string s's
+ * unique codes and counts, unpadded, to staging arrays of offsets[n] int32
+ * each at [offsets[s], offsets[s] + lengths[s]), writes lengths and mags [n],
+ * and returns the width or a negative status.  siml_compile_scatter then
+ * writes the zero-padded [n, width] rows (width >= the returned width, else
+ * SIML_ERR_INVALID). */
+int64_t siml_compile_stage(const char* buf, const int64_t* offsets, int64_t n,
+                           int32_t* stage_codes, int32_t* stage_counts, int32_t* lengths,
+                           int32_t* mags);
+int siml_compile_scatter(const int64_t* offsets, int64_t n, const int32_t* stage_codes,
+                         const int32_t* stage_counts, const int32_t* lengths,
+                         int32_t* lingos, int32_t* counts, int64_t width);
 /* The same compiler on the GPU (the reference compiles on the CPU only;
  * same rules and output bytes as siml_compile_smiles).  buf (offsets[n]
  * bytes) and offsets (n+1 int64) are device memory, as are the outputs;

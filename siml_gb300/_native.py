@@ -83,6 +83,8 @@ _SIGNATURES = {
     "siml_batch_destroy": (_I32, [_P]),
     "siml_compile_width": (_I64, [_P, _P, _I64]),
     "siml_compile_smiles": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _I64]),
+    "siml_compile_stage": (_I64, [_P, _P, _I64, _P, _P, _P, _P]),
+    "siml_compile_scatter": (_I32, [_P, _I64, _P, _P, _P, _P, _P, _I64]),
     "siml_row_histogram101": (_I32, [_P, _P, _I64, _I64, _I64, _P, _I32]),
     "siml_row_histogram101_f64": (_I32, [_P, _P, _I64, _I64, _I64, _P, _I32]),
     "siml_synth_lengths": (_I32, [_U64, _I32, _I64, _I64, _P]),

@@ -40,15 +40,22 @@ def compile_buffer(buf: bytes, offsets: np.ndarray):
     offsets = np.ascontiguousarray(offsets, dtype=np.int64)
     n = offsets.shape[0] - 1
     cbuf = buf if buf else b"\0"
-    w = L.siml_compile_width(cbuf, offsets.ctypes.data, n)
-    if w < 0:
-        N.check(int(-w), "siml_compile_width")
-    lingos = np.empty((n, w), dtype=np.int32)
-    counts = np.empty((n, w), dtype=np.int32)
+    # one pass: each string compiled once into staging sized like the text
+    # (a string has at most as many unique windows as bytes), then scattered
+    total = int(offsets[-1]) if n > 0 else 0
+    stage_codes = np.empty(max(total, 1), dtype=np.int32)
+    stage_counts = np.empty(max(total, 1), dtype=np.int32)
     lengths = np.empty(n, dtype=np.int32)
     mags = np.empty(n, dtype=np.int32)
-    N.check(L.siml_compile_smiles(cbuf, offsets.ctypes.data, n, lingos.ctypes.data, counts.ctypes.data,
-                                  lengths.ctypes.data, mags.ctypes.data, w), "siml_compile_smiles")
+    w = L.siml_compile_stage(cbuf, offsets.ctypes.data, n, stage_codes.ctypes.data, stage_counts.ctypes.data,
+                             lengths.ctypes.data, mags.ctypes.data)
+    if w < 0:
+        N.check(int(-w), "siml_compile_stage")
+    lingos = np.empty((n, w), dtype=np.int32)
+    counts = np.empty((n, w), dtype=np.int32)
+    N.check(L.siml_compile_scatter(offsets.ctypes.data, n, stage_codes.ctypes.data, stage_counts.ctypes.data,
+                                   lengths.ctypes.data, lingos.ctypes.data, counts.ctypes.data, w),
+            "siml_compile_scatter")
     return lingos, counts, lengths, mags
 
 

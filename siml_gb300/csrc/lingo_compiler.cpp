@@ -2,6 +2,7 @@
 // preprocessing and window rules are in lingo_compile_core.h, shared with the
 // GPU compiler.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -129,6 +130,71 @@ int siml_compile_smiles(const char* buf, const int64_t* offsets, int64_t n,
         }
     }, 1);
     if (overflow) return siml::fail(SIML_ERR_INVALID, "siml_compile_smiles: width smaller than a string's unique LINGO count");
+    return SIML_OK;
+}
+
+// One-pass form: every string compiled once into staging (its unique codes
+// and counts at [offsets[s], offsets[s] + lengths[s]), within its own byte
+// stretch since a string has at most as many unique windows as bytes), then
+// scattered into zero-padded rows.
+int64_t siml_compile_stage(const char* buf, const int64_t* offsets, int64_t n, int32_t* stage_codes,
+                           int32_t* stage_counts, int32_t* lengths, int32_t* mags) {
+    siml::clear_error();
+    if (!check_args(buf, offsets, n) || (n > 0 && (!stage_codes || !stage_counts || !lengths || !mags)))
+        return -siml::fail(SIML_ERR_INVALID, "siml_compile_stage: bad arguments");
+    const int64_t chunk = chunk_of(n);
+    const int64_t nchunks = (n + chunk - 1) / chunk;
+    std::vector<int64_t> chunk_max((size_t)nchunks, 0);
+    siml::parallel_for(nchunks, [&](int64_t c) {
+        Bag bag;
+        int64_t mx = 0;
+        const int64_t e = std::min(n, (c + 1) * chunk);
+        for (int64_t s = c * chunk; s < e; s++) {
+            bag.build((const unsigned char*)buf + offsets[s], offsets[s + 1] - offsets[s]);
+            if (bag.n) {
+                std::memcpy(stage_codes + offsets[s], bag.codes.data(), (size_t)bag.n * sizeof(int32_t));
+                std::memcpy(stage_counts + offsets[s], bag.counts.data(), (size_t)bag.n * sizeof(int32_t));
+            }
+            lengths[s] = bag.n;
+            mags[s] = bag.mag;
+            mx = std::max<int64_t>(mx, bag.n);
+        }
+        chunk_max[(size_t)c] = mx;
+    }, 1);
+    int64_t w = 0;
+    for (auto v : chunk_max) w = std::max(w, v);
+    return w;
+}
+
+int siml_compile_scatter(const int64_t* offsets, int64_t n, const int32_t* stage_codes,
+                         const int32_t* stage_counts, const int32_t* lengths, int32_t* lingos, int32_t* counts,
+                         int64_t width) {
+    siml::clear_error();
+    if (n < 0 || width < 0 || (n > 0 && (!offsets || !stage_codes || !stage_counts || !lengths ||
+                                         (width > 0 && (!lingos || !counts)))))
+        return siml::fail(SIML_ERR_INVALID, "siml_compile_scatter: bad arguments");
+    const int64_t chunk = chunk_of(n);
+    const int64_t nchunks = (n + chunk - 1) / chunk;
+    std::atomic<int> overflow{0};
+    siml::parallel_for(nchunks, [&](int64_t c) {
+        const int64_t e = std::min(n, (c + 1) * chunk);
+        for (int64_t s = c * chunk; s < e; s++) {
+            // a count is bounded by the string's stretch, so no read leaves it
+            const int64_t nu = std::min<int64_t>(std::max(lengths[s], 0), offsets[s + 1] - offsets[s]);
+            if (nu > width) { overflow = 1; continue; }
+            int32_t* lr = lingos + s * width;
+            int32_t* cr = counts + s * width;
+            if (nu) {
+                std::memcpy(lr, stage_codes + offsets[s], (size_t)nu * sizeof(int32_t));
+                std::memcpy(cr, stage_counts + offsets[s], (size_t)nu * sizeof(int32_t));
+            }
+            if (width > nu) {
+                std::memset(lr + nu, 0, (size_t)(width - nu) * sizeof(int32_t));
+                std::memset(cr + nu, 0, (size_t)(width - nu) * sizeof(int32_t));
+            }
+        }
+    }, 1);
+    if (overflow) return siml::fail(SIML_ERR_INVALID, "siml_compile_scatter: width smaller than a string's unique LINGO count");
     return SIML_OK;
 }
 

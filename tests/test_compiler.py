@@ -88,3 +88,28 @@ def test_synthetic_generator_is_deterministic(native):
 # sha256 of the first 64 strings of the 4,096-string set joined by "|" (pinned on x86;
 # the GPU hosts are Arm and must produce the same bytes)
 SYNTH_SHA256_64 = "c795cb381d2b390216d0a9e0db24c6a813d8aba11f2bc650651bf9366db59a30"
+
+
+def test_host_compiler_two_pass_entries_and_scatter_width(native):
+    """The two-pass C entries (width, then fill) give what the one-pass
+    staging path of compile_buffer gives, and the scatter refuses a width
+    below the widest string."""
+    from siml_gb300 import _native as N, synthetic as S
+    from siml_gb300.compiler import compile_buffer
+    buf, off = S.smiles_buffer(S.SEED_RAGGED, S.BIMODAL_35_110, 3000)
+    one = compile_buffer(buf, off)
+    L = N.lib()
+    n = len(off) - 1
+    w = L.siml_compile_width(buf, off.ctypes.data, n)
+    assert w == one[0].shape[1]
+    two = [np.empty((n, w), np.int32), np.empty((n, w), np.int32), np.empty(n, np.int32), np.empty(n, np.int32)]
+    N.check(L.siml_compile_smiles(buf, off.ctypes.data, n, *(a.ctypes.data for a in two), w))
+    for a, b in zip(one, two):
+        assert np.array_equal(a, b)
+    sc, sn = np.empty(int(off[-1]), np.int32), np.empty(int(off[-1]), np.int32)
+    ln, mg = np.empty(n, np.int32), np.empty(n, np.int32)
+    assert L.siml_compile_stage(buf, off.ctypes.data, n, sc.ctypes.data, sn.ctypes.data, ln.ctypes.data,
+                                mg.ctypes.data) == w
+    narrow = [np.empty((n, w - 1), np.int32) for _ in range(2)]
+    assert L.siml_compile_scatter(off.ctypes.data, n, sc.ctypes.data, sn.ctypes.data, ln.ctypes.data,
+                                  narrow[0].ctypes.data, narrow[1].ctypes.data, w - 1) == N.SIML_ERR_INVALID
