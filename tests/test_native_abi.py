@@ -71,3 +71,26 @@ def test_stream_argument_maps_torch_default_stream_to_legacy():
 
     assert N.stream_arg(_S(0)).value == N.CUDA_STREAM_LEGACY == 1
     assert N.stream_arg(_S(0x7F001234)).value == 0x7F001234
+
+
+def test_header_is_plain_c_and_links(native, tmp_path):
+    """include/siml_gb300.h compiles as strict C99 and a C caller links
+    against the library, as a cgo or C binding would."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "caller.c"
+    src.write_text('#include "siml_gb300.h"\n'
+                   'int main(void) {\n'
+                   '    siml_engine* h = 0;\n'
+                   '    int rc = siml_create(0, &h);\n'
+                   '    if (rc == SIML_OK) siml_destroy(h);\n'
+                   '    return siml_last_error() == 0;\n'
+                   '}\n')
+    lib_dir = os.path.join(REPO, "siml_gb300")
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", str(src), "-o",
+                        str(tmp_path / "caller"), "-I", os.path.join(REPO, "include"), "-L", lib_dir,
+                        "-lsiml_gb300", "-Wl,-rpath," + lib_dir], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
