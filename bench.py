@@ -121,9 +121,10 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------- CPU arm ----
-def cpu_reference_rate(db, q, target_s=12.0, max_rows=1024):
+def cpu_reference_rate(db, q, target_s=12.0, max_rows=1024, first_row=4):
     """Times the reference's CPU path (its compiled C code when built here,
-    else the oracle's restatement) with all host threads on R rows x full DB."""
+    else the oracle's restatement) with all host threads on R rows x full DB.
+    Returns (rate record, first row, the computed fp32 block)."""
     from oracle import cpulingo as O
     ref_mod = O.reference_module("_CPULingo")
     nthreads = os.cpu_count() or 1
@@ -142,12 +143,27 @@ def cpu_reference_rate(db, q, target_s=12.0, max_rows=1024):
     dt = max(time.time() - t, 1e-3)
     rows = int(max(4, min(max_rows, 4 * target_s / dt)))
     t = time.time()
-    run(4, 4 + rows)
+    block = run(first_row, first_row + rows)
     dt = time.time() - t
     pairs = rows * L.shape[0]
-    return {"value": pairs / dt / 1e9, "unit": "Gpairs/s", "cores": nthreads,
-            "kind": "reference" if ref_mod is not None else "port",
-            "sample": "%d query rows x %d database molecules (%.2e pairs) in %.2f s" % (rows, L.shape[0], pairs, dt)}
+    rec = {"value": pairs / dt / 1e9, "unit": "Gpairs/s", "cores": nthreads,
+           "kind": "reference" if ref_mod is not None else "port",
+           "sample": "%d query rows x %d database molecules (%.2e pairs) in %.2f s" % (rows, L.shape[0], pairs, dt)}
+    return rec, first_row, np.asarray(block, dtype=np.float32)
+
+
+def oracle_sets():
+    """The rows_1m workload generated and compiled by the oracle library alone
+    (its copy of the seeded generator and its restatement of the reference
+    compiler, pysiml/_ccompiler.cpp:276-381): the reference arm loads no
+    product code."""
+    from oracle import cpulingo as O
+    from oracle.workloads import SEED_DB_1M, LOGNORMAL_45
+    t = time.time()
+    db = O.synth_set(SEED_DB_1M, LOGNORMAL_45, DB_N)
+    q = O.synth_set(SEED_DB_1M, LOGNORMAL_45, QUERY_N, first=DB_N)
+    log("oracle generated + compiled %d + %d molecules in %.1f s" % (DB_N, QUERY_N, time.time() - t))
+    return db, q
 
 
 def reference_arm(args):
@@ -155,12 +171,13 @@ def reference_arm(args):
     if rank != 0:
         return 0
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "port"], check=True)
-    db, q = make_sets()
+    db, q = oracle_sets()
     from oracle import cpulingo as O
     ref_mod = O.reference_module("_CPULingo")
     nthreads = os.cpu_count() or 1
-    # each step: a bounded sample of the workload (rows x full database)
-    probe = cpu_reference_rate(db, q, target_s=2.0, max_rows=64)
+    # each step: a bounded sample of the workload (rows x full database),
+    # about 6 s of host time, so warm-up + steps end within a few minutes
+    probe, _, _ = cpu_reference_rate(db, q, target_s=2.0, max_rows=64)
     rows = int(max(2, min(BLOCK, probe["value"] * 1e9 * 6.0 / DB_N)))
     L, C, ln, mg = db
 
@@ -185,7 +202,10 @@ def reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "rows_per_step": rows, "db_molecules": DB_N},
+        "data": "synthetic", "config": {"workload": WORKLOAD, "rows_per_step": rows, "db_molecules": DB_N,
+                                        "subsample": "each step computes %d of the 1,024 rows of a block against the "
+                                                     "full database (about 6 s of host time), so the run ends "
+                                                     "within minutes; the metric is per pair" % rows},
         "cpu_baseline": {"value": value, "unit": "Gpairs/s", "cores": nthreads, "kind": kind,
                          "sample": "%d query rows x %d molecules per step" % (rows, DB_N)},
         "e2e": {"value": value, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -325,32 +345,43 @@ def gpu_arm(args):
 
     e2e = None
     cpu = None
+    parity_rows = None
     if rank == 0 and not args.no_extras and not fused:
         e2e = measure_e2e(gl, q, stream, dev, steps=min(3, args.steps))
         if world == 1:
-            cpu = cpu_reference_rate(db, q)
-    if rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded SMILES-like strings)",
-            "config": {"workload": {"rows_1m": WORKLOAD, "nbr_1m": NBR_WORKLOAD, "topk_1m": TOPK_WORKLOAD,
-                                    "hist_1m": HIST_WORKLOAD}[wl], "rows_per_step": rows_step, "db_molecules": DB_N,
-                       "query_rows": QUERY_N, "parallelism": "replicas" if world > 1 else "single",
-                       "rows_window": gl.rowsWindow(), "rows_entries": gl.rowsEntries(),
-                       "l2": "flushed between steps by a 256 MB write; each step also writes a 4 GB block",
-                       "db_layout": stats},
-            "roofline": roofline,
-            "int_roofline": int_roofline(value / world, np.mean(q[2]), np.mean(db[2]),
-                                         clk.get("sm_mhz") or 2070.0, local),
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk, "parity_spot_check": parity, "wall_s_timed": wall,
-            "evaluated_pairs_per_step": evaluated,
-            "evaluated_fraction": None if evaluated is None else evaluated / pairs_per_step,
-        }
-        print(json.dumps(line), flush=True)
+            # the CPU baseline's rows, compared bit for bit with the GPU's
+            cpu, r0c, want = cpu_reference_rate(db, q)
+            got = torch.empty((want.shape[0], DB_N), dtype=torch.float32, device=dev)
+            gl.getMultipleRowsDevice(r0c, r0c + want.shape[0], out=got)
+            same = bool(np.array_equal(got.cpu().numpy().view(np.uint32), want.view(np.uint32)))
+            parity_rows = {"rows": int(want.shape[0]), "first_row": r0c, "pairs": int(want.size),
+                           "bit_exact": same, "against": "the CPU baseline's own block (%s)" % cpu["kind"]}
+            parity = parity and same
+            del got, want
+    if rank != 0:
+        replicas.finish()
+        return None
+    line = {
+        "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded SMILES-like strings)",
+        "config": {"workload": {"rows_1m": WORKLOAD, "nbr_1m": NBR_WORKLOAD, "topk_1m": TOPK_WORKLOAD,
+                                "hist_1m": HIST_WORKLOAD}[wl], "rows_per_step": rows_step, "db_molecules": DB_N,
+                   "query_rows": QUERY_N, "parallelism": "replicas" if world > 1 else "single",
+                   "rows_window": gl.rowsWindow(), "rows_entries": gl.rowsEntries(),
+                   "l2": "flushed between steps by a 256 MB write; each step also writes a 4 GB block",
+                   "db_layout": stats},
+        "roofline": roofline,
+        "compute_side": compute_side(roofline["kernel"], wl),
+        "merge_work_ratio": merge_work_ratio(value / world, np.mean(q[2]), np.mean(db[2]),
+                                             clk.get("sm_mhz") or 2070.0, local),
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+        "clocks": clk, "parity_spot_check": parity, "parity_rows_checked": parity_rows, "wall_s_timed": wall,
+        "evaluated_pairs_per_step": evaluated,
+        "evaluated_fraction": None if evaluated is None else evaluated / pairs_per_step,
+    }
     replicas.finish()
-    return 0
+    return line
 
 
 # ------------------------------------------------------ ragged jobs ----
@@ -430,10 +461,13 @@ def ragged_reference_arm(args):
     return 0
 
 
-def ragged_arm(args):
+def ragged_arm(args, summary=False):
     """Batched ragged jobs: one persistent launch per step, replayed from a
     CUDA graph, against the plain path (one getNeighbors-over-a-range call per
-    job) on the same GPU, outputs compared bit for bit."""
+    job) on the same GPU, outputs compared bit for bit.  With summary=True
+    (the default bench run's second part) it runs 3 warm-up and at most 5
+    timed steps, skips the end-to-end and CPU legs and returns a compact
+    record instead of printing a line."""
     import torch
     from siml_gb300 import replicas
     rank, world, local = dist_env()
@@ -448,6 +482,7 @@ def ragged_arm(args):
     gl.set_qsmiles(*db)
     gl.set_refsmiles(*db)
     stats = gl.dbStats()
+    steps, warmup = (min(args.steps, 5), 3) if summary else (args.steps, args.warmup)
     torch.cuda.synchronize()
     log("database layout ready in %.2f s: %s" % (time.time() - t, stats))
     t = time.time()
@@ -469,7 +504,7 @@ def ragged_arm(args):
         plan.run(idx, sims, cnt, stream=torch.cuda.current_stream())
     kernels_per_run = 2   # k_batch_nbr + k_nbr_finish
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         graph.replay()
     torch.cuda.synchronize()
     gl.evaluatedPairs(reset=True)
@@ -478,10 +513,10 @@ def ragged_arm(args):
     clocks.start()
     time.sleep(0.5)
     cur = torch.cuda.current_stream()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     torch.cuda.synchronize()
     wall0 = time.time()
-    for k in range(args.steps):
+    for k in range(steps):
         flush.fill_(float(k))
         ev[k][0].record(cur)
         graph.replay()
@@ -489,12 +524,12 @@ def ragged_arm(args):
     torch.cuda.synchronize()
     wall = time.time() - wall0
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    evaluated = gl.evaluatedPairs(reset=True) / args.steps
+    evaluated = gl.evaluatedPairs(reset=True) / steps
     total_ms = replicas.max_over_ranks(sum(step_ms), dev)
     replicas.barrier()
     clk = clocks.stop()
-    value = world * args.steps * plan.pairs / (total_ms / 1e3) / 1e9
-    ms_per_step = total_ms / args.steps
+    value = world * steps * plan.pairs / (total_ms / 1e3) / 1e9
+    ms_per_step = total_ms / steps
 
     # plain path: one call per job on the same resident database
     idx2 = torch.empty_like(idx)
@@ -546,6 +581,7 @@ def ragged_arm(args):
             oracle_ok &= bool(np.array_equal(hi_[o + r, :kk], oi[r, :kk]) and
                               np.array_equal(hs[o + r, :kk].view(np.uint32), os_[r, :kk].view(np.uint32)))
 
+    plan_tile, plan_items, plan_pairs = plan.tile_chunks, plan.nitems, plan.pairs
     # roofline of k_batch_nbr: database bytes streamed per run / step time
     peaks = {}
     try:
@@ -565,7 +601,7 @@ def ragged_arm(args):
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback"}
 
     e2e = cpu = None
-    if rank == 0 and not args.no_extras:
+    if rank == 0 and not args.no_extras and not summary:
         # public API with host buffers: plan from the host job list, run,
         # results back to pinned host memory
         hidx = torch.empty(idx.shape, dtype=torch.int32).pin_memory()
@@ -592,6 +628,18 @@ def ragged_arm(args):
                "steps": n_e2e, "note": "includes planning (fixed tile) and the host job-list upload"}
         if world == 1:
             cpu = ragged_cpu_rate(db, jobs)
+    if summary:
+        del graph, idx, sims, cnt, idx2, sims2, cnt2, plan, gl
+        torch.cuda.empty_cache()
+        return {"workload": RAGGED_WORKLOAD, "batched_gpairs_per_s": value, "plain_gpairs_per_s": plain_value,
+                "batched_over_plain": value / plain_value, "batched_ms": ms_per_step, "plain_ms": plain_ms,
+                "steps": steps, "warmup": warmup, "jobs": args.ragged_jobs, "tile_chunks": plan_tile,
+                "items": plan_items, "pairs_per_step": plan_pairs, "plain_launches": plain_launches,
+                "batched_launches_per_step": kernels_per_run, "evaluated_fraction": evaluated / plan_pairs,
+                "bit_exact_batched_equals_plain": same, "oracle_spot_jobs_equal": oracle_ok,
+                "clocks": clk, "batched_path": "one persistent k_batch_nbr launch + k_nbr_finish per step, "
+                                               "replayed from a CUDA graph",
+                "plain_path": "one siml_neighbors_range call per job (the reference's one-call-per-job pattern)"}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
@@ -607,8 +655,8 @@ def ragged_arm(args):
                       "path": "one neighborsRangeDevice call per job (siml_neighbors_range)"},
             "batched_over_plain": value / plain_value,
             "roofline": roofline,
-            "int_roofline": int_roofline(value / world, *job_mean_lengths(db[2], jobs),
-                                         clk.get("sm_mhz") or 2070.0, local),
+            "merge_work_ratio": merge_work_ratio(value / world, *job_mean_lengths(db[2], jobs),
+                                                 clk.get("sm_mhz") or 2070.0, local),
             "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": args.steps * kernels_per_run, "clocks": clk,
             "parity_batched_equals_plain": same, "parity_spot_check": oracle_ok, "wall_s_timed": wall,
@@ -674,7 +722,12 @@ def serving_stats(reqs, nq):
     return st
 
 
-def serving_arm(args):
+def serving_arm(args, summary=False):
+    """Request loop over the resident 10M-molecule database: each rate runs
+    open-loop batched and then through the per-request path, then the
+    saturated capacity of both.  With summary=True (the default bench run's
+    third part) each rate runs 2 s of warm-up plus 4 s timed and a compact
+    record is returned instead of printing a line."""
     import torch
     rank, world, local = dist_env()
     if rank != 0:   # one request loop: the other ranks have nothing to serve
@@ -743,12 +796,13 @@ def serving_arm(args):
                       "the database is set from; resident: set-up, vocabulary, layouts and the warm-up batches"}
     nq = SERVING_DB_N
     rates = [float(x) for x in args.serving_rates.split(",")]
+    warm_s, timed_s = (2.0, 4.0) if summary else (float(args.warmup), float(args.steps))
     results = []
     first = SERVING_DB_N + 64
     clocks = ClockSampler(local)
     clocks.start()
     for ri, rate in enumerate(rates):
-        sched = serving_requests(rate, args.warmup + args.steps, first, S.SEED_SERVING + ri)
+        sched = serving_requests(rate, warm_s + timed_s, first, S.SEED_SERVING + ri)
         first += sum(len(x[2]) for x in sched)
         # batched: open-loop arrivals into the running server
         srv.gpu_ms, srv.launch_s, srv.deliver_s = 0.0, 0.0, 0.0
@@ -758,7 +812,7 @@ def serving_arm(args):
         for r in reqs:
             r.done.wait()
         srv.stop()
-        timed = [r for r in reqs if r.arrival - t0 >= args.warmup]
+        timed = [r for r in reqs if r.arrival - t0 >= warm_s]
         b = serving_stats(timed, nq)
         b["batches"] = srv.batches
         span_all = max(r.t_done for r in reqs) - min(r.arrival for r in reqs)
@@ -797,7 +851,7 @@ def serving_arm(args):
             stop_u[0] = True
             cvu.notify()
         th.join()
-        utimed = [r for r in ureqs if r.arrival - t0u >= args.warmup]
+        utimed = [r for r in ureqs if r.arrival - t0u >= warm_s]
         u = serving_stats(utimed, nq)
         # identical answers alone and in the mix (every request of the window)
         same = all(_same_result(a.result, c.result) for a, c in zip(timed, utimed))
@@ -806,7 +860,7 @@ def serving_arm(args):
             % (rate, b["p50_ms"], b["p99_ms"], b["gpairs_per_s"], u["p50_ms"], u["p99_ms"]))
     clk = clocks.stop()
     # saturated capacity: every request of the first schedule submitted at once
-    sched = serving_requests(rates[0], args.warmup + args.steps, SERVING_DB_N + 64, S.SEED_SERVING)
+    sched = serving_requests(rates[0], warm_s + timed_s, SERVING_DB_N + 64, S.SEED_SERVING)
     srv.gpu_ms, srv.launch_s, srv.deliver_s = 0.0, 0.0, 0.0
     srv.start()
     tb = time.perf_counter()
@@ -842,12 +896,26 @@ def serving_arm(args):
                 want = [(oi[q, :oc[q]], osm[q, :oc[q]]) for q in range(r.rows)]
             spot_ok &= _same_result(r.result, want)
     head = results[0]["batched"]
+    if summary:
+        keys = ("p50_ms", "p95_ms", "p99_ms", "p50_ms_ge256", "p99_ms_ge256", "gpairs_per_s", "requests", "errors")
+        per_rate = [{"rate_req_s": x["rate_req_s"], "alone_equals_mix": x["alone_equals_mix"],
+                     "batched": {k: x["batched"].get(k) for k in keys + ("gpu_busy_frac", "batches")},
+                     "unbatched": {k: x["unbatched"].get(k) for k in keys}} for x in results]
+        del srv, gl
+        torch.cuda.empty_cache()
+        return {"workload": SERVING_WORKLOAD, "seconds_per_rate": warm_s + timed_s, "timed_after_s": warm_s,
+                "server": vars(cfg), "rates": per_rate,
+                "capacity_batched_gpairs_per_s": cap["gpairs_per_s"],
+                "capacity_unbatched_gpairs_per_s": ucap["gpairs_per_s"],
+                "batched_over_unbatched_capacity": cap["gpairs_per_s"] / ucap["gpairs_per_s"],
+                "capacity_alone_equals_mix": cap_same, "oracle_spot_requests_equal": spot_ok, "clocks": clk,
+                "db_ingest_s": {"compile_gpu": t_compile_gpu, "resident": t_resident}}
     line = {
         "metric": METRIC, "value": cap["gpairs_per_s"], "unit": "Gpairs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded SMILES-like strings)",
         "config": {"workload": SERVING_WORKLOAD, "db_molecules": SERVING_DB_N, "rates_req_s": rates,
-                   "seconds_per_rate": args.warmup + args.steps, "timed_after_s": args.warmup,
+                   "seconds_per_rate": warm_s + timed_s, "timed_after_s": warm_s,
                    "server": vars(cfg), "db_layout": stats},
         "value_note": "saturated capacity: the first rate's requests all submitted at once",
         "serving": results, "capacity": cap, "capacity_unbatched": ucap,
@@ -872,42 +940,54 @@ def _same_result(a, b):
     return True
 
 
-_INT_PEAK = {}
+def read_profile_value(name, key):
+    """A "key: value" line of a committed ncu summary under profiles/, or None."""
+    try:
+        for ln in open(os.path.join(REPO, "profiles", name)):
+            if ln.startswith(key + ":"):
+                return float(ln.split(":", 1)[1].strip().split()[0])
+    except (OSError, ValueError):
+        pass
+    return None
 
 
-def int_peak(device):
-    """Measured 32-bit integer instruction rates of this GPU (siml_int_peak:
-    rings of LOP3, IADD3 and IMNMX), once per process."""
-    if device not in _INT_PEAK:
-        import ctypes
-        from siml_gb300 import _native as N
-        out = (ctypes.c_double * 3)()
-        N.check(N.lib().siml_int_peak(int(device), out), "siml_int_peak")
-        _INT_PEAK[device] = {"lop3": out[0], "iadd3": out[1], "imnmx": out[2]}
-    return _INT_PEAK[device]
-
-
-def int_roofline(gpairs_per_s, la, lb, sm_mhz, device):
-    """The integer roofline of the reference's merge for the same pairs:
-    3 ops per merge step (compare, select/advance, min-accumulate) over
+def merge_work_ratio(gpairs_per_s, la, lb, sm_mhz, device):
+    """How much integer work the reference's sorted merge would need for the
+    achieved pair rate, relative to this GPU's integer lane rate.  The merge
+    takes 3 ops per step (compare, select/advance, min-accumulate) over
     La + Lb steps plus 4 for the epilogue (pysiml/_CPULingo.c:53-71; La, Lb
-    the pair-weighted mean unique LINGOs of the row and database molecules), against
-    SMs x 128 lanes x the SM clock under load, and against the measured
-    instruction rates.  The bit-sliced kernels do less work per pair than the
-    merge, so the fraction can exceed 1: it says how far past the merge's
-    integer ceiling the path runs."""
+    the pair-weighted mean unique LINGOs of the row and database molecules).
+    The lane rate is SMs x the measured 32-bit integer lanes per SM per
+    clock (profiles/int_issue_probe.md) x the SM clock under load.  The
+    bit-sliced kernels do far less work per pair than the merge, so the ratio
+    exceeds 1: it is a work-reduction figure, not a roofline fraction; the
+    kernel's own compute bound is in compute_side."""
     import torch
     la, lb = float(la), float(lb)
     ops_pair = 3.0 * (la + lb) + 4.0
     achieved = gpairs_per_s * 1e9 * ops_pair
     sms = torch.cuda.get_device_properties(device).multi_processor_count
-    nominal = sms * 128.0 * float(sm_mhz) * 1e6
-    meas = int_peak(device)
-    best = max(meas.values())
-    return {"ops_per_pair": ops_pair, "La": la, "Lb": lb, "achieved_ops_per_s": achieved,
-            "peak_nominal_ops_per_s": nominal, "frac_nominal": achieved / nominal,
-            "peak_measured_ops_per_s": meas, "frac_measured": achieved / best,
-            "formula": "3*(La+Lb)+4 ops per pair; nominal peak = SMs x 128 x SM clock under load"}
+    lanes = read_profile_value("int_issue_probe.md", "int_lanes_per_sm_per_clock") or 64.0
+    rate = sms * lanes * float(sm_mhz) * 1e6
+    return {"ops_per_pair": ops_pair, "La": la, "Lb": lb, "merge_equivalent_ops_per_s": achieved,
+            "int_lane_rate_ops_per_s": rate, "int_lanes_per_sm_per_clock": lanes,
+            "merge_work_over_int_lane_rate": achieved / rate,
+            "formula": "(3*(La+Lb)+4) x pairs/s over SMs x measured int lanes/SM/clock x SM clock"}
+
+
+def compute_side(kernel, workload):
+    """The dominant kernel's issue-slot and ALU-pipe utilisation from its
+    committed ncu --set full summary (small case of the same kernel): the
+    compute-side fraction beside the HBM roofline."""
+    name = {"rows_1m": "k_rows_rows1m.md", "nbr_1m": "k_nbr_nbr1m.md", "topk_1m": "k_topk_topk1m.md",
+            "hist_1m": "k_hist_hist1m.md"}.get(workload)
+    if not name:
+        return None
+    issue = read_profile_value(name, "issue_active_pct")
+    alu = read_profile_value(name, "alu_pipe_pct")
+    return {"kernel": kernel, "issue_active_frac": None if issue is None else issue / 100.0,
+            "alu_pipe_frac": None if alu is None else alu / 100.0,
+            "source": "profiles/" + name + " (ncu --set full, small case of the same kernel)"}
 
 
 def read_profile_traffic(name="k_rows_rows1m.md"):
@@ -983,7 +1063,9 @@ def main():
     ap.add_argument("--tile-chunks", type=int, default=0,
                     help="ragged_2m: chunks per work item (0: autotuned when the plan is made)")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the end-to-end and CPU-baseline legs (profiler runs)")
+                    help="skip the end-to-end, CPU-baseline, batched and serving legs (profiler runs)")
+    ap.add_argument("--rows-only", action="store_true",
+                    help="rows_1m without the batched-vs-plain and serving parts")
     args = ap.parse_args()
     if args.workload == "ragged_2m":
         return ragged_reference_arm(args) if args.impl == "reference" else ragged_arm(args)
@@ -995,7 +1077,24 @@ def main():
         return serving_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
-    return gpu_arm(args)
+    line = gpu_arm(args)
+    if line is None:   # ranks other than 0
+        return 0
+    rank, world, _ = dist_env()
+    if args.workload == "rows_1m" and world == 1 and not args.no_extras and not args.rows_only:
+        # the metric's other two parts, on the same GPU in the same run:
+        # batched ragged jobs against the plain per-job path, and the
+        # serving loop's latency
+        import torch
+        torch.cuda.empty_cache()
+        t = time.time()
+        line["batched_vs_plain"] = ragged_arm(args, summary=True)
+        log("batched vs plain part: %.1f s" % (time.time() - t))
+        t = time.time()
+        line["serving"] = serving_arm(args, summary=True)
+        log("serving part: %.1f s" % (time.time() - t))
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 if __name__ == "__main__":

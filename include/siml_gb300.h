@@ -142,12 +142,16 @@ int siml_async_status(siml_engine* h);
  * let a request trigger cudaMalloc): all scratch comes from one 16 MiB static
  * __device__ array of the library, held by every GPU that loads it until the
  * process exits.  idx / sims are device pointers [rows, k].  The engine's
- * device layout must already exist (any earlier similarity call builds it),
- * else SIML_ERR_STATE; requests needing more than 16 MiB of scratch are
- * refused with SIML_ERR_INVALID.  All calls share the array and it keeps the
- * last call's contents: calls that overlap on the GPU race, so serialize
- * them.  The first call on each device looks up the array's address; make it
- * before any stream capture. */
+ * window-sorted layout must already exist (siml_topk, siml_neighbors,
+ * siml_neighbors_range, siml_hist101, siml_hist_global, siml_vocab_stats or
+ * siml_batch_create builds it; siml_rows and siml_db_stats do not), else
+ * SIML_ERR_STATE; requests needing more than 16 MiB of scratch are refused
+ * with SIML_ERR_INVALID.  All calls share the array and it keeps the last
+ * call's contents: calls that overlap on the GPU race, so serialize them.
+ * The call waits for its kernels before returning (it synchronizes the
+ * engine's stream).  siml_create looks up the array's address on its device;
+ * if that failed there, the first call does it, and should come before any
+ * stream capture. */
 int siml_topk_noalloc(siml_engine* h, int64_t rowbase, int64_t rowlimit, int64_t k,
                       int32_t* idx, float* sims);
 /* Global similarity histogram over all pairs of a row block (no reference
@@ -345,13 +349,6 @@ int siml_debug_fail_alloc(int64_t nth);
 /* Average device time (ms) of the dominant kernel of the last call on this
  * engine, measured with CUDA events on the engine's stream (0 if none). */
 double siml_last_kernel_ms(siml_engine* h);
-/* Measurement support (no counterpart in the reference): the measured rate
- * of 32-bit integer instructions on `device`, out[0..2] = LOP3, IADD3 and
- * IMNMX instructions per second (eight independent ring chains per thread,
- * eight 256-thread CTAs per SM, best of three ~ms launches).  It is the
- * measured peak beside the nominal SMs x 128 x clock used for the integer
- * roofline of the reference's merge (pysiml/_CPULingo.c:53-71). */
-int siml_int_peak(int device, double out[3]);
 
 #ifdef __cplusplus
 }

@@ -25,9 +25,23 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liblingo_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-# Root of the reference project (read in place, never copied); its C sources
-# are compiled by `make -C oracle ref` (REF_SRC there).
-REFERENCE_ROOT = os.environ.get("SIML_REFERENCE_ROOT", "/root/reference")
+
+
+def _reference_root():
+    """Root of the reference project (read in place, never copied): the
+    SIML_REFERENCE_ROOT environment variable, else the root the reference
+    build in oracle/_ref was made from (oracle/_ref/SOURCE), else None."""
+    env = os.environ.get("SIML_REFERENCE_ROOT")
+    if env:
+        return env
+    try:
+        with open(os.path.join(REF_DIR, "SOURCE")) as fh:
+            return fh.read().strip() or None
+    except OSError:
+        return None
+
+
+REFERENCE_ROOT = _reference_root()
 
 _lib = None
 
@@ -57,6 +71,10 @@ def lib() -> ctypes.CDLL:
             "oracle_compile_one": (I32, [ctypes.c_char_p, I64, P, P, P]),
             "oracle_compile_batch": (I64, [ctypes.c_char_p, P, I64, P, P, P, P, I64]),
             "oracle_tanimoto_pair": (F32, [P, P, P, P, I32, I32, I32, I32]),
+            "oracle_synth_lengths": (I32, [ctypes.c_uint64, I32, I64, I64, P]),
+            "oracle_synth_smiles": (I32, [ctypes.c_uint64, I32, I64, I64, P, I64, P]),
+            "oracle_scan_block": (I32, [P, P, P, P, I64, I64, P, P, P, P, I64, I64, P, I64, F32, F32, I64,
+                                        P, P, P, I64, P, P, P, P, I32]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -126,6 +144,44 @@ def compile_strings(strings):
                                  k.ctypes.data, ctypes.addressof(m))
             mags[s] = m.value
     return lingos, counts, lengths, mags
+
+
+def synth_buffer(seed, model, n, first=0):
+    """(bytes, offsets[n+1]) of molecules [first, first+n) of the seeded
+    synthetic workload (model 0 uniform 20-90, 1 lognormal 45, 2 bimodal
+    35/110), from the oracle's own copy of the generator."""
+    L = lib()
+    lens = np.empty(max(n, 1), np.int32)
+    assert L.oracle_synth_lengths(int(seed), int(model), int(first), int(n), lens.ctypes.data) == 0
+    total = int(lens[:n].sum(dtype=np.int64))
+    buf = np.empty(max(total, 1), np.uint8)
+    off = np.empty(n + 1, np.int64)
+    assert L.oracle_synth_smiles(int(seed), int(model), int(first), int(n), buf.ctypes.data, buf.shape[0],
+                                 off.ctypes.data) == 0
+    return buf[:total].tobytes(), off
+
+
+def compile_buffer(buf, off):
+    """compile_strings over a concatenated buffer and its offsets[n+1]."""
+    off = np.ascontiguousarray(off, dtype=np.int64)
+    n = len(off) - 1
+    L = lib()
+    data = buf if len(buf) else b"\0"
+    w = int(L.oracle_compile_batch(data, off.ctypes.data, n, None, None, None, None, 0))
+    lingos = np.zeros((n, max(w, 1)), np.int32)
+    counts = np.zeros((n, max(w, 1)), np.int32)
+    lengths = np.zeros(n, np.int32)
+    mags = np.zeros(n, np.int32)
+    if n and w:
+        assert L.oracle_compile_batch(data, off.ctypes.data, n, lingos.ctypes.data, counts.ctypes.data,
+                                      lengths.ctypes.data, mags.ctypes.data, w) >= 0
+        return lingos, counts, lengths, mags
+    return compile_strings([buf[off[i]:off[i + 1]] for i in range(n)])
+
+
+def synth_set(seed, model, n, first=0):
+    """Compiled synthetic set (lingos, counts, lengths, mags), oracle-side."""
+    return compile_buffer(*synth_buffer(seed, model, n, first))
 
 
 def cSMILEStoMatrices(smileslist):
@@ -311,6 +367,44 @@ def topk_block(ref, qry, rowbase, rowlimit, k, nthreads=0):
     rc = lib().oracle_topk_block(*a, int(k), idx.ctypes.data, sims.ctypes.data, int(nthreads))
     assert rc == 0
     return idx, sims
+
+
+def scan_block(ref, qry, rowbase, rowlimit, rows=True, lo=None, hi=1.1, maxneighbors=None, k=0,
+               hist101=False, hist1000=None, nthreads=0):
+    """Every product of a row block from one merge per pair (oracle_scan_block):
+    a dict with 'rows' (fp32 [rows, nq]), 'nbr' (idx, sims, counts as
+    neighbors_block, when lo is given), 'topk' (idx, sims as topk_block, when
+    k > 0), 'hist101' (int32 [rows, 101]); hist1000, a uint64 [1000] array, is
+    accumulated into when given."""
+    a, keep = _args(ref, qry, rowbase, rowlimit)
+    nr, nq = a[4], a[10]
+    res = {}
+    out = np.empty((nr, nq), np.float32) if rows else None
+    nb = None
+    if lo is not None:
+        pitch = pitch_of(nq if maxneighbors is None else maxneighbors)
+        nb = (np.full((nr, pitch), -1, np.int32), np.full((nr, pitch), np.nan, np.float32), np.zeros(nr, np.int32))
+    else:
+        pitch = 0
+    tk = (np.empty((nr, k), np.int32), np.empty((nr, k), np.float32)) if k > 0 else None
+    h101 = np.zeros((nr, 101), np.int32) if hist101 else None
+    if hist1000 is not None:
+        assert hist1000.dtype == np.uint64 and hist1000.shape == (1000,) and hist1000.flags.c_contiguous
+    ptr = lambda x: None if x is None else x.ctypes.data
+    rc = lib().oracle_scan_block(*a, ptr(out), max(nq, 1), np.float32(lo if lo is not None else 0.0),
+                                 np.float32(hi), pitch, ptr(nb[0] if nb else None), ptr(nb[1] if nb else None),
+                                 ptr(nb[2] if nb else None), int(k), ptr(tk[0] if tk else None),
+                                 ptr(tk[1] if tk else None), ptr(h101), ptr(hist1000), int(nthreads))
+    assert rc == 0
+    if out is not None:
+        res["rows"] = out
+    if nb is not None:
+        res["nbr"] = nb
+    if tk is not None:
+        res["topk"] = tk
+    if h101 is not None:
+        res["hist101"] = h101
+    return res
 
 
 def rowHistogram101(M):

@@ -322,6 +322,106 @@ ORACLE_API int oracle_topk_block(
 }
 
 /* ------------------------------------------------------------------------- */
+/* Every product of a row block from one merge per pair, for parity checks at
+ * database sizes where separate passes would take minutes.  Each output
+ * follows the rule of its single-purpose function above and may be NULL:
+ *   out      fp32 [nref, ldo]     oracle_tanimoto_block (_CPULingo.c:53-71)
+ *   nb_*     [nref, pitch], [nref] oracle_neighbors_block (kernels.py:393-475:
+ *                                  magnitude bound, [lo, hi), 128-wide waves)
+ *   tk_*     [nref, k]            oracle_topk_block (ties to the lower index)
+ *   h101     int32 [nref, 101]    oracle_hist101_block (kernels.py:606-666)
+ *   h1000    uint64 [1000]        oracle_hist1000_block, accumulated into.    */
+ORACLE_API int oracle_scan_block(
+        const int32_t* rl, const int32_t* rc, const int32_t* rlen, const int32_t* rmag,
+        int64_t nref, int64_t rstride,
+        const int32_t* ql, const int32_t* qc, const int32_t* qlen, const int32_t* qmag,
+        int64_t nq, int64_t qstride,
+        float* out, int64_t ldo,
+        float lo, float hi, int64_t pitch, int32_t* nb_idx, float* nb_sims, int32_t* nb_counts,
+        int64_t k, int32_t* tk_idx, float* tk_sims,
+        int32_t* h101, uint64_t* h1000, int nthreads) {
+    int nt = 1;
+#ifdef _OPENMP
+    nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#endif
+    uint64_t* part = (uint64_t*)calloc((size_t)nt * 1000, sizeof(uint64_t));
+    float* rowbuf = (float*)malloc((size_t)nt * (size_t)(nq > 0 ? nq : 1) * sizeof(float));
+    o_cand* heaps = (o_cand*)malloc((size_t)nt * (size_t)(k > 0 ? k : 1) * sizeof(o_cand));
+    if (!part || !rowbuf || !heaps) { free(part); free(rowbuf); free(heaps); return -1; }
+    int64_t row;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt) if (nt != 1)
+#endif
+    for (row = 0; row < nref; row++) {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        float* t = out ? out + row * ldo : rowbuf + (size_t)tid * (size_t)(nq > 0 ? nq : 1);
+        for (int64_t col = 0; col < nq; col++)
+            t[col] = oracle_pair(rl + row * rstride, ql + col * qstride, rc + row * rstride, qc + col * qstride,
+                                 rlen[row], qlen[col], rmag[row], qmag[col], NULL);
+        if (h1000) {
+            uint64_t* h = part + (size_t)tid * 1000;
+            for (int64_t col = 0; col < nq; col++) h[bin1000(t[col])]++;
+        }
+        if (h101) {
+            int32_t* h = h101 + row * 101;
+            memset(h, 0, 101 * sizeof(int32_t));
+            for (int64_t col = 0; col < nq; col++) h[bin101(t[col])]++;
+        }
+        if (nb_counts) {
+            const int32_t ma = rmag[row];
+            int64_t count = 0;
+            for (int64_t base = 0; base < nq; base += 128) {
+                int64_t wave_valid = 0;
+                const int64_t wend = base + 128 < nq ? base + 128 : nq;
+                for (int64_t col = base; col < wend; col++) {
+                    const int32_t mb = qmag[col];
+                    const int32_t mn = ma < mb ? ma : mb, mx = ma > mb ? ma : mb;
+                    const float bound = mn / ((float)mx);
+                    if (!(bound >= lo)) continue;
+                    if (t[col] >= lo && t[col] < hi) {
+                        const int64_t pos = count + wave_valid;
+                        if (pos < pitch) {
+                            nb_idx[row * pitch + pos] = (int32_t)col;
+                            if (nb_sims) nb_sims[row * pitch + pos] = t[col];
+                        }
+                        wave_valid++;
+                    }
+                }
+                count += wave_valid;
+                if (count > pitch) break;
+            }
+            nb_counts[row] = (int32_t)count;
+        }
+        if (tk_idx && k > 0) {
+            o_cand* h = heaps + (size_t)tid * (size_t)k;
+            int64_t n = 0;
+            for (int64_t col = 0; col < nq; col++) {
+                o_cand c;
+                c.t = t[col];
+                c.i = (int32_t)col;
+                if (n < k) { h[n] = c; o_sift_up(h, n); n++; }
+                else if (o_worse(h[0], c)) { h[0] = c; o_sift_down(h, n, 0); }
+            }
+            qsort(h, (size_t)n, sizeof(o_cand), o_cmp_best_first);
+            for (int64_t j = 0; j < k; j++) {
+                tk_idx[row * k + j] = j < n ? h[j].i : -1;
+                tk_sims[row * k + j] = j < n ? h[j].t : -1.0f;
+            }
+        }
+    }
+    if (h1000)
+        for (int t = 0; t < nt; t++)
+            for (int b = 0; b < 1000; b++) h1000[b] += part[(size_t)t * 1000 + b];
+    free(part);
+    free(rowbuf);
+    free(heaps);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
 /* SMILES -> LINGO multiset compiler.
  * Preprocessing state machine — pysiml/_ccompiler.cpp:178-264
  * (processSMILESdigits): digits become '0' except while copying the digits
@@ -443,7 +543,13 @@ ORACLE_API int64_t oracle_compile_batch(const char* buf, const int64_t* offsets,
                                         int32_t* lingos, int32_t* counts,
                                         int32_t* lengths, int32_t* mags, int64_t width) {
     int64_t maxw = 0;
-    for (int64_t s = 0; s < n; s++) {
+    int too_wide = 0;
+    int64_t s;
+    /* strings are independent: OpenMP over them (the reference loops serially) */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256) reduction(max : maxw) reduction(| : too_wide)
+#endif
+    for (s = 0; s < n; s++) {
         int64_t len = offsets[s + 1] - offsets[s];
         int32_t* c = (int32_t*)malloc(((size_t)len + 8) * sizeof(int32_t));
         int32_t* k = (int32_t*)malloc(((size_t)len + 8) * sizeof(int32_t));
@@ -451,16 +557,19 @@ ORACLE_API int64_t oracle_compile_batch(const char* buf, const int64_t* offsets,
         int32_t u = oracle_compile_one(buf + offsets[s], len, c, k, &mag);
         if (u > maxw) maxw = u;
         if (width > 0) {
-            if (u > width) { free(c); free(k); return -1; }
-            memset(lingos + s * width, 0, (size_t)width * sizeof(int32_t));
-            memset(counts + s * width, 0, (size_t)width * sizeof(int32_t));
-            memcpy(lingos + s * width, c, (size_t)u * sizeof(int32_t));
-            memcpy(counts + s * width, k, (size_t)u * sizeof(int32_t));
-            lengths[s] = u;
-            mags[s] = mag;
+            if (u > width) {
+                too_wide = 1;
+            } else {
+                memset(lingos + s * width, 0, (size_t)width * sizeof(int32_t));
+                memset(counts + s * width, 0, (size_t)width * sizeof(int32_t));
+                memcpy(lingos + s * width, c, (size_t)u * sizeof(int32_t));
+                memcpy(counts + s * width, k, (size_t)u * sizeof(int32_t));
+                lengths[s] = u;
+                mags[s] = mag;
+            }
         }
         free(c);
         free(k);
     }
-    return maxw;
+    return too_wide ? -1 : maxw;
 }

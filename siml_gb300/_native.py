@@ -93,7 +93,6 @@ _SIGNATURES = {
     "siml_set_tuning": (_I32, [_P, _I32, _I64]),
     "siml_get_tuning": (_I32, [_P, _I32, ctypes.POINTER(_I64)]),
     "siml_launch_count": (_I64, [_P]),
-    "siml_int_peak": (_I32, [_I32, ctypes.POINTER(ctypes.c_double)]),
     "siml_vocab_stats": (_I32, [_P, _P]),
     "siml_compile_width_gpu": (_I64, [_P, _P, _P, _I64]),
     "siml_compile_smiles_gpu": (_I32, [_P, _P, _P, _I64, _P, _P, _P, _P, _I64]),

@@ -969,6 +969,7 @@ int siml_create(int device, siml_engine** out) {
     SIML_CUDA(cudaHostGetDevicePointer((void**)&h->d_async_err, h->h_async_err, 0));
     SIML_CUDA(cudaEventCreate(&h->ev0));
     SIML_CUDA(cudaEventCreate(&h->ev1));
+    noalloc_prepare(device);
     *out = h;
     return SIML_OK;
 }

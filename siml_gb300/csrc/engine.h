@@ -160,6 +160,9 @@ int raise_smem_limit(const void* kernel, size_t need);
 // Reports (and clears) an expired top-k lock wait recorded by queued kernels;
 // call only once their work is known to be complete.
 int take_async_error(siml_engine* h);
+// topk_noalloc.cu: resolves the no-allocation entry point's static scratch on
+// `device` (the current device); called when an engine is created.
+void noalloc_prepare(int device);
 
 // kernels.cu — launchers; all queue work on h->stream and return a status.
 struct RowsArgs {

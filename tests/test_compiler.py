@@ -90,6 +90,24 @@ def test_synthetic_generator_is_deterministic(native):
 SYNTH_SHA256_64 = "c795cb381d2b390216d0a9e0db24c6a813d8aba11f2bc650651bf9366db59a30"
 
 
+def test_oracle_generator_equals_the_product_generator(native, oracle):
+    """The oracle's copy of the workload generator (used by the CPU reference
+    arm, which loads no product code) gives the product's bytes for every
+    length model, and the oracle compiler its arrays."""
+    from oracle import workloads as W
+    assert (W.UNIFORM_20_90, W.LOGNORMAL_45, W.BIMODAL_35_110) == (S.UNIFORM_20_90, S.LOGNORMAL_45, S.BIMODAL_35_110)
+    assert (W.SEED_ALLPAIRS, W.SEED_DB_1M, W.SEED_RAGGED, W.SEED_SERVING) == \
+        (S.SEED_ALLPAIRS, S.SEED_DB_1M, S.SEED_RAGGED, S.SEED_SERVING)
+    for seed, model in ((S.SEED_ALLPAIRS, S.UNIFORM_20_90), (S.SEED_DB_1M, S.LOGNORMAL_45),
+                        (S.SEED_RAGGED, S.BIMODAL_35_110)):
+        a = S.smiles_buffer(seed, model, 3000, first=999_000)
+        b = oracle.synth_buffer(seed, model, 3000, first=999_000)
+        assert a[0] == b[0] and np.array_equal(a[1], b[1])
+        want = S.smiles_set(seed, model, 3000, first=999_000)
+        got = oracle.synth_set(seed, model, 3000, first=999_000)
+        assert all(np.array_equal(x, y) for x, y in zip(got, want))
+
+
 def test_host_compiler_two_pass_entries_and_scatter_width(native):
     """The two-pass C entries (width, then fill) give what the one-pass
     staging path of compile_buffer gives, and the scatter refuses a width
