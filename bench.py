@@ -233,6 +233,11 @@ def gpu_arm(args):
         gl.setRowsWindow(args.rows_window)
     if args.rows_entries >= 0:
         gl.setRowsEntries(args.rows_entries)
+    from siml_gb300 import _native as N
+    if args.rows_layout >= 0:
+        N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_ROWS_LAYOUT, args.rows_layout), "rows layout")
+    if args.sched_groups:
+        N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_SCHED_GROUPS, args.sched_groups), "sched groups")
     stats = gl.dbStats()
     torch.cuda.synchronize()
     log("database layout ready in %.2f s: %s" % (time.time() - t, stats))
@@ -323,10 +328,17 @@ def gpu_arm(args):
         want = O.tanimoto_block(q, db, r0, r0 + 2, nthreads=os.cpu_count() or 1)
         parity = bool(np.array_equal(got, want))
 
-    # roofline of the dominant kernel (k_rows): algorithmic bytes per launch
+    # roofline of the dominant kernel: algorithmic bytes per launch = the fp32
+    # block (rows) + the database layout streamed once: 16-byte entry groups,
+    # and per chunk (padded layouts) or per work item (scheduled layout) the
+    # 32 lanes' 16-byte molecule records plus the chunk / item tables
     kms = statistics.mean(kernel_ms)
     out_bytes = 0 if fused else pairs_per_step * 4
-    db_bytes = stats["ngroups_total"] * 16 + stats["nchunks"] * 32 * 8 + stats["nchunks"] * 12
+    rows_info = gl.rowsInfo() if not fused else {"scheduled": 0}
+    if rows_info["scheduled"]:
+        db_bytes = stats["ngroups_total"] * 16 + rows_info["items"] * (32 * 16 + 8)
+    else:
+        db_bytes = stats["ngroups_total"] * 16 + stats["nchunks"] * 32 * 8 + stats["nchunks"] * 12
     alg_bytes = out_bytes + db_bytes
     achieved = alg_bytes / (kms / 1e3) / 1e9
     peaks = {}
@@ -338,8 +350,10 @@ def gpu_arm(args):
     traffic = read_profile_traffic({"rows_1m": "k_rows_rows1m.md", "nbr_1m": "k_nbr_nbr1m.md",
                                     "topk_1m": "k_topk_topk1m.md", "hist_1m": "k_hist_hist1m.md"}[wl])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": {"rows_1m": "k_rows_bal", "nbr_1m": "k_nbr", "topk_1m": "k_loghist+k_collect+k_topk_select",
-                                               "hist_1m": "k_hist"}[wl], "kernel_ms": kms,
+                "traffic": traffic,
+                "kernel": {"rows_1m": "k_rows_sched" if rows_info["scheduled"] else "k_rows_bal", "nbr_1m": "k_nbr",
+                           "topk_1m": "k_loghist+k_collect+k_topk_select", "hist_1m": "k_hist"}[wl],
+                "kernel_ms": kms,
                 "algorithmic_bytes_per_launch": alg_bytes,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback"}
 
@@ -368,7 +382,7 @@ def gpu_arm(args):
         "config": {"workload": {"rows_1m": WORKLOAD, "nbr_1m": NBR_WORKLOAD, "topk_1m": TOPK_WORKLOAD,
                                 "hist_1m": HIST_WORKLOAD}[wl], "rows_per_step": rows_step, "db_molecules": DB_N,
                    "query_rows": QUERY_N, "parallelism": "replicas" if world > 1 else "single",
-                   "rows_window": gl.rowsWindow(), "rows_entries": gl.rowsEntries(),
+                   "rows_window": gl.rowsWindow(), "rows_entries": gl.rowsEntries(), "rows_path": rows_info,
                    "l2": "flushed between steps by a 256 MB write; each step also writes a 4 GB block",
                    "db_layout": stats},
         "roofline": roofline,
@@ -1057,6 +1071,10 @@ def main():
                     help="serving_10m: query rows per batch while the queue is short")
     ap.add_argument("--rows-window", type=int, default=0,
                     help="sort window of the full-matrix layout (32, 64, 128, 256; 0: library default)")
+    ap.add_argument("--sched-groups", type=int, default=0,
+                    help="warp groups of the scheduled full-matrix kernel (2 or 4; 0: library default)")
+    ap.add_argument("--rows-layout", type=int, default=-1,
+                    help="full-matrix layout (0 padded, 1 balanced, 2 scheduled; -1: library default)")
     ap.add_argument("--rows-entries", type=int, default=-1,
                     help="entry format of the full-matrix layout (0 auto, 1 u16, 2 u32, 3 byte offsets; "
                          "-1: library default)")

@@ -47,6 +47,7 @@ extern "C" {
 #define SIML_SYNTH_UNIFORM_20_90 0
 #define SIML_SYNTH_LOGNORMAL_45 1
 #define SIML_SYNTH_BIMODAL_35_110 2
+#define SIML_SYNTH_CHEM_45 3         /* lognormal 45 with bracket atoms, charges, %nn rings */
 
 typedef struct siml_engine siml_engine;
 
@@ -189,6 +190,20 @@ typedef struct siml_batch siml_batch;
 int siml_batch_create(siml_engine* h, int64_t njobs, const int64_t* jobs,
                       float lo, float hi, int64_t pitch, int64_t tile_chunks,
                       siml_batch** out);
+/* siml_batch_create with the plan's shape given (no reference counterpart):
+ * tile_chunks chunks per work item, rows_cap ref rows per item (16 or 32),
+ * and jobs of at most merge_rows rows given to the per-pair merge (0: none).
+ * tile_chunks <= 0 tunes all three on a sample of the jobs, or reuses the
+ * shape tuned earlier in the process for the same kind of plan (database
+ * length distribution, job sizes and bound); siml_batch_create tunes the
+ * same way when its tile_chunks <= 0 and otherwise uses rows_cap 32, no
+ * merge jobs. */
+int siml_batch_create_shaped(siml_engine* h, int64_t njobs, const int64_t* jobs,
+                             float lo, float hi, int64_t pitch, int64_t tile_chunks,
+                             int64_t rows_cap, int64_t merge_rows, siml_batch** out);
+/* The plan's shape: out = {tile_chunks, rows_cap, merge_rows, 1 when it was
+ * reused from an earlier plan of the same kind rather than timed}. */
+int siml_batch_shape(siml_batch* b, int64_t out[4]);
 /* rows_out: output rows the plan writes (max out_row + rows over jobs);
  * nitems: work items; tile_chunks: the tile the plan uses; stream_bytes:
  * database bytes (entries and per-molecule metadata) one run streams, every
@@ -321,24 +336,58 @@ int siml_vocab_stats(siml_engine* h, int64_t out[4]);
  * out to whole windows.  Changing it drops the layout and invalidates
  * batch plans. */
 #define SIML_TUNE_SORT_WINDOW 4
-/* SIML_TUNE_ROWS_LAYOUT: how the natural-order full-matrix layout packs a
- * chunk of 32 molecules into its 32 lanes: SIML_ROWS_PADDED (lane i holds
+/* SIML_TUNE_ROWS_LAYOUT: the layout of the full-matrix path.
+ * SIML_ROWS_SCHEDULED (the default): molecules sorted by entry count inside
+ * windows (2048 / SIML_TUNE_SCHED_GROUPS molecules), each window's chunks
+ * split into equal per-warp work schedules, counts staged in shared memory
+ * and written out in natural order.  The natural-order layouts, which the other settings (and calls
+ * the scheduled kernel does not serve) use: SIML_ROWS_PADDED (lane i holds
  * molecule i, padded to the chunk's longest) or SIML_ROWS_BALANCED (the
  * chunk's entries dealt evenly to the lanes, partial counts merged before
- * the row epilogue; the default).  Changing it drops the full-matrix
- * layout. */
+ * the row epilogue).  Changing it drops the full-matrix layouts. */
 #define SIML_TUNE_ROWS_LAYOUT 5
 #define SIML_ROWS_PADDED 0
 #define SIML_ROWS_BALANCED 1
+#define SIML_ROWS_SCHEDULED 2
+/* SIML_TUNE_SCHED_GROUPS: the scheduled full-matrix kernel splits a CTA's
+ * 32 warps into this many groups (2 or 4; default 4), each working on its
+ * own window of 2048 / groups database columns, so the groups' stream and
+ * store phases overlap.  Changing it drops the scheduled layout. */
+#define SIML_TUNE_SCHED_GROUPS 6
 int siml_set_tuning(siml_engine* h, int key, int64_t value);
 int siml_get_tuning(siml_engine* h, int key, int64_t* value);
+/* The full-matrix path the current sets and settings use (no reference
+ * counterpart): out[0] = 1 when getMultipleRows runs on the scheduled layout
+ * (SIML_ROWS_SCHEDULED), out[1..3] = its work items, windows and the most
+ * 8-entry steps of one item; out[0] = 0 (and zeros) otherwise.  Builds the
+ * layout if needed. */
+int siml_rows_info(siml_engine* h, int64_t out[4]);
 /* Pairs the threshold kernels (neighbours, batched jobs, top-k collection,
  * histograms) actually evaluated: 32 x group rows per streamed chunk, i.e.
  * without the chunks skipped by the magnitude bound.  Waits for the engine's
  * stream; reset != 0 zeroes the counter afterwards. */
 int siml_eval_pairs(siml_engine* h, uint64_t* out, int reset);
+/* Free and total device memory of the engine's GPU in bytes
+ * (cudaMemGetInfo; no counterpart in the reference, which allocates per
+ * call).  The request loop admits batches against it. */
+int siml_mem_info(siml_engine* h, int64_t* free_bytes, int64_t* total_bytes);
 /* Number of kernel launches this engine has issued since creation. */
 int64_t siml_launch_count(siml_engine* h);
+/* Test support (no counterpart in the reference): overwrites entry `pos` of
+ * ref row `row`'s device vid list, the list the table kernels set their
+ * shared table from, to exercise the kernels' and the plans' checks without
+ * a GPU fault.  The kernels skip an entry they cannot hold and report it
+ * (SIML_ERR_STATE from the call, or from siml_sync for queued calls); batch
+ * plans refuse rows whose lists hold such entries.  The next siml_set_ref
+ * rebuilds the lists. */
+int siml_debug_set_row_vid(siml_engine* h, int64_t row, int64_t pos, uint32_t vid);
+/* Test support (no counterpart in the reference; needs no GPU): the status
+ * and siml_last_error() message that siml_sync / siml_async_status give for
+ * an asynchronous error word the kernels wrote.  Value 1: a top-k lock wait
+ * ran out (SIML_ERR_TIMEOUT); 2: a batch work item outside its plan
+ * (SIML_ERR_STATE); 4: a ref-row vid the table cannot hold (SIML_ERR_STATE).
+ * The lowest set bit decides. */
+int siml_debug_async_status(int word);
 /* Fault injection for tests (no counterpart in the reference): the nth
  * device allocation from now through the engines' array allocator, in any
  * engine of the process, returns SIML_ERR_NOMEM without calling cudaMalloc,

@@ -12,7 +12,8 @@
  *
  * Length models (characters): 0 uniform [20, 90]; 1 lognormal median 45,
  * sigma 0.5, clipped [10, 200]; 2 bimodal, 70% lognormal median 35 (sigma
- * 0.35), 30% median 110 (sigma 0.3), clipped [10, 250].
+ * 0.35), 30% median 110 (sigma 0.3), clipped [10, 250]; 3 as 1 with the
+ * chemistry-like tokens (bracket atoms, '/' '\\' bonds, %nn ring labels).
  */
 #include <stdint.h>
 #include <stdlib.h>
@@ -79,7 +80,8 @@ static int32_t o_lognormal(o_rng* r, double median, double sigma, int32_t lo, in
 static int32_t o_length(o_rng* r, int model) {
     switch (model) {
         case 0: return 20 + (int32_t)o_below(r, 71);
-        case 1: return o_lognormal(r, 45.0, 0.5, 10, 200);
+        case 1:
+        case 3: return o_lognormal(r, 45.0, 0.5, 10, 200);
         case 2:
             if (o_below(r, 100) < 70) return o_lognormal(r, 35.0, 0.35, 10, 250);
             return o_lognormal(r, 110.0, 0.3, 10, 250);
@@ -93,30 +95,48 @@ static const int o_tok_w[] = {250, 250, 50, 50, 50, 40, 30, 20, 20, 20, 70, 40, 
 static const int o_tok_k[] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 2, 1, 1, 3};
 #define O_NTOK 14
 
+static const char* const o_bracket[] = {"[NH+]", "[NH2+]", "[NH3+]", "[O-]", "[N+]", "[nH]", "[C@@H]", "[C@H]",
+                                       "[S@@]", "[Na+]", "[Cl-]", "[N-]", "[13CH3]", "[2H]", "[Fe+2]", "[Si]",
+                                       "[Se]", "[B-]", "[P+]", "[Co+3]"};
+#define O_NBRACKET 20
+
 typedef struct {
     char* out;
     int32_t len;
-    int depth, nrings, last_atom;
-    int rings[6];
+    int depth, nrings, last_atom, chem;
+    int rings[6];   /* 1: written as digit i+1, 2: as "%1" + digit i */
 } o_gen;
 
 static void o_put(o_gen* g, const char* s) { while (*s) g->out[g->len++] = *s++; }
 
 static void o_atom(o_gen* g, o_rng* r) {
-    uint32_t u = o_below(r, 780);   /* sum of the atom weights */
-    int acc = 0;
-    for (int t = 0; t < 10; t++) {
-        acc += o_tok_w[t];
-        if ((int)u < acc) { o_put(g, o_tok_s[t]); break; }
+    if (g->chem && o_below(r, 100) < 12) {
+        o_put(g, o_bracket[o_below(r, O_NBRACKET)]);
+    } else {
+        uint32_t u = o_below(r, 780);   /* sum of the atom weights */
+        int acc = 0;
+        for (int t = 0; t < 10; t++) {
+            acc += o_tok_w[t];
+            if ((int)u < acc) { o_put(g, o_tok_s[t]); break; }
+        }
     }
     g->last_atom = 1;
 }
 
-/* one molecule into out (capacity >= target + 16); returns its length */
-static int32_t o_gen_one(o_rng* r, int32_t target, char* out) {
+static void o_ring_label(o_gen* g, int k, int kind) {
+    if (kind == 2) {
+        g->out[g->len++] = '%';
+        g->out[g->len++] = '1';
+    }
+    g->out[g->len++] = (char)((kind == 2 ? '0' : '1') + k);
+}
+
+/* one molecule into out (capacity >= target + 24); returns its length */
+static int32_t o_gen_one(o_rng* r, int32_t target, char* out, int chem) {
     o_gen g;
     memset(&g, 0, sizeof(g));
     g.out = out;
+    g.chem = chem;
     o_atom(&g, r);
     while (g.len + g.depth + g.nrings < target) {
         if (g.last_atom && g.depth > 0 && o_below(r, 100) < 30) {
@@ -129,7 +149,7 @@ static int32_t o_gen_one(o_rng* r, int32_t target, char* out) {
         if (g.last_atom && g.nrings > 0 && o_below(r, 100) < 25) {
             int k = (int)o_below(r, 6);
             while (!g.rings[k]) k = (k + 1) % 6;
-            g.out[g.len++] = (char)('1' + k);
+            o_ring_label(&g, k, g.rings[k]);
             g.rings[k] = 0;
             g.nrings--;
             continue;
@@ -142,37 +162,44 @@ static int32_t o_gen_one(o_rng* r, int32_t target, char* out) {
         }
         switch (o_tok_k[t]) {
             case 0: o_put(&g, o_tok_s[t]); g.last_atom = 1; break;
-            case 1: if (g.last_atom) { o_put(&g, o_tok_s[t]); o_atom(&g, r); } break;
+            case 1:
+                if (g.last_atom) {
+                    if (g.chem && o_below(r, 100) < 20) o_put(&g, o_below(r, 2) ? "/" : "\\");
+                    else o_put(&g, o_tok_s[t]);
+                    o_atom(&g, r);
+                }
+                break;
             case 2: if (g.last_atom && g.depth < 4) { o_put(&g, "("); g.depth++; o_atom(&g, r); } break;
             case 3:
                 if (g.last_atom && g.nrings < 6) {
                     int k = (int)o_below(r, 6);
                     while (g.rings[k]) k = (k + 1) % 6;
-                    g.out[g.len++] = (char)('1' + k);
-                    g.rings[k] = 1;
+                    const int kind = g.chem && o_below(r, 100) < 20 ? 2 : 1;
+                    o_ring_label(&g, k, kind);
+                    g.rings[k] = kind;
                     g.nrings++;
                 }
                 break;
         }
     }
     for (int k = 0; k < 6; k++)
-        if (g.rings[k]) g.out[g.len++] = (char)('1' + k);
+        if (g.rings[k]) o_ring_label(&g, k, g.rings[k]);
     while (g.depth-- > 0) o_put(&g, ")");
     return g.len;
 }
 
 /* Byte lengths of molecules [first, first + n) of the set (seed, model). */
 ORACLE_API int oracle_synth_lengths(uint64_t seed, int model, int64_t first, int64_t n, int32_t* lens) {
-    if (n < 0 || first < 0 || model < 0 || model > 2) return -1;
+    if (n < 0 || first < 0 || model < 0 || model > 3) return -1;
     int64_t i;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
     for (i = 0; i < n; i++) {
         o_rng r;
-        char tmp[600];
+        char tmp[640];
         o_rng_init(&r, seed, (uint64_t)(first + i));
-        lens[i] = o_gen_one(&r, o_length(&r, model), tmp);
+        lens[i] = o_gen_one(&r, o_length(&r, model), tmp, model == 3);
     }
     return 0;
 }
@@ -181,7 +208,7 @@ ORACLE_API int oracle_synth_lengths(uint64_t seed, int model, int64_t first, int
  * of string s, offsets[n] the total; no separators). */
 ORACLE_API int oracle_synth_smiles(uint64_t seed, int model, int64_t first, int64_t n, char* buf, int64_t bufcap,
                                    int64_t* offsets) {
-    if (n < 0 || first < 0 || model < 0 || model > 2) return -1;
+    if (n < 0 || first < 0 || model < 0 || model > 3) return -1;
     int32_t* lens = (int32_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int32_t));
     if (!lens) return -1;
     oracle_synth_lengths(seed, model, first, n, lens);
@@ -195,8 +222,10 @@ ORACLE_API int oracle_synth_smiles(uint64_t seed, int model, int64_t first, int6
 #endif
     for (i = 0; i < n; i++) {
         o_rng r;
+        char tmp[640];
         o_rng_init(&r, seed, (uint64_t)(first + i));
-        o_gen_one(&r, o_length(&r, model), buf + offsets[i]);
+        const int32_t L = o_gen_one(&r, o_length(&r, model), tmp, model == 3);
+        memcpy(buf + offsets[i], tmp, (size_t)L);
     }
     return 0;
 }

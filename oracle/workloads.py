@@ -8,8 +8,10 @@ product package.  They equal siml_gb300.synthetic's constants
 UNIFORM_20_90 = 0
 LOGNORMAL_45 = 1
 BIMODAL_35_110 = 2
+CHEM_45 = 3
 
 SEED_ALLPAIRS = 20260001
 SEED_DB_1M = 20260002
 SEED_RAGGED = 20260004
 SEED_SERVING = 20260005
+SEED_CHEM = 20260006

@@ -361,11 +361,14 @@ class GPULingo:
         self._queue_neighbors(rowbase, rowlimit, lowerbound, upperbound, maxneighbors, False, (colbegin, colend))
         return self.retrieveAsyncResult()
 
-    def planNeighborBatch(self, jobs, lowerbound, upperbound=1.1, maxneighbors=None, tile_chunks=0):
+    def planNeighborBatch(self, jobs, lowerbound, upperbound=1.1, maxneighbors=None, tile_chunks=0, rows_cap=32,
+                          merge_rows=0):
         """A reusable plan (siml_gb300.batch.NeighborBatch) of ragged jobs
-        (row_begin, row_end, col_begin, col_end[, out_row])."""
+        (row_begin, row_end, col_begin, col_end[, out_row]).  tile_chunks <= 0
+        tunes the plan's shape (or reuses one tuned for the same kind of
+        plan); otherwise tile_chunks, rows_cap and merge_rows are used."""
         from .batch import NeighborBatch
-        return NeighborBatch(self, jobs, lowerbound, upperbound, maxneighbors, tile_chunks)
+        return NeighborBatch(self, jobs, lowerbound, upperbound, maxneighbors, tile_chunks, rows_cap, merge_rows)
 
     def getNeighborsBatch(self, jobs, lowerbound, upperbound=1.1, maxneighbors=None, with_sims=False):
         """Runs ragged jobs in one batch; returns one getNeighbors-style
@@ -481,6 +484,20 @@ class GPULingo:
         N.check(N.lib().siml_db_stats(self._h, a), "siml_db_stats")
         keys = ["nvid", "entry_bytes", "ngroups_total", "nchunks", "max_ng", "n", "ref_max_entries", "qry_max_entries"]
         return dict(zip(keys, [int(x) for x in a]))
+
+    def memInfo(self):
+        """(free, total) device memory of this object's GPU in bytes."""
+        f, t = ctypes.c_int64(0), ctypes.c_int64(0)
+        N.check(N.lib().siml_mem_info(self._h, ctypes.byref(f), ctypes.byref(t)), "siml_mem_info")
+        return int(f.value), int(t.value)
+
+    def rowsInfo(self):
+        """The full-matrix path of the current sets (dict): scheduled (1 when
+        getMultipleRows runs on the scheduled layout), its work items,
+        windows and the most steps of one item."""
+        a = (ctypes.c_int64 * 4)()
+        N.check(N.lib().siml_rows_info(self._h, a), "siml_rows_info")
+        return dict(zip(["scheduled", "items", "windows", "max_item_steps"], [int(x) for x in a]))
 
     def vocabStats(self):
         """Vocabulary split of the resident database (dict): pairs, common

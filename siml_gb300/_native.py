@@ -31,6 +31,8 @@ SIML_TUNE_SORT_WINDOW = 4
 SIML_TUNE_ROWS_LAYOUT = 5
 SIML_ROWS_PADDED = 0
 SIML_ROWS_BALANCED = 1
+SIML_ROWS_SCHEDULED = 2
+SIML_TUNE_SCHED_GROUPS = 6
 SIML_ENTRIES_AUTO = 0
 SIML_ENTRIES_U16 = 1
 SIML_ENTRIES_U32 = 2
@@ -39,6 +41,7 @@ SIML_ENTRIES_OFFSETS = 3
 SYNTH_UNIFORM_20_90 = 0
 SYNTH_LOGNORMAL_45 = 1
 SYNTH_BIMODAL_35_110 = 2
+SYNTH_CHEM_45 = 3
 
 
 class SimlError(RuntimeError):
@@ -78,6 +81,8 @@ _SIGNATURES = {
     "siml_topk_noalloc": (_I32, [_P, _I64, _I64, _I64, _P, _P]),
     "siml_neighbors_range": (_I32, [_P, _I64, _I64, _I64, _I64, _F32, _F32, _I64, _P, _P, _P, _I32]),
     "siml_batch_create": (_I32, [_P, _I64, _P, _F32, _F32, _I64, _I64, _P]),
+    "siml_batch_create_shaped": (_I32, [_P, _I64, _P, _F32, _F32, _I64, _I64, _I64, _I64, _P]),
+    "siml_batch_shape": (_I32, [_P, _P]),
     "siml_batch_info": (_I32, [_P, _P, _P, _P, _P, _P]),
     "siml_batch_run": (_I32, [_P, _P, _P, _P, _P]),
     "siml_batch_destroy": (_I32, [_P]),
@@ -93,11 +98,15 @@ _SIGNATURES = {
     "siml_set_tuning": (_I32, [_P, _I32, _I64]),
     "siml_get_tuning": (_I32, [_P, _I32, ctypes.POINTER(_I64)]),
     "siml_launch_count": (_I64, [_P]),
+    "siml_debug_set_row_vid": (_I32, [_P, _I64, _I64, ctypes.c_uint32]),
+    "siml_mem_info": (_I32, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
+    "siml_rows_info": (_I32, [_P, ctypes.POINTER(ctypes.c_int64)]),
     "siml_vocab_stats": (_I32, [_P, _P]),
     "siml_compile_width_gpu": (_I64, [_P, _P, _P, _I64]),
     "siml_compile_smiles_gpu": (_I32, [_P, _P, _P, _I64, _P, _P, _P, _P, _I64]),
     "siml_compile_stage_gpu": (_I64, [_P, _P, _P, _I64, _P, _P, _P, _P]),
     "siml_debug_fail_alloc": (_I32, [_I64]),
+    "siml_debug_async_status": (_I32, [ctypes.c_int]),
     "siml_compile_scatter_gpu": (_I32, [_P, _P, _I64, _P, _P, _P, _P, _P, _I64]),
     "siml_last_kernel_ms": (ctypes.c_double, [_P]),
 }

@@ -43,7 +43,11 @@ class NeighborBatch:
     ``pitch`` is 16*ceil(maxneighbors/16) as getNeighbors computes it.  The
     plan stays valid until the object's ref or query set is replaced."""
 
-    def __init__(self, gl, jobs, lowerbound, upperbound=1.1, maxneighbors=None, tile_chunks=0):
+    def __init__(self, gl, jobs, lowerbound, upperbound=1.1, maxneighbors=None, tile_chunks=0, rows_cap=32,
+                 merge_rows=0):
+        """tile_chunks <= 0: the plan's shape (tile, row cap, merge cut-off)
+        is tuned, or taken from an earlier plan of the same kind; otherwise
+        the given shape is used as is."""
         self._gl = gl
         self._b = ctypes.c_void_p()
         self.jobs = job_array(jobs)
@@ -54,13 +58,17 @@ class NeighborBatch:
         self.lowerbound = float(lowerbound)
         self.upperbound = float(upperbound)
         gl._check_rows(0, 0)
-        N.check(N.lib().siml_batch_create(gl._h, self.jobs.shape[0], self.jobs.ctypes.data,
-                                          ctypes.c_float(lowerbound), ctypes.c_float(upperbound), self.pitch,
-                                          int(tile_chunks), ctypes.byref(self._b)), "siml_batch_create")
+        N.check(N.lib().siml_batch_create_shaped(gl._h, self.jobs.shape[0], self.jobs.ctypes.data,
+                                                 ctypes.c_float(lowerbound), ctypes.c_float(upperbound), self.pitch,
+                                                 int(tile_chunks), int(rows_cap), int(merge_rows),
+                                                 ctypes.byref(self._b)), "siml_batch_create")
         r, n, t, sb, ub = (ctypes.c_int64() for _ in range(5))
         N.check(N.lib().siml_batch_info(self._b, ctypes.byref(r), ctypes.byref(n), ctypes.byref(t),
                                         ctypes.byref(sb), ctypes.byref(ub)), "siml_batch_info")
         self.rows_out, self.nitems, self.tile_chunks = int(r.value), int(n.value), int(t.value)
+        sh = (ctypes.c_int64 * 4)()
+        N.check(N.lib().siml_batch_shape(self._b, sh), "siml_batch_shape")
+        self.rows_cap, self.merge_rows, self.shape_from_cache = int(sh[1]), int(sh[2]), bool(sh[3])
         self.stream_bytes = int(sb.value)   # database bytes one run streams (every work item)
         self.unique_bytes = int(ub.value)   # every job's database range once
         self.pairs = int(sum(max(0, j[1] - j[0]) * max(0, j[3] - j[2]) for j in self.jobs.tolist()))

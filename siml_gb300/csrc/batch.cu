@@ -9,11 +9,21 @@
 // caller's stream (no host synchronization, no allocation), so it can be
 // captured in a CUDA graph and replayed.
 //
-// The chunk range of one work item (tile_chunks) is the tile shape.  With
-// tile_chunks <= 0 the plan times the candidate shapes on a sample of the
-// jobs and keeps the fastest; siml_batch_info reports the choice, so later
-// plans of similar jobs can pass it and skip the timing.
+// The plan's shape has three parts: the chunk range of one work item
+// (tile_chunks), the most ref rows one item takes (rows_cap, 16 or 32: fewer
+// rows per table, more items in flight) and the jobs given to the per-pair
+// merge instead of the table kernel (merge_rows: jobs of at most that many
+// rows, recomputed by the ordered finish kernel).  With tile_chunks <= 0 the
+// plan times candidate shapes on a sample of the jobs (tiles first, then the
+// row cap, then the merge cut-off) and keeps the fastest; the choice is kept
+// per database length distribution and job shape (a signature of both), so
+// later plans of the same kind reuse it without timing.  siml_batch_shape
+// reports the choice.
 #include <algorithm>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "engine.h"
@@ -32,6 +42,9 @@ struct siml_batch {
     float lo = 0.f, hi = 0.f;
     int64_t pitch = 0;
     int64_t tile_chunks = 0;
+    int64_t rows_cap = 32;
+    int64_t merge_rows = 0;
+    int from_cache = 0;
     int64_t stream_bytes = 0;
     int64_t unique_bytes = 0;
 };
@@ -47,8 +60,15 @@ struct HostJob {
 // cuts each job into items of at most 32 consecutive ordered rows x `tile`
 // chunks, largest items first.  Rows of one item then have close
 // magnitudes, so whole chunks out of the bound's reach are skipped.
-void make_items(const DbLayout* d, const std::vector<HostJob>& jobs, const std::vector<int32_t>& mag, int64_t tile,
-                std::vector<int4>& items, std::vector<int32_t>& order) {
+struct Shape {
+    int64_t tile = 128;
+    int64_t rows_cap = 32;
+    int64_t merge_rows = 0;
+};
+
+void make_items(const DbLayout* d, const std::vector<HostJob>& jobs, const std::vector<int32_t>& mag,
+                const Shape& sh, std::vector<int4>& items, std::vector<int32_t>& order) {
+    const int64_t tile = sh.tile;
     struct It {
         int4 a, b;
         int64_t cost;
@@ -57,6 +77,7 @@ void make_items(const DbLayout* d, const std::vector<HostJob>& jobs, const std::
     order.clear();
     for (const HostJob& j : jobs) {
         if (j.re <= j.rb || j.ce <= j.cb) continue;
+        if (j.re - j.rb <= sh.merge_rows) continue;   // the ordered finish kernel computes it
         const int64_t pos0 = (int64_t)order.size();
         for (int64_t r = j.rb; r < j.re; r++) order.push_back((int32_t)r);
         std::stable_sort(order.begin() + pos0, order.end(),
@@ -64,8 +85,8 @@ void make_items(const DbLayout* d, const std::vector<HostJob>& jobs, const std::
         int64_t c0, c1;
         sorted_chunk_range(d, j.cb, j.ce, c0, c1);
         const int64_t nrows = j.re - j.rb;
-        for (int64_t r = 0; r < nrows; r += 32) {
-            const int nr = (int)std::min<int64_t>(32, nrows - r);
+        for (int64_t r = 0; r < nrows; r += sh.rows_cap) {
+            const int nr = (int)std::min<int64_t>(sh.rows_cap, nrows - r);
             for (int64_t c = c0; c < c1; c += tile) {
                 const int64_t ce = std::min(c1, c + tile);
                 It it;
@@ -107,15 +128,25 @@ int host_mags(siml_engine* h, std::vector<int32_t>& mag) {
     return SIML_OK;
 }
 
-// Times the persistent kernel for each candidate tile on a sample of the
-// jobs and returns the fastest tile.  The sample takes jobs at an even
-// stride until it holds about kTuneBudget pairs, so tuning costs a fraction
-// of a second whatever the batch size.
+// Rows of the jobs given to the per-pair merge carry w = 1 in their row
+// info (the finish kernel recomputes them in order).
+void mark_merge_rows(const std::vector<HostJob>& jobs, int64_t merge_rows, std::vector<int4>& rowinfo) {
+    for (const HostJob& j : jobs)
+        if (j.re > j.rb && j.re - j.rb <= merge_rows)
+            for (int64_t r = j.rb; r < j.re; r++) rowinfo[(size_t)(j.out + r - j.rb)].w = 1;
+}
+
+// Times the plan on a sample of the jobs for a sequence of candidate shapes
+// and returns the fastest: tiles first (row cap 32, no merge jobs), then the
+// row cap 16 at the best tile, then merge cut-offs.  The sample takes jobs
+// at an even stride until it holds about kTuneBudget pairs, so tuning costs a
+// fraction of a second whatever the batch size.
 constexpr double kTuneBudget = 1.0e10;
 
-int autotune_tile(siml_engine* h, const DbLayout* d, const std::vector<HostJob>& jobs,
-                  const std::vector<int32_t>& mag, float lo, float hi, int64_t pitch, int64_t* best_tile) {
-    static const int64_t cand[] = {32, 64, 128, 256, 512, 1024, 2048};
+int autotune_shape(siml_engine* h, const DbLayout* d, const std::vector<HostJob>& jobs,
+                   const std::vector<int32_t>& mag, float lo, float hi, int64_t pitch, Shape* best_shape) {
+    static const int64_t tiles[] = {64, 128, 256, 512, 1024, 2048, 4096, 8192};
+    static const int64_t merges[] = {1, 2, 4, 8};
     std::vector<HostJob> sample;
     int64_t rows = 0;
     double pairs = 0.0;
@@ -130,19 +161,18 @@ int autotune_tile(siml_engine* h, const DbLayout* d, const std::vector<HostJob>&
         pairs += jp;
         sample.push_back(j);
     }
-    *best_tile = 128;
+    *best_shape = Shape();
     if (rows == 0) return SIML_OK;
-    std::vector<int4> rowinfo((size_t)rows, make_int4(-1, 0, 0, 0));
+    std::vector<int4> rowinfo0((size_t)rows, make_int4(-1, 0, 0, 0));
     for (const HostJob& j : sample)
         for (int64_t r = j.rb; r < j.re; r++)
-            rowinfo[(size_t)(j.out + r - j.rb)] = make_int4((int)r, (int)j.cb, (int)j.ce, 0);
+            rowinfo0[(size_t)(j.out + r - j.rb)] = make_int4((int)r, (int)j.cb, (int)j.ce, 0);
     int4* d_rowinfo = nullptr;
-    int32_t *d_idx = nullptr, *d_cnt = nullptr, *d_order = nullptr;
+    int32_t *d_idx = nullptr, *d_cnt = nullptr;
     unsigned int* d_head = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     int rc = SIML_OK;
     auto cleanup = [&]() {
-        if (d_order) cudaFree(d_order);
         if (d_rowinfo) cudaFree(d_rowinfo);
         if (d_idx) cudaFree(d_idx);
         if (d_cnt) cudaFree(d_cnt);
@@ -151,10 +181,7 @@ int autotune_tile(siml_engine* h, const DbLayout* d, const std::vector<HostJob>&
         if (e1) cudaEventDestroy(e1);
     };
     cudaError_t e = cudaSuccess;
-    if ((e = cudaMalloc((void**)&d_rowinfo, rowinfo.size() * sizeof(int4))) != cudaSuccess ||
-        (e = cudaMemcpyAsync(d_rowinfo, rowinfo.data(), rowinfo.size() * sizeof(int4), cudaMemcpyHostToDevice,
-                             h->stream)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(h->stream)) != cudaSuccess ||
+    if ((e = cudaMalloc((void**)&d_rowinfo, rowinfo0.size() * sizeof(int4))) != cudaSuccess ||
         (e = cudaMalloc((void**)&d_idx, (size_t)rows * (size_t)std::max<int64_t>(pitch, 1) * 4)) != cudaSuccess ||
         (e = cudaMalloc((void**)&d_cnt, (size_t)rows * 4)) != cudaSuccess ||
         (e = cudaMalloc((void**)&d_head, sizeof(unsigned int))) != cudaSuccess ||
@@ -162,37 +189,143 @@ int autotune_tile(siml_engine* h, const DbLayout* d, const std::vector<HostJob>&
         cleanup();
         return cuda_fail(e, "batch autotune set-up");
     }
-    double best = 1e300;
     bool warmed = false;
-    for (int64_t t : cand) {
-        std::vector<int4> items;
+    // time of one run of the sample with shape sh (ms), or a negative status
+    auto time_shape = [&](const Shape& sh, double* ms_out) -> int {
+        std::vector<int4> items, rowinfo = rowinfo0;
         std::vector<int32_t> order;
-        make_items(d, sample, mag, t, items, order);
+        make_items(d, sample, mag, sh, items, order);
+        mark_merge_rows(sample, sh.merge_rows, rowinfo);
         int4* d_items = nullptr;
-        if (!d_order && (rc = upload_items(h, order, &d_order))) break;   // the same for every tile
-        if ((rc = upload_items(h, items, &d_items))) break;
+        int32_t* d_order = nullptr;
+        int r2 = upload_items(h, items, &d_items);
+        if (!r2) r2 = upload_items(h, order, &d_order);
+        if (!r2 && cudaMemcpyAsync(d_rowinfo, rowinfo.data(), rowinfo.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                                   h->stream) != cudaSuccess)
+            r2 = fail(SIML_ERR_CUDA, "batch autotune upload");
         const int64_t ni = (int64_t)items.size() / 2;
-        if (!warmed) {   // first launch pays one-time costs; keep it out of the comparison
-            rc = launch_batch_neighbors(h, d, d_items, ni, d_head, d_order, (int64_t)order.size(), d_rowinfo, rows,
+        if (!r2 && !warmed) {   // the first launch pays one-time costs; keep it out of the comparison
+            r2 = launch_batch_neighbors(h, d, d_items, ni, d_head, d_order, (int64_t)order.size(), d_rowinfo, rows,
                                         lo, hi, pitch, d_idx, nullptr, d_cnt, h->stream);
             warmed = true;
         }
-        if (!rc) {
+        if (!r2) {
             cudaEventRecord(e0, h->stream);
-            rc = launch_batch_neighbors(h, d, d_items, ni, d_head, d_order, (int64_t)order.size(), d_rowinfo, rows,
+            r2 = launch_batch_neighbors(h, d, d_items, ni, d_head, d_order, (int64_t)order.size(), d_rowinfo, rows,
                                         lo, hi, pitch, d_idx, nullptr, d_cnt, h->stream);
             cudaEventRecord(e1, h->stream);
         }
-        e = cudaEventSynchronize(e1);
-        cudaFree(d_items);
-        if (rc) break;
-        if (e != cudaSuccess) { rc = cuda_fail(e, "batch autotune"); break; }
+        cudaError_t e2 = cudaEventSynchronize(e1);
+        if (d_items) cudaFree(d_items);
+        if (d_order) cudaFree(d_order);
+        if (r2) return r2;
+        if (e2 != cudaSuccess) return cuda_fail(e2, "batch autotune");
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best * 0.98) { best = ms; *best_tile = t; }
+        *ms_out = ms;
+        return SIML_OK;
+    };
+    double best = 1e300;
+    Shape cur;
+    for (int64_t t : tiles) {
+        cur.tile = t;
+        double ms = 0.0;
+        if ((rc = time_shape(cur, &ms))) break;
+        if (ms < best * 0.98) { best = ms; *best_shape = cur; }
+    }
+    if (!rc) {
+        cur = *best_shape;
+        cur.rows_cap = 16;
+        double ms = 0.0;
+        rc = time_shape(cur, &ms);
+        if (!rc && ms < best * 0.98) { best = ms; *best_shape = cur; }
+    }
+    for (int64_t m : merges) {
+        if (rc) break;
+        cur = *best_shape;
+        cur.merge_rows = m;
+        double ms = 0.0;
+        if ((rc = time_shape(cur, &ms))) break;
+        if (ms < best * 0.98) { best = ms; *best_shape = cur; }
     }
     cleanup();
     return rc;
+}
+
+// Shapes chosen by the timing, per (database length distribution, job
+// shape, bound) signature, for the whole process.
+std::mutex g_shape_mu;
+std::map<std::tuple<int64_t, int64_t, int64_t, int64_t, int64_t, int64_t>, Shape> g_shapes;
+
+// Signature of a plan's kind: the database's mean 8-entry steps per chunk
+// (quarter steps) and their spread (tenths of the mean), its size (log2),
+// the jobs' median rows and columns (log2) and the bound (hundredths).
+int plan_signature(siml_engine* h, const DbLayout* d, const std::vector<HostJob>& jobs, float lo,
+                   std::tuple<int64_t, int64_t, int64_t, int64_t, int64_t, int64_t>* sig) {
+    std::vector<int32_t> ng((size_t)std::max<int64_t>(d->nchunks, 1), 0);
+    if (d->nchunks > 0) {
+        SIML_CUDA(cudaMemcpyAsync(ng.data(), d->ng, (size_t)d->nchunks * 4, cudaMemcpyDeviceToHost, h->stream));
+        SIML_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    double sum = 0.0, sq = 0.0;
+    for (int64_t c = 0; c < d->nchunks; c++) {
+        sum += ng[(size_t)c];
+        sq += (double)ng[(size_t)c] * ng[(size_t)c];
+    }
+    const double nc = (double)std::max<int64_t>(d->nchunks, 1);
+    const double mean = sum / nc, sd = std::sqrt(std::max(0.0, sq / nc - mean * mean));
+    std::vector<int64_t> r, c;
+    for (const HostJob& j : jobs) {
+        r.push_back(j.re - j.rb);
+        c.push_back(j.ce - j.cb);
+    }
+    auto median_log2 = [](std::vector<int64_t>& v) -> int64_t {
+        if (v.empty()) return -1;
+        std::nth_element(v.begin(), v.begin() + v.size() / 2, v.end());
+        int64_t x = std::max<int64_t>(v[v.size() / 2], 1), b = 0;
+        while ((1ll << (b + 1)) <= x) b++;
+        return b;
+    };
+    int64_t nlog = 0;
+    while ((1ll << (nlog + 1)) <= std::max<int64_t>(d->n, 1)) nlog++;
+    *sig = std::make_tuple((int64_t)std::llround(mean * 4.0), (int64_t)std::llround(mean > 0 ? 10.0 * sd / mean : 0),
+                           nlog, median_log2(r), median_log2(c), (int64_t)std::llround((double)lo * 100.0));
+    return SIML_OK;
+}
+
+// Sets *bad when a ref row named by the plan holds a vid outside the
+// database vocabulary (1..limit) in its entry list: such a list was damaged
+// after it was built, and the plan refuses it rather than let the table
+// builds skip entries.  One warp per ordered row.
+__global__ void k_check_row_vids(const int32_t* __restrict__ order, int64_t n, const uint32_t* __restrict__ row_vid,
+                                 int64_t stride, int64_t nref, uint32_t limit, int* bad) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const int32_t r = order[w];
+    if (r < 0 || r >= nref) {
+        if (lane == 0) atomicOr(bad, 1);
+        return;
+    }
+    bool b = false;
+    for (int64_t e = lane; e < stride; e += 32) b |= row_vid[(int64_t)r * stride + e] > limit;
+    if (__any_sync(0xFFFFFFFFu, b) && lane == 0) atomicOr(bad, 1);
+}
+
+int check_plan_rows(siml_engine* h, const int32_t* d_order, int64_t n) {
+    if (n == 0) return SIML_OK;
+    int* d_bad = reinterpret_cast<int*>(h->d_counter);
+    int bad = 0;
+    SIML_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(int), h->stream));
+    k_check_row_vids<<<(unsigned)((n * 32 + 255) / 256), 256, 0, h->stream>>>(
+        d_order, n, h->rows.vid, h->rows.stride, h->ref.n, (uint32_t)h->vocab.nvid, d_bad);
+    SIML_CUDA(cudaGetLastError());
+    h->launches++;
+    SIML_CUDA(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    SIML_CUDA(cudaStreamSynchronize(h->stream));
+    if (bad) return fail(SIML_ERR_STATE, "siml_batch_create: a ref row's entry list holds a vid outside the "
+                                         "database vocabulary (damaged after it was built)");
+    return SIML_OK;
 }
 
 // Bytes one run reads: *streamed = every item's chunks (entry groups and
@@ -228,6 +361,11 @@ extern "C" {
 
 int siml_batch_create(siml_engine* h, int64_t njobs, const int64_t* jobs, float lo, float hi, int64_t pitch,
                       int64_t tile_chunks, siml_batch** out) {
+    return siml_batch_create_shaped(h, njobs, jobs, lo, hi, pitch, tile_chunks, 32, 0, out);
+}
+
+int siml_batch_create_shaped(siml_engine* h, int64_t njobs, const int64_t* jobs, float lo, float hi, int64_t pitch,
+                             int64_t tile_chunks, int64_t rows_cap, int64_t merge_rows, siml_batch** out) {
     clear_error();
     if (!h || !out) return fail(SIML_ERR_INVALID, "siml_batch_create: NULL argument");
     *out = nullptr;
@@ -257,16 +395,44 @@ int siml_batch_create(siml_engine* h, int64_t njobs, const int64_t* jobs, float 
                                        (long long)(x.out + r - x.rb));
             ri = make_int4((int)r, (int)x.cb, (int)x.ce, 0);
         }
+    // every job row's entry list must hold vocabulary vids only (checked
+    // before the tile timing launches the kernel on them)
+    {
+        std::vector<int32_t> jrows;
+        for (const HostJob& x : hj)
+            for (int64_t r = x.rb; r < x.re; r++) jrows.push_back((int32_t)r);
+        int32_t* d_rows = nullptr;
+        if ((rc = upload_items(h, jrows, &d_rows))) return rc;
+        rc = check_plan_rows(h, d_rows, (int64_t)jrows.size());
+        cudaFree(d_rows);
+        if (rc) return rc;
+    }
     std::vector<int32_t> mag;
     if ((rc = host_mags(h, mag))) return rc;
-    int64_t tile = tile_chunks;
-    if (tile <= 0) {
-        if (batch_nbr_usable(h, d)) {
-            if ((rc = autotune_tile(h, d, hj, mag, lo, hi, pitch, &tile))) return rc;
+    Shape sh;
+    int from_cache = 0;
+    if (tile_chunks > 0) {
+        sh.tile = tile_chunks;
+        sh.rows_cap = rows_cap == 16 ? 16 : 32;
+        sh.merge_rows = std::max<int64_t>(0, merge_rows);
+    } else if (batch_nbr_usable(h, d)) {
+        std::tuple<int64_t, int64_t, int64_t, int64_t, int64_t, int64_t> sig;
+        if ((rc = plan_signature(h, d, hj, lo, &sig))) return rc;
+        bool hit = false;
+        {
+            std::lock_guard<std::mutex> lk(g_shape_mu);
+            auto it = g_shapes.find(sig);
+            if (it != g_shapes.end()) { sh = it->second; hit = true; }
+        }
+        if (hit) {
+            from_cache = 1;
         } else {
-            tile = 128;
+            if ((rc = autotune_shape(h, d, hj, mag, lo, hi, pitch, &sh))) return rc;
+            std::lock_guard<std::mutex> lk(g_shape_mu);
+            g_shapes[sig] = sh;
         }
     }
+    mark_merge_rows(hj, sh.merge_rows, rowinfo);
     siml_batch* b = new siml_batch();
     b->h = h;
     b->d = d;
@@ -274,11 +440,14 @@ int siml_batch_create(siml_engine* h, int64_t njobs, const int64_t* jobs, float 
     b->lo = lo;
     b->hi = hi;
     b->pitch = pitch;
-    b->tile_chunks = tile;
+    b->tile_chunks = sh.tile;
+    b->rows_cap = sh.rows_cap;
+    b->merge_rows = sh.merge_rows;
+    b->from_cache = from_cache;
     b->rows_out = rows_out;
     std::vector<int4> items;
     std::vector<int32_t> order;
-    make_items(d, hj, mag, tile, items, order);
+    make_items(d, hj, mag, sh, items, order);
     b->nitems = (int64_t)items.size() / 2;
     b->order_len = (int64_t)order.size();
     if ((rc = plan_bytes(h, d, hj, items, &b->stream_bytes, &b->unique_bytes)) ||
@@ -305,6 +474,16 @@ int siml_batch_info(siml_batch* b, int64_t* rows_out, int64_t* nitems, int64_t* 
     if (tile_chunks) *tile_chunks = b->tile_chunks;
     if (stream_bytes) *stream_bytes = b->stream_bytes;
     if (unique_bytes) *unique_bytes = b->unique_bytes;
+    return SIML_OK;
+}
+
+int siml_batch_shape(siml_batch* b, int64_t out[4]) {
+    clear_error();
+    if (!b || !out) return fail(SIML_ERR_INVALID, "siml_batch_shape: NULL argument");
+    out[0] = b->tile_chunks;
+    out[1] = b->rows_cap;
+    out[2] = b->merge_rows;
+    out[3] = b->from_cache;
     return SIML_OK;
 }
 

@@ -139,22 +139,26 @@ int row_order_by_magnitude(siml_engine* h, int64_t rowbase, int64_t rowlimit, co
 }
 
 namespace {
-
 // siml_debug_fail_alloc: allocations left before one is refused (0: none).
 std::atomic<int64_t> g_fail_alloc{0};
+}  // namespace
 
-template <class T>
-int dev_alloc(T** p, size_t count) {
+int dev_alloc_bytes(void** p, size_t bytes) {
     *p = nullptr;
-    if (count == 0) count = 1;
     int64_t left = g_fail_alloc.load();
     while (left > 0 && !g_fail_alloc.compare_exchange_weak(left, left - 1)) {
     }
     if (left == 1)
-        return fail(SIML_ERR_NOMEM, "device allocation of %zu bytes refused (siml_debug_fail_alloc)",
-                    count * sizeof(T));
-    SIML_CUDA(cudaMalloc((void**)p, count * sizeof(T)));
+        return fail(SIML_ERR_NOMEM, "device allocation of %zu bytes refused (siml_debug_fail_alloc)", bytes);
+    SIML_CUDA(cudaMalloc(p, bytes));
     return SIML_OK;
+}
+
+namespace {
+
+template <class T>
+int dev_alloc(T** p, size_t count) {
+    return dev_alloc_bytes(reinterpret_cast<void**>(p), (count == 0 ? 1 : count) * sizeof(T));
 }
 template <class T>
 void dev_free(T*& p) {
@@ -173,6 +177,7 @@ void free_layout(DbLayout& d) {
     dev_free(d.rare_off); dev_free(d.rare_vid);
     if (d.crange) cudaFree(d.crange);
     if (d.entries) cudaFree(d.entries);
+    free_sched(d);
     d = DbLayout();
 }
 void free_rows(RowEntries& r) { dev_free(r.vid); r = RowEntries(); }
@@ -536,10 +541,10 @@ __global__ void k_row_entries(const int32_t* __restrict__ lingos, const int32_t*
                               const unsigned long long* __restrict__ keys,
                               const uint32_t* __restrict__ vid, int64_t cap,
                               uint32_t* __restrict__ out, int64_t stride, int64_t ncommon, int64_t ncommon_bal,
-                              int* max_rare) {
+                              int64_t ncommon_sched, int* max_rare) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
-    int nrare = 0, nrare_bal = 0;
+    int nrare = 0, nrare_bal = 0, nrare_sched = 0;
     const int32_t L = len[r];
     const int32_t* lr = lingos + r * width;
     const int32_t* cr = counts + r * width;
@@ -553,11 +558,13 @@ __global__ void k_row_entries(const int32_t* __restrict__ lingos, const int32_t*
             o[e++] = v;
             nrare += (int64_t)v > ncommon;
             nrare_bal += (int64_t)v > ncommon_bal;
+            nrare_sched += (int64_t)v > ncommon_sched;
         }
     }
     for (; e < stride; e++) o[e] = 0u;
     if (nrare) atomicMax(max_rare, nrare);
     if (nrare_bal) atomicMax(max_rare + 1, nrare_bal);
+    if (nrare_sched) atomicMax(max_rare + 2, nrare_sched);
 }
 
 // ------------------------------------------------------------ host helpers --
@@ -621,6 +628,13 @@ int split_vocab(siml_engine* h, int64_t ncommon);
 // fewer with a split vocabulary (room for the piece buffers).
 int64_t balanced_ncommon(siml_engine* h) {
     return h->vocab.split ? std::min<int64_t>(h->vocab.ncommon, split_balanced_capacity(h)) : h->vocab.ncommon;
+}
+
+// Common vids of the scheduled full-matrix layout: the vocabulary's when
+// its whole table fits beside the staging, else those of a split vocabulary
+// up to the kernel's capacity.
+int64_t sched_ncommon(siml_engine* h) {
+    return std::min<int64_t>(h->vocab.ncommon, sched_capacity(h));
 }
 
 int build_vocab(siml_engine* h) {
@@ -733,20 +747,24 @@ struct DevTemp {
     ~DevTemp() { if (p) cudaFree(p); }
 };
 
-int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
+int build_layout(siml_engine* h, DbLayout& d, bool sorted, bool scheduled = false) {
     free_layout(d);
     const RawSet& q = h->qry;
     cudaStream_t st = h->stream;
     const bool vsplit = h->vocab.split;
+    if (scheduled) sorted = true;
     d.n = q.n;
     d.sorted = sorted;
-    d.window = sorted ? h->sorted_window : h->rows_window;
+    d.scheduled = scheduled;
+    d.window = scheduled ? kSchedColumns / h->sched_groups : (sorted ? h->sorted_window : h->rows_window);
+    d.sched_warps = scheduled ? 32 / h->sched_groups : 0;
     d.offsets = !vsplit && !sorted && h->rows_entries == SIML_ENTRIES_OFFSETS;
     // the balanced kernel reads vids, not byte offsets; with a split
     // vocabulary its piece buffers leave room for fewer common vids
-    d.balanced = !sorted && h->rows_window == kChunk && h->rows_layout == SIML_ROWS_BALANCED && !d.offsets &&
+    d.balanced = !sorted && h->rows_window == kChunk &&
+                 (h->rows_layout == SIML_ROWS_BALANCED || h->rows_layout == SIML_ROWS_SCHEDULED) && !d.offsets &&
                  rows_balanced_fits(h);
-    d.ncommon = vsplit && d.balanced ? balanced_ncommon(h) : h->vocab.ncommon;
+    d.ncommon = scheduled ? sched_ncommon(h) : (vsplit && d.balanced ? balanced_ncommon(h) : h->vocab.ncommon);
     const bool split = d.ncommon < h->vocab.nvid;
     d.entry_bytes = d.ncommon < 65535 ? 2 : 4;
     if (!vsplit && !sorted && (h->rows_entries == SIML_ENTRIES_U32 || d.offsets)) d.entry_bytes = 4;
@@ -847,6 +865,7 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted) {
     h->launches++;
     SIML_CUDA(cudaGetLastError());
     SIML_CUDA(cudaStreamSynchronize(st));
+    if (scheduled) return sched_arrange(h, d);
     return SIML_OK;
 }
 
@@ -858,20 +877,23 @@ int build_rows(siml_engine* h) {
     re.stride = std::max<int64_t>(std::max<int64_t>(1, r.max_entries), h->row_stride_hint);
     int rc;
     if ((rc = dev_alloc(&re.vid, (size_t)(std::max<int64_t>(r.n, 1) * re.stride)))) return rc;
-    int max_rare[2] = {0, 0};   // against the vocabulary's common set and the balanced layout's
+    // rare entries per row against the vocabulary's common set, the balanced
+    // layout's and the scheduled layout's
+    int max_rare[3] = {0, 0, 0};
     int* d_max = reinterpret_cast<int*>(h->d_counter);
     if (r.n > 0) {
-        SIML_CUDA(cudaMemsetAsync(d_max, 0, 2 * sizeof(int), h->stream));
+        SIML_CUDA(cudaMemsetAsync(d_max, 0, 3 * sizeof(int), h->stream));
         k_row_entries<<<(unsigned)((r.n + 127) / 128), 128, 0, h->stream>>>(
             r.lingos, r.counts, r.len, r.n, r.width, h->vocab.keys, h->vocab.vid, h->vocab.cap, re.vid, re.stride,
-            h->vocab.ncommon, balanced_ncommon(h), d_max);
+            h->vocab.ncommon, balanced_ncommon(h), sched_ncommon(h), d_max);
         h->launches++;
         SIML_CUDA(cudaGetLastError());
-        SIML_CUDA(cudaMemcpyAsync(max_rare, d_max, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+        SIML_CUDA(cudaMemcpyAsync(max_rare, d_max, 3 * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     }
     SIML_CUDA(cudaStreamSynchronize(h->stream));
     re.max_rare = max_rare[0];
     re.max_rare_bal = max_rare[1];
+    re.max_rare_sched = max_rare[2];
     return SIML_OK;
 }
 
@@ -882,9 +904,10 @@ int ensure_prepared(siml_engine* h) {
     int rc;
     if (!h->layout_valid) {
         h->rows_valid = false;
-        h->nat_valid = h->sorted_valid = false;
+        h->nat_valid = h->sorted_valid = h->sched_valid = false;
         free_layout(h->db_nat);
         free_layout(h->db_sorted);
+        free_layout(h->db_sched);
         if ((rc = build_vocab(h))) return rc;
         h->layout_valid = true;
     }
@@ -911,20 +934,49 @@ int ensure_layout(siml_engine* h, bool sorted, const DbLayout** out) {
     return SIML_OK;
 }
 
+bool rows_use_sched(siml_engine* h) {
+    return h->rows_layout == SIML_ROWS_SCHEDULED && h->rows_window == kChunk &&
+           (h->rows_entries == SIML_ENTRIES_AUTO || h->rows_entries == SIML_ENTRIES_U16) && rows_sched_fits(h);
+}
+
+int ensure_sched_layout(siml_engine* h, const DbLayout** out) {
+    int rc = ensure_prepared(h);
+    if (rc) return rc;
+    if (!h->sched_valid) {
+        if ((rc = build_layout(h, h->db_sched, true, true))) {
+            free_layout(h->db_sched);
+            return rc;
+        }
+        h->sched_valid = true;
+    }
+    *out = &h->db_sched;
+    return SIML_OK;
+}
+
 }  // namespace siml
 
 namespace siml {
+
+// Status (and message) of an asynchronous error word; the lowest set bit
+// decides when several are set.
+int async_error_status(int v) {
+    if (!v) return SIML_OK;
+    if (v & 1)
+        return fail(SIML_ERR_TIMEOUT, "a top-k heap lock wait exceeded its bound in a queued call; that call's "
+                    "result is invalid");
+    if (v & 2)
+        return fail(SIML_ERR_STATE, "a batched neighbour run met a work item outside its plan's extents and "
+                    "skipped it; that run's result is invalid");
+    return fail(SIML_ERR_STATE, "a ref row's entry list held a vid that fits neither the shared table nor the "
+                "rare-vid hash; the entry was not used and the call's result is invalid");
+}
 
 int take_async_error(siml_engine* h) {
     volatile int* w = h->h_async_err;
     const int v = w ? *w : 0;
     if (!v) return SIML_OK;
     *w = 0;
-    if (v & 1)
-        return fail(SIML_ERR_TIMEOUT, "a top-k heap lock wait exceeded its bound in a queued call; that call's "
-                    "result is invalid");
-    return fail(SIML_ERR_STATE, "a batched neighbour run met a work item outside its plan's extents and skipped "
-                "it; that run's result is invalid");
+    return async_error_status(v);
 }
 
 }  // namespace siml
@@ -984,6 +1036,7 @@ int siml_destroy(siml_engine* h) {
     free_vocab(h->vocab);
     free_layout(h->db_nat);
     free_layout(h->db_sorted);
+    free_layout(h->db_sched);
     free_rows(h->rows);
     for (int i = 0; i < 4; i++)
         if (h->scratch[i]) cudaFree(h->scratch[i]);
@@ -1104,20 +1157,21 @@ int siml_write_ref_rows(siml_engine* h, int64_t row0, const int32_t* lingos, con
             // whether the table kernels may run, so it is read back (a
             // stream synchronization only for split vocabularies)
             int* d_max = reinterpret_cast<int*>(h->d_counter);
-            if (h->vocab.split) SIML_CUDA(cudaMemsetAsync(d_max, 0, 2 * sizeof(int), st));
+            if (h->vocab.split) SIML_CUDA(cudaMemsetAsync(d_max, 0, 3 * sizeof(int), st));
             k_row_entries<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(dl, dc, s.len + row0, n, s.width,
                                                                        h->vocab.keys, h->vocab.vid, h->vocab.cap,
                                                                        h->rows.vid + row0 * h->rows.stride,
                                                                        h->rows.stride, h->vocab.ncommon,
-                                                                       balanced_ncommon(h), d_max);
+                                                                       balanced_ncommon(h), sched_ncommon(h), d_max);
             h->launches++;
             SIML_CUDA(cudaGetLastError());
             if (h->vocab.split) {
-                int mr[2] = {0, 0};
-                SIML_CUDA(cudaMemcpyAsync(mr, d_max, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+                int mr[3] = {0, 0, 0};
+                SIML_CUDA(cudaMemcpyAsync(mr, d_max, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
                 SIML_CUDA(cudaStreamSynchronize(st));
                 h->rows.max_rare = std::max<int64_t>(h->rows.max_rare, mr[0]);
                 h->rows.max_rare_bal = std::max<int64_t>(h->rows.max_rare_bal, mr[1]);
+                h->rows.max_rare_sched = std::max<int64_t>(h->rows.max_rare_sched, mr[2]);
             }
         }
     }
@@ -1145,7 +1199,10 @@ int siml_db_stats(siml_engine* h, int64_t out[8]) {
     SIML_GUARD(h);
     if (!out) return fail(SIML_ERR_INVALID, "siml_db_stats: NULL output");
     const DbLayout* d = nullptr;
-    int rc = ensure_layout(h, false, &d);
+    int rc = ensure_prepared(h);
+    if (rc) return rc;
+    // the layout getMultipleRows streams
+    rc = rows_use_sched(h) ? ensure_sched_layout(h, &d) : ensure_layout(h, false, &d);
     if (rc) return rc;
     out[0] = h->vocab.nvid;
     out[1] = d->entry_bytes;
@@ -1155,6 +1212,22 @@ int siml_db_stats(siml_engine* h, int64_t out[8]) {
     out[5] = d->n;
     out[6] = h->ref.max_entries;
     out[7] = h->qry.max_entries;
+    return SIML_OK;
+}
+
+int siml_rows_info(siml_engine* h, int64_t out[4]) {
+    SIML_GUARD(h);
+    if (!out) return fail(SIML_ERR_INVALID, "siml_rows_info: NULL output");
+    int rc = ensure_prepared(h);
+    if (rc) return rc;
+    out[0] = out[1] = out[2] = out[3] = 0;
+    if (!rows_use_sched(h)) return SIML_OK;
+    const DbLayout* d = nullptr;
+    if ((rc = ensure_sched_layout(h, &d))) return rc;
+    out[0] = 1;
+    out[1] = d->nitems;
+    out[2] = d->nwin;
+    out[3] = d->max_item_steps;
     return SIML_OK;
 }
 
@@ -1185,13 +1258,14 @@ int siml_set_tuning(siml_engine* h, int key, int64_t value) {
         }
         return SIML_OK;
     case SIML_TUNE_ROWS_LAYOUT:
-        if (value != SIML_ROWS_PADDED && value != SIML_ROWS_BALANCED)
-            return fail(SIML_ERR_INVALID, "rows layout must be SIML_ROWS_PADDED or SIML_ROWS_BALANCED (got %lld)",
-                        (long long)value);
+        if (value != SIML_ROWS_PADDED && value != SIML_ROWS_BALANCED && value != SIML_ROWS_SCHEDULED)
+            return fail(SIML_ERR_INVALID, "rows layout must be SIML_ROWS_PADDED, SIML_ROWS_BALANCED or "
+                        "SIML_ROWS_SCHEDULED (got %lld)", (long long)value);
         if (value != h->rows_layout) {
             SIML_CUDA(cudaStreamSynchronize(h->stream));
             free_layout(h->db_nat);
-            h->nat_valid = false;
+            free_layout(h->db_sched);
+            h->nat_valid = h->sched_valid = false;
             h->rows_layout = (int)value;
         }
         return SIML_OK;
@@ -1212,6 +1286,16 @@ int siml_set_tuning(siml_engine* h, int key, int64_t value) {
             return fail(SIML_ERR_INVALID, "row stride hint must be in [0, 2^20] (got %lld)", (long long)value);
         if (value > h->row_stride_hint && h->rows_valid && value > h->rows.stride) h->rows_valid = false;
         h->row_stride_hint = value;
+        return SIML_OK;
+    case SIML_TUNE_SCHED_GROUPS:
+        if (value != 2 && value != 4)
+            return fail(SIML_ERR_INVALID, "scheduled kernel warp groups must be 2 or 4 (got %lld)", (long long)value);
+        if (value != h->sched_groups) {
+            SIML_CUDA(cudaStreamSynchronize(h->stream));
+            free_layout(h->db_sched);
+            h->sched_valid = false;
+            h->sched_groups = (int)value;
+        }
         return SIML_OK;
     case SIML_TUNE_ROWS_ENTRIES:
         if (value < SIML_ENTRIES_AUTO || value > SIML_ENTRIES_OFFSETS)
@@ -1237,16 +1321,44 @@ int siml_get_tuning(siml_engine* h, int key, int64_t* value) {
     case SIML_TUNE_ROW_STRIDE: *value = h->row_stride_hint; return SIML_OK;
     case SIML_TUNE_SORT_WINDOW: *value = h->sorted_window; return SIML_OK;
     case SIML_TUNE_ROWS_LAYOUT: *value = h->rows_layout; return SIML_OK;
+    case SIML_TUNE_SCHED_GROUPS: *value = h->sched_groups; return SIML_OK;
     default: return fail(SIML_ERR_INVALID, "unknown tuning key %d", key);
     }
 }
 
 int64_t siml_launch_count(siml_engine* h) { return h ? h->launches : -1; }
 
+int siml_mem_info(siml_engine* h, int64_t* free_bytes, int64_t* total_bytes) {
+    SIML_GUARD(h);
+    size_t f = 0, t = 0;
+    SIML_CUDA(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = (int64_t)f;
+    if (total_bytes) *total_bytes = (int64_t)t;
+    return SIML_OK;
+}
+
 int siml_debug_fail_alloc(int64_t nth) {
     clear_error();
     if (nth < 0) return fail(SIML_ERR_INVALID, "siml_debug_fail_alloc: nth must be >= 0");
     siml::g_fail_alloc.store(nth);
+    return SIML_OK;
+}
+
+int siml_debug_async_status(int word) {
+    clear_error();
+    return async_error_status(word);
+}
+
+int siml_debug_set_row_vid(siml_engine* h, int64_t row, int64_t pos, uint32_t vid) {
+    SIML_GUARD(h);
+    int rc = ensure_prepared(h);
+    if (rc) return rc;
+    if (row < 0 || row >= h->rows.n || pos < 0 || pos >= h->rows.stride)
+        return fail(SIML_ERR_RANGE, "siml_debug_set_row_vid: entry (%lld, %lld) outside the row lists",
+                    (long long)row, (long long)pos);
+    SIML_CUDA(cudaMemcpyAsync(h->rows.vid + row * h->rows.stride + pos, &vid, sizeof(uint32_t),
+                              cudaMemcpyHostToDevice, h->stream));
+    SIML_CUDA(cudaStreamSynchronize(h->stream));
     return SIML_OK;
 }
 
@@ -1278,7 +1390,7 @@ static int rows_common(siml_engine* h, int64_t rowbase, int64_t rowlimit, float*
     if ((rc = launch_rows(h, a))) return rc;
     SIML_CUDA(cudaMemcpy2DAsync(out, ldo * 4, dbuf, nq * 4, nq * 4, rows, cudaMemcpyDefault, h->stream));
     SIML_CUDA(cudaStreamSynchronize(h->stream));
-    return SIML_OK;
+    return take_async_error(h);   // a table build that met an unusable row entry
 }
 
 int siml_rows(siml_engine* h, int64_t rowbase, int64_t rowlimit, float* out, int64_t ldo, int where) {
@@ -1316,7 +1428,7 @@ int siml_neighbors_range(siml_engine* h, int64_t rowbase, int64_t rowlimit, int6
     if (ib && sims) SIML_CUDA(cudaMemcpyAsync(sims, c.sims, ib, cudaMemcpyDefault, h->stream));
     SIML_CUDA(cudaMemcpyAsync(counts, c.counts, cb, cudaMemcpyDefault, h->stream));
     SIML_CUDA(cudaStreamSynchronize(h->stream));
-    return SIML_OK;
+    return take_async_error(h);   // a table build that met an unusable row entry
 }
 
 int siml_neighbors(siml_engine* h, int64_t rowbase, int64_t rowlimit, float lo, float hi, int64_t pitch,
@@ -1348,7 +1460,7 @@ int siml_hist101(siml_engine* h, int64_t rowbase, int64_t rowlimit, int32_t* out
     if ((rc = launch_hist(h, rowbase, rowlimit, false, buf, 101))) return rc;
     SIML_CUDA(cudaMemcpy2DAsync(out, ldo * 4, buf, 101 * 4, 101 * 4, rows, cudaMemcpyDefault, h->stream));
     SIML_CUDA(cudaStreamSynchronize(h->stream));
-    return SIML_OK;
+    return take_async_error(h);   // a table build that met an unusable row entry
 }
 
 int siml_hist_global(siml_engine* h, int64_t rowbase, int64_t rowlimit, uint64_t* out, int where) {
@@ -1365,7 +1477,7 @@ int siml_hist_global(siml_engine* h, int64_t rowbase, int64_t rowlimit, uint64_t
     if ((rc = launch_hist(h, rowbase, rowlimit, true, buf, 0))) return rc;
     SIML_CUDA(cudaMemcpyAsync(out, buf, 1000 * 8, cudaMemcpyDefault, h->stream));
     SIML_CUDA(cudaStreamSynchronize(h->stream));
-    return SIML_OK;
+    return take_async_error(h);   // a table build that met an unusable row entry
 }
 
 static int row_hist_common(siml_engine* h, const void* data, bool f64, int64_t rows, int64_t cols, int64_t ld,

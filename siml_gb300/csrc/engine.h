@@ -80,6 +80,18 @@ struct DbLayout {
     uint32_t* rare_vid = nullptr;
     int64_t nrare = 0;
     int64_t ncommon = 0;          // vids the layout streams (<= the vocabulary's ncommon)
+    // scheduled full-matrix layout (window-sorted): the entries of each
+    // (window, warp of a group) are one contiguous run of work items, each
+    // item a chunk or a range of a chunk's steps (rows_sched.cu)
+    bool scheduled = false;
+    int2* sched_items = nullptr;  // [nitems + 1] {chunk, steps | kItemSplit | kItemFirst}, padding record last
+    int2* sched_lanes = nullptr;  // [nitems + 1][32] {window position or -1, column magnitude bits}
+    int2* sched_wrun = nullptr;   // [nwin * warps] {first item, end item} of (window, warp of a group)
+    int64_t* sched_grun = nullptr; // [nwin * warps][2] first and end 16-byte group of (window, warp)
+    int64_t nitems = 0;
+    int64_t nwin = 0;
+    int64_t max_item_steps = 0;
+    int sched_warps = 0;          // warps of a group (one window per group; 2048 / window groups per CTA)
 };
 
 // Ref-set rows as vid lists (levels expanded, codes absent from the database
@@ -90,6 +102,7 @@ struct RowEntries {
     uint32_t* vid = nullptr;
     int64_t max_rare = 0;      // most rare-vid entries in one row (split vocabulary)
     int64_t max_rare_bal = 0;  // the same against the balanced layout's smaller common set
+    int64_t max_rare_sched = 0; // the same against the scheduled layout's common set
 };
 
 }  // namespace siml
@@ -104,8 +117,8 @@ struct siml_engine {
     bool layout_valid = false;   // vocabulary of the current query set
     bool rows_valid = false;
     siml::Vocab vocab;
-    siml::DbLayout db_nat, db_sorted;
-    bool nat_valid = false, sorted_valid = false;
+    siml::DbLayout db_nat, db_sorted, db_sched;
+    bool nat_valid = false, sorted_valid = false, sched_valid = false;
     siml::RowEntries rows;
     // device scratch reused across calls, one buffer per purpose (siml::kSlot*)
     void* scratch[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -127,7 +140,8 @@ struct siml_engine {
     int rows_entries = 0;                 // entry format of the full-matrix layout (SIML_TUNE_ROWS_ENTRIES)
     int64_t row_stride_hint = 0;          // least entries per ref row list (SIML_TUNE_ROW_STRIDE)
     int sorted_window = 2048;             // sort window of the fused-kernel layout (SIML_TUNE_SORT_WINDOW)
-    int rows_layout = SIML_ROWS_BALANCED; // lane packing of the full-matrix layout (SIML_TUNE_ROWS_LAYOUT)
+    int rows_layout = SIML_ROWS_SCHEDULED; // full-matrix layout (SIML_TUNE_ROWS_LAYOUT)
+    int sched_groups = 4;                  // warp groups of the scheduled kernel (SIML_TUNE_SCHED_GROUPS)
 };
 
 namespace siml {
@@ -136,6 +150,22 @@ namespace siml {
 int ensure_prepared(siml_engine* h);
 // Natural-order (sorted == false) or window-sorted database layout.
 int ensure_layout(siml_engine* h, bool sorted, const DbLayout** out);
+// The scheduled full-matrix layout (window-sorted, entries in per-warp
+// schedule order); rows_sched.cu arranges it.  A CTA's 32 warps form
+// sched_groups groups, each on its own window of 2048 / sched_groups columns.
+constexpr int kSchedColumns = 2048;
+int ensure_sched_layout(siml_engine* h, const DbLayout** out);
+// getMultipleRows runs on the scheduled layout (settings and sets allow it;
+// the sets must be prepared).
+bool rows_use_sched(siml_engine* h);
+// rows_sched.cu: common vids the scheduled kernel's table can hold beside its
+// staging (with a split vocabulary), whether it fits the current sets, the
+// schedule and entry permutation of a freshly built window-sorted layout,
+// and the launch (*done = false when the call is not one it serves).
+int64_t sched_capacity(siml_engine* h);
+bool rows_sched_fits(siml_engine* h);
+int sched_arrange(siml_engine* h, DbLayout& d);
+void free_sched(DbLayout& d);
 // Scratch slots: host-call staging, per-call row order, top-k partial heaps,
 // small counters.
 constexpr int kSlotStage = 0;
@@ -150,6 +180,8 @@ int row_order_by_magnitude(siml_engine* h, int64_t rowbase, int64_t rowlimit, co
 constexpr int kOrderBuckets = 4096;
 int row_order_into(siml_engine* h, int64_t rowbase, int64_t rowlimit, int32_t* order, int32_t* bucket);
 int cuda_fail(cudaError_t e, const char* what);
+// cudaMalloc through the engines' allocator (siml_debug_fail_alloc can refuse it).
+int dev_alloc_bytes(void** p, size_t bytes);
 // Lets `kernel` launch with up to `need` bytes of dynamic shared memory on
 // the current device.  The limit is an attribute of the function, shared by
 // every engine and host thread, so it is raised once per kernel and device
@@ -174,6 +206,7 @@ struct RowsArgs {
 constexpr int kModeRows = 0;    // getMultipleRows: CPU-order fp32 union, zero test on magnitudes
 constexpr int kModeSingle = 1;  // getTanimotoRow: count-sum magnitudes, zero test on lengths
 int launch_rows(siml_engine* h, const RowsArgs& a);
+int launch_rows_sched(siml_engine* h, const RowsArgs& a, bool* done);
 // The balanced full-matrix kernel's shared memory (table + per-warp pieces)
 // fits for the current sets.
 bool rows_balanced_fits(siml_engine* h);

@@ -1,0 +1,615 @@
+// getMultipleRows over the scheduled layout (sm_103a).
+//
+// A CTA holds the shared-memory table of 32 ref rows and splits its 32 warps
+// into G independent groups of P = 32 / G warps.  Each group writes the
+// group's 32 rows x one window of W = 2048 / G database columns at a time,
+// and the groups work on different windows, synchronised only among
+// themselves (named barriers), so one group's stream phase runs beside
+// another's store phase and the table is shared by all.
+//
+// The layout sorts database molecules by entry count inside windows of W, so
+// the 32 molecules of a chunk (one per lane) have nearly equal lists and a
+// warp streams whole molecules, with no partial counters to merge.  Work is
+// balanced at layout build, not at run time: each window's chunks, longest
+// first, are dealt to the group's P warps in equal shares, where an item (a
+// chunk, or a range of a chunk's 8-entry steps) costs its steps plus a fixed
+// overhead for its epilogue, and the share is the smallest for which the
+// wrap-around fill fits P warps (found by bisection).  A chunk whose steps
+// straddle two shares is split into items that add into the same counts.
+// Each (window, warp) run of items is stored contiguously, so a warp's loads
+// stream one array, two steps ahead, with no bounds tests (the array carries
+// two steps of padding), and the run of the group's next window is pulled
+// into L2 while the current one streams.
+//
+// Phase 1 (per window): the group's warps stream their items through the
+// bit-sliced counter (lingo_core.cuh); at the end of an item the 8 planes
+// are transposed into 32 byte counts and stored, 8 words per molecule, into
+// the group's staging area at the molecule's natural position in the window
+// (a split item adds its words atomically; bytes cannot carry, the counts of
+// a whole molecule being below 256).
+// Phase 2 (per window, after the group's barrier): each thread takes 4
+// consecutive columns and 4 rows per staging word and forms the reference's
+// fp32 Tanimoto, ((float)amag + bmag) - isct and isct / union, with packed
+// f32x2 arithmetic and Markstein's correction of the reciprocal estimate
+// (exact for the integer ranges fast_mag admits; other pairs take the IEEE
+// division), then writes 16 bytes per row: a warp's store covers 512
+// contiguous bytes of one row.  The staging words are zeroed as they are
+// read.
+#include <vector>
+
+#include "table_core.cuh"
+
+namespace siml {
+namespace {
+
+constexpr int kSThreads = 1024;
+constexpr int kSWarpsAll = kSThreads / 32;
+constexpr int kSColsAll = 2048;       // columns in flight per CTA: G windows of kSColsAll / G
+constexpr double kItemCost = 2.0;     // an item's epilogue, in 8-entry steps, for the schedule
+constexpr int kItemStepsMask = 0xFFFF;
+constexpr int kItemSplit = 1 << 16;   // the chunk has several items: add counts atomically
+constexpr int kItemFirst = 1 << 17;   // the item holds the chunk's first step: column data, rare entries
+constexpr int kPadSteps = 2;          // steps of zero padding after the entries (loads run two steps ahead)
+// staging (8 count words per column) + column magnitudes, over all groups
+constexpr size_t kSchedExtraSmem = (size_t)9 * kSColsAll * 4;
+
+struct SchedArgs {
+    const int2* items;     // work items, with one padding record after the last
+    const int2* lanes;     // [items + 1][32] per lane: {window position or -1, column magnitude or -1.0f bits}
+    const int2* wrun;      // [nwin * P] {first item, end item} of (window, warp of the group)
+    const int64_t* grun;   // [nwin * P][2] first and end 16-byte group of (window, warp of the group)
+    const int32_t* qmag;   // database magnitudes in natural order (IEEE-division path)
+    int64_t nq;
+    int64_t nwin;
+    float* out;            // row rowbase of the block
+    int64_t ldo;
+};
+
+// ---- packed fp32 pairs (two IEEE round-to-nearest operations each)
+__device__ __forceinline__ uint64_t f2(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void unf2(uint64_t v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ float rcp_est(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Two Tanimotos i / (s - i) at once, each as div_small (lingo_core.cuh) with
+// the reference's union order: u = s - i, q0 = i * y, r = fma(q0, -u, i)
+// (the same value as fma(-q0, u, i)), q = fma(r, y, q0).
+__device__ __forceinline__ uint64_t tanimoto2(uint64_t I, uint64_t S) {
+    const uint64_t U = sub2(S, I), NU = sub2(I, S);
+    float u0, u1;
+    unf2(U, u0, u1);
+    const uint64_t Y = f2(rcp_est(u0), rcp_est(u1));
+    const uint64_t Q0 = mul2(I, Y);
+    const uint64_t R = fma2(Q0, NU, I);
+    return fma2(R, Y, Q0);
+}
+
+// End of an item: the counter's planes become 32 byte counts (word k holds
+// rows k, k + 8, k + 16, k + 24) stored at the molecule's window position.
+template <int WIN>
+__device__ __forceinline__ void flush_item(uint32_t* W, float* colf, int flags, const int2& lr,
+                                           const SlicedCounter<8>& acc) {
+    if (lr.x < 0) return;
+    const int pos = lr.x;
+    uint32_t w[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) w[k] = acc.plane[k];
+    transpose_planes8(w);
+    if (flags & kItemSplit) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) atomicAdd(W + k * WIN + pos, w[k]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++) W[k * WIN + pos] = w[k];
+    }
+    if (flags & kItemFirst) colf[pos] = __int_as_float(lr.y);
+}
+
+__device__ __forceinline__ void group_barrier(int group, int threads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + group), "r"(threads) : "memory");
+}
+
+template <bool RARE, int G>
+__global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p, const SchedArgs a) {
+    constexpr int P = kSWarpsAll / G;          // warps of a group
+    constexpr int TG = P * 32;                 // threads of a group
+    constexpr int WIN = kSColsAll / G;         // columns of a window
+    constexpr int Q = WIN / 4;                 // 4-column quads of a window
+    static_assert(TG == 2 * Q, "phase 2 maps each thread to one quad and two of its count words");
+    extern __shared__ __align__(16) uint32_t T[];
+    __shared__ RowSmem rs;
+    __shared__ __align__(16) float amq[32];   // amq[4 k + j]: magnitude of row k + 8 j
+    const int nr = build_table(T, rs, p);      // synchronizes the block
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int group = warp / P, wg = warp - group * P, tg = threadIdx.x - group * TG;
+    uint32_t* W = T + p.tab_words + (size_t)group * 9 * WIN;   // [8][WIN] staged counts of this group
+    float* colf = reinterpret_cast<float*>(W + 8 * WIN);        // [WIN] column magnitude, -1: IEEE path
+    if (threadIdx.x < 32) amq[(lane & 7) * 4 + (lane >> 3)] = rs.amagf[lane];
+    for (int i = tg * 4; i < 8 * WIN; i += TG * 4) *reinterpret_cast<uint4*>(W + i) = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    const int64_t w0 = a.nwin * blockIdx.y / gridDim.y, w1 = a.nwin * (blockIdx.y + 1) / gridDim.y;
+    float* outg = a.out + (int64_t)blockIdx.x * 32 * a.ldo;
+    const uint4* E = reinterpret_cast<const uint4*>(p.entries) + lane;
+    const char* Eb = reinterpret_cast<const char*>(p.entries);
+    const uint64_t k2p23 = f2(8388608.0f, 8388608.0f);
+    const int q4 = (tg % Q) * 4;   // phase 2: columns q4 .. q4 + 3
+    const int kk = tg / Q;         // phase 2: staging words kk, kk + 2, kk + 4, kk + 6
+    // A warp streams the runs of its windows (w0 + group, then every G-th)
+    // as one sequence: the layout stores them back to back, so the two-step
+    // register prefetch and the next item's record run straight across the
+    // window boundaries.
+    const int64_t wfirst = w0 + group;
+    const uint4* ptr = E;
+    uint4 qa = make_uint4(0u, 0u, 0u, 0u), qb = qa;
+    int it = 0, left = 0;
+    int2 rec = make_int2(0, 0), rec_n = rec;
+    int2 lr = make_int2(-1, 0), lr_n = lr;   // this lane's record of the current and the next item
+    bool phase_b = false;   // the next step is held in qb
+    if (wfirst < w1) {
+        const int64_t sl = wfirst * P + wg;
+        const int64_t g0 = __ldg(a.grun + 2 * sl);
+        ptr = E + g0;
+        qa = __ldg(ptr);
+        qb = __ldg(ptr + 32);
+        it = __ldg(a.wrun + sl).x;
+        rec = __ldg(a.items + it);
+        lr = __ldg(a.lanes + (int64_t)it * 32 + lane);
+        rec_n = __ldg(a.items + it + 1);
+        lr_n = __ldg(a.lanes + (int64_t)(it + 1) * 32 + lane);
+        left = rec.y & kItemStepsMask;
+        if (lane == 0) {   // this window's run and the next one's into L2
+            for (int64_t w2 = wfirst; w2 < w1 && w2 <= wfirst + G; w2 += G) {
+                const int64_t s2 = w2 * P + wg;
+                const int64_t b = __ldg(a.grun + 2 * s2), e = __ldg(a.grun + 2 * s2 + 1);
+                prefetch_l2(Eb + b * 16, (uint32_t)((e - b) * 16));
+            }
+        }
+    }
+    SlicedCounter<8> acc;
+    acc.clear();
+    for (int64_t wnd = wfirst; wnd < w1; wnd += G) {
+        const int64_t wbase = wnd * WIN;
+        // ---------------------------------------------------------- phase 1
+        const int64_t slot = wnd * P + wg;
+        const int ie = __ldg(a.wrun + slot).y;
+        if (lane == 0 && wnd + 2 * G < w1) {   // the run two windows ahead into L2
+            const int64_t s2 = slot + (int64_t)2 * G * P;
+            const int64_t b = __ldg(a.grun + 2 * s2), e = __ldg(a.grun + 2 * s2 + 1);
+            prefetch_l2(Eb + b * 16, (uint32_t)((e - b) * 16));
+        }
+        // ends the items that are complete; false when the window's items are
+        // done (rec and lr then hold the next window's first item)
+        auto advance = [&]() -> bool {
+            while (left == 0) {
+                if constexpr (RARE) {
+                    if ((rec.y & kItemFirst) && lr.x >= 0) rare_add<8>(T, p, (int64_t)rec.x * 32 + lane, acc);
+                }
+                flush_item<WIN>(W, colf, rec.y, lr, acc);
+                acc.clear();
+                ++it;
+                rec = rec_n;
+                lr = lr_n;
+                left = rec.y & kItemStepsMask;
+                rec_n = __ldg(a.items + it + 1);
+                lr_n = __ldg(a.lanes + (int64_t)(it + 1) * 32 + lane);
+                if (it >= ie) return false;
+            }
+            return true;
+        };
+        if (it < ie && advance()) {
+            for (;;) {
+                if (!phase_b) {   // step held in qa; its register takes the step two ahead
+                    const uint32_t x0 = qa.x, x1 = qa.y, x2 = qa.z, x3 = qa.w;
+                    qa = __ldg(ptr + 64);
+                    acc.add8(T[x0 & 0xFFFFu], T[x0 >> 16], T[x1 & 0xFFFFu], T[x1 >> 16],
+                             T[x2 & 0xFFFFu], T[x2 >> 16], T[x3 & 0xFFFFu], T[x3 >> 16]);
+                    --left;
+                    if (!advance()) {
+                        phase_b = true;
+                        break;
+                    }
+                }
+                {   // step held in qb
+                    const uint32_t x0 = qb.x, x1 = qb.y, x2 = qb.z, x3 = qb.w;
+                    qb = __ldg(ptr + 96);
+                    acc.add8(T[x0 & 0xFFFFu], T[x0 >> 16], T[x1 & 0xFFFFu], T[x1 >> 16],
+                             T[x2 & 0xFFFFu], T[x2 >> 16], T[x3 & 0xFFFFu], T[x3 >> 16]);
+                }
+                ptr += 64;
+                phase_b = false;
+                --left;
+                if (!advance()) break;
+            }
+        }
+        group_barrier(group, TG);
+        // ---------------------------------------------------------- phase 2
+        const int64_t left_cols = a.nq - wbase;
+        const int ncols = left_cols < WIN ? (int)left_cols : WIN;
+        if (q4 < ncols) {
+            const float4 cf = *reinterpret_cast<const float4*>(colf + q4);
+            const bool full = q4 + 4 <= ncols;
+            const bool fast = rs.allfast && full && cf.x >= 0.0f && cf.y >= 0.0f && cf.z >= 0.0f && cf.w >= 0.0f;
+            const uint64_t B01 = f2(cf.x, cf.y), B23 = f2(cf.z, cf.w);
+            float* ob = outg + wbase + q4;
+#pragma unroll
+            for (int kq = 0; kq < 4; kq++) {
+                const int k = kk + 2 * kq;
+                uint32_t* wp = W + k * WIN + q4;
+                const uint4 c = *reinterpret_cast<const uint4*>(wp);
+                *reinterpret_cast<uint4*>(wp) = make_uint4(0u, 0u, 0u, 0u);
+                const float4 a4 = *reinterpret_cast<const float4*>(amq + 4 * k);
+                const float av[4] = {a4.x, a4.y, a4.z, a4.w};
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int r = k + 8 * j;
+                    if (r >= nr) break;
+                    float* orow = ob + (int64_t)r * a.ldo;
+                    const uint32_t sel = 0x7440u | (uint32_t)j;   // 0x4B0000cc: the float 2^23 + count
+                    if (fast) {
+                        const uint64_t I01 = sub2(f2(__uint_as_float(__byte_perm(c.x, 0x4B000000u, sel)),
+                                                     __uint_as_float(__byte_perm(c.y, 0x4B000000u, sel))), k2p23);
+                        const uint64_t I23 = sub2(f2(__uint_as_float(__byte_perm(c.z, 0x4B000000u, sel)),
+                                                     __uint_as_float(__byte_perm(c.w, 0x4B000000u, sel))), k2p23);
+                        const uint64_t A = f2(av[j], av[j]);
+                        const uint64_t Q01 = tanimoto2(I01, add2(A, B01));
+                        const uint64_t Q23 = tanimoto2(I23, add2(A, B23));
+                        float t0, t1, t2, t3;
+                        unf2(Q01, t0, t1);
+                        unf2(Q23, t2, t3);
+                        *reinterpret_cast<float4*>(orow) = make_float4(t0, t1, t2, t3);
+                    } else {
+                        const uint32_t cw[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+                        for (int cc = 0; cc < 4; cc++) {
+                            if (q4 + cc < ncols) {
+                                const int is = (int)((cw[cc] >> (8 * j)) & 0xFFu);
+                                orow[cc] = tanimoto_rows(is, rs.amag[r], __ldg(a.qmag + wbase + q4 + cc));
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        group_barrier(group, TG);
+    }
+}
+
+// Permutes 16-byte entry groups into schedule order: new step t (32 groups,
+// one per lane) is old step map[t].
+__global__ void k_sched_gather(const uint4* __restrict__ src, const int64_t* __restrict__ map, int64_t nsteps,
+                               uint4* __restrict__ dst) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsteps * 32) return;
+    dst[i] = src[__ldg(map + (i >> 5)) * 32 + (i & 31)];
+}
+
+// Per item and lane the record phase 1 needs: the molecule's position in
+// its window (-1 for a padding slot) and the column magnitude phase 2 uses
+// (as a float, or -1.0f when the pair takes the IEEE division).
+__global__ void k_sched_lanes(const int2* __restrict__ items, int64_t nitems, const int4* __restrict__ meta,
+                              int64_t per_win, int window, int2* __restrict__ lanes) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (nitems + 1) * 32) return;
+    const int64_t item = i >> 5;
+    if (item == nitems) {   // the padding record's lanes
+        lanes[i] = make_int2(-1, __float_as_int(-1.0f));
+        return;
+    }
+    const int64_t chunk = items[item].x;
+    const int4 m = meta[chunk * 32 + (i & 31)];
+    const int64_t wbase = chunk / per_win * window;
+    lanes[i] = make_int2(m.x >= 0 ? (int)(m.x - wbase) : -1,
+                         __float_as_int(m.x >= 0 && fast_mag(m.y, m.z) ? (float)m.y : -1.0f));
+}
+
+struct SchedItem {
+    int64_t chunk;
+    int s0, ns;
+    bool split;
+};
+
+}  // namespace
+
+int64_t sched_capacity(siml_engine* h) {
+    // table words beside the staging, the column magnitudes, the rare-vid hash
+    // and the row data, with a margin for static shared memory
+    const int64_t extra = (int64_t)kSchedExtraSmem + (int64_t)kRareSlots * 8 + (int64_t)sizeof(RowSmem) + 2048;
+    const int64_t words = ((int64_t)h->smem_optin - extra) / 4;
+    const int64_t cap = std::max<int64_t>(0, words / 4 * 4 - 4);
+    // an unsplit vocabulary keeps slot order, which makes no useful split:
+    // the kernel takes it whole or not at all
+    if (!h->vocab.split) {
+        const int64_t vt = (h->vocab.nvid + 1 + 3) / 4 * 4;
+        const bool whole = (size_t)vt * 4 + kSchedExtraSmem + sizeof(RowSmem) + 2048 <= h->smem_optin;
+        return whole ? h->vocab.nvid : 0;
+    }
+    return cap;
+}
+
+bool rows_sched_fits(siml_engine* h) {
+    const int np = planes_needed(std::min(h->ref.max_entries, h->qry.max_entries));
+    if (np > 8) return false;   // staged counts are bytes
+    const int64_t nc = std::min<int64_t>(h->vocab.ncommon, sched_capacity(h));
+    if (nc <= 0) return false;
+    if (nc < h->vocab.nvid && nc < 1024) return false;   // a split that leaves too little in the table
+    return true;
+}
+
+void free_sched(DbLayout& d) {
+    if (d.sched_items) cudaFree(d.sched_items);
+    if (d.sched_wrun) cudaFree(d.sched_wrun);
+    if (d.sched_grun) cudaFree(d.sched_grun);
+    if (d.sched_lanes) cudaFree(d.sched_lanes);
+    d.sched_lanes = nullptr;
+    d.sched_items = nullptr;
+    d.sched_wrun = nullptr;
+    d.sched_grun = nullptr;
+}
+
+namespace {
+
+// Wrap-around fill of one window's chunks (steps L[0..n), ascending; the
+// longest first) into P warps of capacity M, an item costing its steps plus
+// kItemCost: a chunk goes whole into the current warp while it fits, else
+// the warp is filled to M and the rest continues in the next warp.  Returns
+// false when P warps do not suffice.
+bool fill_window(const int32_t* L, int n, int P, double M, std::vector<SchedItem>* pw, int64_t c0) {
+    for (int w = 0; w < P; w++) pw[w].clear();
+    std::vector<double> load((size_t)P, 0.0);
+    int w = 0;
+    for (int c = n - 1; c >= 0; c--) {
+        int rem = L[c], s0 = 0;
+        if (rem == 0) {   // molecules with no streamed entries: counts 0, column data still written
+            if (load[(size_t)w] + kItemCost > M && w < P - 1) w++;
+            load[(size_t)w] += kItemCost;
+            pw[w].push_back({c0 + c, 0, 0, false});
+            continue;
+        }
+        while (rem > 0) {
+            const int cap = (int)std::floor(M - load[(size_t)w] - kItemCost);
+            if (cap <= 0) {
+                if (w == P - 1) return false;
+                w++;
+                continue;
+            }
+            const int take = rem <= cap ? rem : cap;
+            pw[w].push_back({c0 + c, s0, take, false});
+            load[(size_t)w] += take + kItemCost;
+            s0 += take;
+            rem -= take;
+            if (load[(size_t)w] >= M - 0.5 && rem > 0) {
+                if (w == P - 1) return false;
+                w++;
+            }
+        }
+    }
+    return true;
+}
+
+}  // namespace
+
+// Builds the per-(window, warp) schedule of a freshly built window-sorted
+// layout (windows of d.window, 2-byte entries, chunk c's step s of lane l at
+// group off[c] + 32 s + l) for groups of P warps, and permutes its entries
+// into schedule order.
+int sched_arrange(siml_engine* h, DbLayout& d) {
+    cudaStream_t st = h->stream;
+    const int P = d.sched_warps;
+    if (d.entry_bytes != 2 || P < 1 || P > kSWarpsAll || d.window != (kSColsAll * P) / kSWarpsAll)
+        return fail(SIML_ERR_UNSUPPORTED, "scheduled layout: bad base layout");
+    const int64_t nch = d.nchunks;
+    std::vector<int32_t> ng((size_t)std::max<int64_t>(nch, 1));
+    std::vector<int64_t> off((size_t)nch + 1);
+    if (nch > 0) {
+        SIML_CUDA(cudaMemcpyAsync(ng.data(), d.ng, (size_t)nch * 4, cudaMemcpyDeviceToHost, st));
+        SIML_CUDA(cudaMemcpyAsync(off.data(), d.off, (size_t)(nch + 1) * 8, cudaMemcpyDeviceToHost, st));
+        SIML_CUDA(cudaStreamSynchronize(st));
+    }
+    const int64_t per_win = d.window / kChunk;
+    const int64_t nwin = (d.n + d.window - 1) / d.window;
+    const int G = kSWarpsAll / P;
+    // each (window, warp) run is scheduled first, then the runs are stored in
+    // stream order: a warp of group g takes windows g, g + G, g + 2G, ...,
+    // so its runs of consecutive such windows are stored back to back
+    std::vector<std::vector<SchedItem>> runs((size_t)nwin * P);
+    std::vector<std::vector<SchedItem>> pw((size_t)P);
+    int64_t max_steps = 0;
+    for (int64_t wnd = 0; wnd < nwin; wnd++) {
+        const int64_t c0 = wnd * per_win, c1 = std::min<int64_t>(nch, c0 + per_win);
+        int n = 0;   // chunks with molecules (padding slots sort last)
+        double cost = 0.0;
+        int32_t longest = 0;
+        for (int64_t c = c0; c < c1 && c * kChunk < d.n; c++, n++) {
+            cost += ng[(size_t)c] + kItemCost;
+            longest = std::max(longest, ng[(size_t)c]);
+        }
+        // the smallest share that the fill fits into P warps (bisection)
+        double lo = std::max(1.0, cost / P), hi = 2.0 * cost / P + longest + 4.0 * kItemCost + 1.0;
+        while (!fill_window(ng.data() + c0, n, P, hi, pw.data(), c0)) hi *= 2.0;
+        for (int iter = 0; iter < 24 && hi - lo > 0.25; iter++) {
+            const double mid = 0.5 * (lo + hi);
+            if (fill_window(ng.data() + c0, n, P, mid, pw.data(), c0)) hi = mid;
+            else lo = mid;
+        }
+        fill_window(ng.data() + c0, n, P, hi, pw.data(), c0);
+        // chunks with more than one item add their counts atomically
+        std::vector<int> parts((size_t)per_win, 0);
+        for (auto& v : pw)
+            for (auto& x : v) parts[(size_t)(x.chunk - c0)]++;
+        for (int ww = 0; ww < P; ww++) {
+            auto& r = runs[(size_t)(wnd * P + ww)];
+            r = pw[(size_t)ww];
+            for (auto& x : r) {
+                x.split = parts[(size_t)(x.chunk - c0)] > 1;
+                max_steps = std::max<int64_t>(max_steps, x.ns);
+            }
+        }
+    }
+    std::vector<int2> items;
+    items.reserve((size_t)nch * 2 + 64);
+    std::vector<int2> wrun((size_t)std::max<int64_t>(nwin * P, 1));
+    std::vector<int64_t> grun((size_t)std::max<int64_t>(nwin * P, 1) * 2);
+    std::vector<int64_t> map;
+    map.reserve((size_t)(d.ngroups_total / 32) + 1);
+    int64_t gpos = 0;
+    for (int g = 0; g < G; g++)
+        for (int ww = 0; ww < P; ww++)
+            for (int64_t wnd = g; wnd < nwin; wnd += G) {
+                const size_t sl = (size_t)(wnd * P + ww);
+                wrun[sl].x = (int)items.size();
+                grun[2 * sl] = gpos;
+                for (auto& x : runs[sl]) {
+                    int flags = x.ns;
+                    if (x.split) flags |= kItemSplit;
+                    if (x.s0 == 0) flags |= kItemFirst;
+                    items.push_back(make_int2((int)x.chunk, flags));
+                    for (int s2 = 0; s2 < x.ns; s2++) map.push_back(off[(size_t)x.chunk] / 32 + x.s0 + s2);
+                    gpos += (int64_t)x.ns * 32;
+                }
+                wrun[sl].y = (int)items.size();
+                grun[2 * sl + 1] = gpos;
+            }
+    items.push_back(make_int2(0, 0));   // padding record: the stream reads one record ahead
+    if (gpos != d.ngroups_total) return fail(SIML_ERR_CUDA, "scheduled layout: %lld groups scheduled of %lld",
+                                             (long long)gpos, (long long)d.ngroups_total);
+    if (items.size() > 0x7FFFFFFFu) return fail(SIML_ERR_UNSUPPORTED, "scheduled layout: too many items");
+    int rc;
+    void* p = nullptr;
+    if ((rc = dev_alloc_bytes(&p, items.size() * sizeof(int2)))) return rc;
+    d.sched_items = (int2*)p;
+    if ((rc = dev_alloc_bytes(&p, wrun.size() * sizeof(int2)))) return rc;
+    d.sched_wrun = (int2*)p;
+    if ((rc = dev_alloc_bytes(&p, grun.size() * sizeof(int64_t)))) return rc;
+    d.sched_grun = (int64_t*)p;
+    SIML_CUDA(cudaMemcpyAsync(d.sched_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    if ((rc = dev_alloc_bytes(&p, items.size() * 32 * sizeof(int2)))) return rc;
+    d.sched_lanes = (int2*)p;
+    {
+        const int64_t n = (int64_t)items.size() * 32;
+        k_sched_lanes<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d.sched_items, (int64_t)items.size() - 1, d.meta,
+                                                                   per_win, d.window, d.sched_lanes);
+        h->launches++;
+        SIML_CUDA(cudaGetLastError());
+    }
+    SIML_CUDA(cudaMemcpyAsync(d.sched_wrun, wrun.data(), wrun.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    SIML_CUDA(cudaMemcpyAsync(d.sched_grun, grun.data(), grun.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    d.nitems = (int64_t)items.size() - 1;
+    d.nwin = nwin;
+    d.max_item_steps = max_steps;
+    // entries in schedule order, with kPadSteps steps of zeros after them
+    // (the stream loads run two steps ahead without bounds tests)
+    const int64_t nsteps = (int64_t)map.size();
+    void* dmap = nullptr;
+    void* dst = nullptr;
+    const size_t dst_bytes = (size_t)(nsteps + kPadSteps) * 32 * 16;
+    if ((rc = dev_alloc_bytes(&dst, dst_bytes))) return rc;
+    cudaError_t e = cudaMemsetAsync((char*)dst + (size_t)nsteps * 512, 0, (size_t)kPadSteps * 512, st);
+    if (e == cudaSuccess && nsteps > 0) {
+        if ((rc = dev_alloc_bytes(&dmap, (size_t)nsteps * 8))) {
+            cudaFree(dst);
+            return rc;
+        }
+        e = cudaMemcpyAsync(dmap, map.data(), (size_t)nsteps * 8, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+            const int64_t n = nsteps * 32;
+            k_sched_gather<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const uint4*)d.entries, (const int64_t*)dmap,
+                                                                       nsteps, (uint4*)dst);
+            h->launches++;
+            e = cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (dmap) cudaFree(dmap);
+    if (e != cudaSuccess) {
+        cudaFree(dst);
+        return cuda_fail(e, "scheduled layout: entry permutation");
+    }
+    cudaFree(d.entries);
+    d.entries = dst;
+    return SIML_OK;
+}
+
+int launch_rows_sched(siml_engine* h, const RowsArgs& a, bool* done) {
+    *done = false;
+    if (a.mode != kModeRows || !rows_use_sched(h)) return SIML_OK;
+    if (((uintptr_t)a.out & 15u) || (a.ldo & 3)) return SIML_OK;   // 16-byte row stores
+    const DbLayout* d = nullptr;
+    int rc = ensure_sched_layout(h, &d);
+    if (rc) return rc;
+    const int64_t rows = a.rowlimit - a.rowbase;
+    GroupParams p;
+    size_t smem = 0;
+    int np = 0;
+    if (!table_params(h, d, a.rowbase, rows, kModeRows, p, smem, np) || np != 8 || d->entry_bytes != 2) return SIML_OK;
+    const size_t sm = smem + kSchedExtraSmem;
+    if (sm + sizeof(RowSmem) + 256 > h->smem_optin) return SIML_OK;
+    void (*kern)(const GroupParams, const SchedArgs) = nullptr;
+    switch (kSWarpsAll / d->sched_warps) {
+        case 2: kern = p.rare_slots ? k_rows_sched<true, 2> : k_rows_sched<false, 2>; break;
+        case 4: kern = p.rare_slots ? k_rows_sched<true, 4> : k_rows_sched<false, 4>; break;
+        default: return SIML_OK;
+    }
+    if ((rc = set_smem(kern, sm))) return rc;
+    SchedArgs sa;
+    sa.items = d->sched_items;
+    sa.lanes = d->sched_lanes;
+    sa.wrun = d->sched_wrun;
+    sa.grun = d->sched_grun;
+    sa.qmag = h->qry.mag;
+    sa.nq = h->qry.n;
+    sa.nwin = d->nwin;
+    sa.out = a.out;
+    sa.ldo = a.ldo;
+    const int64_t groups = (rows + 31) / 32;
+    // windows per CTA: groups x splits fills whole waves of one CTA per SM
+    int splits = 1;
+    double best = 1e300;
+    for (int64_t s = 1; s <= std::max<int64_t>(1, std::min<int64_t>(d->nwin, 1024)); s++) {
+        const int64_t waves = (groups * s + h->num_sms - 1) / h->num_sms;
+        const double cost = (double)waves * (1.0 / (double)s + 0.004);
+        if (cost < best * 0.999) {
+            best = cost;
+            splits = (int)s;
+        }
+    }
+    dim3 grid((unsigned)groups, (unsigned)splits);
+    SIML_CUDA(mark(h, h->ev0));
+    kern<<<grid, kSThreads, sm, h->stream>>>(p, sa);
+    SIML_CUDA(cudaGetLastError());
+    SIML_CUDA(mark(h, h->ev1));
+    h->timed = true;
+    h->launches++;
+    *done = true;
+    return SIML_OK;
+}
+
+}  // namespace siml

@@ -12,6 +12,13 @@
 //   SIML_SYNTH_LOGNORMAL_45    lognormal, median 45, sigma 0.5, clipped [10, 200]
 //   SIML_SYNTH_BIMODAL_35_110  70% lognormal median 35 (sigma 0.35),
 //                              30% lognormal median 110 (sigma 0.3), clipped [10, 250]
+//   SIML_SYNTH_CHEM_45         lengths as SIML_SYNTH_LOGNORMAL_45, and real-chemistry
+//                              tokens: 12% of atoms are bracket atoms (charges,
+//                              explicit hydrogens, stereo centres, isotopes, metals),
+//                              '/' and '\\' bonds, and a fifth of ring closures written as
+//                              two-digit %nn labels.  These are the bytes that carry
+//                              state through the reference's preprocessor (digits after
+//                              '+', '-', 'H', '[' are kept; "%nn" becomes "%0").
 #include <cstdint>
 #include <cstring>
 #include <thread>
@@ -78,7 +85,8 @@ int32_t lognormal_len(Rng& r, double median, double sigma, int32_t lo, int32_t h
 int32_t draw_length(Rng& r, int dist) {
     switch (dist) {
         case SIML_SYNTH_UNIFORM_20_90: return 20 + (int32_t)r.below(71);
-        case SIML_SYNTH_LOGNORMAL_45: return lognormal_len(r, 45.0, 0.5, 10, 200);
+        case SIML_SYNTH_LOGNORMAL_45:
+        case SIML_SYNTH_CHEM_45: return lognormal_len(r, 45.0, 0.5, 10, 200);
         case SIML_SYNTH_BIMODAL_35_110:
             if (r.below(100) < 70) return lognormal_len(r, 35.0, 0.35, 10, 250);
             return lognormal_len(r, 110.0, 0.3, 10, 250);
@@ -95,23 +103,40 @@ const Tok kTokens[] = {
 };
 constexpr int kNumTokens = sizeof(kTokens) / sizeof(kTokens[0]);
 
-// Writes one molecule into out (capacity >= target + 16); returns its length.
-int32_t gen_one(Rng& r, int32_t target, char* out) {
+// bracket atoms of the chemistry-like model
+const char* const kBracket[] = {"[NH+]", "[NH2+]", "[NH3+]", "[O-]", "[N+]", "[nH]", "[C@@H]", "[C@H]",
+                                "[S@@]", "[Na+]", "[Cl-]", "[N-]", "[13CH3]", "[2H]", "[Fe+2]", "[Si]",
+                                "[Se]", "[B-]", "[P+]", "[Co+3]"};
+constexpr int kNumBracket = sizeof(kBracket) / sizeof(kBracket[0]);
+
+// Writes one molecule into out (capacity >= target + 24); returns its length.
+int32_t gen_one(Rng& r, int32_t target, char* out, bool chem) {
     int32_t len = 0;
     int depth = 0;             // open branches
-    int open_rings[6] = {0};   // ring digit i+1 open?
+    int open_rings[6] = {0};   // ring i open: 1 written as digit i+1, 2 as "%1" + digit i
     int nopen_rings = 0;
     bool last_atom = false;
     auto put = [&](const char* s) { while (*s) out[len++] = *s++; };
     auto atom = [&]() {
-        // atoms only, same relative weights
-        uint32_t u = r.below(780);  // sum of the atom weights
-        int acc = 0;
-        for (int t = 0; t < 10; t++) {
-            acc += kTokens[t].w;
-            if ((int)u < acc) { put(kTokens[t].s); break; }
+        if (chem && r.below(100) < 12) {
+            put(kBracket[r.below(kNumBracket)]);
+        } else {
+            // atoms only, same relative weights
+            uint32_t u = r.below(780);  // sum of the atom weights
+            int acc = 0;
+            for (int t = 0; t < 10; t++) {
+                acc += kTokens[t].w;
+                if ((int)u < acc) { put(kTokens[t].s); break; }
+            }
         }
         last_atom = true;
+    };
+    auto ring_label = [&](int k, int kind) {
+        if (kind == 2) {
+            out[len++] = '%';
+            out[len++] = '1';
+        }
+        out[len++] = (char)((kind == 2 ? '0' : '1') + k);
     };
     atom();
     while (len + depth + nopen_rings < target) {
@@ -120,7 +145,7 @@ int32_t gen_one(Rng& r, int32_t target, char* out) {
         if (last_atom && nopen_rings > 0 && r.below(100) < 25) {
             int k = (int)r.below(6);
             while (!open_rings[k]) k = (k + 1) % 6;
-            out[len++] = (char)('1' + k);
+            ring_label(k, open_rings[k]);
             open_rings[k] = 0;
             nopen_rings--;
             continue;
@@ -134,21 +159,28 @@ int32_t gen_one(Rng& r, int32_t target, char* out) {
         const Tok& tk = kTokens[t];
         switch (tk.kind) {
             case 0: put(tk.s); last_atom = true; break;
-            case 1: if (last_atom) { put(tk.s); atom(); } break;
+            case 1:
+                if (last_atom) {
+                    if (chem && r.below(100) < 20) put(r.below(2) ? "/" : "\\");
+                    else put(tk.s);
+                    atom();
+                }
+                break;
             case 2: if (last_atom && depth < 4) { put("("); depth++; atom(); } break;
             case 3:
                 if (last_atom && nopen_rings < 6) {
                     int k = (int)r.below(6);
                     while (open_rings[k]) k = (k + 1) % 6;
-                    out[len++] = (char)('1' + k);
-                    open_rings[k] = 1;
+                    const int kind = chem && r.below(100) < 20 ? 2 : 1;
+                    ring_label(k, kind);
+                    open_rings[k] = kind;
                     nopen_rings++;
                 }
                 break;
         }
     }
     for (int k = 0; k < 6; k++)
-        if (open_rings[k]) { out[len++] = (char)('1' + k); }
+        if (open_rings[k]) ring_label(k, open_rings[k]);
     while (depth-- > 0) put(")");
     return len;
 }
@@ -161,13 +193,13 @@ extern "C" {
 // this first to size the buffer for siml_synth_smiles.
 int siml_synth_lengths(uint64_t seed, int dist, int64_t first, int64_t n, int32_t* lens) {
     if (n < 0 || !lens || first < 0) return siml::fail(SIML_ERR_INVALID, "siml_synth_lengths: bad arguments");
-    if (dist < SIML_SYNTH_UNIFORM_20_90 || dist > SIML_SYNTH_BIMODAL_35_110)
+    if (dist < SIML_SYNTH_UNIFORM_20_90 || dist > SIML_SYNTH_CHEM_45)
         return siml::fail(SIML_ERR_INVALID, "siml_synth_lengths: unknown length model");
     siml::parallel_for(n, [&](int64_t i) {
         Rng r(seed, (uint64_t)(first + i));
-        char tmp[600];
+        char tmp[640];
         int32_t target = draw_length(r, dist);
-        lens[i] = gen_one(r, target, tmp);
+        lens[i] = gen_one(r, target, tmp, dist == SIML_SYNTH_CHEM_45);
     });
     return SIML_OK;
 }
@@ -177,7 +209,7 @@ int siml_synth_lengths(uint64_t seed, int dist, int64_t first, int64_t n, int32_
 int siml_synth_smiles(uint64_t seed, int dist, int64_t first, int64_t n,
                       char* buf, int64_t bufcap, int64_t* offsets) {
     if (n < 0 || !buf || !offsets || first < 0) return siml::fail(SIML_ERR_INVALID, "siml_synth_smiles: bad arguments");
-    if (dist < SIML_SYNTH_UNIFORM_20_90 || dist > SIML_SYNTH_BIMODAL_35_110)
+    if (dist < SIML_SYNTH_UNIFORM_20_90 || dist > SIML_SYNTH_CHEM_45)
         return siml::fail(SIML_ERR_INVALID, "siml_synth_smiles: unknown length model");
     std::vector<int32_t> lens((size_t)n);
     int rc = siml_synth_lengths(seed, dist, first, n, lens.data());
@@ -187,9 +219,9 @@ int siml_synth_smiles(uint64_t seed, int dist, int64_t first, int64_t n,
     if (offsets[n] > bufcap) return siml::fail(SIML_ERR_INVALID, "siml_synth_smiles: buffer too small");
     siml::parallel_for(n, [&](int64_t i) {
         Rng r(seed, (uint64_t)(first + i));
-        char tmp[600];
+        char tmp[640];
         int32_t target = draw_length(r, dist);
-        int32_t L = gen_one(r, target, tmp);
+        int32_t L = gen_one(r, target, tmp, dist == SIML_SYNTH_CHEM_45);
         std::memcpy(buf + offsets[i], tmp, (size_t)L);
     });
     return SIML_OK;

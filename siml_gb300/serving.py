@@ -9,9 +9,14 @@ pysiml/kernels.py:393-475).  The reference answers one call at a time
 into the next batch while earlier batches run:
 
 * admission: a request joins the forming batch while the batch's query rows
-  fit one slot region of the ref buffer and its hit buffers fit the region's
-  device memory budget (FIFO: the first request that does not fit waits for
-  the next batch);
+  fit one slot region of the ref buffer and its hit buffers fit the device
+  memory that is free right now (cudaMemGetInfo plus what torch's cache holds
+  unused, less a reserve, capped by the configured budget).  FIFO: the first
+  request that does not fit waits for the next batch, and when not even the
+  oldest request fits the free memory (another tenant holds it) the batch is
+  deferred, not failed, until memory frees up;
+* hit buffers are allocated per batch on the engine's stream and released
+  once the batch's results are handed out;
 * two slot regions alternate, so the next batch is compiled, written and
   queued on the stream while the previous one computes and its results come
   back; a region is reused only after its results have been handed out;
@@ -99,7 +104,9 @@ def compile_into(smiles, L, C, ln, mg, width):
 
 
 class _Region:
-    """One slot region: ref rows [base, base + max_rows) and its buffers."""
+    """One slot region: ref rows [base, base + max_rows), its pinned host
+    staging and result buffers, and the device hit buffers of the batch it
+    holds (allocated when the batch is admitted)."""
 
     def __init__(self, base, cfg, dev):
         self.base = base
@@ -107,11 +114,7 @@ class _Region:
         R, W = cfg.max_rows, cfg.width
         self.hL, self.hC = pin((R, W), torch.int32), pin((R, W), torch.int32)
         self.hlen, self.hmag = pin((R,), torch.int32), pin((R,), torch.int32)
-        self.k_idx = torch.empty((R, cfg.kmax), dtype=torch.int32, device=dev)
-        self.k_sims = torch.empty((R, cfg.kmax), dtype=torch.float32, device=dev)
-        self.n_idx = torch.empty((R, cfg.pitch), dtype=torch.int32, device=dev)
-        self.n_sims = torch.empty((R, cfg.pitch), dtype=torch.float32, device=dev)
-        self.n_cnt = torch.empty((R,), dtype=torch.int32, device=dev)
+        self.k_idx = self.k_sims = self.n_idx = self.n_sims = self.n_cnt = None
         self.o_kidx, self.o_ksims = pin((R, cfg.kmax), torch.int32), pin((R, cfg.kmax), torch.float32)
         self.o_nidx, self.o_nsims = pin((R, cfg.pitch), torch.int32), pin((R, cfg.pitch), torch.float32)
         self.o_ncnt = pin((R,), torch.int32)
@@ -126,10 +129,13 @@ class ServerConfig:
     throughput; width: LINGO columns per query row; kmax: largest k a top-k
     request may ask; pitch: hits per row a threshold batch keeps before an
     overflowing row is re-run alone; hit_budget: device bytes of hit buffers
-    one batch may claim."""
+    one batch may claim; mem_reserve: device bytes left free for others when
+    admitting; mem_probe: callable returning the device bytes free for hit
+    buffers (default: cudaMemGetInfo plus torch's unused cache); mem_poll_s:
+    how often a deferred batch probes the memory again."""
 
     def __init__(self, max_rows=1024, width=256, kmax=64, pitch=256, hit_budget=None, lo=0.75, soft_rows=None,
-                 backlog_rows=None):
+                 backlog_rows=None, mem_reserve=256 << 20, mem_probe=None, mem_poll_s=0.002):
         self.max_rows = int(max_rows)
         self.soft_rows = int(soft_rows) if soft_rows else self.max_rows
         self.backlog_rows = int(backlog_rows) if backlog_rows else 8 * self.max_rows
@@ -137,11 +143,36 @@ class ServerConfig:
         self.kmax = int(kmax)
         self.pitch = int(pitch)
         self.lo = float(lo)
-        self.hit_budget = int(hit_budget) if hit_budget else self.max_rows * max(self.pitch, self.kmax) * 8
+        self.hit_budget = int(hit_budget) if hit_budget else self.max_rows * max(self.pitch * 8 + 4, self.kmax * 8)
+        self.mem_reserve = int(mem_reserve)
+        self.mem_probe = mem_probe
+        self.mem_poll_s = float(mem_poll_s)
 
 
 def _hit_bytes(req, cfg):
-    return req.rows * (cfg.pitch * 8 + 4 if req.kind == THRESHOLD else req.k * 8)
+    """Device bytes of a request's hit buffers: index, similarity (and count)
+    per threshold row at the batch pitch; the top-k lists at the batch's k,
+    bounded by kmax."""
+    return req.rows * (cfg.pitch * 8 + 4 if req.kind == THRESHOLD else cfg.kmax * 8)
+
+
+def admit(queue, cfg, avail_bytes, row_limit):
+    """The requests at the head of `queue` (oldest first) that form the next
+    batch: they are taken while their query rows fit row_limit and their hit
+    buffers fit min(cfg.hit_budget, avail_bytes).  An empty list means the
+    oldest request does not fit the free memory and the batch waits."""
+    budget = min(cfg.hit_budget, avail_bytes)
+    batch, rows, hits = [], 0, 0
+    for r in queue:
+        need = _hit_bytes(r, cfg)
+        if hits + need > budget:
+            break
+        if batch and rows + r.rows > row_limit:
+            break
+        batch.append(r)
+        rows += r.rows
+        hits += need
+    return batch
 
 
 class LingoServer:
@@ -168,6 +199,7 @@ class LingoServer:
         self.batcher_done = False
         self.elock = threading.Lock()   # one host thread at a time on the engine handle
         self.batches = 0
+        self.deferrals = 0      # batch formations put off for lack of free device memory
         self.pairs = 0
         self.batch_rows = []
         self.gpu_ms = 0.0       # device time of the batches (write, search, copy back)
@@ -202,6 +234,8 @@ class LingoServer:
     def submit(self, req):
         if req.rows > self.cfg.max_rows:
             raise ValueError("request of %d queries exceeds the batch size %d" % (req.rows, self.cfg.max_rows))
+        if _hit_bytes(req, self.cfg) > self.cfg.hit_budget:
+            raise ValueError("request of %d queries needs more hit memory than the batch budget" % req.rows)
         if req.kind == TOPK and not 1 <= req.k <= self.cfg.kmax:
             raise ValueError("k must be in [1, %d]" % self.cfg.kmax)
         if req.kind == THRESHOLD and req.lo != self.cfg.lo:
@@ -239,26 +273,37 @@ class LingoServer:
             req.compiled = arrays
 
     # ------------------------------------------------------------- batcher
+    def free_device_bytes(self):
+        """Device bytes hit buffers may take now: the probe's reading (by
+        default cudaMemGetInfo's free bytes plus what torch's cache holds
+        unused) less the reserve."""
+        cfg = self.cfg
+        if cfg.mem_probe is not None:
+            free = int(cfg.mem_probe())
+        else:
+            free, _ = self.gl.memInfo()
+            free += torch.cuda.memory_reserved(self.dev) - torch.cuda.memory_allocated(self.dev)
+        return free - cfg.mem_reserve
+
     def _take_batch(self):
         cfg = self.cfg
         with self.cv:
-            while not self.queue and not self.stop_flag:
-                self.cv.wait()
-            if self.stop_flag and not self.queue:
-                return None
-            batch, rows, hits = [], 0, 0
-            queued = sum(r.rows for r in self.queue)
-            limit = cfg.max_rows if queued > cfg.backlog_rows else cfg.soft_rows
-            while self.queue:
-                r = self.queue[0]
-                need = _hit_bytes(r, cfg)
-                if batch and (rows + r.rows > limit or hits + need > cfg.hit_budget):
-                    break
-                self.queue.popleft()
-                batch.append(r)
-                rows += r.rows
-                hits += need
-            return batch
+            while True:
+                while not self.queue and not self.stop_flag:
+                    self.cv.wait()
+                if self.stop_flag and not self.queue:
+                    return None
+                queued = sum(r.rows for r in self.queue)
+                limit = cfg.max_rows if queued > cfg.backlog_rows else cfg.soft_rows
+                batch = admit(self.queue, cfg, self.free_device_bytes(), limit)
+                if batch:
+                    for _ in batch:
+                        self.queue.popleft()
+                    return batch
+                # the oldest request's hit buffers do not fit the free device
+                # memory: the batch waits for memory, the requests stay queued
+                self.deferrals += 1
+                self.cv.wait(timeout=cfg.mem_poll_s)
 
     def _batcher(self):
         seq = 0
@@ -307,6 +352,16 @@ class LingoServer:
             r.compiled = None
             row += r.rows
         with self.elock:
+            # the batch's hit buffers, on the engine's stream (released after
+            # delivery); admitted against the free memory just read
+            with torch.cuda.stream(gl.stream):
+                if nt:
+                    region.n_idx = torch.empty((nt, cfg.pitch), dtype=torch.int32, device=self.dev)
+                    region.n_sims = torch.empty((nt, cfg.pitch), dtype=torch.float32, device=self.dev)
+                    region.n_cnt = torch.empty((nt,), dtype=torch.int32, device=self.dev)
+                if nk:
+                    region.k_idx = torch.empty((nk, kmax), dtype=torch.int32, device=self.dev)
+                    region.k_sims = torch.empty((nk, kmax), dtype=torch.float32, device=self.dev)
             return self._queue(batch, thr, tk, nt, nk, kmax, region)
 
     def _queue(self, batch, thr, tk, nt, nk, kmax, region):
@@ -326,9 +381,7 @@ class LingoServer:
                                        region.n_idx.data_ptr(), region.n_sims.data_ptr(), region.n_cnt.data_ptr(),
                                        N.SIML_DEVICE), "siml_neighbors")
         if nk:
-            kidx = region.k_idx.view(-1)[:cfg.max_rows * kmax].view(cfg.max_rows, kmax)
-            ksims = region.k_sims.view(-1)[:cfg.max_rows * kmax].view(cfg.max_rows, kmax)
-            N.check(lib.siml_topk(gl._h, b + nt, b + nt + nk, kmax, kidx.data_ptr(), ksims.data_ptr(),
+            N.check(lib.siml_topk(gl._h, b + nt, b + nt + nk, kmax, region.k_idx.data_ptr(), region.k_sims.data_ptr(),
                                   N.SIML_DEVICE), "siml_topk")
         with torch.cuda.stream(st):
             if nt:
@@ -337,8 +390,8 @@ class LingoServer:
                 region.o_nsims[:nt].copy_(region.n_sims[:nt], non_blocking=True)
             if nk:
                 m = nk * kmax
-                region.o_kidx.view(-1)[:m].copy_(region.k_idx.view(-1)[:m], non_blocking=True)
-                region.o_ksims.view(-1)[:m].copy_(region.k_sims.view(-1)[:m], non_blocking=True)
+                region.o_kidx.view(-1)[:m].copy_(region.k_idx.view(-1), non_blocking=True)
+                region.o_ksims.view(-1)[:m].copy_(region.k_sims.view(-1), non_blocking=True)
             ev = torch.cuda.Event(enable_timing=True)
             ev.record(st)
         self.batches += 1
@@ -368,6 +421,7 @@ class LingoServer:
                 for r in batch:
                     r.error = e
             t = time.perf_counter()
+            region.k_idx = region.k_sims = region.n_idx = region.n_sims = region.n_cnt = None
             region.free.set()
             for r in batch:
                 r.t_done = t
@@ -426,6 +480,7 @@ def serve_unbatched(server, req):
     ev.synchronize()
     N.check(N.lib().siml_async_status(server.gl._h), "siml_async_status")
     server._deliver(thr, tk, nt, nk, kmax, region)
+    region.k_idx = region.k_sims = region.n_idx = region.n_sims = region.n_cnt = None
     req.t_done = time.perf_counter()
     req.done.set()
     return req

@@ -13,6 +13,7 @@ from .compiler import compile_buffer
 UNIFORM_20_90 = N.SYNTH_UNIFORM_20_90
 LOGNORMAL_45 = N.SYNTH_LOGNORMAL_45
 BIMODAL_35_110 = N.SYNTH_BIMODAL_35_110
+CHEM_45 = N.SYNTH_CHEM_45           # lognormal 45 with bracket atoms, charges, %nn ring labels
 
 # Seeds of the benchmark workloads.  Query sets are later index ranges of the
 # same generator as their database.
@@ -20,6 +21,7 @@ SEED_ALLPAIRS = 20260001   # 4,096 strings, uniform 20-90 chars, both sets
 SEED_DB_1M = 20260002      # 1M database (lognormal median 45) + its query rows
 SEED_RAGGED = 20260004     # 2M bimodal database of the ragged-job workload
 SEED_SERVING = 20260005    # 10M serving database (uniform 20-90) + requests
+SEED_CHEM = 20260006       # chemistry-like 1M database (bracket atoms, charges)
 
 
 def smiles_buffer(seed: int, dist: int, n: int, first: int = 0):

@@ -95,11 +95,12 @@ def test_oracle_generator_equals_the_product_generator(native, oracle):
     arm, which loads no product code) gives the product's bytes for every
     length model, and the oracle compiler its arrays."""
     from oracle import workloads as W
-    assert (W.UNIFORM_20_90, W.LOGNORMAL_45, W.BIMODAL_35_110) == (S.UNIFORM_20_90, S.LOGNORMAL_45, S.BIMODAL_35_110)
-    assert (W.SEED_ALLPAIRS, W.SEED_DB_1M, W.SEED_RAGGED, W.SEED_SERVING) == \
-        (S.SEED_ALLPAIRS, S.SEED_DB_1M, S.SEED_RAGGED, S.SEED_SERVING)
+    assert (W.UNIFORM_20_90, W.LOGNORMAL_45, W.BIMODAL_35_110, W.CHEM_45) == \
+        (S.UNIFORM_20_90, S.LOGNORMAL_45, S.BIMODAL_35_110, S.CHEM_45)
+    assert (W.SEED_ALLPAIRS, W.SEED_DB_1M, W.SEED_RAGGED, W.SEED_SERVING, W.SEED_CHEM) == \
+        (S.SEED_ALLPAIRS, S.SEED_DB_1M, S.SEED_RAGGED, S.SEED_SERVING, S.SEED_CHEM)
     for seed, model in ((S.SEED_ALLPAIRS, S.UNIFORM_20_90), (S.SEED_DB_1M, S.LOGNORMAL_45),
-                        (S.SEED_RAGGED, S.BIMODAL_35_110)):
+                        (S.SEED_RAGGED, S.BIMODAL_35_110), (S.SEED_CHEM, S.CHEM_45)):
         a = S.smiles_buffer(seed, model, 3000, first=999_000)
         b = oracle.synth_buffer(seed, model, 3000, first=999_000)
         assert a[0] == b[0] and np.array_equal(a[1], b[1])

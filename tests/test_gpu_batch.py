@@ -156,3 +156,56 @@ def test_batch_plan_errors(native, set4096):
     gl.set_qsmiles(*S.smiles_set(S.SEED_ALLPAIRS, S.UNIFORM_20_90, 512))
     with pytest.raises(RuntimeError):   # the plan belongs to the replaced set
         plan.run(idx, sims, cnt)
+
+
+@pytest.mark.parametrize("rows_cap,merge_rows", [(16, 0), (32, 1), (16, 4), (32, 64)])
+def test_batch_shapes_bit_exact(native, oracle, set4096, rows_cap, merge_rows):
+    """Every plan shape (items of 16 or 32 rows; small jobs given to the
+    per-pair merge) gives the oracle's lists; with merge_rows 64 every job
+    of this list goes to the merge."""
+    rng = np.random.default_rng(31 + rows_cap + merge_rows)
+    gl = _engine(set4096, set4096)
+    jobs = _ragged_jobs(rng, 4096, 4096, 20) + [(0, 1, 0, 4096), (7, 9, 100, 2000), (200, 260, 0, 4096)]
+    lo, maxn = 0.06, 48
+    plan = gl.planNeighborBatch(jobs, lo, 1.1, maxn, tile_chunks=64, rows_cap=rows_cap, merge_rows=merge_rows)
+    assert (plan.rows_cap, plan.merge_rows, plan.shape_from_cache) == (rows_cap, merge_rows, False)
+    idx, sims, cnt = plan.buffers(with_sims=True)
+    plan.run(idx, sims, cnt)
+    for job, res in zip(jobs, plan.split(idx, sims, cnt)):
+        _cmp(oracle, set4096, set4096, job, res, lo, 1.1, maxn)
+
+
+def test_batch_shape_tuned_per_distribution(native, oracle):
+    """The tuner picks a shape (tile, row cap, merge cut-off) for each
+    database length distribution and job shape, keeps it, and a second plan
+    of the same kind reuses it without timing; each chosen shape gives the
+    plain per-job path's results bit for bit."""
+    import torch
+    from siml_gb300 import GPULingo, synthetic as S
+    chosen = {}
+    for name, seed, model in (("uniform 20-90", S.SEED_ALLPAIRS, S.UNIFORM_20_90),
+                              ("lognormal 45", S.SEED_DB_1M, S.LOGNORMAL_45),
+                              ("bimodal 35/110", S.SEED_RAGGED, S.BIMODAL_35_110)):
+        db = S.smiles_set(seed, model, 60_000)
+        gl = GPULingo(0)
+        gl.set_qsmiles(*db)
+        gl.set_refsmiles(*db)
+        jobs = S.ragged_jobs(seed, 60_000, 96, rows_max=512, cols_min=1000, cols_max=50_000)
+        plan = gl.planNeighborBatch(jobs, 0.5, 1.1, 64)
+        again = gl.planNeighborBatch(jobs, 0.5, 1.1, 64)
+        assert again.shape_from_cache and (again.tile_chunks, again.rows_cap, again.merge_rows) == \
+            (plan.tile_chunks, plan.rows_cap, plan.merge_rows)
+        chosen[name] = (plan.tile_chunks, plan.rows_cap, plan.merge_rows)
+        idx, sims, cnt = plan.buffers(with_sims=True)
+        plan.run(idx, sims, cnt)
+        p_idx, p_sims, p_cnt = plan.buffers(with_sims=True)
+        for rb, re, cb, ce, o in plan.jobs.tolist():
+            gl.neighborsRangeDevice(rb, re, cb, ce, 0.5, 1.1, plan.pitch, p_idx[o:o + re - rb],
+                                    p_sims[o:o + re - rb], p_cnt[o:o + re - rb])
+        torch.cuda.synchronize()
+        n = plan.rows_out
+        assert torch.equal(cnt[:n], p_cnt[:n]), name
+        listed = torch.arange(plan.pitch, device=cnt.device)[None, :] < torch.clamp(cnt[:n], max=plan.pitch)[:, None]
+        assert torch.equal(idx[:n][listed], p_idx[:n][listed]), name
+        assert torch.equal(sims[:n][listed].view(torch.int32), p_sims[:n][listed].view(torch.int32)), name
+    print("tuned shapes (tile, rows per item, merge cut-off):", chosen)

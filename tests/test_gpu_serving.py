@@ -116,3 +116,40 @@ def test_serving_admission_limits(native):
     # three 5-row requests fit a 16-row batch; the memory budget (16 rows x 8 hits) admits three too
     assert max(srv.batch_rows) <= 15
     assert all(r.error is None for r in reqs)
+
+
+def test_serving_defers_batches_while_device_memory_is_held(native, oracle):
+    """Admission by free device memory: while the free-memory reading is
+    below the oldest request's hit buffers (as when another tenant holds the
+    GPU's memory) no batch forms and no request fails; once the reading
+    rises the queued requests are served, each with the answer it gets
+    alone and the oracle's."""
+    from siml_gb300.serving import serve_unbatched, Request
+    db = _db()
+    state = {"probes": 0}
+
+    def probe():
+        state["probes"] += 1
+        # 64 bytes (below one query row's hit buffers), then plenty
+        return 64 if state["probes"] < 40 else 1 << 34
+
+    srv = _server(db, max_rows=256, width=128, kmax=16, pitch=256, lo=0.75, mem_reserve=0, mem_probe=probe,
+                  mem_poll_s=0.002)
+    rng = np.random.default_rng(11)
+    reqs = _requests(rng, 12, 6000, max_q=60)
+    for r in reqs:
+        srv.submit(r)
+    t0 = time.perf_counter()
+    srv.start()
+    for r in reqs:
+        assert r.done.wait(120), r.rid
+    srv.stop()
+    assert srv.deferrals >= 30 and state["probes"] >= 40
+    assert min(r.t_admit for r in reqs) - t0 > 0.05   # nothing admitted while memory was short
+    for r in reqs:
+        assert r.error is None, r.error
+        a = Request(r.rid, r.smiles, kind=r.kind, k=r.k, lo=r.lo)
+        serve_unbatched(srv, a)
+        assert _same(a.result, r.result), r.rid
+    for r in reqs[:3]:
+        assert _same(r.result, _oracle_answer(oracle, db, r)), r.rid

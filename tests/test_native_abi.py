@@ -32,6 +32,24 @@ def test_version_and_error_reporting(native):
         N.check(rc)
 
 
+def test_async_error_words_decode_on_the_host(native):
+    """How siml_sync reports the error bits the kernels set: bit 1 (a top-k
+    lock wait ran out) as SIML_ERR_TIMEOUT, bit 2 (a batch work item outside
+    its plan) and bit 3 (a ref-row vid the shared table cannot hold) as
+    SIML_ERR_STATE, each with its own message; the lowest bit decides."""
+    from siml_gb300 import _native as N
+    assert native.siml_debug_async_status(0) == N.SIML_OK
+    assert native.siml_debug_async_status(1) == N.SIML_ERR_TIMEOUT
+    assert "lock wait" in N.last_error()
+    assert native.siml_debug_async_status(2) == N.SIML_ERR_STATE
+    assert "work item" in N.last_error()
+    assert native.siml_debug_async_status(4) == N.SIML_ERR_STATE
+    assert "rare-vid hash" in N.last_error()
+    assert native.siml_debug_async_status(6) == N.SIML_ERR_STATE
+    assert "work item" in N.last_error()
+    assert native.siml_debug_async_status(7) == N.SIML_ERR_TIMEOUT
+
+
 def test_null_handle_is_rejected(native):
     from siml_gb300 import _native as N
     assert native.siml_sync(None) == N.SIML_ERR_INVALID

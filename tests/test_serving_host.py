@@ -6,13 +6,18 @@ import threading
 import pytest
 
 
-def _fake_server(max_rows, pitch, kmax, hit_budget):
+def _fake_server(max_rows, pitch, kmax, hit_budget, free=1 << 40):
+    """A server with no engine: the device's free memory is the reading of
+    a probe the test controls (a one-element list)."""
     from siml_gb300.serving import LingoServer, ServerConfig
     srv = object.__new__(LingoServer)
-    srv.cfg = ServerConfig(max_rows=max_rows, width=64, kmax=kmax, pitch=pitch, hit_budget=hit_budget)
+    srv.free = [free]
+    srv.cfg = ServerConfig(max_rows=max_rows, width=64, kmax=kmax, pitch=pitch, hit_budget=hit_budget,
+                           mem_reserve=0, mem_probe=lambda: srv.free[0], mem_poll_s=0.001)
     srv.queue = collections.deque()
     srv.cv = threading.Condition()
     srv.stop_flag = False
+    srv.deferrals = 0
     return srv
 
 
@@ -36,10 +41,41 @@ def test_admission_by_rows_and_memory():
     assert srv._take_batch() is None
 
 
-def test_first_request_always_admitted():
+def test_request_beyond_the_hit_budget_is_refused_at_submit():
     srv = _fake_server(max_rows=8, pitch=64, kmax=8, hit_budget=16)
-    srv.queue.append(_req(0, 8, "threshold"))
-    assert [r.rid for r in srv._take_batch()] == [0]
+    srv._compile = lambda req: None
+    with pytest.raises(ValueError, match="hit memory"):
+        srv.submit(_req(0, 8, "threshold"))
+    assert not srv.queue
+
+
+def test_admit_takes_the_oldest_requests_that_fit():
+    from siml_gb300.serving import ServerConfig, admit
+    cfg = ServerConfig(max_rows=16, width=64, kmax=8, pitch=16, hit_budget=1 << 20)
+    q = [_req(0, 4, "threshold"), _req(1, 4), _req(2, 10), _req(3, 1)]
+    need_thr = 4 * (16 * 8 + 4)
+    assert [r.rid for r in admit(q, cfg, 1 << 20, 16)] == [0, 1]          # 10 more rows would pass 16
+    assert [r.rid for r in admit(q, cfg, need_thr + 4 * 8 * 8, 64)] == [0, 1]   # memory for two requests only
+    assert admit(q, cfg, need_thr - 1, 64) == []                            # not even the oldest: wait
+
+
+def test_low_free_memory_defers_the_batch_until_memory_frees():
+    """Another tenant holds the device memory: the oldest request's hit
+    buffers do not fit, so no batch forms and nothing fails; the requests
+    stay queued and form a batch once the free-memory reading rises."""
+    srv = _fake_server(max_rows=16, pitch=16, kmax=8, hit_budget=1 << 20, free=100)
+    reqs = [_req(0, 4, "threshold"), _req(1, 3)]
+    srv.queue.extend(reqs)
+    got = []
+    th = threading.Thread(target=lambda: got.append(srv._take_batch()))
+    th.start()
+    th.join(0.2)
+    assert th.is_alive() and not got                      # deferred, still waiting
+    assert srv.deferrals > 10 and len(srv.queue) == 2
+    assert all(r.error is None and not r.done.is_set() for r in reqs)
+    srv.free[0] = 1 << 30                                  # the other tenant frees its memory
+    th.join(5)
+    assert not th.is_alive() and [r.rid for r in got[0]] == [0, 1]
 
 
 def test_percentiles():
@@ -62,7 +98,7 @@ def test_batches_grow_under_a_backlog():
     from siml_gb300.serving import ServerConfig
     srv = _fake_server(max_rows=16, pitch=16, kmax=8, hit_budget=1 << 20)
     srv.cfg = ServerConfig(max_rows=16, soft_rows=8, backlog_rows=20, width=64, kmax=8, pitch=16,
-                           hit_budget=1 << 20)
+                           hit_budget=1 << 20, mem_reserve=0, mem_probe=lambda: 1 << 40)
     for i in range(3):
         srv.queue.append(_req(i, 5))
     assert [r.rid for r in srv._take_batch()] == [0]        # 15 queued rows: soft limit 8
