@@ -29,12 +29,14 @@
 // a whole molecule being below 256).
 // Phase 2 (per window, after the group's barrier): each thread takes 4
 // consecutive columns and 4 rows per staging word and forms the reference's
-// fp32 Tanimoto, ((float)amag + bmag) - isct and isct / union, with packed
-// f32x2 arithmetic and Markstein's correction of the reciprocal estimate
-// (exact for the integer ranges fast_mag admits; other pairs take the IEEE
-// division), then writes 16 bytes per row: a warp's store covers 512
-// contiguous bytes of one row.  The staging words are zeroed as they are
-// read.
+// fp32 Tanimoto, ((float)amag + bmag) - isct and isct / union, with
+// Markstein's correction of the reciprocal estimate (exact for the integer
+// ranges fast_mag admits; other pairs take the IEEE division), then writes
+// 16 bytes per row: a warp's store covers 512 contiguous bytes of one row.
+// A full group whose pairs all admit the fast division takes a
+// straight-line path in scalar fp32 (no row or column predicates); scalar
+// code issues faster here than the packed f32x2 form, which the partial
+// path keeps.  The staging words are zeroed as they are read.
 #include <vector>
 
 #include "table_core.cuh"
@@ -49,7 +51,9 @@ constexpr double kItemCost = 2.0;     // an item's epilogue, in 8-entry steps, f
 constexpr int kItemStepsMask = 0xFFFF;
 constexpr int kItemSplit = 1 << 16;   // the chunk has several items: add counts atomically
 constexpr int kItemFirst = 1 << 17;   // the item holds the chunk's first step: column data, rare entries
-constexpr int kPadSteps = 2;          // steps of zero padding after the entries (loads run two steps ahead)
+constexpr int kPadSteps = 2;
+// Largest row stride for which 31 rows of fp32 stay within 32-bit byte offsets.
+constexpr int64_t kFullGroupLdo = (int64_t)(0xFFFFFFFFull / (31ull * 4ull));          // steps of zero padding after the entries (loads run two steps ahead)
 // staging (8 count words per column) + column magnitudes, over all groups
 constexpr size_t kSchedExtraSmem = (size_t)9 * kSColsAll * 4;
 
@@ -163,6 +167,9 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
     const uint64_t k2p23 = f2(8388608.0f, 8388608.0f);
     const int q4 = (tg % Q) * 4;   // phase 2: columns q4 .. q4 + 3
     const int kk = tg / Q;         // phase 2: staging words kk, kk + 2, kk + 4, kk + 6
+    // phase 2's straight-line path: a full 32-row group whose magnitudes all
+    // admit div_small, and rows within 32-bit byte offsets of each other
+    const bool full_fast = rs.allfast && nr == 32 && a.ldo < kFullGroupLdo;
     // A warp streams the runs of its windows (w0 + group, then every G-th)
     // as one sequence: the layout stores them back to back, so the two-step
     // register prefetch and the next item's record run straight across the
@@ -250,14 +257,49 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
                 if (!advance()) break;
             }
         }
+        // every item of the window has been flushed, so the counter is zero
+        // here; saying so frees its registers for phase 2
+        acc.clear();
         group_barrier(group, TG);
         // ---------------------------------------------------------- phase 2
         const int64_t left_cols = a.nq - wbase;
         const int ncols = left_cols < WIN ? (int)left_cols : WIN;
-        if (q4 < ncols) {
-            const float4 cf = *reinterpret_cast<const float4*>(colf + q4);
-            const bool full = q4 + 4 <= ncols;
-            const bool fast = rs.allfast && full && cf.x >= 0.0f && cf.y >= 0.0f && cf.z >= 0.0f && cf.w >= 0.0f;
+        const float4 cf = q4 < ncols ? *reinterpret_cast<const float4*>(colf + q4)
+                                     : make_float4(-1.0f, -1.0f, -1.0f, -1.0f);
+        if (full_fast && q4 + 4 <= ncols && cf.x >= 0.0f && cf.y >= 0.0f && cf.z >= 0.0f && cf.w >= 0.0f) {
+            // 32 rows, a whole quad of columns, every pair exact with
+            // div_small: straight-line code, rows addressed by 32-bit byte
+            // offsets from row kk
+            char* ob = reinterpret_cast<char*>(outg + wbase + q4 + (int64_t)kk * a.ldo);
+            const uint32_t row_bytes = (uint32_t)a.ldo * 4u;
+            const float bcol[4] = {cf.x, cf.y, cf.z, cf.w};
+#pragma unroll
+            for (int kq = 0; kq < 4; kq++) {
+                const int k = kk + 2 * kq;
+                uint32_t* wp = W + k * WIN + q4;
+                const uint4 c = *reinterpret_cast<const uint4*>(wp);
+                *reinterpret_cast<uint4*>(wp) = make_uint4(0u, 0u, 0u, 0u);
+                const float4 a4 = *reinterpret_cast<const float4*>(amq + 4 * k);
+                const float av[4] = {a4.x, a4.y, a4.z, a4.w};
+                const uint32_t cw[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const uint32_t sel = 0x7440u | (uint32_t)j;   // 0x4B0000cc: the float 2^23 + count
+                    float t[4];
+#pragma unroll
+                    for (int cc = 0; cc < 4; cc++) {
+                        const float isf = __fsub_rn(__uint_as_float(__byte_perm(cw[cc], 0x4B000000u, sel)), 8388608.0f);
+                        const float u = __fsub_rn(__fadd_rn(av[j], bcol[cc]), isf);
+                        t[cc] = div_small(isf, u);
+                    }
+                    // row k + 8 j is row kk + 2 kq + 8 j
+                    *reinterpret_cast<float4*>(ob + (uint32_t)(2 * kq + 8 * j) * row_bytes) =
+                        make_float4(t[0], t[1], t[2], t[3]);
+                }
+            }
+        } else if (q4 < ncols) {
+            const bool fast = rs.allfast && q4 + 4 <= ncols && cf.x >= 0.0f && cf.y >= 0.0f && cf.z >= 0.0f &&
+                              cf.w >= 0.0f;
             const uint64_t B01 = f2(cf.x, cf.y), B23 = f2(cf.z, cf.w);
             float* ob = outg + wbase + q4;
 #pragma unroll
@@ -273,7 +315,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
                     const int r = k + 8 * j;
                     if (r >= nr) break;
                     float* orow = ob + (int64_t)r * a.ldo;
-                    const uint32_t sel = 0x7440u | (uint32_t)j;   // 0x4B0000cc: the float 2^23 + count
+                    const uint32_t sel = 0x7440u | (uint32_t)j;
                     if (fast) {
                         const uint64_t I01 = sub2(f2(__uint_as_float(__byte_perm(c.x, 0x4B000000u, sel)),
                                                      __uint_as_float(__byte_perm(c.y, 0x4B000000u, sel))), k2p23);
