@@ -758,6 +758,11 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted, bool scheduled = fals
     d.scheduled = scheduled;
     d.window = scheduled ? kSchedColumns / h->sched_groups : (sorted ? h->sorted_window : h->rows_window);
     d.sched_warps = scheduled ? 32 / h->sched_groups : 0;
+    // k_window_sort is a bitonic sort: a window that is not a power of two
+    // would index past its shared keys
+    if (d.window < kChunk || (d.window & (d.window - 1)) || d.window > kMaxWindow)
+        return fail(SIML_ERR_UNSUPPORTED, "layout window %d is not a power of two in [%d, %d]", d.window, kChunk,
+                    kMaxWindow);
     d.offsets = !vsplit && !sorted && h->rows_entries == SIML_ENTRIES_OFFSETS;
     // the balanced kernel reads vids, not byte offsets; with a split
     // vocabulary its piece buffers leave room for fewer common vids
