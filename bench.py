@@ -19,6 +19,7 @@ restatement) on the host cores, on a bounded sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -834,6 +835,9 @@ def serving_arm(args, summary=False):
         b["host_launch_frac"] = srv.launch_s / span_all
         b["host_deliver_frac"] = srv.deliver_s / span_all
         # unbatched: the same arrivals served one request at a time, in order
+        # (the heap frozen as the server's start freezes it, so that neither
+        # path pays for full collections over the earlier runs' objects)
+        gc.freeze()
         pend = []
         t0u = time.perf_counter() + 0.2
         done_u = []

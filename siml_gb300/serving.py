@@ -31,6 +31,7 @@ from __future__ import annotations
 
 import collections
 import ctypes
+import gc
 import math
 import threading
 import time
@@ -132,10 +133,16 @@ class ServerConfig:
     one batch may claim; mem_reserve: device bytes left free for others when
     admitting; mem_probe: callable returning the device bytes free for hit
     buffers (default: cudaMemGetInfo plus torch's unused cache); mem_poll_s:
-    how often a deferred batch probes the memory again."""
+    how often a deferred batch probes the memory again; gc_freeze: at start,
+    move every object alive into the collector's permanent generation
+    (gc.freeze), so that a full collection while serving scans only objects
+    made since.  A full collection holds the interpreter lock, which the
+    batcher and completer threads need: over a process with a large heap
+    (torch and its modules, earlier results) one took 35-80 ms and every
+    request queued behind it."""
 
     def __init__(self, max_rows=1024, width=256, kmax=64, pitch=256, hit_budget=None, lo=0.75, soft_rows=None,
-                 backlog_rows=None, mem_reserve=256 << 20, mem_probe=None, mem_poll_s=0.002):
+                 backlog_rows=None, mem_reserve=256 << 20, mem_probe=None, mem_poll_s=0.002, gc_freeze=True):
         self.max_rows = int(max_rows)
         self.soft_rows = int(soft_rows) if soft_rows else self.max_rows
         self.backlog_rows = int(backlog_rows) if backlog_rows else 8 * self.max_rows
@@ -147,6 +154,7 @@ class ServerConfig:
         self.mem_reserve = int(mem_reserve)
         self.mem_probe = mem_probe
         self.mem_poll_s = float(mem_poll_s)
+        self.gc_freeze = bool(gc_freeze)
 
 
 def _hit_bytes(req, cfg):
@@ -209,6 +217,8 @@ class LingoServer:
 
     # ------------------------------------------------------------- control
     def start(self):
+        if self.cfg.gc_freeze:
+            gc.freeze()
         self.stop_flag = False
         self.batcher_done = False
         self.threads = [threading.Thread(target=self._batcher, daemon=True),

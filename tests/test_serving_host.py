@@ -121,3 +121,27 @@ def test_cancel_before_admission():
     assert reqs[2].done.is_set() and isinstance(reqs[2].error, RequestCancelled)
     assert not srv.cancel(reqs[2])                 # no longer queued
     assert [r.rid for r in srv._take_batch()] == [3]
+
+
+def test_start_freezes_the_heap_unless_told_not_to():
+    """A server moves the objects alive at start into the collector's
+    permanent generation (a full collection while serving then scans only
+    newer objects); gc_freeze=False leaves the collector alone."""
+    import gc
+    srv = _fake_server(max_rows=8, pitch=64, kmax=8, hit_budget=1 << 20)
+    srv.icv = threading.Condition()
+    srv.threads = []
+    srv._batcher = srv._completer = lambda: None
+    keep = [[i] for i in range(2000)]
+    try:
+        gc.unfreeze()
+        srv.start()
+        srv.stop()
+        assert gc.get_freeze_count() >= len(keep)
+        gc.unfreeze()
+        srv.cfg.gc_freeze = False
+        srv.start()
+        srv.stop()
+        assert gc.get_freeze_count() == 0
+    finally:
+        gc.unfreeze()
