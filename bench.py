@@ -56,11 +56,29 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
-def make_sets():
+# database models of the 1M-molecule workloads: (seed, length model,
+# description); "chem" adds bracket atoms, charges, / \ bonds and %nn ring
+# labels, whose vocabulary is larger than a shared-memory table holds
+DB_MODELS = {"lognormal": ("SEED_DB_1M", "LOGNORMAL_45", "lognormal median 45 chars"),
+             "chem": ("SEED_CHEM", "CHEM_45", "chemistry-like: lognormal median 45 chars with bracket atoms, "
+                                              "charges, / \\ bonds and %nn ring labels")}
+
+
+def workload_name(text, model):
+    """A workload description for the database model (the lognormal model
+    keeps the plain names)."""
+    if model == "lognormal":
+        return text
+    name, rest = text.split(":", 1)
+    return name + "_" + model + ":" + rest.replace(DB_MODELS["lognormal"][2], DB_MODELS[model][2])
+
+
+def make_sets(model="lognormal"):
     from siml_gb300 import synthetic as S
+    seed, length = (getattr(S, x) for x in DB_MODELS[model][:2])
     t = time.time()
-    db = S.smiles_set(S.SEED_DB_1M, S.LOGNORMAL_45, DB_N)
-    q = S.smiles_set(S.SEED_DB_1M, S.LOGNORMAL_45, QUERY_N, first=DB_N)
+    db = S.smiles_set(seed, length, DB_N)
+    q = S.smiles_set(seed, length, QUERY_N, first=DB_N)
     log("generated + compiled %d + %d molecules in %.1f s" % (DB_N, QUERY_N, time.time() - t))
     return db, q
 
@@ -153,16 +171,17 @@ def cpu_reference_rate(db, q, target_s=12.0, max_rows=1024, first_row=4):
     return rec, first_row, np.asarray(block, dtype=np.float32)
 
 
-def oracle_sets():
+def oracle_sets(model="lognormal"):
     """The rows_1m workload generated and compiled by the oracle library alone
     (its copy of the seeded generator and its restatement of the reference
     compiler, pysiml/_ccompiler.cpp:276-381): the reference arm loads no
     product code."""
     from oracle import cpulingo as O
-    from oracle.workloads import SEED_DB_1M, LOGNORMAL_45
+    from oracle import workloads as OW
+    seed, length = (getattr(OW, x) for x in DB_MODELS[model][:2])
     t = time.time()
-    db = O.synth_set(SEED_DB_1M, LOGNORMAL_45, DB_N)
-    q = O.synth_set(SEED_DB_1M, LOGNORMAL_45, QUERY_N, first=DB_N)
+    db = O.synth_set(seed, length, DB_N)
+    q = O.synth_set(seed, length, QUERY_N, first=DB_N)
     log("oracle generated + compiled %d + %d molecules in %.1f s" % (DB_N, QUERY_N, time.time() - t))
     return db, q
 
@@ -172,7 +191,7 @@ def reference_arm(args):
     if rank != 0:
         return 0
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "port"], check=True)
-    db, q = oracle_sets()
+    db, q = oracle_sets(args.db_model)
     from oracle import cpulingo as O
     ref_mod = O.reference_module("_CPULingo")
     nthreads = os.cpu_count() or 1
@@ -203,7 +222,8 @@ def reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "rows_per_step": rows, "db_molecules": DB_N,
+        "data": "synthetic", "config": {"workload": workload_name(WORKLOAD, args.db_model), "rows_per_step": rows,
+                                        "db_molecules": DB_N,
                                         "subsample": "each step computes %d of the 1,024 rows of a block against the "
                                                      "full database (about 6 s of host time), so the run ends "
                                                      "within minutes; the metric is per pair" % rows},
@@ -223,7 +243,7 @@ def gpu_arm(args):
     torch.cuda.set_device(local)
     replicas.init("nccl", torch.device("cuda", local))
     from siml_gb300 import GPULingo
-    db, q = make_sets()
+    db, q = make_sets(args.db_model)
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     gl = GPULingo(local, stream=stream)
@@ -380,12 +400,13 @@ def gpu_arm(args):
         "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded SMILES-like strings)",
-        "config": {"workload": {"rows_1m": WORKLOAD, "nbr_1m": NBR_WORKLOAD, "topk_1m": TOPK_WORKLOAD,
-                                "hist_1m": HIST_WORKLOAD}[wl], "rows_per_step": rows_step, "db_molecules": DB_N,
+        "config": {"workload": workload_name({"rows_1m": WORKLOAD, "nbr_1m": NBR_WORKLOAD, "topk_1m": TOPK_WORKLOAD,
+                                              "hist_1m": HIST_WORKLOAD}[wl], args.db_model),
+                   "rows_per_step": rows_step, "db_molecules": DB_N,
                    "query_rows": QUERY_N, "parallelism": "replicas" if world > 1 else "single",
                    "rows_window": gl.rowsWindow(), "rows_entries": gl.rowsEntries(), "rows_path": rows_info,
                    "l2": "flushed between steps by a 256 MB write; each step also writes a 4 GB block",
-                   "db_layout": stats},
+                   "db_layout": stats, "db_model": args.db_model, "vocab": gl.vocabStats()},
         "roofline": roofline,
         "compute_side": compute_side(roofline["kernel"], wl),
         "merge_work_ratio": merge_work_ratio(value / world, np.mean(q[2]), np.mean(db[2]),
@@ -1067,6 +1088,9 @@ def main():
                          "topk_1m: top-100 per row; hist_1m: 1000-bin histogram of every pair; "
                          "ragged_2m: 4,096 batched neighbour jobs vs the plain per-job path")
     ap.add_argument("--ragged-jobs", type=int, default=RAGGED_JOBS, help="jobs of the ragged_2m workload")
+    ap.add_argument("--db-model", choices=sorted(DB_MODELS), default="lognormal",
+                    help="database of the 1M workloads: lognormal (default) or chem (bracket atoms, charges, "
+                         "%%nn rings: a vocabulary larger than the shared table)")
     ap.add_argument("--serving-rates", default="200,500,1000",
                     help="serving_10m: request rates (req/s), each run for warmup + steps seconds")
     ap.add_argument("--serving-max-rows", type=int, default=1024,
@@ -1103,7 +1127,8 @@ def main():
     if line is None:   # ranks other than 0
         return 0
     rank, world, _ = dist_env()
-    if args.workload == "rows_1m" and world == 1 and not args.no_extras and not args.rows_only:
+    if args.workload == "rows_1m" and args.db_model == "lognormal" and world == 1 and not args.no_extras and \
+            not args.rows_only:
         # the metric's other two parts, on the same GPU in the same run:
         # batched ragged jobs against the plain per-job path, and the
         # serving loop's latency

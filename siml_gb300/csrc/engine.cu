@@ -691,13 +691,19 @@ int build_vocab(siml_engine* h) {
         v.ncommon = acc;
         v.split = false;
         if (!direct_table_fits(h, acc)) return split_vocab(h, split_table_capacity(h));
+        // the whole table fits the kernels with nothing beside it, but not
+        // the scheduled full-matrix kernel with its staging: number the
+        // vids by frequency (nothing is split), so that kernel can take the
+        // most frequent ones as its common set
+        if (!sched_whole_fits(h, acc)) return split_vocab(h, acc);
         return SIML_OK;
     }
     return fail(SIML_ERR_NOMEM, "vocabulary hash could not be sized");
 }
 
 // Renumbers the vocabulary by falling database frequency (ties: slot order)
-// so that vids 1..ncommon are the most frequent pairs, and marks it split.
+// so that vids 1..ncommon are the most frequent pairs, and marks it split
+// when ncommon < nvid.
 int split_vocab(siml_engine* h, int64_t ncommon) {
     Vocab& v = h->vocab;
     const RawSet& q = h->qry;
@@ -738,6 +744,7 @@ int split_vocab(siml_engine* h, int64_t ncommon) {
     SIML_CUDA(cudaStreamSynchronize(st));
     v.ncommon = ncommon;
     v.split = ncommon < v.nvid;
+    v.freq_ordered = true;
     return SIML_OK;
 }
 

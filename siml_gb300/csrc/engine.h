@@ -46,6 +46,10 @@ struct Vocab {
     int64_t nvid = 0;     // number of (code, level) pairs; vids are 1..nvid
     int64_t ncommon = 0;  // vids 1..ncommon go to the shared-memory table
     bool split = false;   // ncommon < nvid
+    // vids numbered by falling database frequency, so that every prefix
+    // 1..k holds the k most frequent pairs (a split vocabulary, or one whose
+    // whole table fits some kernels but not the scheduled one's)
+    bool freq_ordered = false;
 };
 
 // Database (query set) layout.  Molecules are cut into chunks of 32 (one
@@ -163,6 +167,7 @@ bool rows_use_sched(siml_engine* h);
 // schedule and entry permutation of a freshly built window-sorted layout,
 // and the launch (*done = false when the call is not one it serves).
 int64_t sched_capacity(siml_engine* h);
+bool sched_whole_fits(siml_engine* h, int64_t nvid);
 bool rows_sched_fits(siml_engine* h);
 int sched_arrange(siml_engine* h, DbLayout& d);
 void free_sched(DbLayout& d);

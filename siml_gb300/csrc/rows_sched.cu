@@ -387,14 +387,15 @@ int64_t sched_capacity(siml_engine* h) {
     const int64_t extra = (int64_t)kSchedExtraSmem + (int64_t)kRareSlots * 8 + (int64_t)sizeof(RowSmem) + 2048;
     const int64_t words = ((int64_t)h->smem_optin - extra) / 4;
     const int64_t cap = std::max<int64_t>(0, words / 4 * 4 - 4);
-    // an unsplit vocabulary keeps slot order, which makes no useful split:
-    // the kernel takes it whole or not at all
-    if (!h->vocab.split) {
-        const int64_t vt = (h->vocab.nvid + 1 + 3) / 4 * 4;
-        const bool whole = (size_t)vt * 4 + kSchedExtraSmem + sizeof(RowSmem) + 2048 <= h->smem_optin;
-        return whole ? h->vocab.nvid : 0;
-    }
-    return cap;
+    if (sched_whole_fits(h, h->vocab.nvid)) return h->vocab.nvid;
+    // a vocabulary in slot order makes no useful split: the kernel takes it
+    // whole or not at all; one numbered by frequency lends any prefix
+    return h->vocab.freq_ordered ? std::min<int64_t>(cap, h->vocab.nvid) : 0;
+}
+
+bool sched_whole_fits(siml_engine* h, int64_t nvid) {
+    const int64_t vt = (nvid + 1 + 3) / 4 * 4;
+    return (size_t)vt * 4 + kSchedExtraSmem + sizeof(RowSmem) + 2048 <= h->smem_optin;
 }
 
 bool rows_sched_fits(siml_engine* h) {
