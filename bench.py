@@ -368,8 +368,7 @@ def gpu_arm(args):
     except (OSError, ValueError):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = read_profile_traffic({"rows_1m": "k_rows_rows1m.md", "nbr_1m": "k_nbr_nbr1m.md",
-                                    "topk_1m": "k_topk_topk1m.md", "hist_1m": "k_hist_hist1m.md"}[wl])
+    traffic = read_profile_traffic(profile_name(wl, rows_info["scheduled"]))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic,
                 "kernel": {"rows_1m": "k_rows_sched" if rows_info["scheduled"] else "k_rows_bal", "nbr_1m": "k_nbr",
@@ -408,7 +407,7 @@ def gpu_arm(args):
                    "l2": "flushed between steps by a 256 MB write; each step also writes a 4 GB block",
                    "db_layout": stats, "db_model": args.db_model, "vocab": gl.vocabStats()},
         "roofline": roofline,
-        "compute_side": compute_side(roofline["kernel"], wl),
+        "compute_side": compute_side(roofline["kernel"], profile_name(wl, rows_info["scheduled"])),
         "merge_work_ratio": merge_work_ratio(value / world, np.mean(q[2]), np.mean(db[2]),
                                              clk.get("sm_mhz") or 2070.0, local),
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
@@ -1014,14 +1013,17 @@ def merge_work_ratio(gpairs_per_s, la, lb, sm_mhz, device):
             "formula": "(3*(La+Lb)+4) x pairs/s over SMs x measured int lanes/SM/clock x SM clock"}
 
 
-def compute_side(kernel, workload):
+def profile_name(workload, scheduled):
+    """The committed ncu summary of the workload's dominant kernel."""
+    if workload == "rows_1m":
+        return "k_rows_sched_rows1m.md" if scheduled else "k_rows_rows1m.md"
+    return {"nbr_1m": "k_nbr_nbr1m.md", "topk_1m": "k_topk_topk1m.md", "hist_1m": "k_hist_hist1m.md"}[workload]
+
+
+def compute_side(kernel, name):
     """The dominant kernel's issue-slot and ALU-pipe utilisation from its
-    committed ncu --set full summary (small case of the same kernel): the
-    compute-side fraction beside the HBM roofline."""
-    name = {"rows_1m": "k_rows_rows1m.md", "nbr_1m": "k_nbr_nbr1m.md", "topk_1m": "k_topk_topk1m.md",
-            "hist_1m": "k_hist_hist1m.md"}.get(workload)
-    if not name:
-        return None
+    committed ncu --set full summary `name` (small case of the same kernel):
+    the compute-side fraction beside the HBM roofline."""
     issue = read_profile_value(name, "issue_active_pct")
     alu = read_profile_value(name, "alu_pipe_pct")
     return {"kernel": kernel, "issue_active_frac": None if issue is None else issue / 100.0,
