@@ -19,6 +19,7 @@ restatement) on the host cores, on a bounded sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import gc
 import json
 import os
@@ -259,6 +260,8 @@ def gpu_arm(args):
         N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_ROWS_LAYOUT, args.rows_layout), "rows layout")
     if args.sched_groups:
         N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_SCHED_GROUPS, args.sched_groups), "sched groups")
+    if args.sched_rows:
+        N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_SCHED_ROWS, args.sched_rows), "sched rows")
     stats = gl.dbStats()
     torch.cuda.synchronize()
     log("database layout ready in %.2f s: %s" % (time.time() - t, stats))
@@ -356,6 +359,10 @@ def gpu_arm(args):
     kms = statistics.mean(kernel_ms)
     out_bytes = 0 if fused else pairs_per_step * 4
     rows_info = gl.rowsInfo() if not fused else {"scheduled": 0}
+    if rows_info["scheduled"]:
+        v = ctypes.c_int64()
+        N.check(N.lib().siml_get_tuning(gl._h, N.SIML_TUNE_SCHED_ROWS, ctypes.byref(v)), "sched rows")
+        rows_info["rows_per_cta"] = int(v.value)
     if rows_info["scheduled"]:
         db_bytes = stats["ngroups_total"] * 16 + rows_info["items"] * (32 * 16 + 8)
     else:
@@ -1103,6 +1110,8 @@ def main():
                     help="sort window of the full-matrix layout (32, 64, 128, 256; 0: library default)")
     ap.add_argument("--sched-groups", type=int, default=0,
                     help="warp groups of the scheduled full-matrix kernel (2 or 4; 0: library default)")
+    ap.add_argument("--sched-rows", type=int, default=0,
+                    help="ref rows per CTA of the scheduled full-matrix kernel (32 or 64; 0: library default)")
     ap.add_argument("--rows-layout", type=int, default=-1,
                     help="full-matrix layout (0 padded, 1 balanced, 2 scheduled; -1: library default)")
     ap.add_argument("--rows-entries", type=int, default=-1,

@@ -354,6 +354,14 @@ int siml_vocab_stats(siml_engine* h, int64_t out[4]);
  * own window of 2048 / groups database columns, so the groups' stream and
  * store phases overlap.  Changing it drops the scheduled layout. */
 #define SIML_TUNE_SCHED_GROUPS 6
+/* SIML_TUNE_SCHED_ROWS: ref rows per CTA of the scheduled full-matrix kernel,
+ * 64 (the default: one 8-byte table word per database pair serves 64 rows;
+ * windows of 1024 / SIML_TUNE_SCHED_GROUPS molecules) or 32 (one 4-byte word;
+ * windows of 2048 / SIML_TUNE_SCHED_GROUPS).  The 64-row table holds fewer
+ * pairs, so larger vocabularies are numbered by frequency and their rarest
+ * pairs go through a hash.  Changing it rebuilds the vocabulary and layouts
+ * on next use and invalidates batch plans. */
+#define SIML_TUNE_SCHED_ROWS 7
 int siml_set_tuning(siml_engine* h, int key, int64_t value);
 int siml_get_tuning(siml_engine* h, int key, int64_t* value);
 /* The full-matrix path the current sets and settings use (no reference

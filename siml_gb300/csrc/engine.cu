@@ -763,8 +763,10 @@ int build_layout(siml_engine* h, DbLayout& d, bool sorted, bool scheduled = fals
     d.n = q.n;
     d.sorted = sorted;
     d.scheduled = scheduled;
-    d.window = scheduled ? kSchedColumns / h->sched_groups : (sorted ? h->sorted_window : h->rows_window);
+    d.window = scheduled ? (h->sched_rows == 64 ? kSchedColumns64 : kSchedColumns32) / h->sched_groups
+                         : (sorted ? h->sorted_window : h->rows_window);
     d.sched_warps = scheduled ? 32 / h->sched_groups : 0;
+    d.sched_rows = scheduled ? h->sched_rows : 0;
     // k_window_sort is a bitonic sort: a window that is not a power of two
     // would index past its shared keys
     if (d.window < kChunk || (d.window & (d.window - 1)) || d.window > kMaxWindow)
@@ -1309,6 +1311,19 @@ int siml_set_tuning(siml_engine* h, int key, int64_t value) {
             h->sched_groups = (int)value;
         }
         return SIML_OK;
+    case SIML_TUNE_SCHED_ROWS:
+        if (value != 32 && value != 64)
+            return fail(SIML_ERR_INVALID, "scheduled kernel rows per group must be 32 or 64 (got %lld)",
+                        (long long)value);
+        if (value != h->sched_rows) {
+            // the vocabulary's numbering depends on the table the kernel holds:
+            // everything derived from the query set is rebuilt on next use
+            SIML_CUDA(cudaStreamSynchronize(h->stream));
+            h->layout_valid = false;
+            h->sched_rows = (int)value;
+            h->generation++;   // plans hold vids of the old numbering
+        }
+        return SIML_OK;
     case SIML_TUNE_ROWS_ENTRIES:
         if (value < SIML_ENTRIES_AUTO || value > SIML_ENTRIES_OFFSETS)
             return fail(SIML_ERR_INVALID, "rows entry format must be 0..3 (got %lld)", (long long)value);
@@ -1334,6 +1349,7 @@ int siml_get_tuning(siml_engine* h, int key, int64_t* value) {
     case SIML_TUNE_SORT_WINDOW: *value = h->sorted_window; return SIML_OK;
     case SIML_TUNE_ROWS_LAYOUT: *value = h->rows_layout; return SIML_OK;
     case SIML_TUNE_SCHED_GROUPS: *value = h->sched_groups; return SIML_OK;
+    case SIML_TUNE_SCHED_ROWS: *value = h->sched_rows; return SIML_OK;
     default: return fail(SIML_ERR_INVALID, "unknown tuning key %d", key);
     }
 }

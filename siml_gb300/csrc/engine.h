@@ -90,12 +90,14 @@ struct DbLayout {
     bool scheduled = false;
     int2* sched_items = nullptr;  // [nitems + 1] {chunk, steps | kItemSplit | kItemFirst}, padding record last
     int2* sched_lanes = nullptr;  // [nitems + 1][32] {window position or -1, column magnitude bits}
+    int2* sched_rare = nullptr;   // split vocabulary: [nitems + 1][32] {first rare entry, count}
     int2* sched_wrun = nullptr;   // [nwin * warps] {first item, end item} of (window, warp of a group)
     int64_t* sched_grun = nullptr; // [nwin * warps][2] first and end 16-byte group of (window, warp)
     int64_t nitems = 0;
     int64_t nwin = 0;
     int64_t max_item_steps = 0;
-    int sched_warps = 0;          // warps of a group (one window per group; 2048 / window groups per CTA)
+    int sched_warps = 0;          // warps of a group (one window per group)
+    int sched_rows = 0;           // ref rows per CTA of the kernel the layout was built for (32 or 64)
 };
 
 // Ref-set rows as vid lists (levels expanded, codes absent from the database
@@ -146,6 +148,7 @@ struct siml_engine {
     int sorted_window = 2048;             // sort window of the fused-kernel layout (SIML_TUNE_SORT_WINDOW)
     int rows_layout = SIML_ROWS_SCHEDULED; // full-matrix layout (SIML_TUNE_ROWS_LAYOUT)
     int sched_groups = 4;                  // warp groups of the scheduled kernel (SIML_TUNE_SCHED_GROUPS)
+    int sched_rows = 64;                   // ref rows per CTA of the scheduled kernel (SIML_TUNE_SCHED_ROWS)
 };
 
 namespace siml {
@@ -157,7 +160,8 @@ int ensure_layout(siml_engine* h, bool sorted, const DbLayout** out);
 // The scheduled full-matrix layout (window-sorted, entries in per-warp
 // schedule order); rows_sched.cu arranges it.  A CTA's 32 warps form
 // sched_groups groups, each on its own window of 2048 / sched_groups columns.
-constexpr int kSchedColumns = 2048;
+constexpr int kSchedColumns32 = 2048;   // database columns in flight per CTA, 32-row groups
+constexpr int kSchedColumns64 = 1024;   // the same, 64-row groups (twice the staging per column)
 int ensure_sched_layout(siml_engine* h, const DbLayout** out);
 // getMultipleRows runs on the scheduled layout (settings and sets allow it;
 // the sets must be prepared).

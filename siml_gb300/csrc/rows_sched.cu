@@ -46,20 +46,32 @@ namespace {
 
 constexpr int kSThreads = 1024;
 constexpr int kSWarpsAll = kSThreads / 32;
-constexpr int kSColsAll = 2048;       // columns in flight per CTA: G windows of kSColsAll / G
+// Columns in flight per CTA (G windows of kSColsAll / G).  The staging holds
+// a byte count per row and column, so 64-row groups keep half the columns.
+template <int ROWS>
+constexpr int kSColsAll = ROWS == 32 ? kSchedColumns32 : kSchedColumns64;
 constexpr double kItemCost = 2.0;     // an item's epilogue, in 8-entry steps, for the schedule
 constexpr int kItemStepsMask = 0xFFFF;
 constexpr int kItemSplit = 1 << 16;   // the chunk has several items: add counts atomically
 constexpr int kItemFirst = 1 << 17;   // the item holds the chunk's first step: column data, rare entries
-constexpr int kPadSteps = 2;
-// Largest row stride for which 31 rows of fp32 stay within 32-bit byte offsets.
-constexpr int64_t kFullGroupLdo = (int64_t)(0xFFFFFFFFull / (31ull * 4ull));          // steps of zero padding after the entries (loads run two steps ahead)
-// staging (8 count words per column) + column magnitudes, over all groups
-constexpr size_t kSchedExtraSmem = (size_t)9 * kSColsAll * 4;
+constexpr int kPadSteps = 2;          // steps of zero padding after the entries (loads run two steps ahead)
+// Largest row stride for which ROWS - 1 rows of fp32 stay within 32-bit byte offsets.
+template <int ROWS>
+constexpr int64_t kFullGroupLdo = (int64_t)(0xFFFFFFFFull / ((ROWS - 1ull) * 4ull));
+// staging (ROWS / 4 count words per column) + column magnitudes, over all groups
+template <int ROWS>
+constexpr size_t kSchedExtraSmem = (size_t)(ROWS / 4 + 1) * kSColsAll<ROWS> * 4;
+// The 64-row kernel's rare-pair hash: kRare64Slots keys, then a 64-bit row
+// mask per slot.  At most 64 x kRare64RowMax keys: never more than 3/4 full.
+constexpr int kRare64SlotsLog2 = 11;
+constexpr int kRare64Slots = 1 << kRare64SlotsLog2;
+constexpr int kRare64RowMax = 24;
 
 struct SchedArgs {
     const int2* items;     // work items, with one padding record after the last
     const int2* lanes;     // [items + 1][32] per lane: {window position or -1, column magnitude or -1.0f bits}
+    const int2* rare;      // split vocabulary: [items + 1][32] per lane {first rare entry, count}, counted once
+                           // per molecule (items holding the chunk's first step), else null
     const int2* wrun;      // [nwin * P] {first item, end item} of (window, warp of the group)
     const int64_t* grun;   // [nwin * P][2] first and end 16-byte group of (window, warp of the group)
     const int32_t* qmag;   // database magnitudes in natural order (IEEE-division path)
@@ -117,23 +129,160 @@ __device__ __forceinline__ uint64_t tanimoto2(uint64_t I, uint64_t S) {
     return fma2(R, Y, Q0);
 }
 
-// End of an item: the counter's planes become 32 byte counts (word k holds
-// rows k, k + 8, k + 16, k + 24) stored at the molecule's window position.
-template <int WIN>
+// ---- 64-row groups: one 8-byte table word per pair (bits 0-31: rows 0-31,
+// bits 32-63: rows 32-63), read with one 8-byte shared load, so the vid
+// extraction, the lookups, the loop and the entry stream serve 64 rows.
+struct RowSmem64 {
+    int amag[64];
+    __align__(16) float amagf[64];
+    int allfast;
+};
+
+__device__ __forceinline__ uint32_t rare64_hash(uint32_t v) { return (v * 0x9E3779B1u) >> (32 - kRare64SlotsLog2); }
+
+// Sets bit `bit` of half `half` of vid v's mask in the rare-pair hash.
+__device__ __forceinline__ void rare64_insert(uint32_t* keys, uint32_t v, int half, uint32_t bit, int* err) {
+    uint32_t h = rare64_hash(v);
+    for (int probe = 0; probe < kRare64Slots; probe++) {
+        const uint32_t prev = atomicCAS(&keys[h], 0u, v);
+        if (prev == 0u || prev == v) {
+            atomicOr(&keys[kRare64Slots + 2 * h + half], bit);
+            return;
+        }
+        h = (h + 1) & (kRare64Slots - 1);
+    }
+    if (err) atomicOr(err, kErrBadRowVid);   // no free slot: the entry is not used
+}
+
+__device__ __forceinline__ uint2 rare64_lookup(const uint32_t* keys, uint32_t v) {
+    uint32_t h = rare64_hash(v);
+    for (int probe = 0; probe < kRare64Slots; probe++) {
+        const uint32_t k = keys[h];
+        if (k == v) return *reinterpret_cast<const uint2*>(keys + kRare64Slots + 2 * h);
+        if (k == 0u) return make_uint2(0u, 0u);
+        h = (h + 1) & (kRare64Slots - 1);
+    }
+    return make_uint2(0u, 0u);
+}
+
+// Clears the 64-row table (p.vt_words words: 2 per vid) and its rare hash,
+// sets the bits of the group's rows, fills rs.  Full-matrix mode only (the
+// scheduled layout serves getMultipleRows).  Returns the group's rows.
+__device__ __forceinline__ int build_table64(uint32_t* T, RowSmem64& rs, const GroupParams& p) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    const int64_t row0 = (int64_t)blockIdx.x * 64;
+    const int nr = min(64, live_rows(p) - (int)row0);
+    for (int i = threadIdx.x * 4; i < p.tab_words; i += blockDim.x * 4)
+        *reinterpret_cast<uint4*>(T + i) = make_uint4(0u, 0u, 0u, 0u);
+    if (warp == 0) {
+        bool all = true;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int r = 32 * h + lane;
+            const int64_t gr = r < nr ? p.rowbase + row0 + r : p.rowbase;
+            const int am = r < nr ? p.row_mag[gr] : 0;
+            rs.amag[r] = am;
+            rs.amagf[r] = (float)am;
+            all = __all_sync(0xFFFFFFFFu, r >= nr || fast_mag(am, p.row_cmag[gr])) && all;
+        }
+        if (lane == 0) rs.allfast = all;
+    }
+    __syncthreads();
+    uint32_t* keys = T + p.vt_words;
+    for (int r = warp; r < nr; r += nwarps) {
+        const uint32_t* rv = p.row_vid + (p.rowbase + row0 + r) * p.row_stride;
+        const int half = r >> 5;
+        const uint32_t bit = 1u << (r & 31);
+        for (int64_t e = lane; e < p.row_stride; e += 32) {
+            const uint32_t v = rv[e];
+            if (v == 0u) continue;
+            if ((int64_t)v <= p.ncommon) atomicOr(&T[2 * v + half], bit);
+            else if (p.rare_slots) rare64_insert(keys, v, half, bit, p.err);
+            else if (p.err) atomicOr(p.err, kErrBadRowVid);
+        }
+    }
+    __syncthreads();
+    return nr;
+}
+
+// The bit-sliced counters of a ROWS-row group: one 8-plane counter per 32 rows.
+template <int ROWS>
+struct GroupCounter {
+    SlicedCounter<8> c[ROWS / 32];
+
+    __device__ __forceinline__ void clear() {
+#pragma unroll
+        for (int h = 0; h < ROWS / 32; h++) c[h].clear();
+    }
+
+    // one 8-entry step of 2-byte vids
+    __device__ __forceinline__ void step(const uint32_t* T, const uint32_t x0, const uint32_t x1, const uint32_t x2,
+                                         const uint32_t x3) {
+        if constexpr (ROWS == 32) {
+            c[0].add8(T[x0 & 0xFFFFu], T[x0 >> 16], T[x1 & 0xFFFFu], T[x1 >> 16],
+                      T[x2 & 0xFFFFu], T[x2 >> 16], T[x3 & 0xFFFFu], T[x3 >> 16]);
+        } else {
+            const uint2* T2 = reinterpret_cast<const uint2*>(T);
+            const uint2 m0 = T2[x0 & 0xFFFFu], m1 = T2[x0 >> 16], m2 = T2[x1 & 0xFFFFu], m3 = T2[x1 >> 16];
+            const uint2 m4 = T2[x2 & 0xFFFFu], m5 = T2[x2 >> 16], m6 = T2[x3 & 0xFFFFu], m7 = T2[x3 >> 16];
+            c[0].add8(m0.x, m1.x, m2.x, m3.x, m4.x, m5.x, m6.x, m7.x);
+            c[1].add8(m0.y, m1.y, m2.y, m3.y, m4.y, m5.y, m6.y, m7.y);
+        }
+    }
+
+    // adds one rare entry (split vocabulary) through the group's hash
+    __device__ __forceinline__ void add_rare_vid(const uint32_t* T, const GroupParams& p, uint32_t v) {
+        if constexpr (ROWS == 32) {
+            const uint32_t m = rare_lookup(T + p.vt_words, v);
+            if (m) c[0].add1(m);
+        } else {
+            const uint2 m = rare64_lookup(T + p.vt_words, v);
+            if (m.x) c[0].add1(m.x);
+            if (m.y) c[1].add1(m.y);
+        }
+    }
+
+    // a molecule's rare entries: rr = {first, count} in p.rare_vid, the first
+    // two loaded ahead into v0, v1 (when the item started)
+    __device__ __forceinline__ void add_rare(const uint32_t* T, const GroupParams& p, int2 rr, uint32_t v0,
+                                             uint32_t v1) {
+        if (rr.y <= 0) return;
+        add_rare_vid(T, p, v0);
+        if (rr.y <= 1) return;
+        add_rare_vid(T, p, v1);
+        for (int i = 2; i < rr.y; i++) add_rare_vid(T, p, __ldg(p.rare_vid + rr.x + i));
+    }
+};
+
+// The first two rare entries of an item's molecule, loaded when the item
+// starts so that they arrive while it streams.
+__device__ __forceinline__ void rare_prefetch(const GroupParams& p, int2 rr, uint32_t& v0, uint32_t& v1) {
+    v0 = rr.y > 0 ? __ldg(p.rare_vid + rr.x) : 0u;
+    v1 = rr.y > 1 ? __ldg(p.rare_vid + rr.x + 1) : 0u;
+}
+
+// End of an item: each 32-row counter's planes become 32 byte counts, stored
+// at the molecule's window position: staging word 8 h + k holds rows
+// 32 h + k, + 8, + 16, + 24.
+template <int WIN, int ROWS>
 __device__ __forceinline__ void flush_item(uint32_t* W, float* colf, int flags, const int2& lr,
-                                           const SlicedCounter<8>& acc) {
+                                           const GroupCounter<ROWS>& acc) {
     if (lr.x < 0) return;
     const int pos = lr.x;
-    uint32_t w[8];
 #pragma unroll
-    for (int k = 0; k < 8; k++) w[k] = acc.plane[k];
-    transpose_planes8(w);
-    if (flags & kItemSplit) {
+    for (int h = 0; h < ROWS / 32; h++) {
+        uint32_t w[8];
 #pragma unroll
-        for (int k = 0; k < 8; k++) atomicAdd(W + k * WIN + pos, w[k]);
-    } else {
+        for (int k = 0; k < 8; k++) w[k] = acc.c[h].plane[k];
+        transpose_planes8(w);
+        if (flags & kItemSplit) {
 #pragma unroll
-        for (int k = 0; k < 8; k++) W[k * WIN + pos] = w[k];
+            for (int k = 0; k < 8; k++) atomicAdd(W + (8 * h + k) * WIN + pos, w[k]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; k++) W[(8 * h + k) * WIN + pos] = w[k];
+        }
     }
     if (flags & kItemFirst) colf[pos] = __int_as_float(lr.y);
 }
@@ -142,34 +291,46 @@ __device__ __forceinline__ void group_barrier(int group, int threads) {
     asm volatile("bar.sync %0, %1;" ::"r"(1 + group), "r"(threads) : "memory");
 }
 
-template <bool RARE, int G>
+template <bool RARE, int G, int ROWS>
 __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p, const SchedArgs a) {
     constexpr int P = kSWarpsAll / G;          // warps of a group
     constexpr int TG = P * 32;                 // threads of a group
-    constexpr int WIN = kSColsAll / G;         // columns of a window
+    constexpr int WIN = kSColsAll<ROWS> / G;   // columns of a window
     constexpr int Q = WIN / 4;                 // 4-column quads of a window
-    static_assert(TG == 2 * Q, "phase 2 maps each thread to one quad and two of its count words");
+    constexpr int NW = ROWS / 4;               // staging words per column
+    constexpr int KS = TG / Q;                 // phase 2: threads per quad (word stride)
+    static_assert(TG % Q == 0 && NW % KS == 0 && NW / KS == 4,
+                  "phase 2 maps each thread to one quad and four of its count words");
+    static_assert(((KS * 1) & 7) + KS <= 8 && ((KS * 2) & 7) + KS <= 8 && ((KS * 3) & 7) + KS <= 8,
+                  "phase 2's row offsets from row kk are compile-time constants");
+    using RS = typename std::conditional<ROWS == 32, RowSmem, RowSmem64>::type;
     extern __shared__ __align__(16) uint32_t T[];
-    __shared__ RowSmem rs;
-    __shared__ __align__(16) float amq[32];   // amq[4 k + j]: magnitude of row k + 8 j
-    const int nr = build_table(T, rs, p);      // synchronizes the block
+    __shared__ RS rs;
+    // amq[4 w + j]: magnitude of row 32 (w / 8) + w % 8 + 8 j (staging word w, byte j)
+    __shared__ __align__(16) float amq[ROWS];
+    int nr;
+    if constexpr (ROWS == 32) nr = build_table(T, rs, p);   // synchronizes the block
+    else nr = build_table64(T, rs, p);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int group = warp / P, wg = warp - group * P, tg = threadIdx.x - group * TG;
-    uint32_t* W = T + p.tab_words + (size_t)group * 9 * WIN;   // [8][WIN] staged counts of this group
-    float* colf = reinterpret_cast<float*>(W + 8 * WIN);        // [WIN] column magnitude, -1: IEEE path
-    if (threadIdx.x < 32) amq[(lane & 7) * 4 + (lane >> 3)] = rs.amagf[lane];
-    for (int i = tg * 4; i < 8 * WIN; i += TG * 4) *reinterpret_cast<uint4*>(W + i) = make_uint4(0u, 0u, 0u, 0u);
+    uint32_t* W = T + p.tab_words + (size_t)group * (NW + 1) * WIN;   // [NW][WIN] staged counts of this group
+    float* colf = reinterpret_cast<float*>(W + NW * WIN);              // [WIN] column magnitude, -1: IEEE path
+    if (threadIdx.x < ROWS) {
+        const int r = threadIdx.x;
+        amq[4 * (8 * (r >> 5) + (r & 7)) + ((r & 31) >> 3)] = rs.amagf[r];
+    }
+    for (int i = tg * 4; i < NW * WIN; i += TG * 4) *reinterpret_cast<uint4*>(W + i) = make_uint4(0u, 0u, 0u, 0u);
     __syncthreads();
     const int64_t w0 = a.nwin * blockIdx.y / gridDim.y, w1 = a.nwin * (blockIdx.y + 1) / gridDim.y;
-    float* outg = a.out + (int64_t)blockIdx.x * 32 * a.ldo;
+    float* outg = a.out + (int64_t)blockIdx.x * ROWS * a.ldo;
     const uint4* E = reinterpret_cast<const uint4*>(p.entries) + lane;
     const char* Eb = reinterpret_cast<const char*>(p.entries);
     const uint64_t k2p23 = f2(8388608.0f, 8388608.0f);
     const int q4 = (tg % Q) * 4;   // phase 2: columns q4 .. q4 + 3
-    const int kk = tg / Q;         // phase 2: staging words kk, kk + 2, kk + 4, kk + 6
-    // phase 2's straight-line path: a full 32-row group whose magnitudes all
-    // admit div_small, and rows within 32-bit byte offsets of each other
-    const bool full_fast = rs.allfast && nr == 32 && a.ldo < kFullGroupLdo;
+    const int kk = tg / Q;         // phase 2: staging words kk + KS m, m = 0..3
+    // phase 2's straight-line path: a full group whose magnitudes all admit
+    // div_small, and rows within 32-bit byte offsets of each other
+    const bool full_fast = rs.allfast && nr == ROWS && a.ldo < kFullGroupLdo<ROWS>;
     // A warp streams the runs of its windows (w0 + group, then every G-th)
     // as one sequence: the layout stores them back to back, so the two-step
     // register prefetch and the next item's record run straight across the
@@ -180,6 +341,8 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
     int it = 0, left = 0;
     int2 rec = make_int2(0, 0), rec_n = rec;
     int2 lr = make_int2(-1, 0), lr_n = lr;   // this lane's record of the current and the next item
+    int2 rr = make_int2(0, 0), rr_n = rr;     // its rare entries (split vocabulary)
+    uint32_t rv0 = 0u, rv1 = 0u;              // the current item's first two rare entries
     bool phase_b = false;   // the next step is held in qb
     if (wfirst < w1) {
         const int64_t sl = wfirst * P + wg;
@@ -192,6 +355,11 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
         lr = __ldg(a.lanes + (int64_t)it * 32 + lane);
         rec_n = __ldg(a.items + it + 1);
         lr_n = __ldg(a.lanes + (int64_t)(it + 1) * 32 + lane);
+        if constexpr (RARE) {
+            rr = __ldg(a.rare + (int64_t)it * 32 + lane);
+            rr_n = __ldg(a.rare + (int64_t)(it + 1) * 32 + lane);
+            rare_prefetch(p, rr, rv0, rv1);
+        }
         left = rec.y & kItemStepsMask;
         if (lane == 0) {   // this window's run and the next one's into L2
             for (int64_t w2 = wfirst; w2 < w1 && w2 <= wfirst + G; w2 += G) {
@@ -201,7 +369,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
             }
         }
     }
-    SlicedCounter<8> acc;
+    GroupCounter<ROWS> acc;
     acc.clear();
     for (int64_t wnd = wfirst; wnd < w1; wnd += G) {
         const int64_t wbase = wnd * WIN;
@@ -217,10 +385,8 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
         // done (rec and lr then hold the next window's first item)
         auto advance = [&]() -> bool {
             while (left == 0) {
-                if constexpr (RARE) {
-                    if ((rec.y & kItemFirst) && lr.x >= 0) rare_add<8>(T, p, (int64_t)rec.x * 32 + lane, acc);
-                }
-                flush_item<WIN>(W, colf, rec.y, lr, acc);
+                if constexpr (RARE) acc.add_rare(T, p, rr, rv0, rv1);
+                flush_item<WIN, ROWS>(W, colf, rec.y, lr, acc);
                 acc.clear();
                 ++it;
                 rec = rec_n;
@@ -228,6 +394,11 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
                 left = rec.y & kItemStepsMask;
                 rec_n = __ldg(a.items + it + 1);
                 lr_n = __ldg(a.lanes + (int64_t)(it + 1) * 32 + lane);
+                if constexpr (RARE) {
+                    rr = rr_n;
+                    rr_n = __ldg(a.rare + (int64_t)(it + 1) * 32 + lane);
+                    rare_prefetch(p, rr, rv0, rv1);
+                }
                 if (it >= ie) return false;
             }
             return true;
@@ -237,8 +408,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
                 if (!phase_b) {   // step held in qa; its register takes the step two ahead
                     const uint32_t x0 = qa.x, x1 = qa.y, x2 = qa.z, x3 = qa.w;
                     qa = __ldg(ptr + 64);
-                    acc.add8(T[x0 & 0xFFFFu], T[x0 >> 16], T[x1 & 0xFFFFu], T[x1 >> 16],
-                             T[x2 & 0xFFFFu], T[x2 >> 16], T[x3 & 0xFFFFu], T[x3 >> 16]);
+                    acc.step(T, x0, x1, x2, x3);
                     --left;
                     if (!advance()) {
                         phase_b = true;
@@ -248,8 +418,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
                 {   // step held in qb
                     const uint32_t x0 = qb.x, x1 = qb.y, x2 = qb.z, x3 = qb.w;
                     qb = __ldg(ptr + 96);
-                    acc.add8(T[x0 & 0xFFFFu], T[x0 >> 16], T[x1 & 0xFFFFu], T[x1 >> 16],
-                             T[x2 & 0xFFFFu], T[x2 >> 16], T[x3 & 0xFFFFu], T[x3 >> 16]);
+                    acc.step(T, x0, x1, x2, x3);
                 }
                 ptr += 64;
                 phase_b = false;
@@ -267,7 +436,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
         const float4 cf = q4 < ncols ? *reinterpret_cast<const float4*>(colf + q4)
                                      : make_float4(-1.0f, -1.0f, -1.0f, -1.0f);
         if (full_fast && q4 + 4 <= ncols && cf.x >= 0.0f && cf.y >= 0.0f && cf.z >= 0.0f && cf.w >= 0.0f) {
-            // 32 rows, a whole quad of columns, every pair exact with
+            // a full group, a whole quad of columns, every pair exact with
             // div_small: straight-line code, rows addressed by 32-bit byte
             // offsets from row kk
             char* ob = reinterpret_cast<char*>(outg + wbase + q4 + (int64_t)kk * a.ldo);
@@ -275,7 +444,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
             const float bcol[4] = {cf.x, cf.y, cf.z, cf.w};
 #pragma unroll
             for (int kq = 0; kq < 4; kq++) {
-                const int k = kk + 2 * kq;
+                const int k = kk + KS * kq;   // staging word: rows 32 (k / 8) + k % 8 + 8 j
                 uint32_t* wp = W + k * WIN + q4;
                 const uint4 c = *reinterpret_cast<const uint4*>(wp);
                 *reinterpret_cast<uint4*>(wp) = make_uint4(0u, 0u, 0u, 0u);
@@ -292,9 +461,10 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
                         const float u = __fsub_rn(__fadd_rn(av[j], bcol[cc]), isf);
                         t[cc] = div_small(isf, u);
                     }
-                    // row k + 8 j is row kk + 2 kq + 8 j
-                    *reinterpret_cast<float4*>(ob + (uint32_t)(2 * kq + 8 * j) * row_bytes) =
-                        make_float4(t[0], t[1], t[2], t[3]);
+                    // row 32 (k / 8) + k % 8 + 8 j, relative to row kk: kk < KS and
+                    // (KS kq) % 8 + KS <= 8, so k / 8 = (KS kq) / 8 and k % 8 = kk + (KS kq) % 8
+                    const int rel = 32 * ((KS * kq) >> 3) + ((KS * kq) & 7) + 8 * j;
+                    *reinterpret_cast<float4*>(ob + (uint32_t)rel * row_bytes) = make_float4(t[0], t[1], t[2], t[3]);
                 }
             }
         } else if (q4 < ncols) {
@@ -304,7 +474,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
             float* ob = outg + wbase + q4;
 #pragma unroll
             for (int kq = 0; kq < 4; kq++) {
-                const int k = kk + 2 * kq;
+                const int k = kk + KS * kq;
                 uint32_t* wp = W + k * WIN + q4;
                 const uint4 c = *reinterpret_cast<const uint4*>(wp);
                 *reinterpret_cast<uint4*>(wp) = make_uint4(0u, 0u, 0u, 0u);
@@ -312,7 +482,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
                 const float av[4] = {a4.x, a4.y, a4.z, a4.w};
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    const int r = k + 8 * j;
+                    const int r = 32 * (k >> 3) + (k & 7) + 8 * j;
                     if (r >= nr) break;
                     float* orow = ob + (int64_t)r * a.ldo;
                     const uint32_t sel = 0x7440u | (uint32_t)j;
@@ -373,6 +543,25 @@ __global__ void k_sched_lanes(const int2* __restrict__ items, int64_t nitems, co
                          __float_as_int(m.x >= 0 && fast_mag(m.y, m.z) ? (float)m.y : -1.0f));
 }
 
+// Per item and lane the molecule's rare entries {first, count} in the
+// layout's rare list, given to the item that holds the chunk's first step
+// (the others count none, so each molecule's rare entries are added once).
+__global__ void k_sched_rare(const int2* __restrict__ items, int64_t nitems, const int4* __restrict__ meta,
+                             const int64_t* __restrict__ rare_off, int2* __restrict__ rare) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (nitems + 1) * 32) return;
+    const int64_t item = i >> 5;
+    if (item == nitems) {   // the padding record's lanes
+        rare[i] = make_int2(0, 0);
+        return;
+    }
+    const int2 it = items[item];
+    const int64_t slot = (int64_t)it.x * 32 + (i & 31);
+    const bool first = (it.y & kItemFirst) && meta[slot].x >= 0;
+    const int64_t b = rare_off[slot], e = rare_off[slot + 1];
+    rare[i] = first ? make_int2((int)b, (int)(e - b)) : make_int2(0, 0);
+}
+
 struct SchedItem {
     int64_t chunk;
     int s0, ns;
@@ -381,21 +570,41 @@ struct SchedItem {
 
 }  // namespace
 
+namespace {
+
+// Shared memory beside the table: the staging and column magnitudes, the
+// rare-pair hash (when a split needs it), the row data and amq, with a margin
+// for static shared memory.
+int64_t sched_extra_smem(int rows, bool hash) {
+    if (rows == 64)
+        return (int64_t)kSchedExtraSmem<64> + (hash ? (int64_t)kRare64Slots * 12 : 0) + (int64_t)sizeof(RowSmem64) +
+               64 * 4 + 2048;
+    return (int64_t)kSchedExtraSmem<32> + (hash ? (int64_t)kRareSlots * 8 : 0) + (int64_t)sizeof(RowSmem) + 32 * 4 +
+           2048;
+}
+
+// Table words of ncommon common vids: one per vid (32 rows) or two (64 rows),
+// vids 0..ncommon, rounded up to 16 bytes.
+int64_t sched_table_words(int rows, int64_t ncommon) {
+    return rows == 64 ? (ncommon + 1 + 1) / 2 * 4 : (ncommon + 1 + 3) / 4 * 4;
+}
+
+}  // namespace
+
 int64_t sched_capacity(siml_engine* h) {
-    // table words beside the staging, the column magnitudes, the rare-vid hash
-    // and the row data, with a margin for static shared memory
-    const int64_t extra = (int64_t)kSchedExtraSmem + (int64_t)kRareSlots * 8 + (int64_t)sizeof(RowSmem) + 2048;
-    const int64_t words = ((int64_t)h->smem_optin - extra) / 4;
-    const int64_t cap = std::max<int64_t>(0, words / 4 * 4 - 4);
     if (sched_whole_fits(h, h->vocab.nvid)) return h->vocab.nvid;
     // a vocabulary in slot order makes no useful split: the kernel takes it
     // whole or not at all; one numbered by frequency lends any prefix
-    return h->vocab.freq_ordered ? std::min<int64_t>(cap, h->vocab.nvid) : 0;
+    if (!h->vocab.freq_ordered) return 0;
+    const int rows = h->sched_rows;
+    const int64_t words = ((int64_t)h->smem_optin - sched_extra_smem(rows, true)) / 4;
+    int64_t cap = rows == 64 ? words / 4 * 2 - 2 : words / 4 * 4 - 4;   // sched_table_words(cap) <= words
+    return std::max<int64_t>(0, std::min<int64_t>(cap, h->vocab.nvid));
 }
 
 bool sched_whole_fits(siml_engine* h, int64_t nvid) {
-    const int64_t vt = (nvid + 1 + 3) / 4 * 4;
-    return (size_t)vt * 4 + kSchedExtraSmem + sizeof(RowSmem) + 2048 <= h->smem_optin;
+    const int rows = h->sched_rows;
+    return sched_table_words(rows, nvid) * 4 + sched_extra_smem(rows, false) <= (int64_t)h->smem_optin;
 }
 
 bool rows_sched_fits(siml_engine* h) {
@@ -412,7 +621,9 @@ void free_sched(DbLayout& d) {
     if (d.sched_wrun) cudaFree(d.sched_wrun);
     if (d.sched_grun) cudaFree(d.sched_grun);
     if (d.sched_lanes) cudaFree(d.sched_lanes);
+    if (d.sched_rare) cudaFree(d.sched_rare);
     d.sched_lanes = nullptr;
+    d.sched_rare = nullptr;
     d.sched_items = nullptr;
     d.sched_wrun = nullptr;
     d.sched_grun = nullptr;
@@ -467,7 +678,8 @@ bool fill_window(const int32_t* L, int n, int P, double M, std::vector<SchedItem
 int sched_arrange(siml_engine* h, DbLayout& d) {
     cudaStream_t st = h->stream;
     const int P = d.sched_warps;
-    if (d.entry_bytes != 2 || P < 1 || P > kSWarpsAll || d.window != (kSColsAll * P) / kSWarpsAll)
+    const int cols = d.sched_rows == 64 ? kSColsAll<64> : kSColsAll<32>;
+    if (d.entry_bytes != 2 || P < 1 || P > kSWarpsAll || d.window != (cols * P) / kSWarpsAll)
         return fail(SIML_ERR_UNSUPPORTED, "scheduled layout: bad base layout");
     const int64_t nch = d.nchunks;
     std::vector<int32_t> ng((size_t)std::max<int64_t>(nch, 1));
@@ -563,6 +775,16 @@ int sched_arrange(siml_engine* h, DbLayout& d) {
         h->launches++;
         SIML_CUDA(cudaGetLastError());
     }
+    if (d.rare_off) {   // split vocabulary: each lane's rare entries, loaded ahead by the kernel
+        if (d.nrare > 0x7FFFFFFF) return fail(SIML_ERR_UNSUPPORTED, "scheduled layout: too many rare entries");
+        if ((rc = dev_alloc_bytes(&p, items.size() * 32 * sizeof(int2)))) return rc;
+        d.sched_rare = (int2*)p;
+        const int64_t n = (int64_t)items.size() * 32;
+        k_sched_rare<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d.sched_items, (int64_t)items.size() - 1, d.meta,
+                                                                  d.rare_off, d.sched_rare);
+        h->launches++;
+        SIML_CUDA(cudaGetLastError());
+    }
     SIML_CUDA(cudaMemcpyAsync(d.sched_wrun, wrun.data(), wrun.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
     SIML_CUDA(cudaMemcpyAsync(d.sched_grun, grun.data(), grun.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
     d.nitems = (int64_t)items.size() - 1;
@@ -613,18 +835,32 @@ int launch_rows_sched(siml_engine* h, const RowsArgs& a, bool* done) {
     size_t smem = 0;
     int np = 0;
     if (!table_params(h, d, a.rowbase, rows, kModeRows, p, smem, np) || np != 8 || d->entry_bytes != 2) return SIML_OK;
-    const size_t sm = smem + kSchedExtraSmem;
-    if (sm + sizeof(RowSmem) + 256 > h->smem_optin) return SIML_OK;
+    const int R = d->sched_rows;
+    const bool split = d->ncommon < h->vocab.nvid;
+    if (R == 64) {
+        // the 64-row table: two words per vid, then the 64-bit-mask hash
+        if (split && h->rows.max_rare_sched > kRare64RowMax) return SIML_OK;
+        p.vt_words = (int)sched_table_words(64, d->ncommon);
+        p.rare_slots = split ? kRare64Slots : 0;
+        p.tab_words = p.vt_words + (split ? 3 * kRare64Slots : 0);
+        smem = (size_t)p.tab_words * 4;
+    }
+    const size_t sm = smem + (R == 64 ? kSchedExtraSmem<64> : kSchedExtraSmem<32>);
+    if ((int64_t)smem + sched_extra_smem(R, false) > (int64_t)h->smem_optin) return SIML_OK;
     void (*kern)(const GroupParams, const SchedArgs) = nullptr;
-    switch (kSWarpsAll / d->sched_warps) {
-        case 2: kern = p.rare_slots ? k_rows_sched<true, 2> : k_rows_sched<false, 2>; break;
-        case 4: kern = p.rare_slots ? k_rows_sched<true, 4> : k_rows_sched<false, 4>; break;
+    switch ((kSWarpsAll / d->sched_warps) * 100 + R) {
+        case 232: kern = split ? k_rows_sched<true, 2, 32> : k_rows_sched<false, 2, 32>; break;
+        case 432: kern = split ? k_rows_sched<true, 4, 32> : k_rows_sched<false, 4, 32>; break;
+        case 264: kern = split ? k_rows_sched<true, 2, 64> : k_rows_sched<false, 2, 64>; break;
+        case 464: kern = split ? k_rows_sched<true, 4, 64> : k_rows_sched<false, 4, 64>; break;
         default: return SIML_OK;
     }
     if ((rc = set_smem(kern, sm))) return rc;
     SchedArgs sa;
     sa.items = d->sched_items;
     sa.lanes = d->sched_lanes;
+    sa.rare = d->sched_rare;
+    if (split && !sa.rare) return SIML_OK;
     sa.wrun = d->sched_wrun;
     sa.grun = d->sched_grun;
     sa.qmag = h->qry.mag;
@@ -632,7 +868,7 @@ int launch_rows_sched(siml_engine* h, const RowsArgs& a, bool* done) {
     sa.nwin = d->nwin;
     sa.out = a.out;
     sa.ldo = a.ldo;
-    const int64_t groups = (rows + 31) / 32;
+    const int64_t groups = (rows + R - 1) / R;
     // windows per CTA: groups x splits fills whole waves of one CTA per SM
     int splits = 1;
     double best = 1e300;

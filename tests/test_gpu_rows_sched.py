@@ -1,8 +1,10 @@
 """The scheduled full-matrix kernel (k_rows_sched, the default path of
-getMultipleRows): bit-exact against the oracle at window edges (database
-sizes around the 2,048-molecule window and not multiples of 4), row counts
-that are not multiples of 32, molecules long enough that chunks are split
-across warps, magnitudes outside the fast division's range, empty molecules,
+getMultipleRows), with 64-row groups (the default) and 32-row groups:
+bit-exact against the oracle at window edges (database sizes around the
+window and not multiples of 4), row counts that are not multiples of the
+group, molecules long enough that chunks are split across warps, magnitudes
+outside the fast division's range, empty molecules, a vocabulary larger than
+the 64-row table (numbered by frequency, its rarest pairs through the hash),
 and the fallbacks when the output cannot take 16-byte stores."""
 import numpy as np
 import pytest
@@ -10,9 +12,16 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _engine():
-    from siml_gb300 import GPULingo
-    return GPULingo(0)
+@pytest.fixture(params=[64, 32], ids=["rows64", "rows32"])
+def rows(request):
+    return request.param
+
+
+def _engine(rows=64):
+    from siml_gb300 import GPULingo, _native as N
+    gl = GPULingo(0)
+    N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_SCHED_ROWS, rows))
+    return gl
 
 
 def _load(gl, ref, qry):
@@ -26,16 +35,16 @@ def _bimodal(n, first=0):
 
 
 @pytest.mark.parametrize("groups", [2, 4])
-@pytest.mark.parametrize("nq", [1, 33, 511, 512, 513, 1025, 2049, 4099, 6150])
-def test_sched_window_edges(native, oracle, nq, groups):
+@pytest.mark.parametrize("nq", [1, 33, 255, 257, 511, 512, 513, 1025, 2049, 4099, 6150])
+def test_sched_window_edges(native, oracle, nq, groups, rows):
     from siml_gb300 import _native as N
     db = _bimodal(nq)
     ref = _bimodal(77, first=100_000)
-    gl = _engine()
+    gl = _engine(rows)
     N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_SCHED_GROUPS, groups))
     _load(gl, ref, db)
     info = gl.rowsInfo()
-    win = 2048 // groups
+    win = (2048 if rows == 32 else 1024) // groups
     assert info["scheduled"] == 1 and info["windows"] == (nq + win - 1) // win
     want = oracle.tanimoto_block(ref, db, 0, 77)
     for r0, r1 in [(0, 77), (0, 1), (5, 36), (40, 73)]:
@@ -43,13 +52,13 @@ def test_sched_window_edges(native, oracle, nq, groups):
         assert np.array_equal(got.view(np.uint32), want[r0:r1].view(np.uint32)), (r0, r1)
 
 
-def test_sched_splits_long_chunks(native, oracle):
+def test_sched_splits_long_chunks(native, oracle, rows):
     """A bimodal database (30% of molecules around 110 characters): windows
     hold chunks several times longer than the mean share of a warp, so they
     are split into items whose counts add in shared memory."""
     db = _bimodal(20_000)
     ref = _bimodal(64, first=50_000)
-    gl = _engine()
+    gl = _engine(rows)
     _load(gl, ref, db)
     info = gl.rowsInfo()
     nchunks = (20_000 + 31) // 32
@@ -58,7 +67,7 @@ def test_sched_splits_long_chunks(native, oracle):
     assert np.array_equal(got.view(np.uint32), oracle.tanimoto_block(ref, db, 0, 64).view(np.uint32))
 
 
-def test_sched_magnitudes_outside_the_fast_range(native, oracle):
+def test_sched_magnitudes_outside_the_fast_range(native, oracle, rows):
     """User magnitudes of zero, below the count sum or above 32,768, on rows
     and on columns, take the IEEE division; the rest of each 4-column group
     with them."""
@@ -74,7 +83,7 @@ def test_sched_magnitudes_outside_the_fast_range(native, oracle):
     rm[[3, 17]] = [0, 50000]
     db2 = (db[0], db[1], db[2], qm)
     ref2 = (ref[0], ref[1], ref[2], rm)
-    gl = _engine()
+    gl = _engine(rows)
     _load(gl, ref2, db2)
     assert gl.rowsInfo()["scheduled"] == 1
     assert np.array_equal(gl.getMultipleRows(0, 40).view(np.uint32),
@@ -87,7 +96,7 @@ def test_sched_magnitudes_outside_the_fast_range(native, oracle):
                           oracle.tanimoto_block(ref3, db2, 0, len(ok)).view(np.uint32))
 
 
-def test_sched_empty_molecules(native, oracle):
+def test_sched_empty_molecules(native, oracle, rows):
     from siml_gb300.compiler import cSMILEStoMatrices
     from siml_gb300 import synthetic as S
     smi = S.smiles_list(S.SEED_ALLPAIRS, S.UNIFORM_20_90, 2500)
@@ -96,14 +105,14 @@ def test_sched_empty_molecules(native, oracle):
     L, C, ln, mg, _ = cSMILEStoMatrices(smi)
     db = (L, C, ln.reshape(-1), mg.reshape(-1))
     ref = tuple(a[:50] for a in db)
-    gl = _engine()
+    gl = _engine(rows)
     _load(gl, ref, db)
     assert gl.rowsInfo()["scheduled"] == 1
     assert np.array_equal(gl.getMultipleRows(0, 50).view(np.uint32),
                           oracle.tanimoto_block(ref, db, 0, 50).view(np.uint32))
 
 
-def test_sched_output_strides_and_fallbacks(native, oracle):
+def test_sched_output_strides_and_fallbacks(native, oracle, rows):
     """A row stride that is a multiple of 4 takes the scheduled kernel with
     padding left untouched; a stride that is not, or an output not on a
     16-byte boundary, takes the natural-order kernel; all agree."""
@@ -111,7 +120,7 @@ def test_sched_output_strides_and_fallbacks(native, oracle):
     db = _bimodal(5000)
     ref = _bimodal(45, first=70_000)
     want = oracle.tanimoto_block(ref, db, 0, 45)
-    gl = _engine()
+    gl = _engine(rows)
     _load(gl, ref, db)
     for ld, off in [(5004, 0), (5001, 0), (5004, 1)]:
         buf = torch.full((45 * ld + 8,), -3.0, dtype=torch.float32, device="cuda")
@@ -123,9 +132,9 @@ def test_sched_output_strides_and_fallbacks(native, oracle):
         assert bool((pad == -3.0).all()), (ld, off)
 
 
-def test_sched_equals_balanced_layout(native, set4096):
+def test_sched_equals_balanced_layout(native, set4096, rows):
     from siml_gb300 import _native as N
-    gl = _engine()
+    gl = _engine(rows)
     _load(gl, tuple(a[:300] for a in set4096), set4096)
     a = gl.getMultipleRowsDevice(0, 300).cpu()
     N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_ROWS_LAYOUT, N.SIML_ROWS_BALANCED))
@@ -136,3 +145,21 @@ def test_sched_equals_balanced_layout(native, set4096):
     import torch
     assert torch.equal(a.view(torch.int32), b.view(torch.int32)) and torch.equal(a.view(torch.int32),
                                                                                  c.view(torch.int32))
+
+
+def test_sched_vocabulary_larger_than_the_64_row_table(native, oracle):
+    """200,000 lognormal molecules hold more pairs than the 64-row table
+    (about 16.9K): the vocabulary is numbered by frequency, the kernel keeps
+    the most frequent pairs and looks the rest up in its 64-bit-mask hash.
+    Equal to the oracle and to 32-row groups, which hold the whole table."""
+    from siml_gb300 import synthetic as S
+    db = S.smiles_set(S.SEED_DB_1M, S.LOGNORMAL_45, 200_000)
+    ref = S.smiles_set(S.SEED_DB_1M, S.LOGNORMAL_45, 130, first=1_000_000)
+    want = oracle.tanimoto_block(ref, db, 0, 130)
+    for r in (64, 32):
+        gl = _engine(r)
+        _load(gl, ref, db)
+        assert gl.vocabStats()["nvid"] > 20_000
+        assert gl.rowsInfo()["scheduled"] == 1
+        got = gl.getMultipleRows(0, 130)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), r
