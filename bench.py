@@ -262,6 +262,8 @@ def gpu_arm(args):
         N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_SCHED_GROUPS, args.sched_groups), "sched groups")
     if args.sched_rows:
         N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_SCHED_ROWS, args.sched_rows), "sched rows")
+    if args.rare_fixup >= 0:
+        N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_RARE_FIXUP, args.rare_fixup), "rare fix-up")
     stats = gl.dbStats()
     torch.cuda.synchronize()
     log("database layout ready in %.2f s: %s" % (time.time() - t, stats))
@@ -1112,6 +1114,9 @@ def main():
                     help="warp groups of the scheduled full-matrix kernel (2 or 4; 0: library default)")
     ap.add_argument("--sched-rows", type=int, default=0,
                     help="ref rows per CTA of the scheduled full-matrix kernel (32 or 64; 0: library default)")
+    ap.add_argument("--rare-fixup", type=int, default=-1,
+                    help="split vocabularies: 1 recompute rare pairs after the table pass when few, 0 count them "
+                         "through the kernel's hash (-1: library default)")
     ap.add_argument("--rows-layout", type=int, default=-1,
                     help="full-matrix layout (0 padded, 1 balanced, 2 scheduled; -1: library default)")
     ap.add_argument("--rows-entries", type=int, default=-1,

@@ -362,6 +362,12 @@ int siml_vocab_stats(siml_engine* h, int64_t out[4]);
  * pairs go through a hash.  Changing it rebuilds the vocabulary and layouts
  * on next use and invalidates batch plans. */
 #define SIML_TUNE_SCHED_ROWS 7
+/* SIML_TUNE_RARE_FIXUP: with a split vocabulary, 1 (the default) lets the
+ * scheduled full-matrix kernel skip the rare pairs when few pairs share one
+ * (at most 1/64 of a row's columns) and recompute those pairs afterwards with
+ * the reference's merge (k_rare_fix); 0 always counts rare pairs through the
+ * kernel's hash. */
+#define SIML_TUNE_RARE_FIXUP 8
 int siml_set_tuning(siml_engine* h, int key, int64_t value);
 int siml_get_tuning(siml_engine* h, int key, int64_t* value);
 /* The full-matrix path the current sets and settings use (no reference

@@ -34,6 +34,7 @@ SIML_ROWS_BALANCED = 1
 SIML_ROWS_SCHEDULED = 2
 SIML_TUNE_SCHED_GROUPS = 6
 SIML_TUNE_SCHED_ROWS = 7
+SIML_TUNE_RARE_FIXUP = 8
 SIML_ENTRIES_AUTO = 0
 SIML_ENTRIES_U16 = 1
 SIML_ENTRIES_U32 = 2

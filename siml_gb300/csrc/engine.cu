@@ -1311,6 +1311,11 @@ int siml_set_tuning(siml_engine* h, int key, int64_t value) {
             h->sched_groups = (int)value;
         }
         return SIML_OK;
+    case SIML_TUNE_RARE_FIXUP:
+        if (value != 0 && value != 1)
+            return fail(SIML_ERR_INVALID, "rare fix-up must be 0 or 1 (got %lld)", (long long)value);
+        h->rare_fixup = (int)value;
+        return SIML_OK;
     case SIML_TUNE_SCHED_ROWS:
         if (value != 32 && value != 64)
             return fail(SIML_ERR_INVALID, "scheduled kernel rows per group must be 32 or 64 (got %lld)",
@@ -1350,6 +1355,7 @@ int siml_get_tuning(siml_engine* h, int key, int64_t* value) {
     case SIML_TUNE_ROWS_LAYOUT: *value = h->rows_layout; return SIML_OK;
     case SIML_TUNE_SCHED_GROUPS: *value = h->sched_groups; return SIML_OK;
     case SIML_TUNE_SCHED_ROWS: *value = h->sched_rows; return SIML_OK;
+    case SIML_TUNE_RARE_FIXUP: *value = h->rare_fixup; return SIML_OK;
     default: return fail(SIML_ERR_INVALID, "unknown tuning key %d", key);
     }
 }

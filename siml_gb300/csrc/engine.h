@@ -91,6 +91,12 @@ struct DbLayout {
     int2* sched_items = nullptr;  // [nitems + 1] {chunk, steps | kItemSplit | kItemFirst}, padding record last
     int2* sched_lanes = nullptr;  // [nitems + 1][32] {window position or -1, column magnitude bits}
     int2* sched_rare = nullptr;   // split vocabulary: [nitems + 1][32] {first rare entry, count}
+    // split vocabulary, scheduled layout: the molecules (natural index) that
+    // hold each rare vid, vid ncommon + 1 + i at post_mol[post_off[i] ..
+    // post_off[i + 1]); post_max is the longest list
+    int64_t* post_off = nullptr;
+    int32_t* post_mol = nullptr;
+    int64_t post_max = 0;
     int2* sched_wrun = nullptr;   // [nwin * warps] {first item, end item} of (window, warp of a group)
     int64_t* sched_grun = nullptr; // [nwin * warps][2] first and end 16-byte group of (window, warp)
     int64_t nitems = 0;
@@ -149,6 +155,7 @@ struct siml_engine {
     int rows_layout = SIML_ROWS_SCHEDULED; // full-matrix layout (SIML_TUNE_ROWS_LAYOUT)
     int sched_groups = 4;                  // warp groups of the scheduled kernel (SIML_TUNE_SCHED_GROUPS)
     int sched_rows = 64;                   // ref rows per CTA of the scheduled kernel (SIML_TUNE_SCHED_ROWS)
+    int rare_fixup = 1;                    // rare pairs by a second pass when few (SIML_TUNE_RARE_FIXUP)
 };
 
 namespace siml {

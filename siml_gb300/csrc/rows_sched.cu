@@ -50,7 +50,11 @@ constexpr int kSWarpsAll = kSThreads / 32;
 // a byte count per row and column, so 64-row groups keep half the columns.
 template <int ROWS>
 constexpr int kSColsAll = ROWS == 32 ? kSchedColumns32 : kSchedColumns64;
-constexpr double kItemCost = 2.0;     // an item's epilogue, in 8-entry steps, for the schedule
+// An item's flush and record loads, in 8-entry steps, for the schedule: a
+// higher cost makes fewer split items at some cost in balance.  Measured
+// best: 2 for 32-row groups, 4 for 64-row groups (two counters to flush,
+// windows half as long).
+constexpr double item_cost(int rows) { return rows == 64 ? 4.0 : 2.0; }
 constexpr int kItemStepsMask = 0xFFFF;
 constexpr int kItemSplit = 1 << 16;   // the chunk has several items: add counts atomically
 constexpr int kItemFirst = 1 << 17;   // the item holds the chunk's first step: column data, rare entries
@@ -199,7 +203,7 @@ __device__ __forceinline__ int build_table64(uint32_t* T, RowSmem64& rs, const G
             if (v == 0u) continue;
             if ((int64_t)v <= p.ncommon) atomicOr(&T[2 * v + half], bit);
             else if (p.rare_slots) rare64_insert(keys, v, half, bit, p.err);
-            else if (p.err) atomicOr(p.err, kErrBadRowVid);
+            else if (p.err && !p.rare_fixup) atomicOr(p.err, kErrBadRowVid);
         }
     }
     __syncthreads();
@@ -562,6 +566,139 @@ __global__ void k_sched_rare(const int2* __restrict__ items, int64_t nitems, con
     rare[i] = first ? make_int2((int)b, (int)(e - b)) : make_int2(0, 0);
 }
 
+// Inverted lists of the rare vids (split vocabulary): pass 0 counts each
+// vid's molecules, pass 1 places them (cursor starts at the list offsets).
+__global__ void k_post_build(const int4* __restrict__ meta, int64_t slots, const int64_t* __restrict__ rare_off,
+                             const uint32_t* __restrict__ rare_vid, int64_t ncommon, int pass,
+                             unsigned long long* __restrict__ cnt, int32_t* __restrict__ post_mol) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= slots) return;
+    const int32_t m = meta[s].x;
+    if (m < 0) return;
+    for (int64_t i = rare_off[s]; i < rare_off[s + 1]; i++) {
+        const int64_t k = (int64_t)rare_vid[i] - ncommon - 1;
+        if (pass == 0) atomicAdd(cnt + k, 1ull);
+        else post_mol[atomicAdd(cnt + k, 1ull)] = m;
+    }
+}
+
+// Sorted-list merge intersection of two compiled molecules
+// (pysiml/_CPULingo.c:53-71).
+__device__ __forceinline__ int merge_count(const int32_t* a, const int32_t* as, int32_t alen, const int32_t* b,
+                                           const int32_t* bs, int32_t blen) {
+    int32_t i = 0, j = 0, isct = 0;
+    while (i < alen && j < blen) {
+        const int32_t x = a[i], y = b[j];
+        if (x == y) { isct += min(as[i], bs[j]); i++; j++; }
+        else if (x < y) i++;
+        else j++;
+    }
+    return isct;
+}
+
+struct FixArgs {
+    const uint32_t* row_vid;
+    int64_t row_stride;
+    int64_t ncommon;
+    const int64_t* post_off;
+    const int32_t* post_mol;
+    const int32_t *rl, *rc, *rlen, *rmag;   // ref set
+    int64_t rw;
+    const int32_t *ql, *qc, *qlen, *qmag;   // query set
+    int64_t qw;
+    int64_t rowbase;
+    float* out;
+    int64_t ldo;
+    int* err;   // asynchronous error word (a row whose pairs overfill the hash: not possible within the
+                // launch's bound, reported rather than dropped)
+};
+
+// Fix-up pass limits: a row's rare vids and the (row, molecule) pairs they
+// touch, counted in a per-row shared-memory hash at most 3/4 full.
+constexpr int kFixSlots = 4096;
+constexpr int kFixMaxPairs = 3072;
+constexpr int kFixMaxVids = 256;
+
+// The common-entry intersection of a pair from the fp32 Tanimoto the table
+// pass wrote (t = isct / (amag + bmag - isct), increasing in isct): the
+// estimate t S / (1 + t) and its neighbours, each checked by recomputing the
+// reference's quotient bit for bit; -1 when none matches or when magnitudes
+// this large could make two counts round to the same quotient.
+__device__ __forceinline__ int recover_isct(float t, int amag, int bmag) {
+    if (amag == 0 || bmag == 0) return 0;   // t is 0 whatever the count
+    const float S = (float)amag + (float)bmag;
+    if (!(S <= 1048576.0f)) return -1;
+    const int c = __float2int_rn(t * S / (1.0f + t));
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int cand = c + (d == 0 ? 0 : (d == 1 ? -1 : 1));
+        if (cand >= 0 && __float_as_uint(tanimoto_rows(cand, amag, bmag)) == __float_as_uint(t)) return cand;
+    }
+    return -1;
+}
+
+// The pairs of a full-matrix block that share a rare vid (one CTA per row).
+// The table pass counted their common entries only.  Each molecule's shared
+// rare vids are counted in shared memory from the rare vids' molecule lists;
+// its common count comes back from the quotient already written, and the
+// quotient is written again for the full count (the reference's merge when
+// the count cannot be recovered).
+__global__ void __launch_bounds__(256) k_rare_fix(const FixArgs f) {
+    __shared__ int32_t key[kFixSlots];   // molecule + 1, 0: empty
+    __shared__ int32_t add[kFixSlots];   // shared rare vids
+    __shared__ uint32_t rv_s[kFixMaxVids];
+    __shared__ int nrv;
+    const int tid = threadIdx.x;
+    const int64_t r = f.rowbase + blockIdx.x;
+    for (int i = tid; i < kFixSlots; i += blockDim.x) {
+        key[i] = 0;
+        add[i] = 0;
+    }
+    if (tid == 0) nrv = 0;
+    __syncthreads();
+    const uint32_t* rv = f.row_vid + r * f.row_stride;
+    for (int64_t e = tid; e < f.row_stride; e += blockDim.x) {
+        const uint32_t v = rv[e];
+        if ((int64_t)v > f.ncommon) {
+            const int k = atomicAdd(&nrv, 1);
+            if (k < kFixMaxVids) rv_s[k] = v;
+        }
+    }
+    __syncthreads();
+    const int n = min(nrv, kFixMaxVids);   // the launch admits rows of at most kFixMaxVids rare vids
+    for (int j = 0; j < n; j++) {
+        const int64_t k = (int64_t)rv_s[j] - f.ncommon - 1;
+        const int64_t b = f.post_off[k], en = f.post_off[k + 1];
+        for (int64_t i = b + tid; i < en; i += blockDim.x) {
+            const int32_t m = f.post_mol[i];
+            uint32_t h = ((uint32_t)m * 0x9E3779B1u) >> (32 - 12);
+            int probe = 0;
+            for (; probe < kFixSlots; probe++) {   // at most 3/4 full: ends
+                const int32_t prev = atomicCAS(&key[h], 0, m + 1);
+                if (prev == 0 || prev == m + 1) {
+                    atomicAdd(&add[h], 1);
+                    break;
+                }
+                h = (h + 1) & (kFixSlots - 1);
+            }
+            if (probe == kFixSlots && f.err) atomicOr(f.err, kErrBadRowVid);
+        }
+    }
+    __syncthreads();
+    const int32_t alen = f.rlen[r], amag = f.rmag[r];
+    float* orow = f.out + (int64_t)blockIdx.x * f.ldo;
+    for (int s = tid; s < kFixSlots; s += blockDim.x) {
+        const int32_t km = key[s];
+        if (km == 0) continue;
+        const int32_t m = km - 1, bmag = f.qmag[m];
+        const int i0 = recover_isct(orow[m], amag, bmag);
+        const int is = i0 >= 0 ? i0 + add[s]
+                               : merge_count(f.rl + r * f.rw, f.rc + r * f.rw, alen, f.ql + (int64_t)m * f.qw,
+                                             f.qc + (int64_t)m * f.qw, f.qlen[m]);
+        orow[m] = tanimoto_rows(is, amag, bmag);
+    }
+}
+
 struct SchedItem {
     int64_t chunk;
     int s0, ns;
@@ -622,8 +759,13 @@ void free_sched(DbLayout& d) {
     if (d.sched_grun) cudaFree(d.sched_grun);
     if (d.sched_lanes) cudaFree(d.sched_lanes);
     if (d.sched_rare) cudaFree(d.sched_rare);
+    if (d.post_off) cudaFree(d.post_off);
+    if (d.post_mol) cudaFree(d.post_mol);
     d.sched_lanes = nullptr;
     d.sched_rare = nullptr;
+    d.post_off = nullptr;
+    d.post_mol = nullptr;
+    d.post_max = 0;
     d.sched_items = nullptr;
     d.sched_wrun = nullptr;
     d.sched_grun = nullptr;
@@ -633,23 +775,23 @@ namespace {
 
 // Wrap-around fill of one window's chunks (steps L[0..n), ascending; the
 // longest first) into P warps of capacity M, an item costing its steps plus
-// kItemCost: a chunk goes whole into the current warp while it fits, else
+// icost: a chunk goes whole into the current warp while it fits, else
 // the warp is filled to M and the rest continues in the next warp.  Returns
 // false when P warps do not suffice.
-bool fill_window(const int32_t* L, int n, int P, double M, std::vector<SchedItem>* pw, int64_t c0) {
+bool fill_window(const int32_t* L, int n, int P, double M, std::vector<SchedItem>* pw, int64_t c0, double icost) {
     for (int w = 0; w < P; w++) pw[w].clear();
     std::vector<double> load((size_t)P, 0.0);
     int w = 0;
     for (int c = n - 1; c >= 0; c--) {
         int rem = L[c], s0 = 0;
         if (rem == 0) {   // molecules with no streamed entries: counts 0, column data still written
-            if (load[(size_t)w] + kItemCost > M && w < P - 1) w++;
-            load[(size_t)w] += kItemCost;
+            if (load[(size_t)w] + icost > M && w < P - 1) w++;
+            load[(size_t)w] += icost;
             pw[w].push_back({c0 + c, 0, 0, false});
             continue;
         }
         while (rem > 0) {
-            const int cap = (int)std::floor(M - load[(size_t)w] - kItemCost);
+            const int cap = (int)std::floor(M - load[(size_t)w] - icost);
             if (cap <= 0) {
                 if (w == P - 1) return false;
                 w++;
@@ -657,7 +799,7 @@ bool fill_window(const int32_t* L, int n, int P, double M, std::vector<SchedItem
             }
             const int take = rem <= cap ? rem : cap;
             pw[w].push_back({c0 + c, s0, take, false});
-            load[(size_t)w] += take + kItemCost;
+            load[(size_t)w] += take + icost;
             s0 += take;
             rem -= take;
             if (load[(size_t)w] >= M - 0.5 && rem > 0) {
@@ -670,6 +812,66 @@ bool fill_window(const int32_t* L, int n, int P, double M, std::vector<SchedItem
 }
 
 }  // namespace
+
+// The molecules of each rare vid of a split layout (d.post_off, d.post_mol,
+// d.post_max): counted on the device, offsets on the host, placed on the
+// device.
+static int build_postings(siml_engine* h, DbLayout& d) {
+    cudaStream_t st = h->stream;
+    const int64_t nrv = h->vocab.nvid - d.ncommon, slots = d.nchunks * 32;
+    std::vector<unsigned long long> hc((size_t)nrv + 1, 0ull);
+    std::vector<int64_t> ho((size_t)nrv + 1, 0);
+    int rc;
+    void* cnt = nullptr;
+    if ((rc = dev_alloc_bytes(&cnt, hc.size() * 8))) return rc;
+    cudaError_t e = cudaMemsetAsync(cnt, 0, hc.size() * 8, st);
+    if (e == cudaSuccess && slots > 0) {
+        k_post_build<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(d.meta, slots, d.rare_off, d.rare_vid,
+                                                                      d.ncommon, 0, (unsigned long long*)cnt, nullptr);
+        h->launches++;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hc.data(), cnt, hc.size() * 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    int64_t total = 0, longest = 0;
+    for (int64_t i = 0; i < nrv; i++) {
+        ho[(size_t)i] = total;
+        longest = std::max<int64_t>(longest, (int64_t)hc[(size_t)i]);
+        total += (int64_t)hc[(size_t)i];
+        hc[(size_t)i] = (unsigned long long)ho[(size_t)i];   // cursor of the placing pass
+    }
+    ho[(size_t)nrv] = total;
+    void* off = nullptr;
+    void* mol = nullptr;
+    if (e == cudaSuccess) {
+        if ((rc = dev_alloc_bytes(&off, ho.size() * 8)) ||
+            (rc = dev_alloc_bytes(&mol, (size_t)std::max<int64_t>(total, 1) * 4))) {
+            if (off) cudaFree(off);
+            cudaFree(cnt);
+            return rc;
+        }
+        e = cudaMemcpyAsync(off, ho.data(), ho.size() * 8, cudaMemcpyHostToDevice, st);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cnt, hc.data(), hc.size() * 8, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && slots > 0) {
+        k_post_build<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(d.meta, slots, d.rare_off, d.rare_vid,
+                                                                      d.ncommon, 1, (unsigned long long*)cnt,
+                                                                      (int32_t*)mol);
+        h->launches++;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(cnt);
+    if (e != cudaSuccess) {
+        if (off) cudaFree(off);
+        if (mol) cudaFree(mol);
+        return cuda_fail(e, "scheduled layout: rare-vid lists");
+    }
+    d.post_off = (int64_t*)off;
+    d.post_mol = (int32_t*)mol;
+    d.post_max = longest;
+    return SIML_OK;
+}
 
 // Builds the per-(window, warp) schedule of a freshly built window-sorted
 // layout (windows of d.window, 2-byte entries, chunk c's step s of lane l at
@@ -692,6 +894,7 @@ int sched_arrange(siml_engine* h, DbLayout& d) {
     const int64_t per_win = d.window / kChunk;
     const int64_t nwin = (d.n + d.window - 1) / d.window;
     const int G = kSWarpsAll / P;
+    const double icost = item_cost(d.sched_rows);
     // each (window, warp) run is scheduled first, then the runs are stored in
     // stream order: a warp of group g takes windows g, g + G, g + 2G, ...,
     // so its runs of consecutive such windows are stored back to back
@@ -704,18 +907,18 @@ int sched_arrange(siml_engine* h, DbLayout& d) {
         double cost = 0.0;
         int32_t longest = 0;
         for (int64_t c = c0; c < c1 && c * kChunk < d.n; c++, n++) {
-            cost += ng[(size_t)c] + kItemCost;
+            cost += ng[(size_t)c] + icost;
             longest = std::max(longest, ng[(size_t)c]);
         }
         // the smallest share that the fill fits into P warps (bisection)
-        double lo = std::max(1.0, cost / P), hi = 2.0 * cost / P + longest + 4.0 * kItemCost + 1.0;
-        while (!fill_window(ng.data() + c0, n, P, hi, pw.data(), c0)) hi *= 2.0;
+        double lo = std::max(1.0, cost / P), hi = 2.0 * cost / P + longest + 4.0 * icost + 1.0;
+        while (!fill_window(ng.data() + c0, n, P, hi, pw.data(), c0, icost)) hi *= 2.0;
         for (int iter = 0; iter < 24 && hi - lo > 0.25; iter++) {
             const double mid = 0.5 * (lo + hi);
-            if (fill_window(ng.data() + c0, n, P, mid, pw.data(), c0)) hi = mid;
+            if (fill_window(ng.data() + c0, n, P, mid, pw.data(), c0, icost)) hi = mid;
             else lo = mid;
         }
-        fill_window(ng.data() + c0, n, P, hi, pw.data(), c0);
+        fill_window(ng.data() + c0, n, P, hi, pw.data(), c0, icost);
         // chunks with more than one item add their counts atomically
         std::vector<int> parts((size_t)per_win, 0);
         for (auto& v : pw)
@@ -784,6 +987,7 @@ int sched_arrange(siml_engine* h, DbLayout& d) {
                                                                   d.rare_off, d.sched_rare);
         h->launches++;
         SIML_CUDA(cudaGetLastError());
+        if ((rc = build_postings(h, d))) return rc;
     }
     SIML_CUDA(cudaMemcpyAsync(d.sched_wrun, wrun.data(), wrun.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
     SIML_CUDA(cudaMemcpyAsync(d.sched_grun, grun.data(), grun.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
@@ -837,22 +1041,36 @@ int launch_rows_sched(siml_engine* h, const RowsArgs& a, bool* done) {
     if (!table_params(h, d, a.rowbase, rows, kModeRows, p, smem, np) || np != 8 || d->entry_bytes != 2) return SIML_OK;
     const int R = d->sched_rows;
     const bool split = d->ncommon < h->vocab.nvid;
+    // Split vocabulary: when the pairs that share a rare vid are few (at most
+    // kFixMaxPairs per row, bounded by the row with the most rare entries
+    // and the longest molecule list), the table pass skips rare vids and a
+    // second pass adds them to those pairs; otherwise the rare vids go
+    // through the group's hash inside the table pass.
+    const bool fixup = split && h->rare_fixup && d->post_off != nullptr &&
+                       h->rows.max_rare_sched <= kFixMaxVids &&
+                       h->rows.max_rare_sched * d->post_max <= kFixMaxPairs;
+    const bool hash = split && !fixup;
     if (R == 64) {
         // the 64-row table: two words per vid, then the 64-bit-mask hash
-        if (split && h->rows.max_rare_sched > kRare64RowMax) return SIML_OK;
+        if (hash && h->rows.max_rare_sched > kRare64RowMax) return SIML_OK;
         p.vt_words = (int)sched_table_words(64, d->ncommon);
-        p.rare_slots = split ? kRare64Slots : 0;
-        p.tab_words = p.vt_words + (split ? 3 * kRare64Slots : 0);
+        p.rare_slots = hash ? kRare64Slots : 0;
+        p.tab_words = p.vt_words + (hash ? 3 * kRare64Slots : 0);
+        smem = (size_t)p.tab_words * 4;
+    } else if (fixup) {
+        p.rare_slots = 0;
+        p.tab_words = p.vt_words;
         smem = (size_t)p.tab_words * 4;
     }
+    p.rare_fixup = fixup ? 1 : 0;
     const size_t sm = smem + (R == 64 ? kSchedExtraSmem<64> : kSchedExtraSmem<32>);
     if ((int64_t)smem + sched_extra_smem(R, false) > (int64_t)h->smem_optin) return SIML_OK;
     void (*kern)(const GroupParams, const SchedArgs) = nullptr;
     switch ((kSWarpsAll / d->sched_warps) * 100 + R) {
-        case 232: kern = split ? k_rows_sched<true, 2, 32> : k_rows_sched<false, 2, 32>; break;
-        case 432: kern = split ? k_rows_sched<true, 4, 32> : k_rows_sched<false, 4, 32>; break;
-        case 264: kern = split ? k_rows_sched<true, 2, 64> : k_rows_sched<false, 2, 64>; break;
-        case 464: kern = split ? k_rows_sched<true, 4, 64> : k_rows_sched<false, 4, 64>; break;
+        case 232: kern = hash ? k_rows_sched<true, 2, 32> : k_rows_sched<false, 2, 32>; break;
+        case 432: kern = hash ? k_rows_sched<true, 4, 32> : k_rows_sched<false, 4, 32>; break;
+        case 264: kern = hash ? k_rows_sched<true, 2, 64> : k_rows_sched<false, 2, 64>; break;
+        case 464: kern = hash ? k_rows_sched<true, 4, 64> : k_rows_sched<false, 4, 64>; break;
         default: return SIML_OK;
     }
     if ((rc = set_smem(kern, sm))) return rc;
@@ -860,7 +1078,7 @@ int launch_rows_sched(siml_engine* h, const RowsArgs& a, bool* done) {
     sa.items = d->sched_items;
     sa.lanes = d->sched_lanes;
     sa.rare = d->sched_rare;
-    if (split && !sa.rare) return SIML_OK;
+    if (hash && !sa.rare) return SIML_OK;
     sa.wrun = d->sched_wrun;
     sa.grun = d->sched_grun;
     sa.qmag = h->qry.mag;
@@ -884,6 +1102,16 @@ int launch_rows_sched(siml_engine* h, const RowsArgs& a, bool* done) {
     SIML_CUDA(mark(h, h->ev0));
     kern<<<grid, kSThreads, sm, h->stream>>>(p, sa);
     SIML_CUDA(cudaGetLastError());
+    if (fixup && rows > 0) {
+        const RawSet &rs = h->ref, &qs = h->qry;
+        FixArgs f{h->rows.vid, h->rows.stride, d->ncommon, d->post_off, d->post_mol,
+                  rs.lingos, rs.counts, rs.len, rs.mag, rs.width,
+                  qs.lingos, qs.counts, qs.len, qs.mag, qs.width,
+                  a.rowbase, a.out, a.ldo, h->d_async_err};
+        k_rare_fix<<<(unsigned)rows, 256, 0, h->stream>>>(f);
+        SIML_CUDA(cudaGetLastError());
+        h->launches++;
+    }
     SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
     h->launches++;

@@ -69,6 +69,7 @@ struct GroupParams {
     unsigned long long* eval; // counts the pairs of streamed (not skipped) chunks, or null
     int* err;                 // asynchronous error word: bit 3 when a ref row's vid fits neither the
                               // table nor the rare-vid hash (the entry is not used)
+    int rare_fixup;           // rare vids are counted by a later pass (k_rare_fix): the table skips them
 };
 
 // Bit of the asynchronous error word set when a table build meets a vid it
@@ -139,7 +140,7 @@ __device__ __forceinline__ void table_set(uint32_t* T, const GroupParams& p, uin
     if (v == 0u) return;
     if ((int64_t)v <= p.ncommon) atomicOr(&T[v], bit);
     else if (p.rare_slots) rare_insert(T + p.vt_words, v, bit, p.err);
-    else if (p.err) atomicOr(p.err, kErrBadRowVid);
+    else if (p.err && !p.rare_fixup) atomicOr(p.err, kErrBadRowVid);
 }
 
 // Adds the rare entries of layout slot `slot` (split vocabulary) to acc.
@@ -279,6 +280,7 @@ bool table_params(siml_engine* h, const DbLayout* d, int64_t rowbase, int64_t ro
     p.crange = d->crange;
     p.eval = h->d_eval;
     p.err = h->d_async_err;
+    p.rare_fixup = 0;
     return true;
 }
 
