@@ -356,8 +356,9 @@ def gpu_arm(args):
 
     # roofline of the dominant kernel: algorithmic bytes per launch = the fp32
     # block (rows) + the database layout streamed once: 16-byte entry groups,
-    # and per chunk (padded layouts) or per work item (scheduled layout) the
-    # 32 lanes' 16-byte molecule records plus the chunk / item tables
+    # and per chunk the 32 lanes' 8-byte records plus the chunk tables
+    # (natural-order layouts), or per work item the 32 lanes' 8-byte records
+    # and the item's 8-byte record (scheduled layout)
     kms = statistics.mean(kernel_ms)
     out_bytes = 0 if fused else pairs_per_step * 4
     rows_info = gl.rowsInfo() if not fused else {"scheduled": 0}
@@ -366,7 +367,7 @@ def gpu_arm(args):
         N.check(N.lib().siml_get_tuning(gl._h, N.SIML_TUNE_SCHED_ROWS, ctypes.byref(v)), "sched rows")
         rows_info["rows_per_cta"] = int(v.value)
     if rows_info["scheduled"]:
-        db_bytes = stats["ngroups_total"] * 16 + rows_info["items"] * (32 * 16 + 8)
+        db_bytes = stats["ngroups_total"] * 16 + rows_info["items"] * (32 * 8 + 8)
     else:
         db_bytes = stats["ngroups_total"] * 16 + stats["nchunks"] * 32 * 8 + stats["nchunks"] * 12
     alg_bytes = out_bytes + db_bytes
