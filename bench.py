@@ -356,7 +356,7 @@ def gpu_arm(args):
 
     # roofline of the dominant kernel: algorithmic bytes per launch = the fp32
     # block (rows) + the database layout streamed once: 16-byte entry groups,
-    # and per chunk the 32 lanes' 8-byte records plus the chunk tables
+    # and per chunk the 32 lanes' 16-byte records plus the chunk tables
     # (natural-order layouts), or per work item the 32 lanes' 8-byte records
     # and the item's 8-byte record (scheduled layout)
     kms = statistics.mean(kernel_ms)
@@ -369,7 +369,7 @@ def gpu_arm(args):
     if rows_info["scheduled"]:
         db_bytes = stats["ngroups_total"] * 16 + rows_info["items"] * (32 * 8 + 8)
     else:
-        db_bytes = stats["ngroups_total"] * 16 + stats["nchunks"] * 32 * 8 + stats["nchunks"] * 12
+        db_bytes = stats["ngroups_total"] * 16 + stats["nchunks"] * 32 * 16 + stats["nchunks"] * 12
     alg_bytes = out_bytes + db_bytes
     achieved = alg_bytes / (kms / 1e3) / 1e9
     peaks = {}
