@@ -4,10 +4,9 @@
 // a database can be compiled and made resident without a host round trip.
 //
 // One warp per string.  A string free of the bytes that carry state (see
-// lingo::stateful_byte) is preprocessed by all lanes at once; otherwise lane
-// 0 runs the preprocessing state machine in place over the string's bytes
-// (each input byte yields at most one output byte, so the writes trail the
-// reads).  The lanes then form the windows in parallel, sort them with a
+// lingo::stateful_byte) is preprocessed by all lanes at once, each mapping
+// its own bytes; otherwise the warp runs the preprocessing state machine in
+// parallel over segments of the string (preprocess_warp), in place.  The lanes then form the windows in parallel, sort them with a
 // bitonic network, and mark run starts with ballots: the unique codes and
 // their counts go straight to the string's output row.  Strings of up to
 // kCompileCap bytes work in shared memory; longer ones are listed and
@@ -23,6 +22,107 @@ namespace {
 
 constexpr int kCompileCap = 1024;       // bytes of a string held in shared memory
 constexpr int kCompileWarps = 8;        // warps (strings in flight) per CTA
+
+// ---- warp-parallel preprocessing.  lingo::preprocess is a transducer over
+// four states plus a terminal one (a terminator or NUL ends the string);
+// each input byte yields at most one output byte.  A warp takes the string
+// in rounds of 32 segments of kSeg bytes: each lane maps every start state
+// to the state its segment ends in, a warp scan composes the maps to give
+// each lane its true start state, each lane replays its segment from it, and
+// a prefix sum of the bytes they keep places their output.
+constexpr int kSeg = 2;
+constexpr int kDone = 4;   // terminal state
+
+// One step of lingo::preprocess: the next state, and the byte kept (-1: none).
+__device__ __forceinline__ int pp_step(int st, unsigned char ch, int& emit) {
+    emit = -1;
+    if (st == kDone || ch == 0) return kDone;
+    if (st == 1) return 2;   // kSwallow: the byte after '%' is dropped
+    if (st == 3) {           // kVerbatimDigits: copied until a non-digit
+        emit = ch;
+        return lingo::is_digit(ch) ? 3 : 0;
+    }
+    if (ch == ' ' || ch == '\n' || ch == '\r') return kDone;
+    if (lingo::is_digit(ch)) {
+        emit = '0';
+        return 2;
+    }
+    emit = ch;
+    if (ch == '%') return 1;
+    if (st == 0 && (ch == '+' || ch == '-' || ch == 'H' || ch == '[')) return 3;
+    return 0;
+}
+
+// Map of 5 start states to end states, 3 bits each: (g after f)[s] = g[f[s]].
+__device__ __forceinline__ uint32_t pp_compose(uint32_t f, uint32_t g) {
+    uint32_t r = 0;
+#pragma unroll
+    for (int s = 0; s < 5; s++) r |= ((g >> (3 * ((f >> (3 * s)) & 7u))) & 7u) << (3 * s);
+    return r;
+}
+
+// lingo::preprocess of buf[0, inlen) in place, by the calling warp; returns
+// the processed length.
+__device__ int32_t preprocess_warp(unsigned char* buf, int64_t inlen) {
+    const int lane = threadIdx.x & 31;
+    int state = 0;
+    int32_t n = 0;
+    for (int64_t base = 0; base < inlen && state != kDone; base += 32 * kSeg) {
+        const int64_t b = base + (int64_t)lane * kSeg;
+        const int64_t left = inlen - b;
+        const int cnt = left <= 0 ? 0 : (left < kSeg ? (int)left : kSeg);
+        unsigned char in[kSeg];
+#pragma unroll
+        for (int i = 0; i < kSeg; i++) in[i] = i < cnt ? buf[b + i] : 0;
+        // this segment's map of start states to end states
+        uint32_t map = 0;
+#pragma unroll
+        for (int s = 0; s < 5; s++) {
+            int st = s, e;
+#pragma unroll
+            for (int i = 0; i < kSeg; i++)
+                if (i < cnt) st = pp_step(st, in[i], e);
+            map |= (uint32_t)st << (3 * s);
+        }
+        // inclusive scan of the maps: lane l gets segments 0..l composed
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t prev = __shfl_up_sync(0xFFFFFFFFu, map, o);
+            if (lane >= o) map = pp_compose(prev, map);
+        }
+        const int end = (int)((map >> (3 * state)) & 7u);
+        int st = __shfl_up_sync(0xFFFFFFFFu, end, 1);
+        if (lane == 0) st = state;
+        // replay from the true start state
+        uint32_t kept[(kSeg + 3) / 4] = {};
+        int k = 0;
+#pragma unroll
+        for (int i = 0; i < kSeg; i++) {
+            if (i < cnt) {
+                int e;
+                st = pp_step(st, in[i], e);
+                if (e >= 0) {
+                    kept[k >> 2] |= (uint32_t)e << (8 * (k & 3));
+                    k++;
+                }
+            }
+        }
+        int pre = k;   // exclusive prefix of the kept counts
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xFFFFFFFFu, pre, o);
+            if (lane >= o) pre += t;
+        }
+        const int total = __shfl_sync(0xFFFFFFFFu, pre, 31);
+        pre -= k;
+        __syncwarp();   // every lane has read its input before any output lands
+        for (int i = 0; i < k; i++) buf[n + pre + i] = (unsigned char)(kept[i >> 2] >> (8 * (i & 3)));
+        __syncwarp();
+        n += total;
+        state = __shfl_sync(0xFFFFFFFFu, end, 31);
+    }
+    return n;
+}
 
 // Compiles one string with the calling warp.  buf holds >= inlen + 8 bytes
 // and codes >= max(next power of two >= inlen, 32) words of scratch.
@@ -47,8 +147,7 @@ __device__ void compile_one(const unsigned char* __restrict__ raw, int64_t inlen
             if (lingo::is_digit(buf[i])) buf[i] = '0';
     } else {
         __syncwarp();
-        if (lane == 0) len = lingo::preprocess(buf, inlen, buf);
-        len = __shfl_sync(0xFFFFFFFFu, len, 0);
+        len = preprocess_warp(buf, inlen);
     }
     __syncwarp();
     int32_t m = 0;
