@@ -665,7 +665,10 @@ __global__ void __launch_bounds__(256) k_rare_fix(const FixArgs f) {
         }
     }
     __syncthreads();
-    const int n = min(nrv, kFixMaxVids);   // the launch admits rows of at most kFixMaxVids rare vids
+    // the launch admits rows of at most kFixMaxVids rare vids; more is
+    // reported, not dropped unseen
+    if (nrv > kFixMaxVids && tid == 0 && f.err) atomicOr(f.err, kErrBadRowVid);
+    const int n = min(nrv, kFixMaxVids);
     for (int j = 0; j < n; j++) {
         const int64_t k = (int64_t)rv_s[j] - f.ncommon - 1;
         const int64_t b = f.post_off[k], en = f.post_off[k + 1];

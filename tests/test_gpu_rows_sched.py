@@ -167,3 +167,10 @@ def test_sched_vocabulary_larger_than_the_64_row_table(native, oracle):
         assert gl.rowsInfo()["scheduled"] == 1
         got = gl.getMultipleRows(0, 130)
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (r, fix)
+        # a row range that does not start at 0, into a strided device output
+        torch = pytest.importorskip("torch")
+        buf = torch.full((64, 200_008), -5.0, dtype=torch.float32, device="cuda")
+        out = buf[:, :200_000]
+        gl.getMultipleRowsDevice(37, 101, out=out)
+        assert np.array_equal(out.cpu().numpy().view(np.uint32), want[37:101].view(np.uint32)), (r, fix)
+        assert bool((buf[:, 200_000:] == -5.0).all())
