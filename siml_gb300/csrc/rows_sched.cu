@@ -58,6 +58,11 @@ constexpr double item_cost(int rows) { return rows == 64 ? 4.0 : 2.0; }
 constexpr int kItemStepsMask = 0xFFFF;
 constexpr int kItemSplit = 1 << 16;   // the chunk has several items: add counts atomically
 constexpr int kItemFirst = 1 << 17;   // the item holds the chunk's first step: column data, rare entries
+constexpr int kItemLast = 1 << 18;    // the last item of its (window, warp) run
+constexpr int kItemEmpty = 1 << 19;   // a placeholder for a run with no items (no steps, no lanes)
+// L2 prefetch distance of the entry stream, in 8-entry steps ahead of a
+// warp's read position: about two windows of 64-row groups ahead
+constexpr int kPrefetchFrom = 12, kPrefetchTo = 28;
 constexpr int kPadSteps = 2;          // steps of zero padding after the entries (loads run two steps ahead)
 // Largest row stride for which ROWS - 1 rows of fp32 stay within 32-bit byte offsets.
 template <int ROWS>
@@ -83,6 +88,7 @@ struct SchedArgs {
     int64_t nwin;
     float* out;            // row rowbase of the block
     int64_t ldo;
+    int64_t ngroups;       // 16-byte groups of the entry array, padding included (prefetch bound)
 };
 
 // ---- packed fp32 pairs (two IEEE round-to-nearest operations each)
@@ -378,12 +384,10 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
     for (int64_t wnd = wfirst; wnd < w1; wnd += G) {
         const int64_t wbase = wnd * WIN;
         // ---------------------------------------------------------- phase 1
-        const int64_t slot = wnd * P + wg;
-        const int ie = __ldg(a.wrun + slot).y;
-        if (lane == 0 && wnd + 2 * G < w1) {   // the run two windows ahead into L2
-            const int64_t s2 = slot + (int64_t)2 * G * P;
-            const int64_t b = __ldg(a.grun + 2 * s2), e = __ldg(a.grun + 2 * s2 + 1);
-            prefetch_l2(Eb + b * 16, (uint32_t)((e - b) * 16));
+        if (lane == 0) {   // the stream about two windows ahead into L2 (no record to wait for)
+            const int64_t g = ptr - E;   // this step's first group
+            const int64_t b = g + (int64_t)kPrefetchFrom * 32, e = min(g + (int64_t)kPrefetchTo * 32, a.ngroups);
+            if (e > b) prefetch_l2(Eb + b * 16, (uint32_t)((e - b) * 16));
         }
         // ends the items that are complete; false when the window's items are
         // done (rec and lr then hold the next window's first item)
@@ -392,6 +396,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
                 if constexpr (RARE) acc.add_rare(T, p, rr, rv0, rv1);
                 flush_item<WIN, ROWS>(W, colf, rec.y, lr, acc);
                 acc.clear();
+                const bool last = (rec.y & kItemLast) != 0;
                 ++it;
                 rec = rec_n;
                 lr = lr_n;
@@ -403,11 +408,11 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
                     rr_n = __ldg(a.rare + (int64_t)(it + 1) * 32 + lane);
                     rare_prefetch(p, rr, rv0, rv1);
                 }
-                if (it >= ie) return false;
+                if (last) return false;
             }
             return true;
         };
-        if (it < ie && advance()) {
+        if (advance()) {
             for (;;) {
                 if (!phase_b) {   // step held in qa; its register takes the step two ahead
                     const uint32_t x0 = qa.x, x1 = qa.y, x2 = qa.z, x3 = qa.w;
@@ -540,6 +545,10 @@ __global__ void k_sched_lanes(const int2* __restrict__ items, int64_t nitems, co
         lanes[i] = make_int2(-1, __float_as_int(-1.0f));
         return;
     }
+    if (items[item].y & kItemEmpty) {   // a placeholder: no lanes
+        lanes[i] = make_int2(-1, __float_as_int(-1.0f));
+        return;
+    }
     const int64_t chunk = items[item].x;
     const int4 m = meta[chunk * 32 + (i & 31)];
     const int64_t wbase = chunk / per_win * window;
@@ -561,7 +570,7 @@ __global__ void k_sched_rare(const int2* __restrict__ items, int64_t nitems, con
     }
     const int2 it = items[item];
     const int64_t slot = (int64_t)it.x * 32 + (i & 31);
-    const bool first = (it.y & kItemFirst) && meta[slot].x >= 0;
+    const bool first = (it.y & kItemFirst) && !(it.y & kItemEmpty) && meta[slot].x >= 0;
     const int64_t b = rare_off[slot], e = rare_off[slot + 1];
     rare[i] = first ? make_int2((int)b, (int)(e - b)) : make_int2(0, 0);
 }
@@ -611,12 +620,14 @@ struct FixArgs {
     int64_t ldo;
     int* err;   // asynchronous error word (a row whose pairs overfill the hash: not possible within the
                 // launch's bound, reported rather than dropped)
+    int slots_log2;   // the per-row hash: 2^slots_log2 slots of dynamic shared memory (key, count)
 };
 
 // Fix-up pass limits: a row's rare vids and the (row, molecule) pairs they
-// touch, counted in a per-row shared-memory hash at most 3/4 full.
-constexpr int kFixSlots = 4096;
-constexpr int kFixMaxPairs = 3072;
+// touch, counted in a per-row shared-memory hash at most 3/4 full, sized per
+// launch (a power of two up to kFixMaxSlots).
+constexpr int kFixMaxSlotsLog2 = 13;
+constexpr int kFixMaxSlots = 1 << kFixMaxSlotsLog2;
 constexpr int kFixMaxVids = 256;
 
 // The common-entry intersection of a pair from the fp32 Tanimoto the table
@@ -644,13 +655,15 @@ __device__ __forceinline__ int recover_isct(float t, int amag, int bmag) {
 // quotient is written again for the full count (the reference's merge when
 // the count cannot be recovered).
 __global__ void __launch_bounds__(256) k_rare_fix(const FixArgs f) {
-    __shared__ int32_t key[kFixSlots];   // molecule + 1, 0: empty
-    __shared__ int32_t add[kFixSlots];   // shared rare vids
+    extern __shared__ int32_t fix_hash[];
+    const int nslots = 1 << f.slots_log2;
+    int32_t* key = fix_hash;            // molecule + 1, 0: empty
+    int32_t* add = fix_hash + nslots;   // shared rare vids
     __shared__ uint32_t rv_s[kFixMaxVids];
     __shared__ int nrv;
     const int tid = threadIdx.x;
     const int64_t r = f.rowbase + blockIdx.x;
-    for (int i = tid; i < kFixSlots; i += blockDim.x) {
+    for (int i = tid; i < nslots; i += blockDim.x) {
         key[i] = 0;
         add[i] = 0;
     }
@@ -674,23 +687,23 @@ __global__ void __launch_bounds__(256) k_rare_fix(const FixArgs f) {
         const int64_t b = f.post_off[k], en = f.post_off[k + 1];
         for (int64_t i = b + tid; i < en; i += blockDim.x) {
             const int32_t m = f.post_mol[i];
-            uint32_t h = ((uint32_t)m * 0x9E3779B1u) >> (32 - 12);
+            uint32_t h = ((uint32_t)m * 0x9E3779B1u) >> (32 - f.slots_log2);
             int probe = 0;
-            for (; probe < kFixSlots; probe++) {   // at most 3/4 full: ends
+            for (; probe < nslots; probe++) {   // at most 3/4 full: ends
                 const int32_t prev = atomicCAS(&key[h], 0, m + 1);
                 if (prev == 0 || prev == m + 1) {
                     atomicAdd(&add[h], 1);
                     break;
                 }
-                h = (h + 1) & (kFixSlots - 1);
+                h = (h + 1) & (nslots - 1);
             }
-            if (probe == kFixSlots && f.err) atomicOr(f.err, kErrBadRowVid);
+            if (probe == nslots && f.err) atomicOr(f.err, kErrBadRowVid);
         }
     }
     __syncthreads();
     const int32_t alen = f.rlen[r], amag = f.rmag[r];
     float* orow = f.out + (int64_t)blockIdx.x * f.ldo;
-    for (int s = tid; s < kFixSlots; s += blockDim.x) {
+    for (int s = tid; s < nslots; s += blockDim.x) {
         const int32_t km = key[s];
         if (km == 0) continue;
         const int32_t m = km - 1, bmag = f.qmag[m];
@@ -956,6 +969,10 @@ int sched_arrange(siml_engine* h, DbLayout& d) {
                     for (int s2 = 0; s2 < x.ns; s2++) map.push_back(off[(size_t)x.chunk] / 32 + x.s0 + s2);
                     gpos += (int64_t)x.ns * 32;
                 }
+                // the kernel ends a window's run at its flagged last item;
+                // a run with no items gets a placeholder to carry the flag
+                if (runs[sl].empty()) items.push_back(make_int2((int)(wnd * per_win), kItemEmpty));
+                items.back().y |= kItemLast;
                 wrun[sl].y = (int)items.size();
                 grun[2 * sl + 1] = gpos;
             }
@@ -1045,13 +1062,13 @@ int launch_rows_sched(siml_engine* h, const RowsArgs& a, bool* done) {
     const int R = d->sched_rows;
     const bool split = d->ncommon < h->vocab.nvid;
     // Split vocabulary: when the pairs that share a rare vid are few (at most
-    // kFixMaxPairs per row, bounded by the row with the most rare entries
-    // and the longest molecule list), the table pass skips rare vids and a
-    // second pass adds them to those pairs; otherwise the rare vids go
+    // 3/4 of kFixMaxSlots per row, bounded by the row with the most rare
+    // entries and the longest molecule list), the table pass skips rare vids
+    // and a second pass adds them to those pairs; otherwise the rare vids go
     // through the group's hash inside the table pass.
+    const int64_t fix_pairs = h->rows.max_rare_sched * d->post_max;   // bound on one row's pairs
     const bool fixup = split && h->rare_fixup && d->post_off != nullptr &&
-                       h->rows.max_rare_sched <= kFixMaxVids &&
-                       h->rows.max_rare_sched * d->post_max <= kFixMaxPairs;
+                       h->rows.max_rare_sched <= kFixMaxVids && fix_pairs * 4 <= (int64_t)kFixMaxSlots * 3;
     const bool hash = split && !fixup;
     if (R == 64) {
         // the 64-row table: two words per vid, then the 64-bit-mask hash
@@ -1089,6 +1106,7 @@ int launch_rows_sched(siml_engine* h, const RowsArgs& a, bool* done) {
     sa.nwin = d->nwin;
     sa.out = a.out;
     sa.ldo = a.ldo;
+    sa.ngroups = d->ngroups_total + (int64_t)kPadSteps * 32;
     const int64_t groups = (rows + R - 1) / R;
     // windows per CTA: groups x splits fills whole waves of one CTA per SM
     int splits = 1;
@@ -1110,8 +1128,11 @@ int launch_rows_sched(siml_engine* h, const RowsArgs& a, bool* done) {
         FixArgs f{h->rows.vid, h->rows.stride, d->ncommon, d->post_off, d->post_mol,
                   rs.lingos, rs.counts, rs.len, rs.mag, rs.width,
                   qs.lingos, qs.counts, qs.len, qs.mag, qs.width,
-                  a.rowbase, a.out, a.ldo, h->d_async_err};
-        k_rare_fix<<<(unsigned)rows, 256, 0, h->stream>>>(f);
+                  a.rowbase, a.out, a.ldo, h->d_async_err, 10};
+        while (f.slots_log2 < kFixMaxSlotsLog2 && (int64_t)(1 << f.slots_log2) * 3 < fix_pairs * 4) f.slots_log2++;
+        const size_t fsm = (size_t)2 * 4 << f.slots_log2;
+        if ((rc = set_smem(k_rare_fix, fsm))) return rc;
+        k_rare_fix<<<(unsigned)rows, 256, fsm, h->stream>>>(f);
         SIML_CUDA(cudaGetLastError());
         h->launches++;
     }
