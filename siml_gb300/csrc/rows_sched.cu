@@ -52,17 +52,18 @@ template <int ROWS>
 constexpr int kSColsAll = ROWS == 32 ? kSchedColumns32 : kSchedColumns64;
 // An item's flush and record loads, in 8-entry steps, for the schedule: a
 // higher cost makes fewer split items at some cost in balance.  Measured
-// best: 2 for 32-row groups, 4 for 64-row groups (two counters to flush,
-// windows half as long).
-constexpr double item_cost(int rows) { return rows == 64 ? 4.0 : 2.0; }
+// best: 2 for 32-row groups, 6 for 64-row groups (two counters to flush,
+// windows half as long; 3, 4 and 8 were slower).
+constexpr double item_cost(int rows) { return rows == 64 ? 6.0 : 2.0; }
 constexpr int kItemStepsMask = 0xFFFF;
 constexpr int kItemSplit = 1 << 16;   // the chunk has several items: add counts atomically
 constexpr int kItemFirst = 1 << 17;   // the item holds the chunk's first step: column data, rare entries
 constexpr int kItemLast = 1 << 18;    // the last item of its (window, warp) run
 constexpr int kItemEmpty = 1 << 19;   // a placeholder for a run with no items (no steps, no lanes)
 // L2 prefetch distance of the entry stream, in 8-entry steps ahead of a
-// warp's read position: about two windows of 64-row groups ahead
-constexpr int kPrefetchFrom = 12, kPrefetchTo = 28;
+// warp's read position: about one to three windows of 64-row groups ahead
+// (measured best of 4-12 ... 24-56)
+constexpr int kPrefetchFrom = 8, kPrefetchTo = 24;
 constexpr int kPadSteps = 2;          // steps of zero padding after the entries (loads run two steps ahead)
 // Largest row stride for which ROWS - 1 rows of fp32 stay within 32-bit byte offsets.
 template <int ROWS>
