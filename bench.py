@@ -415,7 +415,8 @@ def gpu_arm(args):
                    "query_rows": QUERY_N, "parallelism": "replicas" if world > 1 else "single",
                    "rows_window": gl.rowsWindow(), "rows_entries": gl.rowsEntries(), "rows_path": rows_info,
                    "l2": "flushed between steps by a 256 MB write; each step also writes a 4 GB block",
-                   "db_layout": stats, "db_model": args.db_model, "vocab": gl.vocabStats()},
+                   "db_layout": stats, "db_model": args.db_model, "vocab": gl.vocabStats(),
+                   "rows_vocab": gl.rowsVocab()},
         "roofline": roofline,
         "compute_side": compute_side(roofline["kernel"], profile_name(wl, rows_info["scheduled"])),
         "merge_work_ratio": merge_work_ratio(value / world, np.mean(q[2]), np.mean(db[2]),

@@ -376,6 +376,15 @@ int siml_get_tuning(siml_engine* h, int key, int64_t* value);
  * 8-entry steps of one item; out[0] = 0 (and zeros) otherwise.  Builds the
  * layout if needed. */
 int siml_rows_info(siml_engine* h, int64_t out[4]);
+/* The scheduled layout's vocabulary split (no reference counterpart):
+ * out[0] = pairs its shared-memory table holds (the most frequent ones),
+ * out[1] = database entries of the other ("rare") pairs, out[2] = most rare
+ * entries in one ref row, out[3] = how the last getMultipleRows launch on
+ * that layout counted the rare pairs: 0 none to count, 1 a per-group hash
+ * inside the table pass, 2 a second pass over the pairs that share one,
+ * -1 before such a launch.  Zeros (and -1) when getMultipleRows does not run
+ * on the scheduled layout.  Builds the layout if needed. */
+int siml_rows_vocab(siml_engine* h, int64_t out[4]);
 /* Pairs the threshold kernels (neighbours, batched jobs, top-k collection,
  * histograms) actually evaluated: 32 x group rows per streamed chunk, i.e.
  * without the chunks skipped by the magnitude bound.  Waits for the engine's

@@ -499,6 +499,16 @@ class GPULingo:
         N.check(N.lib().siml_rows_info(self._h, a), "siml_rows_info")
         return dict(zip(["scheduled", "items", "windows", "max_item_steps"], [int(x) for x in a]))
 
+    def rowsVocab(self):
+        """Vocabulary split of the scheduled full-matrix layout (dict): pairs
+        in its shared-memory table, rare database entries, most rare entries
+        in one ref row, and how the last getMultipleRows launch counted the
+        rare pairs (rare_path: 0 none, 1 hash in the table pass, 2 second
+        pass, -1 before a launch)."""
+        a = (ctypes.c_int64 * 4)()
+        N.check(N.lib().siml_rows_vocab(self._h, a), "siml_rows_vocab")
+        return dict(zip(["table_pairs", "nrare", "row_max_rare", "rare_path"], [int(x) for x in a]))
+
     def vocabStats(self):
         """Vocabulary split of the resident database (dict): pairs, common
         pairs (shared-memory table), rare database entries, most rare entries

@@ -103,6 +103,7 @@ _SIGNATURES = {
     "siml_debug_set_row_vid": (_I32, [_P, _I64, _I64, ctypes.c_uint32]),
     "siml_mem_info": (_I32, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
     "siml_rows_info": (_I32, [_P, ctypes.POINTER(ctypes.c_int64)]),
+    "siml_rows_vocab": (_I32, [_P, ctypes.POINTER(ctypes.c_int64)]),
     "siml_vocab_stats": (_I32, [_P, _P]),
     "siml_compile_width_gpu": (_I64, [_P, _P, _P, _I64]),
     "siml_compile_smiles_gpu": (_I32, [_P, _P, _P, _I64, _P, _P, _P, _P, _I64]),

@@ -1245,6 +1245,23 @@ int siml_rows_info(siml_engine* h, int64_t out[4]) {
     return SIML_OK;
 }
 
+int siml_rows_vocab(siml_engine* h, int64_t out[4]) {
+    SIML_GUARD(h);
+    if (!out) return fail(SIML_ERR_INVALID, "siml_rows_vocab: NULL output");
+    int rc = ensure_prepared(h);
+    if (rc) return rc;
+    out[0] = out[1] = out[2] = 0;
+    out[3] = -1;
+    if (!rows_use_sched(h)) return SIML_OK;
+    const DbLayout* d = nullptr;
+    if ((rc = ensure_sched_layout(h, &d))) return rc;
+    out[0] = d->ncommon;
+    out[1] = d->nrare;
+    out[2] = h->rows.max_rare_sched;
+    out[3] = h->rows_rare_gen == h->generation ? h->rows_rare_path : -1;
+    return SIML_OK;
+}
+
 int siml_vocab_stats(siml_engine* h, int64_t out[4]) {
     SIML_GUARD(h);
     if (!out) return fail(SIML_ERR_INVALID, "siml_vocab_stats: NULL output");

@@ -88,9 +88,9 @@ struct DbLayout {
     // (window, warp of a group) are one contiguous run of work items, each
     // item a chunk or a range of a chunk's steps (rows_sched.cu)
     bool scheduled = false;
-    int2* sched_items = nullptr;  // [nitems + 1] {chunk, steps | kItemSplit | kItemFirst}, padding record last
-    int2* sched_lanes = nullptr;  // [nitems + 1][32] {window position or -1, column magnitude bits}
-    int2* sched_rare = nullptr;   // split vocabulary: [nitems + 1][32] {first rare entry, count}
+    int2* sched_items = nullptr;  // [nitems + 2] {chunk, steps | kItemSplit | kItemFirst}, two padding records last
+    int2* sched_lanes = nullptr;  // [nitems + 2][32] {window position or -1, column magnitude bits}
+    int2* sched_rare = nullptr;   // split vocabulary: [nitems + 2][32] {first rare entry, count}
     // split vocabulary, scheduled layout: the molecules (natural index) that
     // hold each rare vid, vid ncommon + 1 + i at post_mol[post_off[i] ..
     // post_off[i + 1]); post_max is the longest list
@@ -156,6 +156,8 @@ struct siml_engine {
     int sched_groups = 4;                  // warp groups of the scheduled kernel (SIML_TUNE_SCHED_GROUPS)
     int sched_rows = 64;                   // ref rows per CTA of the scheduled kernel (SIML_TUNE_SCHED_ROWS)
     int rare_fixup = 1;                    // rare pairs by a second pass when few (SIML_TUNE_RARE_FIXUP)
+    int rows_rare_path = -1;               // the last scheduled launch: 0 no rare pairs, 1 hash, 2 second pass
+    uint64_t rows_rare_gen = 0;            // generation of that launch
 };
 
 namespace siml {

@@ -78,9 +78,9 @@ constexpr int kRare64Slots = 1 << kRare64SlotsLog2;
 constexpr int kRare64RowMax = 24;
 
 struct SchedArgs {
-    const int2* items;     // work items, with one padding record after the last
-    const int2* lanes;     // [items + 1][32] per lane: {window position or -1, column magnitude or -1.0f bits}
-    const int2* rare;      // split vocabulary: [items + 1][32] per lane {first rare entry, count}, counted once
+    const int2* items;     // work items, with two padding records after the last
+    const int2* lanes;     // [items + 2][32] per lane: {window position or -1, column magnitude or -1.0f bits}
+    const int2* rare;      // split vocabulary: [items + 2][32] per lane {first rare entry, count}, counted once
                            // per molecule (items holding the chunk's first step), else null
     const int2* wrun;      // [nwin * P] {first item, end item} of (window, warp of the group)
     const int64_t* grun;   // [nwin * P][2] first and end 16-byte group of (window, warp of the group)
@@ -349,9 +349,13 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
     const int64_t wfirst = w0 + group;
     const uint4* ptr = E;
     uint4 qa = make_uint4(0u, 0u, 0u, 0u), qb = qa;
+    // item records loaded RA items ahead (two, or one when the rare-pair
+    // hash's registers leave no room): rec/lr the current item's, rec_n/lr_n
+    // the next's, rec_n2/lr_n2 the one after (RA == 2)
+    constexpr int RA = RARE ? 1 : 2;
     int it = 0, left = 0;
-    int2 rec = make_int2(0, 0), rec_n = rec;
-    int2 lr = make_int2(-1, 0), lr_n = lr;   // this lane's record of the current and the next item
+    int2 rec = make_int2(0, 0), rec_n = rec, rec_n2 = rec;
+    int2 lr = make_int2(-1, 0), lr_n = lr, lr_n2 = lr;   // this lane's records
     int2 rr = make_int2(0, 0), rr_n = rr;     // its rare entries (split vocabulary)
     uint32_t rv0 = 0u, rv1 = 0u;              // the current item's first two rare entries
     bool phase_b = false;   // the next step is held in qb
@@ -366,6 +370,10 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
         lr = __ldg(a.lanes + (int64_t)it * 32 + lane);
         rec_n = __ldg(a.items + it + 1);
         lr_n = __ldg(a.lanes + (int64_t)(it + 1) * 32 + lane);
+        if constexpr (RA == 2) {
+            rec_n2 = __ldg(a.items + it + 2);
+            lr_n2 = __ldg(a.lanes + (int64_t)(it + 2) * 32 + lane);
+        }
         if constexpr (RARE) {
             rr = __ldg(a.rare + (int64_t)it * 32 + lane);
             rr_n = __ldg(a.rare + (int64_t)(it + 1) * 32 + lane);
@@ -402,8 +410,15 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
                 rec = rec_n;
                 lr = lr_n;
                 left = rec.y & kItemStepsMask;
-                rec_n = __ldg(a.items + it + 1);
-                lr_n = __ldg(a.lanes + (int64_t)(it + 1) * 32 + lane);
+                if constexpr (RA == 2) {
+                    rec_n = rec_n2;
+                    lr_n = lr_n2;
+                    rec_n2 = __ldg(a.items + it + 2);
+                    lr_n2 = __ldg(a.lanes + (int64_t)(it + 2) * 32 + lane);
+                } else {
+                    rec_n = __ldg(a.items + it + 1);
+                    lr_n = __ldg(a.lanes + (int64_t)(it + 1) * 32 + lane);
+                }
                 if constexpr (RARE) {
                     rr = rr_n;
                     rr_n = __ldg(a.rare + (int64_t)(it + 1) * 32 + lane);
@@ -540,9 +555,9 @@ __global__ void k_sched_gather(const uint4* __restrict__ src, const int64_t* __r
 __global__ void k_sched_lanes(const int2* __restrict__ items, int64_t nitems, const int4* __restrict__ meta,
                               int64_t per_win, int window, int2* __restrict__ lanes) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (nitems + 1) * 32) return;
+    if (i >= (nitems + 2) * 32) return;
     const int64_t item = i >> 5;
-    if (item == nitems) {   // the padding record's lanes
+    if (item >= nitems) {   // the padding records' lanes
         lanes[i] = make_int2(-1, __float_as_int(-1.0f));
         return;
     }
@@ -563,9 +578,9 @@ __global__ void k_sched_lanes(const int2* __restrict__ items, int64_t nitems, co
 __global__ void k_sched_rare(const int2* __restrict__ items, int64_t nitems, const int4* __restrict__ meta,
                              const int64_t* __restrict__ rare_off, int2* __restrict__ rare) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (nitems + 1) * 32) return;
+    if (i >= (nitems + 2) * 32) return;
     const int64_t item = i >> 5;
-    if (item == nitems) {   // the padding record's lanes
+    if (item >= nitems) {   // the padding records' lanes
         rare[i] = make_int2(0, 0);
         return;
     }
@@ -977,7 +992,9 @@ int sched_arrange(siml_engine* h, DbLayout& d) {
                 wrun[sl].y = (int)items.size();
                 grun[2 * sl + 1] = gpos;
             }
-    items.push_back(make_int2(0, 0));   // padding record: the stream reads one record ahead
+    // padding records: the stream reads up to two records ahead
+    items.push_back(make_int2(0, 0));
+    items.push_back(make_int2(0, 0));
     if (gpos != d.ngroups_total) return fail(SIML_ERR_CUDA, "scheduled layout: %lld groups scheduled of %lld",
                                              (long long)gpos, (long long)d.ngroups_total);
     if (items.size() > 0x7FFFFFFFu) return fail(SIML_ERR_UNSUPPORTED, "scheduled layout: too many items");
@@ -994,7 +1011,7 @@ int sched_arrange(siml_engine* h, DbLayout& d) {
     d.sched_lanes = (int2*)p;
     {
         const int64_t n = (int64_t)items.size() * 32;
-        k_sched_lanes<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d.sched_items, (int64_t)items.size() - 1, d.meta,
+        k_sched_lanes<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d.sched_items, (int64_t)items.size() - 2, d.meta,
                                                                    per_win, d.window, d.sched_lanes);
         h->launches++;
         SIML_CUDA(cudaGetLastError());
@@ -1004,7 +1021,7 @@ int sched_arrange(siml_engine* h, DbLayout& d) {
         if ((rc = dev_alloc_bytes(&p, items.size() * 32 * sizeof(int2)))) return rc;
         d.sched_rare = (int2*)p;
         const int64_t n = (int64_t)items.size() * 32;
-        k_sched_rare<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d.sched_items, (int64_t)items.size() - 1, d.meta,
+        k_sched_rare<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d.sched_items, (int64_t)items.size() - 2, d.meta,
                                                                   d.rare_off, d.sched_rare);
         h->launches++;
         SIML_CUDA(cudaGetLastError());
@@ -1012,7 +1029,7 @@ int sched_arrange(siml_engine* h, DbLayout& d) {
     }
     SIML_CUDA(cudaMemcpyAsync(d.sched_wrun, wrun.data(), wrun.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
     SIML_CUDA(cudaMemcpyAsync(d.sched_grun, grun.data(), grun.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
-    d.nitems = (int64_t)items.size() - 1;
+    d.nitems = (int64_t)items.size() - 2;
     d.nwin = nwin;
     d.max_item_steps = max_steps;
     // entries in schedule order, with kPadSteps steps of zeros after them
@@ -1140,6 +1157,8 @@ int launch_rows_sched(siml_engine* h, const RowsArgs& a, bool* done) {
     SIML_CUDA(mark(h, h->ev1));
     h->timed = true;
     h->launches++;
+    h->rows_rare_path = fixup ? 2 : hash ? 1 : 0;
+    h->rows_rare_gen = h->generation;
     *done = true;
     return SIML_OK;
 }

@@ -2,11 +2,11 @@
 / and \\ bonds, %nn ring labels): its 57K-pair vocabulary fills a shared-
 memory table on its own, leaving no room for the scheduled full-matrix
 kernel's staging, so the pairs are numbered by database frequency and that
-kernel takes the most frequent ones, the rare ones going through the
-per-group hash.  The full matrix must run on the scheduled table kernel and
-give the oracle's bits; neighbours and top-k likewise; and the GPU compiler,
-whose strings now carry the state-carrying bytes, must give the host
-compiler's arrays."""
+kernel takes the most frequent ones, the pairs that share a rare one
+being recomputed by a second pass.  The full matrix must run on the
+scheduled table kernel and give the oracle's bits; neighbours and top-k
+likewise; and the GPU compiler, whose strings now carry the state-carrying
+bytes, must give the host compiler's arrays."""
 import numpy as np
 import pytest
 
@@ -31,12 +31,14 @@ def test_chem_rows_stay_on_the_table_kernel(native, oracle, chem):
     gl.set_refsmiles(*ref)
     # a table of every pair fits shared memory alone, not beside the
     # scheduled kernel's staging: the pairs are numbered by frequency and
-    # that kernel takes the most frequent ones, the rest through the hash
+    # that kernel takes the most frequent ones, the rest by a second pass
     assert gl.vocabStats()["nvid"] > 50_000
     assert gl.rowsInfo()["scheduled"] == 1   # the scheduled table kernel, not the padded one or the merge
     got = gl.getMultipleRows(0, 96)
     want = oracle.tanimoto_block(ref, db, 0, 96)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    rv = gl.rowsVocab()
+    assert 0 < rv["table_pairs"] < 50_000 and rv["nrare"] > 0 and rv["rare_path"] == 2, rv
 
 
 def test_chem_neighbors_and_topk(native, oracle, chem):

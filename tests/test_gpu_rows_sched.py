@@ -167,6 +167,11 @@ def test_sched_vocabulary_larger_than_the_64_row_table(native, oracle):
         assert gl.rowsInfo()["scheduled"] == 1
         got = gl.getMultipleRows(0, 130)
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (r, fix)
+        rv = gl.rowsVocab()
+        split = rv["table_pairs"] < gl.vocabStats()["nvid"]
+        assert split == (r == 64) and (rv["nrare"] > 0) == split, (r, rv)
+        # the path the launch took: 2 second pass, 1 hash, 0 nothing rare
+        assert rv["rare_path"] == ((2 if fix else 1) if split else 0), (r, fix, rv)
         # a row range that does not start at 0, into a strided device output
         torch = pytest.importorskip("torch")
         buf = torch.full((64, 200_008), -5.0, dtype=torch.float32, device="cuda")
