@@ -367,7 +367,9 @@ def gpu_arm(args):
         N.check(N.lib().siml_get_tuning(gl._h, N.SIML_TUNE_SCHED_ROWS, ctypes.byref(v)), "sched rows")
         rows_info["rows_per_cta"] = int(v.value)
     if rows_info["scheduled"]:
-        db_bytes = stats["ngroups_total"] * 16 + rows_info["items"] * (32 * 8 + 8)
+        # entry groups, then per work item 32 four-byte lane records and its
+        # four-byte steps and flags
+        db_bytes = stats["ngroups_total"] * 16 + rows_info["items"] * (32 * 4 + 4)
     else:
         db_bytes = stats["ngroups_total"] * 16 + stats["nchunks"] * 32 * 16 + stats["nchunks"] * 12
     alg_bytes = out_bytes + db_bytes

@@ -89,7 +89,7 @@ struct DbLayout {
     // item a chunk or a range of a chunk's steps (rows_sched.cu)
     bool scheduled = false;
     int2* sched_items = nullptr;  // [nitems + 2] {chunk, steps | kItemSplit | kItemFirst}, two padding records last
-    int2* sched_lanes = nullptr;  // [nitems + 2][32] {window position or -1, column magnitude bits}
+    int* sched_lanes = nullptr;   // [nitems + 2][32] window position << 16 | fast magnitude, or -1
     int2* sched_rare = nullptr;   // split vocabulary: [nitems + 2][32] {first rare entry, count}
     // split vocabulary, scheduled layout: the molecules (natural index) that
     // hold each rare vid, vid ncommon + 1 + i at post_mol[post_off[i] ..

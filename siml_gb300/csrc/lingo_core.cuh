@@ -65,6 +65,35 @@ struct SlicedCounter {
         }
     }
 
+    // eight masks into planes 0..2; returns their weight-8 carry, not yet
+    // added (add_eights or add_eights2 adds it)
+    SIML_HD uint32_t add8_open(uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3,
+                               uint32_t m4, uint32_t m5, uint32_t m6, uint32_t m7) {
+        uint32_t twos_a, twos_b, fours_a, fours_b, eights;
+        full_add(twos_a, plane[0], plane[0], m0, m1);
+        full_add(twos_b, plane[0], plane[0], m2, m3);
+        full_add(fours_a, plane[1], plane[1], twos_a, twos_b);
+        full_add(twos_a, plane[0], plane[0], m4, m5);
+        full_add(twos_b, plane[0], plane[0], m6, m7);
+        full_add(fours_b, plane[1], plane[1], twos_a, twos_b);
+        full_add(eights, plane[2], plane[2], fours_a, fours_b);
+        return eights;
+    }
+
+    // two weight-8 carries at once: plane 3 absorbs them as a carry-save
+    // accumulator and one weight-16 carry ripples on (9 operations where two
+    // add_eights take 18)
+    SIML_HD void add_eights2(uint32_t ea, uint32_t eb) {
+        uint32_t carry;
+        full_add(carry, plane[3], plane[3], ea, eb);
+#pragma unroll
+        for (int p = 4; p < NP; p++) {
+            const uint32_t t = plane[p] & carry;
+            plane[p] ^= carry;
+            carry = t;
+        }
+    }
+
     // add eight 32-row masks (each contributes 1 to every row whose bit is set)
     SIML_HD void add8(uint32_t m0, uint32_t m1, uint32_t m2, uint32_t m3,
                       uint32_t m4, uint32_t m5, uint32_t m6, uint32_t m7) {

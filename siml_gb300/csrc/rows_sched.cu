@@ -79,7 +79,8 @@ constexpr int kRare64RowMax = 24;
 
 struct SchedArgs {
     const int2* items;     // work items, with two padding records after the last
-    const int2* lanes;     // [items + 2][32] per lane: {window position or -1, column magnitude or -1.0f bits}
+    const int* lanes;      // [items + 2][32] per lane: window position << 16 | fast column magnitude (0 for
+                           // the IEEE path), or -1 for no molecule
     const int2* rare;      // split vocabulary: [items + 2][32] per lane {first rare entry, count}, counted once
                            // per molecule (items holding the chunk's first step), else null
     const int2* wrun;      // [nwin * P] {first item, end item} of (window, warp of the group)
@@ -227,6 +228,30 @@ struct GroupCounter {
         for (int h = 0; h < ROWS / 32; h++) c[h].clear();
     }
 
+    // one 8-entry step of 2-byte vids into planes 0..2, its weight-8 carries
+    // returned in e (close1 or close2 adds them)
+    __device__ __forceinline__ void step_open(const uint32_t* T, const uint32_t x0, const uint32_t x1,
+                                              const uint32_t x2, const uint32_t x3, uint32_t (&e)[ROWS / 32]) {
+        if constexpr (ROWS == 32) {
+            e[0] = c[0].add8_open(T[x0 & 0xFFFFu], T[x0 >> 16], T[x1 & 0xFFFFu], T[x1 >> 16],
+                                  T[x2 & 0xFFFFu], T[x2 >> 16], T[x3 & 0xFFFFu], T[x3 >> 16]);
+        } else {
+            const uint2* T2 = reinterpret_cast<const uint2*>(T);
+            const uint2 m0 = T2[x0 & 0xFFFFu], m1 = T2[x0 >> 16], m2 = T2[x1 & 0xFFFFu], m3 = T2[x1 >> 16];
+            const uint2 m4 = T2[x2 & 0xFFFFu], m5 = T2[x2 >> 16], m6 = T2[x3 & 0xFFFFu], m7 = T2[x3 >> 16];
+            e[0] = c[0].add8_open(m0.x, m1.x, m2.x, m3.x, m4.x, m5.x, m6.x, m7.x);
+            e[1] = c[1].add8_open(m0.y, m1.y, m2.y, m3.y, m4.y, m5.y, m6.y, m7.y);
+        }
+    }
+    __device__ __forceinline__ void close1(const uint32_t (&e)[ROWS / 32]) {
+#pragma unroll
+        for (int h = 0; h < ROWS / 32; h++) c[h].add_eights(e[h]);
+    }
+    __device__ __forceinline__ void close2(const uint32_t (&ea)[ROWS / 32], const uint32_t (&eb)[ROWS / 32]) {
+#pragma unroll
+        for (int h = 0; h < ROWS / 32; h++) c[h].add_eights2(ea[h], eb[h]);
+    }
+
     // one 8-entry step of 2-byte vids
     __device__ __forceinline__ void step(const uint32_t* T, const uint32_t x0, const uint32_t x1, const uint32_t x2,
                                          const uint32_t x3) {
@@ -277,10 +302,10 @@ __device__ __forceinline__ void rare_prefetch(const GroupParams& p, int2 rr, uin
 // at the molecule's window position: staging word 8 h + k holds rows
 // 32 h + k, + 8, + 16, + 24.
 template <int WIN, int ROWS>
-__device__ __forceinline__ void flush_item(uint32_t* W, float* colf, int flags, const int2& lr,
+__device__ __forceinline__ void flush_item(uint32_t* W, float* colf, int flags, int lr,
                                            const GroupCounter<ROWS>& acc) {
-    if (lr.x < 0) return;
-    const int pos = lr.x;
+    const int pos = lr >> 16;
+    if (pos < 0) return;
 #pragma unroll
     for (int h = 0; h < ROWS / 32; h++) {
         uint32_t w[8];
@@ -295,7 +320,10 @@ __device__ __forceinline__ void flush_item(uint32_t* W, float* colf, int flags, 
             for (int k = 0; k < 8; k++) W[(8 * h + k) * WIN + pos] = w[k];
         }
     }
-    if (flags & kItemFirst) colf[pos] = __int_as_float(lr.y);
+    if (flags & kItemFirst) {
+        const uint32_t mag = (uint32_t)lr & 0xFFFFu;
+        colf[pos] = mag ? small_int_to_float(mag) : -1.0f;
+    }
 }
 
 __device__ __forceinline__ void group_barrier(int group, int threads) {
@@ -351,11 +379,17 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
     uint4 qa = make_uint4(0u, 0u, 0u, 0u), qb = qa;
     // item records loaded RA items ahead (two, or one when the rare-pair
     // hash's registers leave no room): rec/lr the current item's, rec_n/lr_n
-    // the next's, rec_n2/lr_n2 the one after (RA == 2)
+    // the next's, rec_n2/lr_n2 the one after (RA == 2).  rec is the item's
+    // steps and flags (the .y of its record; the kernel needs no chunk).
     constexpr int RA = RARE ? 1 : 2;
+    // the two steps of a loop iteration share one carry-save addition of
+    // their weight-8 carries (64-row groups of the hash kernel lack the
+    // registers)
+    constexpr bool PAIRED = !RARE || ROWS == 32;
     int it = 0, left = 0;
-    int2 rec = make_int2(0, 0), rec_n = rec, rec_n2 = rec;
-    int2 lr = make_int2(-1, 0), lr_n = lr, lr_n2 = lr;   // this lane's records
+    const int* iflags = reinterpret_cast<const int*>(a.items) + 1;   // item i's steps and flags: iflags[2 i]
+    int rec = 0, rec_n = 0, rec_n2 = 0;
+    int lr = -1, lr_n = -1, lr_n2 = -1;   // this lane's records
     int2 rr = make_int2(0, 0), rr_n = rr;     // its rare entries (split vocabulary)
     uint32_t rv0 = 0u, rv1 = 0u;              // the current item's first two rare entries
     bool phase_b = false;   // the next step is held in qb
@@ -366,12 +400,12 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
         qa = __ldg(ptr);
         qb = __ldg(ptr + 32);
         it = __ldg(a.wrun + sl).x;
-        rec = __ldg(a.items + it);
+        rec = __ldg(iflags + 2 * (int64_t)it);
         lr = __ldg(a.lanes + (int64_t)it * 32 + lane);
-        rec_n = __ldg(a.items + it + 1);
+        rec_n = __ldg(iflags + 2 * (int64_t)(it + 1));
         lr_n = __ldg(a.lanes + (int64_t)(it + 1) * 32 + lane);
         if constexpr (RA == 2) {
-            rec_n2 = __ldg(a.items + it + 2);
+            rec_n2 = __ldg(iflags + 2 * (int64_t)(it + 2));
             lr_n2 = __ldg(a.lanes + (int64_t)(it + 2) * 32 + lane);
         }
         if constexpr (RARE) {
@@ -379,7 +413,7 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
             rr_n = __ldg(a.rare + (int64_t)(it + 1) * 32 + lane);
             rare_prefetch(p, rr, rv0, rv1);
         }
-        left = rec.y & kItemStepsMask;
+        left = rec & kItemStepsMask;
         if (lane == 0) {   // this window's run and the next one's into L2
             for (int64_t w2 = wfirst; w2 < w1 && w2 <= wfirst + G; w2 += G) {
                 const int64_t s2 = w2 * P + wg;
@@ -403,20 +437,20 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
         auto advance = [&]() -> bool {
             while (left == 0) {
                 if constexpr (RARE) acc.add_rare(T, p, rr, rv0, rv1);
-                flush_item<WIN, ROWS>(W, colf, rec.y, lr, acc);
+                flush_item<WIN, ROWS>(W, colf, rec, lr, acc);
                 acc.clear();
-                const bool last = (rec.y & kItemLast) != 0;
+                const bool last = (rec & kItemLast) != 0;
                 ++it;
                 rec = rec_n;
                 lr = lr_n;
-                left = rec.y & kItemStepsMask;
+                left = rec & kItemStepsMask;
                 if constexpr (RA == 2) {
                     rec_n = rec_n2;
                     lr_n = lr_n2;
-                    rec_n2 = __ldg(a.items + it + 2);
+                    rec_n2 = __ldg(iflags + 2 * (int64_t)(it + 2));
                     lr_n2 = __ldg(a.lanes + (int64_t)(it + 2) * 32 + lane);
                 } else {
-                    rec_n = __ldg(a.items + it + 1);
+                    rec_n = __ldg(iflags + 2 * (int64_t)(it + 1));
                     lr_n = __ldg(a.lanes + (int64_t)(it + 1) * 32 + lane);
                 }
                 if constexpr (RARE) {
@@ -430,20 +464,50 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
         };
         if (advance()) {
             for (;;) {
-                if (!phase_b) {   // step held in qa; its register takes the step two ahead
-                    const uint32_t x0 = qa.x, x1 = qa.y, x2 = qa.z, x3 = qa.w;
-                    qa = __ldg(ptr + 64);
-                    acc.step(T, x0, x1, x2, x3);
-                    --left;
-                    if (!advance()) {
-                        phase_b = true;
-                        break;
+                if constexpr (PAIRED) {
+                    // ea: the qa step's weight-8 carries while they wait for
+                    // the qb step's (zero when qa ended an item or was not run)
+                    uint32_t ea[ROWS / 32];
+#pragma unroll
+                    for (int h = 0; h < ROWS / 32; h++) ea[h] = 0u;
+                    if (!phase_b) {   // step held in qa; its register takes the step two ahead
+                        const uint32_t x0 = qa.x, x1 = qa.y, x2 = qa.z, x3 = qa.w;
+                        qa = __ldg(ptr + 64);
+                        acc.step_open(T, x0, x1, x2, x3, ea);
+                        --left;
+                        if (left == 0) {   // the item ends: its counts complete before the flush
+                            acc.close1(ea);
+#pragma unroll
+                            for (int h = 0; h < ROWS / 32; h++) ea[h] = 0u;
+                            if (!advance()) {
+                                phase_b = true;
+                                break;
+                            }
+                        }
                     }
-                }
-                {   // step held in qb
-                    const uint32_t x0 = qb.x, x1 = qb.y, x2 = qb.z, x3 = qb.w;
-                    qb = __ldg(ptr + 96);
-                    acc.step(T, x0, x1, x2, x3);
+                    {   // step held in qb
+                        const uint32_t x0 = qb.x, x1 = qb.y, x2 = qb.z, x3 = qb.w;
+                        qb = __ldg(ptr + 96);
+                        uint32_t eb[ROWS / 32];
+                        acc.step_open(T, x0, x1, x2, x3, eb);
+                        acc.close2(ea, eb);
+                    }
+                } else {
+                    if (!phase_b) {   // step held in qa; its register takes the step two ahead
+                        const uint32_t x0 = qa.x, x1 = qa.y, x2 = qa.z, x3 = qa.w;
+                        qa = __ldg(ptr + 64);
+                        acc.step(T, x0, x1, x2, x3);
+                        --left;
+                        if (!advance()) {
+                            phase_b = true;
+                            break;
+                        }
+                    }
+                    {   // step held in qb
+                        const uint32_t x0 = qb.x, x1 = qb.y, x2 = qb.z, x3 = qb.w;
+                        qb = __ldg(ptr + 96);
+                        acc.step(T, x0, x1, x2, x3);
+                    }
                 }
                 ptr += 64;
                 phase_b = false;
@@ -549,27 +613,25 @@ __global__ void k_sched_gather(const uint4* __restrict__ src, const int64_t* __r
     dst[i] = src[__ldg(map + (i >> 5)) * 32 + (i & 31)];
 }
 
-// Per item and lane the record phase 1 needs: the molecule's position in
-// its window (-1 for a padding slot) and the column magnitude phase 2 uses
-// (as a float, or -1.0f when the pair takes the IEEE division).
+// Per item and lane the record phase 1 needs, in one word: the molecule's
+// position in its window << 16 | the column magnitude phase 2 divides by
+// (fast magnitudes are 1..32768; 0 when the pair takes the IEEE division),
+// or -1 for a padding slot.
+static_assert(kMaxWindow <= 32768, "a window position takes the upper 16 bits of a lane record");
 __global__ void k_sched_lanes(const int2* __restrict__ items, int64_t nitems, const int4* __restrict__ meta,
-                              int64_t per_win, int window, int2* __restrict__ lanes) {
+                              int64_t per_win, int window, int* __restrict__ lanes) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (nitems + 2) * 32) return;
     const int64_t item = i >> 5;
-    if (item >= nitems) {   // the padding records' lanes
-        lanes[i] = make_int2(-1, __float_as_int(-1.0f));
-        return;
-    }
-    if (items[item].y & kItemEmpty) {   // a placeholder: no lanes
-        lanes[i] = make_int2(-1, __float_as_int(-1.0f));
+    if (item >= nitems || (items[item].y & kItemEmpty)) {   // padding records and placeholders: no lanes
+        lanes[i] = -1;
         return;
     }
     const int64_t chunk = items[item].x;
     const int4 m = meta[chunk * 32 + (i & 31)];
     const int64_t wbase = chunk / per_win * window;
-    lanes[i] = make_int2(m.x >= 0 ? (int)(m.x - wbase) : -1,
-                         __float_as_int(m.x >= 0 && fast_mag(m.y, m.z) ? (float)m.y : -1.0f));
+    const uint32_t mag = fast_mag(m.y, m.z) ? (uint32_t)m.y : 0u;
+    lanes[i] = m.x >= 0 ? (int)(((uint32_t)(m.x - wbase) << 16) | mag) : -1;
 }
 
 // Per item and lane the molecule's rare entries {first, count} in the
@@ -1007,8 +1069,8 @@ int sched_arrange(siml_engine* h, DbLayout& d) {
     if ((rc = dev_alloc_bytes(&p, grun.size() * sizeof(int64_t)))) return rc;
     d.sched_grun = (int64_t*)p;
     SIML_CUDA(cudaMemcpyAsync(d.sched_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
-    if ((rc = dev_alloc_bytes(&p, items.size() * 32 * sizeof(int2)))) return rc;
-    d.sched_lanes = (int2*)p;
+    if ((rc = dev_alloc_bytes(&p, items.size() * 32 * sizeof(int)))) return rc;
+    d.sched_lanes = (int*)p;
     {
         const int64_t n = (int64_t)items.size() * 32;
         k_sched_lanes<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d.sched_items, (int64_t)items.size() - 2, d.meta,
