@@ -228,17 +228,15 @@ struct GroupCounter {
         for (int h = 0; h < ROWS / 32; h++) c[h].clear();
     }
 
-    // one 8-entry step of 2-byte vids into planes 0..2, its weight-8 carries
-    // returned in e (close1 or close2 adds them)
-    __device__ __forceinline__ void step_open(const uint32_t* T, const uint32_t x0, const uint32_t x1,
-                                              const uint32_t x2, const uint32_t x3, uint32_t (&e)[ROWS / 32]) {
+    // one 8-entry step (vids ix, see step_vids) into planes 0..2, its
+    // weight-8 carries returned in e (close1 or close2 adds them)
+    __device__ __forceinline__ void step_open(const uint32_t* T, const uint32_t (&ix)[8], uint32_t (&e)[ROWS / 32]) {
         if constexpr (ROWS == 32) {
-            e[0] = c[0].add8_open(T[x0 & 0xFFFFu], T[x0 >> 16], T[x1 & 0xFFFFu], T[x1 >> 16],
-                                  T[x2 & 0xFFFFu], T[x2 >> 16], T[x3 & 0xFFFFu], T[x3 >> 16]);
+            e[0] = c[0].add8_open(T[ix[0]], T[ix[1]], T[ix[2]], T[ix[3]], T[ix[4]], T[ix[5]], T[ix[6]], T[ix[7]]);
         } else {
             const uint2* T2 = reinterpret_cast<const uint2*>(T);
-            const uint2 m0 = T2[x0 & 0xFFFFu], m1 = T2[x0 >> 16], m2 = T2[x1 & 0xFFFFu], m3 = T2[x1 >> 16];
-            const uint2 m4 = T2[x2 & 0xFFFFu], m5 = T2[x2 >> 16], m6 = T2[x3 & 0xFFFFu], m7 = T2[x3 >> 16];
+            const uint2 m0 = T2[ix[0]], m1 = T2[ix[1]], m2 = T2[ix[2]], m3 = T2[ix[3]];
+            const uint2 m4 = T2[ix[4]], m5 = T2[ix[5]], m6 = T2[ix[6]], m7 = T2[ix[7]];
             e[0] = c[0].add8_open(m0.x, m1.x, m2.x, m3.x, m4.x, m5.x, m6.x, m7.x);
             e[1] = c[1].add8_open(m0.y, m1.y, m2.y, m3.y, m4.y, m5.y, m6.y, m7.y);
         }
@@ -250,21 +248,6 @@ struct GroupCounter {
     __device__ __forceinline__ void close2(const uint32_t (&ea)[ROWS / 32], const uint32_t (&eb)[ROWS / 32]) {
 #pragma unroll
         for (int h = 0; h < ROWS / 32; h++) c[h].add_eights2(ea[h], eb[h]);
-    }
-
-    // one 8-entry step of 2-byte vids
-    __device__ __forceinline__ void step(const uint32_t* T, const uint32_t x0, const uint32_t x1, const uint32_t x2,
-                                         const uint32_t x3) {
-        if constexpr (ROWS == 32) {
-            c[0].add8(T[x0 & 0xFFFFu], T[x0 >> 16], T[x1 & 0xFFFFu], T[x1 >> 16],
-                      T[x2 & 0xFFFFu], T[x2 >> 16], T[x3 & 0xFFFFu], T[x3 >> 16]);
-        } else {
-            const uint2* T2 = reinterpret_cast<const uint2*>(T);
-            const uint2 m0 = T2[x0 & 0xFFFFu], m1 = T2[x0 >> 16], m2 = T2[x1 & 0xFFFFu], m3 = T2[x1 >> 16];
-            const uint2 m4 = T2[x2 & 0xFFFFu], m5 = T2[x2 >> 16], m6 = T2[x3 & 0xFFFFu], m7 = T2[x3 >> 16];
-            c[0].add8(m0.x, m1.x, m2.x, m3.x, m4.x, m5.x, m6.x, m7.x);
-            c[1].add8(m0.y, m1.y, m2.y, m3.y, m4.y, m5.y, m6.y, m7.y);
-        }
     }
 
     // adds one rare entry (split vocabulary) through the group's hash
@@ -290,6 +273,24 @@ struct GroupCounter {
         for (int i = 2; i < rr.y; i++) add_rare_vid(T, p, __ldg(p.rare_vid + rr.x + i));
     }
 };
+
+// The 8 vids of a step's 16-byte entry group.  The empty asm makes them
+// complete before the caller's next statement, which reloads the register
+// that held the group with the step two ahead: the load then writes the
+// registers the group held instead of others that a move must bring back
+// at the end of the loop.
+__device__ __forceinline__ void step_vids(const uint4 q, uint32_t (&ix)[8]) {
+    ix[0] = q.x & 0xFFFFu;
+    ix[1] = q.x >> 16;
+    ix[2] = q.y & 0xFFFFu;
+    ix[3] = q.y >> 16;
+    ix[4] = q.z & 0xFFFFu;
+    ix[5] = q.z >> 16;
+    ix[6] = q.w & 0xFFFFu;
+    ix[7] = q.w >> 16;
+    asm volatile("" : "+r"(ix[0]), "+r"(ix[1]), "+r"(ix[2]), "+r"(ix[3]), "+r"(ix[4]), "+r"(ix[5]), "+r"(ix[6]),
+                 "+r"(ix[7]));
+}
 
 // The first two rare entries of an item's molecule, loaded when the item
 // starts so that they arrive while it streams.
@@ -471,9 +472,10 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
 #pragma unroll
                     for (int h = 0; h < ROWS / 32; h++) ea[h] = 0u;
                     if (!phase_b) {   // step held in qa; its register takes the step two ahead
-                        const uint32_t x0 = qa.x, x1 = qa.y, x2 = qa.z, x3 = qa.w;
+                        uint32_t ix[8];
+                        step_vids(qa, ix);
                         qa = __ldg(ptr + 64);
-                        acc.step_open(T, x0, x1, x2, x3, ea);
+                        acc.step_open(T, ix, ea);
                         --left;
                         if (left == 0) {   // the item ends: its counts complete before the flush
                             acc.close1(ea);
@@ -486,17 +488,19 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
                         }
                     }
                     {   // step held in qb
-                        const uint32_t x0 = qb.x, x1 = qb.y, x2 = qb.z, x3 = qb.w;
+                        uint32_t ix[8], eb[ROWS / 32];
+                        step_vids(qb, ix);
                         qb = __ldg(ptr + 96);
-                        uint32_t eb[ROWS / 32];
-                        acc.step_open(T, x0, x1, x2, x3, eb);
+                        acc.step_open(T, ix, eb);
                         acc.close2(ea, eb);
                     }
                 } else {
                     if (!phase_b) {   // step held in qa; its register takes the step two ahead
-                        const uint32_t x0 = qa.x, x1 = qa.y, x2 = qa.z, x3 = qa.w;
+                        uint32_t ix[8], e[ROWS / 32];
+                        step_vids(qa, ix);
                         qa = __ldg(ptr + 64);
-                        acc.step(T, x0, x1, x2, x3);
+                        acc.step_open(T, ix, e);
+                        acc.close1(e);
                         --left;
                         if (!advance()) {
                             phase_b = true;
@@ -504,9 +508,11 @@ __global__ void __launch_bounds__(kSThreads, 1) k_rows_sched(const GroupParams p
                         }
                     }
                     {   // step held in qb
-                        const uint32_t x0 = qb.x, x1 = qb.y, x2 = qb.z, x3 = qb.w;
+                        uint32_t ix[8], e[ROWS / 32];
+                        step_vids(qb, ix);
                         qb = __ldg(ptr + 96);
-                        acc.step(T, x0, x1, x2, x3);
+                        acc.step_open(T, ix, e);
+                        acc.close1(e);
                     }
                 }
                 ptr += 64;
