@@ -42,6 +42,11 @@ extern "C" {
 /* pointer location */
 #define SIML_HOST 0
 #define SIML_DEVICE 1
+/* siml_rows and siml_row_single: host memory the device can address (pinned and mapped,
+ * e.g. from cudaHostAlloc); the kernels write the block into it directly and
+ * the call returns at once, like a device-pointer call (siml_sync /
+ * siml_query_done).  Other host memory is refused (SIML_ERR_INVALID). */
+#define SIML_HOST_QUEUED 2
 
 /* synthetic length models (siml_synth_*) */
 #define SIML_SYNTH_UNIFORM_20_90 0
@@ -102,7 +107,9 @@ int siml_set_sizes(siml_engine* h, int64_t* nref, int64_t* nquery);
 /* ---- similarity calls --------------------------------------------------- */
 /* getMultipleRows[_async](rowbase, rowlimit) — pysiml/GPULingo.py:354-404,
  * kernel gpuLingoSim3_multirow pysiml/kernels.py:315-352.  out: fp32
- * [rowlimit-rowbase, nquery] with row stride ldo (>= nquery). */
+ * [rowlimit-rowbase, nquery] with row stride ldo (>= nquery).  A SIML_HOST
+ * block in pinned, mapped host memory is written there by the kernels
+ * directly; other host memory receives a copy of a device block. */
 int siml_rows(siml_engine* h, int64_t rowbase, int64_t rowlimit,
               float* out, int64_t ldo, int where);
 /* getTanimotoRow[_async](row) — pysiml/GPULingo.py:316-351, kernel

@@ -194,18 +194,15 @@ class GPULingo:
         self._check_rows(rowbase, rowlimit)
         rows, nq = rowlimit - rowbase, self.nquery
         if torch is not None:
-            out = torch.empty((rows, max(nq, 1)), dtype=torch.float32, device=self._device())
-            self._enter()
-            N.check(N.lib().siml_rows(self._h, int(rowbase), int(rowlimit), out.data_ptr(), max(nq, 1),
-                                      N.SIML_DEVICE), "getMultipleRows")
-            # the block comes back into pinned host memory (reused by torch's
-            # host allocator), queued behind the kernel on the engine's stream
+            # the kernels write the block straight into pinned host memory
+            # (reused by torch's host allocator) over the host link, queued on
+            # the engine's stream: no device block and no separate copy
             host = torch.empty((rows, max(nq, 1)), dtype=torch.float32, pin_memory=True)
-            with torch.cuda.stream(self._stream):
-                host.copy_(out, non_blocking=True)
-            out.record_stream(self._stream)
+            self._enter()
+            N.check(N.lib().siml_rows(self._h, int(rowbase), int(rowlimit), host.data_ptr(), max(nq, 1),
+                                      N.SIML_HOST_QUEUED), "getMultipleRows")
             self.last_async_width = nq
-            self._pending = ("matrix", host, nq, out)
+            self._pending = ("matrix", host, nq)
             return
         else:
             out = np.empty((rows, max(nq, 1)), dtype=np.float32)

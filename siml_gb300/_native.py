@@ -23,6 +23,7 @@ SIML_ERR_RANGE = 7
 
 SIML_HOST = 0
 SIML_DEVICE = 1
+SIML_HOST_QUEUED = 2   # siml_rows: pinned, mapped host memory written directly, call queued
 
 SIML_TUNE_ROWS_WINDOW = 1
 SIML_TUNE_ROWS_ENTRIES = 2

@@ -1434,6 +1434,30 @@ static int rows_common(siml_engine* h, int64_t rowbase, int64_t rowlimit, float*
     if (!out) return fail(SIML_ERR_INVALID, "NULL output");
     RowsArgs a{rowbase, rowlimit, out, ldo, mode};
     if (where == SIML_DEVICE) return launch_rows(h, a);
+    if (where != SIML_HOST && where != SIML_HOST_QUEUED)
+        return fail(SIML_ERR_INVALID, "unknown output location %d", where);
+    // Pinned host memory mapped for the device: the kernels write the block
+    // there directly, over the host link, instead of into a device buffer
+    // that a copy then moves (the link bounds both; the direct write saves
+    // the device buffer and the copy's start-up).
+    float* mapped = nullptr;
+    {
+        cudaPointerAttributes attr;
+        if (cudaPointerGetAttributes(&attr, out) == cudaSuccess) {
+            if (attr.type == cudaMemoryTypeHost && attr.devicePointer) mapped = (float*)attr.devicePointer;
+        } else {
+            cudaGetLastError();   // not a pointer the runtime knows: plain host memory
+        }
+    }
+    if (where == SIML_HOST_QUEUED && !mapped)
+        return fail(SIML_ERR_INVALID, "SIML_HOST_QUEUED output must be pinned host memory mapped for the device");
+    if (mapped) {
+        a.out = mapped;
+        if ((rc = launch_rows(h, a))) return rc;
+        if (where == SIML_HOST_QUEUED) return SIML_OK;
+        SIML_CUDA(cudaStreamSynchronize(h->stream));
+        return take_async_error(h);
+    }
     void* dbuf = nullptr;
     if ((rc = scratch_reserve(h, (size_t)(rows * nq) * sizeof(float), &dbuf))) return rc;
     a.out = (float*)dbuf;

@@ -338,3 +338,47 @@ def test_two_engines_in_two_threads(native, set4096):
     for t in ts:
         t.join()
     assert not errors, errors
+
+
+def test_rows_output_locations(native, oracle, set4096):
+    """siml_rows into each output location gives the same bits: pageable
+    host memory (a device block, then a copy), pinned host memory written by
+    the kernels directly (SIML_HOST, and SIML_HOST_QUEUED, which returns at
+    once), and device memory; padded row strides are kept; an unknown
+    location is refused."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    from siml_gb300 import GPULingo, _native as N
+    gl = GPULingo(0)
+    _load(gl, tuple(a[:300] for a in set4096), set4096)
+    want = oracle.tanimoto_block(tuple(a[:300] for a in set4096), set4096, 0, 300)
+    lib, rows = N.lib(), (20, 292)
+    ld = 4100
+    # pageable host memory
+    page = np.full((rows[1] - rows[0], ld), -5.0, np.float32)
+    N.check(lib.siml_rows(gl._h, rows[0], rows[1], page.ctypes.data, ld, N.SIML_HOST), "rows host")
+    # pinned host memory, synchronous and queued
+    pinned = torch.full((rows[1] - rows[0], ld), -5.0, dtype=torch.float32, pin_memory=True)
+    N.check(lib.siml_rows(gl._h, rows[0], rows[1], pinned.data_ptr(), ld, N.SIML_HOST), "rows pinned")
+    queued = torch.full((rows[1] - rows[0], ld), -5.0, dtype=torch.float32, pin_memory=True)
+    N.check(lib.siml_rows(gl._h, rows[0], rows[1], queued.data_ptr(), ld, N.SIML_HOST_QUEUED), "rows queued")
+    N.check(lib.siml_sync(gl._h), "sync")
+    dev = torch.full((rows[1] - rows[0], ld), -5.0, dtype=torch.float32, device="cuda")
+    N.check(lib.siml_rows(gl._h, rows[0], rows[1], dev.data_ptr(), ld, N.SIML_DEVICE), "rows device")
+    N.check(lib.siml_sync(gl._h), "sync")
+    for got in (page, pinned.numpy(), queued.numpy(), dev.cpu().numpy()):
+        assert np.array_equal(got[:, :4096].view(np.uint32), want[rows[0]:rows[1]].view(np.uint32))
+        assert np.all(got[:, 4096:] == -5.0)
+    # pageable memory: refused, unless the runtime reports it as mapped host
+    # memory (then it must be written correctly)
+    page[:] = -5.0
+    rc = lib.siml_rows(gl._h, 0, 8, page.ctypes.data, ld, N.SIML_HOST_QUEUED)
+    assert rc in (N.SIML_OK, N.SIML_ERR_INVALID)
+    if rc == N.SIML_OK:
+        N.check(lib.siml_sync(gl._h), "sync")
+        assert np.array_equal(page[:8, :4096].view(np.uint32), want[:8].view(np.uint32))
+    assert lib.siml_rows(gl._h, 0, 8, page.ctypes.data, ld, 5) == N.SIML_ERR_INVALID
+    # the public call (pinned output, queued) and its async form
+    assert np.array_equal(gl.getMultipleRows(0, 300).view(np.uint32), want.view(np.uint32))
+    gl.getMultipleRows_async(7, 70)
+    assert np.array_equal(gl.retrieveAsyncResult().view(np.uint32), want[7:70].view(np.uint32))
