@@ -77,6 +77,38 @@ def test_split_vocabulary_rows_neighbors_hist_topk(native, oracle):
     assert np.array_equal(idx, oi) and np.array_equal(np.asarray(sims).view(np.uint32), os_.view(np.uint32))
 
 
+@pytest.mark.parametrize("rows", [64, 32])
+def test_split_vocabulary_rows_each_rare_path(native, oracle, rows):
+    """The full matrix on a split vocabulary through each way of counting
+    the rare pairs (a second pass over the pairs that share one, or the
+    kernel's hash), for 64-row and 32-row groups: equal to the oracle, and
+    a launch of the scheduled kernel took the path asked for whenever its
+    table leaves rare pairs (rare_path -1: the call ran on another kernel,
+    as the 64-row hash does for rows with more than 24 rare entries)."""
+    from siml_gb300 import GPULingo, _native as N
+    rng = np.random.default_rng(37)
+    ref, qry = _mixed(rng, 30_000, 72)
+    want = oracle.tanimoto_block(ref, qry, 0, ref[0].shape[0])
+    seen = set()
+    for fix in (1, 0):
+        gl = GPULingo(0)
+        N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_SCHED_ROWS, rows), "sched rows")
+        N.check(N.lib().siml_set_tuning(gl._h, N.SIML_TUNE_RARE_FIXUP, fix), "rare fixup")
+        gl.set_refsmiles(*ref)
+        gl.set_qsmiles(*qry)
+        got = gl.getMultipleRows(0, ref[0].shape[0])
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (rows, fix)
+        rv = gl.rowsVocab()
+        if rv["rare_path"] >= 0:
+            split = rv["table_pairs"] < gl.vocabStats()["nvid"]
+            assert (rv["rare_path"] == 0) == (not split), rv
+            if split and not fix:
+                assert rv["rare_path"] == 1, rv
+        seen.add(rv["rare_path"])
+    if rows == 32:
+        assert 1 in seen and 2 in seen, seen   # both ways ran
+
+
 def test_split_vocabulary_batched_jobs(native, oracle):
     rng = np.random.default_rng(32)
     ref, qry = _mixed(rng, 20_000, 64)
