@@ -182,7 +182,7 @@ class GPULingo:
             out = np.empty((1, max(nq, 1)), dtype=np.float32)
             N.check(N.lib().siml_row_single(self._h, int(rowidx), out.ctypes.data, N.SIML_HOST), "getTanimotoRow")
         self.last_async_width = nq
-        self._pending = ("matrix", out, nq)
+        self._set_pending(("matrix", out, nq))
 
     def getMultipleRows(self, rowbase, rowlimit):
         """Tanimoto rows [rowbase, rowlimit) x all queries (pysiml/GPULingo.py:354-363)."""
@@ -202,14 +202,14 @@ class GPULingo:
             N.check(N.lib().siml_rows(self._h, int(rowbase), int(rowlimit), host.data_ptr(), max(nq, 1),
                                       N.SIML_HOST_QUEUED), "getMultipleRows")
             self.last_async_width = nq
-            self._pending = ("matrix", host, nq)
+            self._set_pending(("matrix", host, nq))
             return
         else:
             out = np.empty((rows, max(nq, 1)), dtype=np.float32)
             N.check(N.lib().siml_rows(self._h, int(rowbase), int(rowlimit), out.ctypes.data, max(nq, 1),
                                       N.SIML_HOST), "getMultipleRows")
         self.last_async_width = nq
-        self._pending = ("matrix", out, nq)
+        self._set_pending(("matrix", out, nq))
 
     def getMultipleRowsDevice(self, rowbase, rowlimit, out=None):
         """Row block left in device memory as a CUDA float32 tensor [rows, nquery]
@@ -251,7 +251,7 @@ class GPULingo:
                 N.check(L.siml_hist101(self._h, int(rowbase), int(rowlimit), out.ctypes.data, 112, N.SIML_HOST),
                         "getMultipleHistogrammedRows")
         self.last_async_width = 101
-        self._pending = ("matrix", out, 101)
+        self._set_pending(("matrix", out, 101))
 
     def getSimilarityHistogram(self, rowbase, rowlimit, out=None):
         """One 1000-bin histogram of every similarity of rows [rowbase,
@@ -403,9 +403,19 @@ class GPULingo:
             cnt = np.empty(max(rows, 1), dtype=np.int32)
             N.check(fn(*args, idx.ctypes.data, N.ptr(sims), cnt.ctypes.data, N.SIML_HOST), "getNeighbors")
         self.last_async_width = maxneighbors
-        self._pending = ("neighbors", idx, sims, cnt, pitch, rows)
+        self._set_pending(("neighbors", idx, sims, cnt, pitch, rows))
 
     # ----------------------------------------------------------- async glue
+    def _set_pending(self, pending):
+        """Makes *pending* the one outstanding result (pysiml/GPULingo.py:350,
+        400, 460, 512).  A result never retrieved is dropped, as the reference
+        drops it, but only once the engine's stream has finished writing its
+        buffers: torch's allocators know nothing of the engine's kernels and
+        would otherwise hand those buffers out again while a kernel writes."""
+        if self._pending is not None:
+            N.check(N.lib().siml_sync(self._h), "siml_sync")
+        self._pending = pending
+
     def retrieveAsyncResult(self):
         """Result of the last async call (pysiml/GPULingo.py:538-640)."""
         if self._pending is None:

@@ -70,6 +70,13 @@ def test_async_protocol(native, oracle, set4096):
     gl.getNeighbors_async(0, 3, 0.5)
     idx2, cnt2 = gl.retrieveAsyncMatrixVectorResult()
     assert np.array_equal(idx, idx2) and np.array_equal(cnt, cnt2)
+    # a result never retrieved is dropped by the next call (after its
+    # kernels are done with its buffers); the next retrieve gives the new one
+    gl.getMultipleRows_async(0, 700)
+    gl.getMultipleRows_async(1000, 1100)
+    gl.getNeighbors_async(0, 3, 0.5)
+    gl.getMultipleRows_async(2000, 2300)
+    assert np.array_equal(gl.retrieveAsyncResult(), oracle.tanimoto_block(set4096, set4096, 2000, 2300))
 
 
 def test_row_ranges(native, set4096):
