@@ -199,8 +199,12 @@ class GPULingo:
             # the engine's stream: no device block and no separate copy
             host = torch.empty((rows, max(nq, 1)), dtype=torch.float32, pin_memory=True)
             self._enter()
-            N.check(N.lib().siml_rows(self._h, int(rowbase), int(rowlimit), host.data_ptr(), max(nq, 1),
-                                      N.SIML_HOST_QUEUED), "getMultipleRows")
+            try:
+                N.check(N.lib().siml_rows(self._h, int(rowbase), int(rowlimit), host.data_ptr(), max(nq, 1),
+                                          N.SIML_HOST_QUEUED), "getMultipleRows")
+            except Exception:
+                N.lib().siml_sync(self._h)   # kernels queued before the failure may still write `host`
+                raise
             self.last_async_width = nq
             self._set_pending(("matrix", host, nq))
             return
