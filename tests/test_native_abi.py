@@ -112,3 +112,21 @@ def test_header_is_plain_c_and_links(native, tmp_path):
                         str(tmp_path / "caller"), "-I", os.path.join(REPO, "include"), "-L", lib_dir,
                         "-lsiml_gb300", "-Wl,-rpath," + lib_dir], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_header_constants_match_the_python_binding():
+    """Every #define of the C header has the same value on the Python side:
+    status codes, pointer locations and tuning keys in _native, the synthetic
+    generator's models in synthetic."""
+    import os
+    import re
+    from siml_gb300 import _native as N
+    from siml_gb300 import synthetic as S
+    path = os.path.join(os.path.dirname(__file__), "..", "include", "siml_gb300.h")
+    defs = re.findall(r"^#define (SIML_[A-Z0-9_]+)\s+(-?\w+)", open(path).read(), re.M)
+    assert len(defs) > 20
+    for name, value in defs:
+        if name.startswith("SIML_SYNTH_"):
+            assert getattr(S, name[len("SIML_SYNTH_"):]) == int(value, 0), name
+        else:
+            assert getattr(N, name) == int(value, 0), name
